@@ -1,0 +1,223 @@
+/*
+ * porsol_gpu.h -- C ABI of the GB300 (sm_103a) mimetic pressure / upstream transport library.
+ *
+ * This is the drop-in boundary for OPM/opm-porsol's incompressible hot path.  The
+ * reference is header-only C++ templates with no FFI; the C++ shim in
+ * opm-porsol_gb300/host/opm/porsol/gpu/ keeps the reference's template names and
+ * method signatures and forwards to the functions below.  Each entry point names the
+ * reference member function it replaces (path:line inside the opm-porsol project).
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Functions without a `_device` suffix take host
+ *     pointers; `_device` variants take device pointers (CUDA global memory of the
+ *     device that was current when the handle was created).
+ *   - Every call returns a porsol_status; on failure porsol_last_error() holds a
+ *     message.  The C++ shim turns non-zero codes into std::runtime_error with the
+ *     reference's message text.
+ *   - A handle owns one CUDA stream and all device buffers.  A handle is not
+ *     thread-safe; distinct handles are independent.
+ *   - Cells are numbered in the grid's iteration order; half-faces are grouped by cell
+ *     in the cell's local face order (the layout of the reference's SparseTable
+ *     `cellFaces_` / `outflux_`, IncompFlowSolverHybrid.hpp:435-438).
+ */
+#ifndef PORSOL_GPU_H
+#define PORSOL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum porsol_status {
+    PORSOL_OK = 0,
+    PORSOL_ERR_NOT_CONVERGED = 1,  /* linear solver hit maxit (IncompFlowSolverHybrid.hpp:1416-1419) */
+    PORSOL_ERR_BAD_ARG = 2,        /* invalid argument or inconsistent grid/BC data */
+    PORSOL_ERR_NONFINITE = 3,      /* NaN/Inf detected in an input or an intermediate */
+    PORSOL_ERR_SAT_RANGE = 4,      /* transport retries exhausted (EulerUpstream_impl.hpp:203-207) */
+    PORSOL_ERR_CUDA = 5,           /* CUDA runtime error */
+    PORSOL_ERR_TIMEOUT = 6,        /* a bounded device-side wait gave up */
+    PORSOL_ERR_STATE = 7,          /* call out of order (e.g. solve before init) */
+    PORSOL_ERR_UNKNOWN_SOLVER = 8, /* linsolver_type not in 0..3 (IncompFlowSolverHybrid.hpp:698-700) */
+    PORSOL_ERR_CFL = 9             /* CFL computation gave dt = 0 (CflCalculator.hpp:75-77) */
+} porsol_status;
+
+/* FlowBC / SatBC type tags, same order as BCBase::BCType (BoundaryConditions.hpp:55).
+ * Interior half-faces carry any value (ignored). */
+enum { PORSOL_BC_DIRICHLET = 0, PORSOL_BC_NEUMANN = 1, PORSOL_BC_PERIODIC = 2 };
+
+/* --------------------------------------------------------------- grid */
+/* Flattened GridInterface (GridInterfaceEuler.hpp:126-214, 346-360, 441-470). */
+typedef struct porsol_grid {
+    int num_cells;
+    const int* cell_facepos;      /* [nc+1] half-face offsets per cell */
+    const int* hf_neighbour;      /* [nhf] Face::neighbourCellIndex(), -1 on the boundary */
+    const int* hf_bid;            /* [nhf] Face::boundaryId(), 0 for interior */
+    const double* hf_area;        /* [nhf] Face::area() */
+    const double* hf_centroid;    /* [3*nhf] Face::centroid() */
+    const double* hf_normal;      /* [3*nhf] Face::normal(), unit outward */
+    const double* cell_volume;    /* [nc] Cell::volume() */
+    const double* cell_centroid;  /* [3*nc] Cell::centroid() */
+} porsol_grid;
+
+/* --------------------------------------------------------------- fluid */
+/* FluidInterface of IncompFlowSolverHybrid::solve (MimeticIPEvaluator.hpp:297-311).
+ * PORSOL_FLUID_CELLWISE: the caller passes total mobility and sum(rho_i * mob_i) per cell.
+ * PORSOL_FLUID_COREY2: two phases, kr1 = s^2, kr2 = (1-s)^2 (ReservoirPropertyCapillary
+ *   without rock tables, ReservoirPropertyCapillary_impl.hpp:118-170), mob_i = kr_i/visc_i,
+ *   evaluated on the GPU from the saturation. */
+enum { PORSOL_FLUID_CELLWISE = 0, PORSOL_FLUID_COREY2 = 1 };
+typedef struct porsol_fluid {
+    int model;
+    double viscosity1, viscosity2;
+    double density1, density2;
+} porsol_fluid;
+
+/* ------------------------------------------------------ pressure solver */
+typedef struct porsol_solver porsol_solver;
+
+/* linsolver_type: 0 = ILU0-preconditioned CG, 1 = AMG-preconditioned CG (default),
+ * 2 = KAMG (runs the type-1 AMG-CG), 3 = FastAMG (runs the type-1 AMG-CG).
+ * precision: PORSOL_FP64 = the plain drop-in; PORSOL_MIXED = FP32 SpMV and
+ * preconditioner inside FP64 iterative refinement. */
+enum { PORSOL_FP64 = 0, PORSOL_MIXED = 1 };
+typedef struct porsol_solve_opts {
+    double residual_tolerance;  /* 1e-8   (IncompFlowSolverHybrid.hpp:662) */
+    int linsolver_verbosity;    /* 1      (:663) */
+    int linsolver_type;         /* 1      (:664) */
+    int same_matrix;            /* 0      (:665) reuse the AMG hierarchy of the previous solve */
+    int linsolver_maxit;        /* 0      (:666) 0 = number of unknowns */
+    double prolongate_factor;   /* 1.6    (:667) coarse-correction damping */
+    int smooth_steps;           /* 1      (:668) pre/post smoothing sweeps */
+    int precision;              /* PORSOL_FP64 */
+    double inner_tolerance;     /* mixed only: residual reduction per FP32 inner solve (1e-3) */
+    int max_outer;              /* mixed only: refinement steps before giving up (30) */
+} porsol_solve_opts;
+
+typedef struct porsol_solve_stats {
+    int iterations;          /* CG iterations (sum of inner iterations in mixed mode) */
+    int outer_iterations;    /* refinement steps (mixed), 1 for FP64 */
+    double reduction;        /* final ||r||/||r0|| */
+    int amg_levels;          /* levels of the AMG hierarchy (0 for ILU0) */
+    double mass_balance;     /* max_c |sum_f v - q_c| / max(max_c |q_c|, max_f |v_f|), FP64 */
+} porsol_solve_stats;
+
+void porsol_solve_opts_default(porsol_solve_opts* opts);
+
+int porsol_create(porsol_solver** out);
+void porsol_destroy(porsol_solver* h);
+const char* porsol_last_error(const porsol_solver* h);
+
+/* IncompFlowSolverHybrid::clear (IncompFlowSolverHybrid.hpp:498-516). */
+int porsol_clear(porsol_solver* h);
+
+/* IncompFlowSolverHybrid::initSystemStructure (IncompFlowSolverHybrid.hpp:534-545):
+ * enumerate face DOFs (:956-1110) and build the sparsity of S incl. periodic couplings
+ * (:1115-1319).  hf_flow_type is FlowBC::type of each boundary half-face, used only to
+ * find periodic faces; hf_partner_bid is getPeriodicPartner(boundaryId) (may be NULL
+ * when nothing is periodic). */
+int porsol_init_system_structure(porsol_solver* h, const porsol_grid* grid,
+                                 const int* hf_flow_type, const int* hf_partner_bid);
+
+/* IncompFlowSolverHybrid::computeInnerProducts (IncompFlowSolverHybrid.hpp:565-578) with
+ * MimeticIPEvaluator::buildStaticContrib (MimeticIPEvaluator.hpp:201-270).
+ * perm: 9 doubles per cell, row-major permeability tensor (host).  grav: 3 doubles. */
+int porsol_compute_inner_products(porsol_solver* h, const double* perm, const double* grav);
+/* Same as porsol_compute_inner_products; the name `assembleStatic` survives only in
+ * commented calls of the reference (common/SimulatorBase.hpp:211). */
+int porsol_assemble_static(porsol_solver* h, const double* perm, const double* grav);
+
+/* IncompFlowSolverHybrid::init (IncompFlowSolverHybrid.hpp:477-488): clear +
+ * initSystemStructure + computeInnerProducts. */
+int porsol_init(porsol_solver* h, const porsol_grid* grid, const double* perm, const double* grav,
+                const int* hf_flow_type, const int* hf_partner_bid);
+
+/* IncompFlowSolverHybrid::solve (IncompFlowSolverHybrid.hpp:658-703): assembleDynamic,
+ * linear solve of the face-pressure system, computePressureAndFluxes.
+ *   sat        [nc]  saturation (COREY2) or total mobility (CELLWISE)
+ *   mobdens    [nc]  CELLWISE only: sum_i rho_i mob_i (may be NULL: zero)
+ *   hf_flow_type/hf_flow_value [nhf]  FlowBC of each boundary half-face
+ *   src        [nc]  source rates
+ * opts may be NULL (defaults); stats may be NULL. */
+int porsol_solve(porsol_solver* h, const porsol_fluid* fluid, const double* sat, const double* mobdens,
+                 const int* hf_flow_type, const double* hf_flow_value, const double* src,
+                 const porsol_solve_opts* opts, porsol_solve_stats* stats);
+/* As porsol_solve with all array arguments in device memory. */
+int porsol_solve_device(porsol_solver* h, const porsol_fluid* fluid, const double* sat,
+                        const double* mobdens, const int* hf_flow_type, const double* hf_flow_value,
+                        const double* src, const porsol_solve_opts* opts, porsol_solve_stats* stats);
+
+/* IncompFlowSolverHybrid::postProcessFluxes (IncompFlowSolverHybrid.hpp:754-807). */
+int porsol_post_process_fluxes(porsol_solver* h, double* max_modification);
+
+/* IncompFlowSolverHybrid::getSolution (IncompFlowSolverHybrid.hpp:818-831), FlowSolution
+ * (:382-447): cell pressure [nc], half-face outflux [nhf], face pressures [ndof].
+ * Any pointer may be NULL. */
+int porsol_get_solution(porsol_solver* h, double* pressure, double* outflux, double* face_pressure);
+int porsol_get_solution_device(porsol_solver* h, const double** pressure, const double** outflux,
+                               const double** face_pressure);
+
+/* Introspection (printStats, IncompFlowSolverHybrid.hpp:849-871; printSystem :895-905). */
+int porsol_num_dofs(porsol_solver* h, int* num_dofs, int* nnz, int* max_ncf, int* num_internal_faces);
+/* cellfaces [nhf], rowptr [ndof+1], colind [nnz] (CSR, sorted), ppartner [ndof] (-1 = none). */
+int porsol_get_structure(porsol_solver* h, int* cellfaces, int* rowptr, int* colind, int* ppartner);
+/* Static inner products: W column-major per cell (sum nf^2), gravity flux per half-face. */
+int porsol_get_inner_products(porsol_solver* h, double* binv, double* gflux);
+/* The assembled system of the last solve before regularisation: S values in the CSR
+ * order of porsol_get_structure, rhs [ndof]. */
+int porsol_get_system(porsol_solver* h, double* values, double* rhs);
+
+/* ------------------------------------------------------ transport */
+typedef struct porsol_transport porsol_transport;
+
+/* EulerUpstream parameters (EulerUpstream_impl.hpp:60-72, 95-108). */
+typedef struct porsol_transport_opts {
+    double courant_number;      /* 0.5 */
+    int method_viscous, method_gravity, method_capillary;    /* 1, 1, 1 */
+    int use_cfl_viscous, use_cfl_gravity, use_cfl_capillary; /* 1, 1, 1 */
+    int minimum_small_steps, maximum_small_steps;            /* 1, 10000 */
+    int check_sat, clamp_sat;                                 /* 1, 0 */
+} porsol_transport_opts;
+
+typedef struct porsol_transport_stats {
+    int small_steps;   /* sub-steps of the successful attempt */
+    int repeats;       /* retries with doubled step count */
+    double cfl_dt;     /* CFL time step (after the Courant factor) */
+} porsol_transport_stats;
+
+void porsol_transport_opts_default(porsol_transport_opts* opts);
+int porsol_transport_create(porsol_transport** out);
+void porsol_transport_destroy(porsol_transport* t);
+const char* porsol_transport_last_error(const porsol_transport* t);
+
+/* EulerUpstream::init(param, g, r, b) / initObj (EulerUpstream_impl.hpp:111-129) with
+ * EulerUpstreamResidual::initFinal (EulerUpstreamResidual_impl.hpp:403-435).
+ * perm 9/cell row-major, poro 1/cell, fluid must be PORSOL_FLUID_COREY2,
+ * hf_sat_type/hf_sat_value = SatBC of boundary half-faces, hf_partner_bid as above. */
+int porsol_transport_init(porsol_transport* t, const porsol_grid* grid, const double* perm,
+                          const double* poro, const porsol_fluid* fluid,
+                          const int* hf_sat_type, const double* hf_sat_value,
+                          const int* hf_partner_bid, const porsol_transport_opts* opts);
+
+/* EulerUpstream::transportSolve (EulerUpstream_impl.hpp:153-218): sat [nc] in/out,
+ * outflux [nhf] half-face fluxes of the pressure solution, injection [nc] (may be NULL). */
+int porsol_transport_solve(porsol_transport* t, double* sat, double time, const double* grav,
+                           const double* outflux, const double* injection,
+                           porsol_transport_stats* stats);
+int porsol_transport_solve_device(porsol_transport* t, double* sat, double time, const double* grav,
+                                  const double* outflux, const double* injection,
+                                  porsol_transport_stats* stats);
+
+/* ------------------------------------------------------ profiling */
+/* Per-kernel CUDA-event timing on the handle's stream (off by default). */
+int porsol_profile_enable(porsol_solver* h, int enable);
+/* Accumulated launches and milliseconds of one kernel class since the last reset.
+ * kernel: 0 = SpMV (FP64), 1 = SpMV (FP32), 2 = assembly, 3 = recovery, 4 = V-cycle. */
+int porsol_profile_get(porsol_solver* h, int kernel, int* launches, double* ms, double* bytes);
+int porsol_profile_reset(porsol_solver* h);
+/* The handle's CUDA stream (cudaStream_t) for callers that time around calls. */
+void* porsol_stream(porsol_solver* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PORSOL_GPU_H */

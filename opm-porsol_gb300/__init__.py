@@ -1,0 +1,353 @@
+"""porsol-gb300: GB300-native mimetic pressure / upstream transport library.
+
+This Python module is the build driver and a thin ctypes binding of the C ABI
+declared in include/porsol_gpu.h, used by the test-suite and the benchmark.
+The product is the CUDA/C++ shared library ``lib/libporsol_gpu.so``; there is
+no Python compute path and no CPU fallback: if the library is missing or
+fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libporsol_gpu.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-I", INCLUDE, "-I", CSRC]
+SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "capi.cu"]
+
+BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
+FLUID_CELLWISE, FLUID_COREY2 = 0, 1
+FP64, MIXED = 0, 1
+ERR = {0: "OK", 1: "NOT_CONVERGED", 2: "BAD_ARG", 3: "NONFINITE", 4: "SAT_RANGE", 5: "CUDA", 6: "TIMEOUT",
+       7: "STATE", 8: "UNKNOWN_SOLVER", 9: "CFL"}
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def build(verbose: bool = False, jobs: int = 8) -> str:
+    """Compile every translation unit for sm_103a in parallel and link the shared library."""
+    obj_dir = os.path.join(LIB_DIR, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+
+    def compile_one(src):
+        out = os.path.join(obj_dir, src + ".o")
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", out]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        return out
+
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+# ----------------------------------------------------------------------------- ctypes
+class Grid(C.Structure):
+    _fields_ = [("num_cells", C.c_int), ("cell_facepos", C.c_void_p), ("hf_neighbour", C.c_void_p),
+                ("hf_bid", C.c_void_p), ("hf_area", C.c_void_p), ("hf_centroid", C.c_void_p),
+                ("hf_normal", C.c_void_p), ("cell_volume", C.c_void_p), ("cell_centroid", C.c_void_p)]
+
+
+class Fluid(C.Structure):
+    _fields_ = [("model", C.c_int), ("viscosity1", C.c_double), ("viscosity2", C.c_double),
+                ("density1", C.c_double), ("density2", C.c_double)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("residual_tolerance", C.c_double), ("linsolver_verbosity", C.c_int),
+                ("linsolver_type", C.c_int), ("same_matrix", C.c_int), ("linsolver_maxit", C.c_int),
+                ("prolongate_factor", C.c_double), ("smooth_steps", C.c_int), ("precision", C.c_int),
+                ("inner_tolerance", C.c_double), ("max_outer", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("reduction", C.c_double),
+                ("amg_levels", C.c_int), ("mass_balance", C.c_double)]
+
+
+class TransportOpts(C.Structure):
+    _fields_ = [("courant_number", C.c_double),
+                ("method_viscous", C.c_int), ("method_gravity", C.c_int), ("method_capillary", C.c_int),
+                ("use_cfl_viscous", C.c_int), ("use_cfl_gravity", C.c_int), ("use_cfl_capillary", C.c_int),
+                ("minimum_small_steps", C.c_int), ("maximum_small_steps", C.c_int),
+                ("check_sat", C.c_int), ("clamp_sat", C.c_int)]
+
+
+class TransportStats(C.Structure):
+    _fields_ = [("small_steps", C.c_int), ("repeats", C.c_int), ("cfl_dt", C.c_double)]
+
+
+# (name, restype, argtypes) of every exported entry point of include/porsol_gpu.h
+_vp, _i, _d = C.c_void_p, C.c_int, C.c_double
+EXPORTS = [
+    ("porsol_solve_opts_default", None, [C.POINTER(SolveOpts)]),
+    ("porsol_create", _i, [C.POINTER(_vp)]),
+    ("porsol_destroy", None, [_vp]),
+    ("porsol_last_error", C.c_char_p, [_vp]),
+    ("porsol_clear", _i, [_vp]),
+    ("porsol_init_system_structure", _i, [_vp, C.POINTER(Grid), _vp, _vp]),
+    ("porsol_compute_inner_products", _i, [_vp, _vp, _vp]),
+    ("porsol_assemble_static", _i, [_vp, _vp, _vp]),
+    ("porsol_init", _i, [_vp, C.POINTER(Grid), _vp, _vp, _vp, _vp]),
+    ("porsol_solve", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts),
+                          C.POINTER(SolveStats)]),
+    ("porsol_solve_device", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts),
+                                 C.POINTER(SolveStats)]),
+    ("porsol_post_process_fluxes", _i, [_vp, C.POINTER(_d)]),
+    ("porsol_get_solution", _i, [_vp, _vp, _vp, _vp]),
+    ("porsol_get_solution_device", _i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
+    ("porsol_num_dofs", _i, [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    ("porsol_get_structure", _i, [_vp, _vp, _vp, _vp, _vp]),
+    ("porsol_get_inner_products", _i, [_vp, _vp, _vp]),
+    ("porsol_get_system", _i, [_vp, _vp, _vp]),
+    ("porsol_transport_opts_default", None, [C.POINTER(TransportOpts)]),
+    ("porsol_transport_create", _i, [C.POINTER(_vp)]),
+    ("porsol_transport_destroy", None, [_vp]),
+    ("porsol_transport_last_error", C.c_char_p, [_vp]),
+    ("porsol_transport_init", _i, [_vp, C.POINTER(Grid), _vp, _vp, C.POINTER(Fluid), _vp, _vp, _vp,
+                                   C.POINTER(TransportOpts)]),
+    ("porsol_transport_solve", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
+    ("porsol_transport_solve_device", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
+    ("porsol_profile_enable", _i, [_vp, _i]),
+    ("porsol_profile_get", _i, [_vp, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_d)]),
+    ("porsol_profile_reset", _i, [_vp]),
+    ("porsol_stream", _vp, [_vp]),
+]
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (fails loudly when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run build() first (there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in EXPORTS:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class PorsolError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{ERR.get(code, code)}] {msg}")
+        self.code = code
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class _GridArrays:
+    def __init__(self, grid):
+        a = grid.arrays()
+        self.a = a
+        self.num_cells = a["num_cells"]
+        self.nhf = int(a["facepos"][-1])
+        self.s = Grid(a["num_cells"], _p(a["facepos"]).value, _p(a["neighbour"]).value, _p(a["bid"]).value,
+                      _p(a["area"]).value, _p(a["fcentroid"]).value, _p(a["fnormal"]).value,
+                      _p(a["volume"]).value, _p(a["ccentroid"]).value)
+
+
+def default_solve_opts(**kw) -> SolveOpts:
+    o = SolveOpts()
+    lib().porsol_solve_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def default_transport_opts(**kw) -> TransportOpts:
+    o = TransportOpts()
+    lib().porsol_transport_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class PressureSolver:
+    """Python face of the C ABI, named like IncompFlowSolverHybrid's methods."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        rc = lib().porsol_create(C.byref(h))
+        if rc != 0:
+            raise PorsolError(rc, "porsol_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().porsol_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PorsolError(rc, lib().porsol_last_error(self.h).decode())
+
+    def init(self, grid, perm, grav=(0.0, 0.0, 0.0), flow_type=None, partner_bid=None):
+        self.grid = _GridArrays(grid)
+        self._ft = None if flow_type is None else _i32(flow_type)
+        self._pb = None if partner_bid is None else _i32(partner_bid)
+        self._check(lib().porsol_init_system_structure(self.h, C.byref(self.grid.s), _p(self._ft), _p(self._pb)))
+        self.compute_inner_products(perm, grav)
+        n, nnz, mx, ni = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().porsol_num_dofs(self.h, C.byref(n), C.byref(nnz), C.byref(mx), C.byref(ni)))
+        self.n, self.nnz, self.max_ncf, self.num_internal_faces = n.value, nnz.value, mx.value, ni.value
+
+    def compute_inner_products(self, perm, grav=(0.0, 0.0, 0.0)):
+        self._perm = _f64(perm)
+        g = _f64(grav)
+        self._check(lib().porsol_compute_inner_products(self.h, _p(self._perm), _p(g)))
+
+    assemble_static = compute_inner_products
+
+    def solve(self, fluid: Fluid, sat, bc_type, bc_value, src, mobdens=None, opts: SolveOpts = None):
+        st = SolveStats()
+        o = opts if opts is not None else default_solve_opts()
+        args = [_f64(sat), None if mobdens is None else _f64(mobdens), _i32(bc_type), _f64(bc_value), _f64(src)]
+        self._check(lib().porsol_solve(self.h, C.byref(fluid), *[_p(a) for a in args], C.byref(o), C.byref(st)))
+        return st
+
+    def solve_device(self, fluid, d_sat, d_bct, d_bcv, d_src, d_mobdens=0, opts=None):
+        """All arrays are raw device addresses (ints)."""
+        st = SolveStats()
+        o = opts if opts is not None else default_solve_opts()
+        self._check(lib().porsol_solve_device(self.h, C.byref(fluid), C.c_void_p(d_sat), C.c_void_p(d_mobdens or None),
+                                              C.c_void_p(d_bct), C.c_void_p(d_bcv), C.c_void_p(d_src), C.byref(o),
+                                              C.byref(st)))
+        return st
+
+    def post_process_fluxes(self):
+        m = C.c_double()
+        self._check(lib().porsol_post_process_fluxes(self.h, C.byref(m)))
+        return m.value
+
+    def solution(self):
+        p = np.empty(self.grid.num_cells)
+        v = np.empty(self.grid.nhf)
+        pi = np.empty(self.n)
+        self._check(lib().porsol_get_solution(self.h, _p(p), _p(v), _p(pi)))
+        return p, v, pi
+
+    def structure(self):
+        cf = np.empty(self.grid.nhf, np.int32)
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        pp = np.empty(self.n, np.int32)
+        self._check(lib().porsol_get_structure(self.h, _p(cf), _p(rp), _p(ci), _p(pp)))
+        return cf, rp, ci, pp
+
+    def inner_products(self):
+        nf = np.diff(self.grid.a["facepos"])
+        B = np.empty(int((nf * nf).sum()))
+        gf = np.empty(self.grid.nhf)
+        self._check(lib().porsol_get_inner_products(self.h, _p(B), _p(gf)))
+        return B, gf
+
+    def system(self):
+        S = np.empty(self.nnz)
+        rhs = np.empty(self.n)
+        self._check(lib().porsol_get_system(self.h, _p(S), _p(rhs)))
+        return S, rhs
+
+    # profiling
+    def profile_enable(self, on=True):
+        self._check(lib().porsol_profile_enable(self.h, int(on)))
+
+    def profile_get(self, kernel):
+        n, ms, b = C.c_int(), C.c_double(), C.c_double()
+        self._check(lib().porsol_profile_get(self.h, kernel, C.byref(n), C.byref(ms), C.byref(b)))
+        return n.value, ms.value, b.value
+
+    def profile_reset(self):
+        self._check(lib().porsol_profile_reset(self.h))
+
+    def stream(self):
+        return lib().porsol_stream(self.h)
+
+
+class TransportSolver:
+    """Python face of the EulerUpstream C ABI."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        rc = lib().porsol_transport_create(C.byref(h))
+        if rc != 0:
+            raise PorsolError(rc, "porsol_transport_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().porsol_transport_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PorsolError(rc, lib().porsol_transport_last_error(self.h).decode())
+
+    def init(self, grid, perm, poro, fluid: Fluid, sat_type, sat_value, partner_bid=None, opts=None):
+        self.grid = _GridArrays(grid)
+        self._keep = [_f64(perm), _f64(poro), _i32(sat_type), _f64(sat_value),
+                      None if partner_bid is None else _i32(partner_bid)]
+        o = opts if opts is not None else default_transport_opts()
+        self._check(lib().porsol_transport_init(self.h, C.byref(self.grid.s), *[_p(a) for a in self._keep[:2]],
+                                                C.byref(fluid), *[_p(a) for a in self._keep[2:]], C.byref(o)))
+
+    def solve(self, sat, time, outflux, injection=None, grav=(0.0, 0.0, 0.0)):
+        s = _f64(sat).copy()
+        st = TransportStats()
+        g = _f64(grav)
+        inj = None if injection is None else _f64(injection)
+        self._check(lib().porsol_transport_solve(self.h, _p(s), float(time), _p(g), _p(_f64(outflux)), _p(inj),
+                                                 C.byref(st)))
+        return s, st

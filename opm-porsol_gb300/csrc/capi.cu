@@ -1,0 +1,650 @@
+// capi.cu -- the pressure-solver handle and the extern "C" entry points of porsol_gpu.h.
+//
+// Order of work in porsol_solve (IncompFlowSolverHybrid::solve, IncompFlowSolverHybrid.hpp:658-703):
+//   1. assembleDynamic: k_assemble_cells (per-cell Schur complements and rhs pieces), then
+//      the recipe gathers write the global matrix (SELL) and right-hand side;
+//   2. pure-Neumann regularisation S[0][0] *= 2 (:1398-1400, :1493-1495);
+//   3. linear solve: ILU0-CG (type 0) or AMG-CG (types 1-3), FP64 or FP32-in-FP64-refinement;
+//   4. computePressureAndFluxes: k_recover.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <sstream>
+
+#include "solver.h"
+
+using namespace porsol;
+
+// ---------------------------------------------------------------- profiler
+namespace porsol {
+
+cudaEvent_t Profiler::get()
+{
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    PORSOL_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void Profiler::begin(cudaStream_t s, int, double, cudaEvent_t* out_a)
+{
+    *out_a = get();
+    PORSOL_CUDA(cudaEventRecord(*out_a, s));
+}
+
+void Profiler::end(cudaStream_t s, int k, double b, cudaEvent_t a)
+{
+    cudaEvent_t e = get();
+    PORSOL_CUDA(cudaEventRecord(e, s));
+    pending.push_back({a, e, k, b});
+    if (pending.size() > 4096) collect();
+}
+
+void Profiler::collect()
+{
+    for (auto& p : pending) {
+        PORSOL_CUDA(cudaEventSynchronize(p.b));
+        float ms_ = 0.f;
+        PORSOL_CUDA(cudaEventElapsedTime(&ms_, p.a, p.b));
+        launches[p.k] += 1;
+        ms[p.k] += ms_;
+        bytes[p.k] += p.bytes;
+        pool.push_back(p.a);
+        pool.push_back(p.b);
+    }
+    pending.clear();
+}
+
+void Profiler::reset()
+{
+    collect();
+    for (int k = 0; k < PK_COUNT; ++k) {
+        launches[k] = 0;
+        ms[k] = 0;
+        bytes[k] = 0;
+    }
+}
+
+Profiler::~Profiler()
+{
+    for (auto& p : pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto& e : pool) cudaEventDestroy(e);
+}
+
+}  // namespace porsol
+
+// ---------------------------------------------------------------- solver
+void porsol_solver::require_structure() const
+{
+    PORSOL_REQUIRE(structure_valid, PORSOL_ERR_STATE, "initSystemStructure must be called first");
+}
+
+void porsol_solver::check_status(const char* where)
+{
+    int st = 0;
+    PORSOL_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    if (st) {
+        PORSOL_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
+        std::ostringstream os;
+        os << where << ": ";
+        if (st & ST_NONFINITE) os << "non-finite value or non-positive pivot/mobility";
+        else if (st & ST_BAD_INDEX) os << "index check failed (too many faces per cell?)";
+        else os << "device status " << st;
+        throw Error((st & ST_NONFINITE) ? PORSOL_ERR_NONFINITE : PORSOL_ERR_BAD_ARG, os.str());
+    }
+}
+
+void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
+{
+    structure_valid = ip_valid = solved = false;
+    R.valid = false;
+    amg_ready = false;
+    ilu_levels = false;
+    S = Structure();
+    S.build(grid, flow_type, partner_bid);
+    PORSOL_REQUIRE(S.max_ncf <= 12, PORSOL_ERR_BAD_ARG, "cells with more than 12 faces are not supported");
+    maxnf = S.max_ncf <= 6 ? 6 : 12;
+    npk = maxnf * (maxnf + 1) / 2;
+    const HostGrid& g = S.g;
+    cudaStream_t s = stream;
+    facepos.upload(g.facepos, s);
+    cf.upload(S.cf, s);
+    pairs.upload(S.pairs, s);
+    area.upload(g.area, s);
+    fcent.upload(g.fcent, s);
+    fnormal.upload(g.fnormal, s);
+    cvol.upload(g.cvol, s);
+    ccent.upload(g.ccent, s);
+    S.pat.upload(s);
+    status.alloc(1);
+    status.zero(s);
+    redbits.alloc(4);
+    const size_t nc = g.nc, nhf = g.nhf, N = S.N;
+    W.alloc(npk * nc);
+    W.zero(s);
+    gflux.alloc(nhf);
+    sloc.alloc(npk * nc);
+    F.alloc(nhf);
+    L.alloc(nc);
+    this->g.alloc(nc);
+    rrow.alloc(nhf);
+    pb.alloc(nhf);
+    totmob.alloc(nc);
+    mobdens.alloc(nc);
+    rhs.alloc(N);
+    x.alloc(N);
+    val.alloc(S.pat.nent);
+    pressure.alloc(nc);
+    outflux.alloc(nhf);
+    pressure.zero(s);
+    outflux.zero(s);
+    x.zero(s);
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    structure_valid = true;
+}
+
+void porsol_solver::compute_inner_products(const double* perm_h, const double* grav)
+{
+    require_structure();
+    PORSOL_REQUIRE(perm_h, PORSOL_ERR_BAD_ARG, "permeability array is null");
+    const double g0[3] = {grav ? grav[0] : 0.0, grav ? grav[1] : 0.0, grav ? grav[2] : 0.0};
+    gravity_zero = (g0[0] == 0.0 && g0[1] == 0.0 && g0[2] == 0.0);
+    perm.upload(perm_h, 9 * size_t(S.g.nc), stream);
+    launch_static_ip(maxnf, stream, S.g.nc, facepos.p, area.p, fcent.p, fnormal.p, cvol.p, ccent.p, perm.p, g0, W.p,
+                     gflux.p, status.p);
+    check_status("computeInnerProducts");
+    ip_valid = true;
+}
+
+void porsol_solver::ensure_recipe(const int* bct_host, const int* bct_dev)
+{
+    // Boundary FlowBC types of this solve; the recipe depends on them only.
+    const std::vector<int>& bh = S.boundary_hf;
+    std::vector<int> types(bh.size());
+    if (bct_host) {
+        for (size_t q = 0; q < bh.size(); ++q) types[q] = bct_host[bh[q]];
+    } else {
+        // gather the boundary entries of the device array (boundary faces only)
+        std::vector<int> all(S.g.nhf);
+        PORSOL_CUDA(cudaMemcpyAsync(all.data(), bct_dev, sizeof(int) * all.size(), cudaMemcpyDeviceToHost, stream));
+        PORSOL_CUDA(cudaStreamSynchronize(stream));
+        for (size_t q = 0; q < bh.size(); ++q) types[q] = all[bh[q]];
+    }
+    if (R.valid && types == recipe_types) return;
+    std::vector<int> full(S.g.nhf, -1);
+    for (size_t q = 0; q < bh.size(); ++q) full[bh[q]] = types[q];
+    R.build(S, full.data(), npk);
+    R.kind_d.upload(R.kind, stream);
+    R.slot_ptr.upload(R.h_slot_ptr, stream);
+    R.slot_ent.upload(R.h_slot_ent, stream);
+    R.rhs_ptr.upload(R.h_rhs_ptr, stream);
+    R.rhs_ent.upload(R.h_rhs_ent, stream);
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    recipe_types = types;
+    amg_ready = false;   // a different matrix structure of values
+}
+
+void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st)
+{
+    const int n = S.N;
+    const int maxit = o.linsolver_maxit > 0 ? o.linsolver_maxit : n;
+    const SellPattern& P = S.pat;
+    st.amg_levels = 0;
+    st.outer_iterations = 1;
+    auto fail = [&](int iters, double red) {
+        std::ostringstream os;
+        os << "Linear solver failed to converge in " << iters << " iterations.\n"
+           << "Residual reduction achieved is " << red << '\n';
+        throw Error(PORSOL_ERR_NOT_CONVERGED, os.str());
+    };
+    if (o.linsolver_type == 0) {
+        // solveLinearSystem (:1387-1420): ILU0(S, 1.0), CG, zero initial guess
+        if (!ilu_levels) {
+            ilu.build_levels(P, stream);
+            ilu_levels = true;
+        }
+        ilu.factor(stream, P, val.p);
+        x.zero(stream);
+        CgResult r = cg64.solve(stream, P, val.p, ilu, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
+        st.iterations = r.iterations;
+        st.reduction = r.reduction;
+        if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+        if (!r.converged) fail(r.iterations, r.reduction);
+        return;
+    }
+    // solveLinearSystemAMG (:1481-1541): hierarchy rebuilt unless same_matrix, initial
+    // guess with Dirichlet rows pre-solved, CG.
+    AmgOpts ao;
+    ao.smooth_steps = std::max(1, o.smooth_steps);
+    ao.prolong = o.prolongate_factor;
+    dirichlet_guess(stream, P, val.p, rhs.p, x.p);
+    if (o.precision == PORSOL_FP64) {
+        if (!(o.same_matrix && amg_ready && amg_precision == PORSOL_FP64)) {
+            amg64.setup(stream, P, val.p, ao);
+            amg_ready = true;
+            amg_precision = PORSOL_FP64;
+        }
+        st.amg_levels = amg64.levels();
+        CgResult r = cg64.solve(stream, P, val.p, amg64, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
+        st.iterations = r.iterations;
+        st.reduction = r.reduction;
+        if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+        if (!r.converged) fail(r.iterations, r.reduction);
+        return;
+    }
+    // Mixed precision: FP32 matrix copy, FP32 AMG hierarchy, FP32 CG on the correction
+    // equation; FP64 outer residual r = b - A x and FP64 update x += d.
+    if (!(o.same_matrix && amg_ready && amg_precision == PORSOL_MIXED)) {
+        amg32.setup(stream, P, val32.p, ao);
+        amg_ready = true;
+        amg_precision = PORSOL_MIXED;
+    }
+    st.amg_levels = amg32.levels();
+    ir_r.alloc(n);
+    ir_r32.alloc(n);
+    ir_d32.alloc(n);
+    ir_d.alloc(n);
+    residual<double, double>(stream, P, val.p, x.p, rhs.p, ir_r.p);
+    const double r0 = norm2<double>(stream, n, ir_r.p, red);
+    double rn = r0;
+    int total = 0, outer = 0;
+    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3;
+    const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
+    while (rn >= o.residual_tolerance * r0 && rn >= 1e-30) {
+        if (outer >= max_outer || total >= maxit) fail(total, r0 > 0 ? rn / r0 : 0.0);
+        // The correction equation A d = r is solved for d / ||r|| so the FP32 vectors stay
+        // O(1) however small the FP64 residual becomes.
+        to_f32_scaled(stream, n, ir_r.p, ir_r32.p, 1.0 / rn);
+        PORSOL_CUDA(cudaMemsetAsync(ir_d32.p, 0, n * sizeof(float), stream));
+        CgResult r = cg32.solve(stream, P, val32.p, amg32, ir_r32.p, ir_d32.p, inner_tol, maxit - total, &prof,
+                                PK_SPMV32);
+        total += r.iterations;
+        ++outer;
+        if (r.breakdown && r.iterations == 0) throw Error(PORSOL_ERR_NONFINITE, "inner CG breakdown");
+        add_f32_scaled(stream, n, ir_d32.p, rn, x.p);
+        residual<double, double>(stream, P, val.p, x.p, rhs.p, ir_r.p);
+        rn = norm2<double>(stream, n, ir_r.p, red);
+        if (!std::isfinite(rn)) throw Error(PORSOL_ERR_NONFINITE, "iterative refinement diverged");
+    }
+    st.iterations = total;
+    st.outer_iterations = outer;
+    st.reduction = r0 > 0 ? rn / r0 : 0.0;
+}
+
+void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const double* mobd, const int* bct,
+                          const double* bcv, const double* src, const porsol_solve_opts* opts_in,
+                          porsol_solve_stats* stats, bool dev)
+{
+    require_structure();
+    PORSOL_REQUIRE(ip_valid, PORSOL_ERR_STATE, "computeInnerProducts must be called before solve");
+    PORSOL_REQUIRE(fluid && sat && bct && bcv && src, PORSOL_ERR_BAD_ARG, "solve: null argument");
+    porsol_solve_opts o;
+    porsol_solve_opts_default(&o);
+    if (opts_in) o = *opts_in;
+    if (o.linsolver_type < 0 || o.linsolver_type > 3) {
+        throw Error(PORSOL_ERR_UNKNOWN_SOLVER, "Unknown linsolver_type");
+    }
+    PORSOL_REQUIRE(o.precision == PORSOL_FP64 || o.precision == PORSOL_MIXED, PORSOL_ERR_BAD_ARG,
+                   "unknown precision mode");
+    PORSOL_REQUIRE(fluid->model == PORSOL_FLUID_CELLWISE || fluid->model == PORSOL_FLUID_COREY2, PORSOL_ERR_BAD_ARG,
+                   "unknown fluid model");
+    if (o.precision == PORSOL_MIXED && o.linsolver_type == 0)
+        o.precision = PORSOL_FP64;   // ILU0 path is FP64 only
+    const int nc = S.g.nc, nhf = S.g.nhf;
+    cudaStream_t s = stream;
+    ensure_recipe(dev ? nullptr : bct, dev ? bct : nullptr);
+    const double *d_sat, *d_md = nullptr, *d_bcv, *d_src;
+    if (dev) {
+        d_sat = sat;
+        d_md = mobd;
+        d_bcv = bcv;
+        d_src = src;
+    } else {
+        in_sat.upload(sat, nc, s);
+        d_sat = in_sat.p;
+        if (mobd) {
+            in_mobdens.upload(mobd, nc, s);
+            d_md = in_mobdens.p;
+        }
+        in_bcval.upload(bcv, nhf, s);
+        d_bcv = in_bcval.p;
+        in_src.upload(src, nc, s);
+        d_src = in_src.p;
+    }
+    last_src = d_src;
+    const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
+    if (mixed) val32.alloc(S.pat.nent);
+    {
+        ProfScope ps(prof, s, PK_ASSEMBLE, double(nc) * (npk * 16.0 + 64) + double(S.pat.nent) * 16.0);
+        AssembleArgs a;
+        a.nc = nc;
+        a.facepos = facepos.p;
+        a.W = W.p;
+        a.gflux = gflux.p;
+        a.gravity_zero = gravity_zero;
+        a.fluid = FluidParams{fluid->model, fluid->viscosity1, fluid->viscosity2, fluid->density1, fluid->density2};
+        a.sat = d_sat;
+        a.mobdens = d_md;
+        a.kind = R.kind_d.p;
+        a.bcval = d_bcv;
+        a.src = d_src;
+        a.sloc = sloc.p;
+        a.F = F.p;
+        a.L = L.p;
+        a.g = this->g.p;
+        a.rrow = rrow.p;
+        a.pb = pb.p;
+        a.totmob = totmob.p;
+        a.mobdens_out = mobdens.p;
+        a.status = status.p;
+        launch_assemble_cells(maxnf, s, a);
+        launch_gather_slots(s, S.pat.nent, R.slot_ptr.p, R.slot_ent.p, sloc.p, val.p, mixed ? val32.p : nullptr);
+        launch_gather_rhs(s, S.N, R.rhs_ptr.p, R.rhs_ent.p, rrow.p, pb.p, rhs.p);
+    }
+    check_status("assembleDynamic");
+    // Regularisation of pure Neumann/periodic problems: the ILU0 path always applies it
+    // (:1398-1400); the AMG paths only when the hierarchy is rebuilt (:1491-1495).
+    reg_applied = false;
+    if (R.do_reg && (o.linsolver_type == 0 || !o.same_matrix)) {
+        launch_scale_entry(s, val.p, S.pat.diag.p, 0, 2.0, mixed ? val32.p : nullptr);
+        reg_applied = true;
+    }
+    porsol_solve_stats st{};
+    linear_solve(o, st);
+    {
+        ProfScope ps(prof, s, PK_RECOVER, double(nc) * (npk * 8.0 + 6 * 8 * 4 + 32) + double(S.N) * 8.0);
+        RecoverArgs ra;
+        ra.nc = nc;
+        ra.facepos = facepos.p;
+        ra.cf = cf.p;
+        ra.x = x.p;
+        ra.W = W.p;
+        ra.gflux = gflux.p;
+        ra.gravity_zero = gravity_zero;
+        ra.F = F.p;
+        ra.L = L.p;
+        ra.g = this->g.p;
+        ra.totmob = totmob.p;
+        ra.mobdens = mobdens.p;
+        ra.pressure = pressure.p;
+        ra.outflux = outflux.p;
+        launch_recover(maxnf, s, ra);
+    }
+    // FP64 mass-balance check
+    PORSOL_CUDA(cudaMemsetAsync(redbits.p, 0, 3 * sizeof(unsigned long long), s));
+    launch_mass_balance(s, nc, facepos.p, outflux.p, d_src, redbits.p);
+    unsigned long long mb[3];
+    PORSOL_CUDA(cudaMemcpyAsync(mb, redbits.p, sizeof(mb), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    double v[3];
+    std::memcpy(v, mb, sizeof(v));
+    st.mass_balance = v[0] / std::max(std::max(v[1], v[2]), 1e-300);
+    solved = true;
+    if (stats) *stats = st;
+}
+
+double porsol_solver::post_process()
+{
+    PORSOL_REQUIRE(solved, PORSOL_ERR_STATE, "postProcessFluxes before solve");
+    PORSOL_CUDA(cudaMemsetAsync(redbits.p + 3, 0, sizeof(unsigned long long), stream));
+    launch_post_process(stream, int(S.pairs.size() / 2), pairs.p, outflux.p, redbits.p + 3);
+    unsigned long long b = 0;
+    PORSOL_CUDA(cudaMemcpyAsync(&b, redbits.p + 3, sizeof(b), cudaMemcpyDeviceToHost, stream));
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+// ---------------------------------------------------------------- C ABI
+namespace {
+
+template <class F>
+int guarded(porsol_solver* h, F&& f)
+{
+    if (!h) return PORSOL_ERR_BAD_ARG;
+    try {
+        PORSOL_CUDA(cudaSetDevice(h->device));
+        f();
+        h->err.clear();
+        return PORSOL_OK;
+    } catch (const Error& e) {
+        h->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return PORSOL_ERR_BAD_ARG;
+    } catch (...) {
+        h->err = "unknown error";
+        return PORSOL_ERR_BAD_ARG;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void porsol_solve_opts_default(porsol_solve_opts* o)
+{
+    if (!o) return;
+    o->residual_tolerance = 1e-8;
+    o->linsolver_verbosity = 1;
+    o->linsolver_type = 1;
+    o->same_matrix = 0;
+    o->linsolver_maxit = 0;
+    o->prolongate_factor = 1.6;
+    o->smooth_steps = 1;
+    o->precision = PORSOL_FP64;
+    o->inner_tolerance = 1e-3;
+    o->max_outer = 30;
+}
+
+int porsol_create(porsol_solver** out)
+{
+    if (!out) return PORSOL_ERR_BAD_ARG;
+    *out = nullptr;
+    auto* h = new (std::nothrow) porsol_solver();
+    if (!h) return PORSOL_ERR_BAD_ARG;
+    if (cudaGetDevice(&h->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return PORSOL_ERR_CUDA;
+    }
+    *out = h;
+    return PORSOL_OK;
+}
+
+void porsol_destroy(porsol_solver* h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    cudaStream_t s = h->stream;
+    delete h;
+    cudaStreamDestroy(s);
+}
+
+const char* porsol_last_error(const porsol_solver* h) { return h ? h->err.c_str() : "null handle"; }
+
+int porsol_clear(porsol_solver* h)
+{
+    return guarded(h, [&] {
+        h->structure_valid = h->ip_valid = h->solved = false;
+        h->R.valid = false;
+        h->amg_ready = false;
+    });
+}
+
+int porsol_init_system_structure(porsol_solver* h, const porsol_grid* grid, const int* flow_type,
+                                 const int* partner_bid)
+{
+    return guarded(h, [&] { h->init_structure(grid, flow_type, partner_bid); });
+}
+
+int porsol_compute_inner_products(porsol_solver* h, const double* perm, const double* grav)
+{
+    return guarded(h, [&] { h->compute_inner_products(perm, grav); });
+}
+
+int porsol_assemble_static(porsol_solver* h, const double* perm, const double* grav)
+{
+    return porsol_compute_inner_products(h, perm, grav);
+}
+
+int porsol_init(porsol_solver* h, const porsol_grid* grid, const double* perm, const double* grav,
+                const int* flow_type, const int* partner_bid)
+{
+    return guarded(h, [&] {
+        if (grid && grid->num_cells == 0) {
+            h->structure_valid = h->ip_valid = false;
+            return;
+        }
+        h->init_structure(grid, flow_type, partner_bid);
+        h->compute_inner_products(perm, grav);
+    });
+}
+
+int porsol_solve(porsol_solver* h, const porsol_fluid* fluid, const double* sat, const double* mobdens,
+                 const int* bct, const double* bcv, const double* src, const porsol_solve_opts* opts,
+                 porsol_solve_stats* stats)
+{
+    return guarded(h, [&] { h->solve(fluid, sat, mobdens, bct, bcv, src, opts, stats, false); });
+}
+
+int porsol_solve_device(porsol_solver* h, const porsol_fluid* fluid, const double* sat, const double* mobdens,
+                        const int* bct, const double* bcv, const double* src, const porsol_solve_opts* opts,
+                        porsol_solve_stats* stats)
+{
+    return guarded(h, [&] { h->solve(fluid, sat, mobdens, bct, bcv, src, opts, stats, true); });
+}
+
+int porsol_post_process_fluxes(porsol_solver* h, double* max_modification)
+{
+    return guarded(h, [&] {
+        const double m = h->post_process();
+        if (max_modification) *max_modification = m;
+    });
+}
+
+int porsol_get_solution(porsol_solver* h, double* p, double* v, double* pi)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "getSolution before solve");
+        if (p) h->pressure.download(p, h->S.g.nc, h->stream);
+        if (v) h->outflux.download(v, h->S.g.nhf, h->stream);
+        if (pi) h->x.download(pi, h->S.N, h->stream);
+        PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int porsol_get_solution_device(porsol_solver* h, const double** p, const double** v, const double** pi)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "getSolution before solve");
+        PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+        if (p) *p = h->pressure.p;
+        if (v) *v = h->outflux.p;
+        if (pi) *pi = h->x.p;
+    });
+}
+
+int porsol_num_dofs(porsol_solver* h, int* num_dofs, int* nnz, int* max_ncf, int* num_internal)
+{
+    return guarded(h, [&] {
+        h->require_structure();
+        if (num_dofs) *num_dofs = h->S.N;
+        if (nnz) *nnz = int(h->S.colind.size());
+        if (max_ncf) *max_ncf = h->S.max_ncf;
+        if (num_internal) *num_internal = h->S.num_internal;
+    });
+}
+
+int porsol_get_structure(porsol_solver* h, int* cellfaces, int* rowptr, int* colind, int* ppartner)
+{
+    return guarded(h, [&] {
+        h->require_structure();
+        const Structure& S = h->S;
+        if (cellfaces) std::copy(S.cf.begin(), S.cf.end(), cellfaces);
+        if (rowptr) std::copy(S.rowptr.begin(), S.rowptr.end(), rowptr);
+        if (colind) std::copy(S.colind.begin(), S.colind.end(), colind);
+        if (ppartner) {
+            if (S.ppartner.empty()) std::fill(ppartner, ppartner + S.N, -1);
+            else std::copy(S.ppartner.begin(), S.ppartner.end(), ppartner);
+        }
+    });
+}
+
+int porsol_get_inner_products(porsol_solver* h, double* binv, double* gflux)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->ip_valid, PORSOL_ERR_STATE, "computeInnerProducts first");
+        const int nc = h->S.g.nc;
+        if (binv) {
+            std::vector<double> W(size_t(h->npk) * nc);
+            h->W.download(W.data(), W.size(), h->stream);
+            PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+            size_t o = 0;
+            for (int c = 0; c < nc; ++c) {
+                const int nf = h->S.g.nf(c);
+                for (int j = 0; j < nf; ++j)
+                    for (int i = 0; i < nf; ++i) binv[o++] = W[size_t(packed_index(i, j)) * nc + c];
+            }
+        }
+        if (gflux) h->gflux.download(gflux, h->S.g.nhf, h->stream);
+        PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int porsol_get_system(porsol_solver* h, double* values, double* rhs)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "get_system before solve");
+        const Structure& S = h->S;
+        if (values) {
+            std::vector<double> v(S.pat.nent);
+            h->val.download(v.data(), v.size(), h->stream);
+            PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+            for (size_t k = 0; k < S.csr2sell.size(); ++k) values[k] = v[S.csr2sell[k]];
+            if (h->reg_applied && S.N > 0) {
+                // report the assembled value before the pure-Neumann regularisation
+                const long long k0 = S.slot(0, 0);
+                for (size_t k = 0; k < S.csr2sell.size(); ++k)
+                    if (S.csr2sell[k] == k0) values[k] = v[k0] / 2.0;
+            }
+        }
+        if (rhs) h->rhs.download(rhs, S.N, h->stream);
+        PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int porsol_profile_enable(porsol_solver* h, int enable)
+{
+    return guarded(h, [&] { h->prof.on = enable != 0; });
+}
+
+int porsol_profile_get(porsol_solver* h, int kernel, int* launches, double* ms, double* bytes)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(kernel >= 0 && kernel < PK_COUNT, PORSOL_ERR_BAD_ARG, "unknown profiled kernel");
+        h->prof.collect();
+        if (launches) *launches = h->prof.launches[kernel];
+        if (ms) *ms = h->prof.ms[kernel];
+        if (bytes) *bytes = h->prof.bytes[kernel];
+    });
+}
+
+int porsol_profile_reset(porsol_solver* h)
+{
+    return guarded(h, [&] { h->prof.reset(); });
+}
+
+void* porsol_stream(porsol_solver* h) { return h ? (void*)h->stream : nullptr; }
+
+}  // extern "C"

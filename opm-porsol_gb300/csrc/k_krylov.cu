@@ -1,0 +1,625 @@
+// k_krylov.cu -- SELL-32 SpMV, fused CG updates with deterministic last-block
+// reductions, and level-scheduled ILU(0).
+//
+// Reductions: every block writes one FP64 partial sum; the last block to arrive (arrival
+// counter + threadfence) adds the partials in block order and updates the CG scalars in
+// device memory.  The summation order is fixed, so results are run-to-run reproducible.
+#include <algorithm>
+#include <cmath>
+
+#include "krylov.h"
+
+namespace porsol {
+
+namespace {
+
+constexpr int RB = 256;  // threads per block of the vector kernels
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block reduce + last-block finalisation.  Returns true in thread 0 of the last block,
+// with *total holding the full sum.
+__device__ bool block_reduce_last(double v, double* partial, unsigned int* counter, double* total)
+{
+    __shared__ double ws[RB / 32];
+    __shared__ bool amlast;
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) {
+            partial[blockIdx.x] = t;
+            __threadfence();
+            const unsigned int prev = atomicAdd(counter, 1u);
+            amlast = (prev == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!amlast) return false;
+    // last block: sum partials in block order
+    __threadfence();
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partial)[b];
+    // fixed-order tree over threads
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        *total = t;
+        *counter = 0u;
+    }
+    return threadIdx.x == 0;
+}
+
+template <class TV, class TX>
+__device__ __forceinline__ double sell_row(const int* __restrict__ sp, const int* __restrict__ col,
+                                           const TV* __restrict__ val, const TX* __restrict__ x, int r)
+{
+    const int s = r >> 5, lane = r & 31;
+    const int b = sp[s], w = (sp[s + 1] - b) >> 5;
+    double acc = 0.0;
+    int k = b + lane;
+    for (int t = 0; t < w; ++t, k += 32) acc += double(val[k]) * double(x[col[k]]);
+    return acc;
+}
+
+template <class TV, class TX>
+__global__ void k_spmv(int n, const int* __restrict__ sp, const int* __restrict__ col, const TV* __restrict__ val,
+                       const TX* __restrict__ x, TX* __restrict__ y)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    y[r] = TX(sell_row(sp, col, val, x, r));
+}
+
+template <class TV, class TX>
+__global__ void k_residual(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                           const TV* __restrict__ val, const TX* __restrict__ x, const TX* __restrict__ b,
+                           TX* __restrict__ y)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    y[r] = TX(double(b[r]) - sell_row(sp, col, val, x, r));
+}
+
+// r = b - A x; def0 = ||r||
+template <class TV, class T>
+__global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                                const TV* __restrict__ val, const T* __restrict__ x,
+                                                const T* __restrict__ b, T* __restrict__ r, CgDev* st,
+                                                double* partial, unsigned int* counter, CgHostView* hv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        const double ri = double(b[i]) - sell_row(sp, col, val, x, i);
+        r[i] = T(ri);
+        const double rr = double(T(ri));
+        v = rr * rr;
+    }
+    double tot;
+    if (block_reduce_last(v, partial, counter, &tot)) {
+        const double d0 = sqrt(tot);
+        st->def0 = d0;
+        st->def = d0;
+        st->iter = 0;
+        st->breakdown = 0;
+        st->converged = (d0 < 1e-30) ? 1 : 0;
+        st->stop = st->converged;
+        hv->def0 = d0;
+        hv->def = d0;
+        hv->iter = 0;
+        hv->converged = st->converged;
+        hv->stop = st->stop;
+        hv->breakdown = 0;
+        __threadfence_system();
+    }
+}
+
+// rho = z . r ; which = 0: first direction p = z, rholast = rho; which = 1: rho for beta
+template <class T>
+__global__ void __launch_bounds__(RB) k_dot_zr(int n, const T* __restrict__ z, const T* __restrict__ r, CgDev* st,
+                                               double* partial, unsigned int* counter)
+{
+    if (st->stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) v = double(z[i]) * double(r[i]);
+    double tot;
+    if (block_reduce_last(v, partial, counter, &tot)) st->rho = tot;
+}
+
+template <class T>
+__global__ void k_first_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st)
+{
+    if (st->stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = z[i];
+    if (i == 0) st->rholast = st->rho;   // other threads do not read rholast here
+}
+
+// q = A p ; alpha = p . q
+template <class TV, class T>
+__global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                                const TV* __restrict__ val, const T* __restrict__ p,
+                                                T* __restrict__ q, CgDev* st, double* partial,
+                                                unsigned int* counter)
+{
+    if (st->stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        const T qi = T(sell_row(sp, col, val, p, i));
+        q[i] = qi;
+        v = double(p[i]) * double(qi);
+    }
+    double tot;
+    if (block_reduce_last(v, partial, counter, &tot)) st->alpha = tot;
+}
+
+// lambda = rholast/alpha; x += lambda p; r -= lambda q; def = ||r||; convergence test
+template <class T>
+__global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* __restrict__ r,
+                                                  const T* __restrict__ p, const T* __restrict__ q, CgDev* st,
+                                                  double* partial, unsigned int* counter, CgHostView* hv)
+{
+    if (st->stop) return;
+    const double alpha = st->alpha;
+    const double lambda = st->rholast / alpha;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        x[i] = T(double(x[i]) + lambda * double(p[i]));
+        const T ri = T(double(r[i]) - lambda * double(q[i]));
+        r[i] = ri;
+        v = double(ri) * double(ri);
+    }
+    double tot;
+    if (block_reduce_last(v, partial, counter, &tot)) {
+        const double def = sqrt(tot);
+        st->def = def;
+        st->iter += 1;
+        if (!(alpha > 0.0) || !isfinite(def)) st->breakdown = 1;
+        if (def < st->def0 * st->tol || def < 1e-30) st->converged = 1;
+        st->stop = st->converged || st->breakdown || st->iter >= st->maxit;
+        hv->def = def;
+        hv->iter = st->iter;
+        hv->converged = st->converged;
+        hv->breakdown = st->breakdown;
+        hv->stop = st->stop;
+        __threadfence_system();
+    }
+}
+
+// beta = rho/rholast; p = z + beta p
+template <class T>
+__global__ void k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st, int* flip)
+{
+    if (st->stop) return;
+    const double beta = st->rho / st->rholast;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = T(double(z[i]) + beta * double(p[i]));
+    (void)flip;
+}
+
+__global__ void k_cg_roll(CgDev* st)
+{
+    if (st->stop) return;
+    st->rholast = st->rho;
+}
+
+template <class TA, class TB>
+__global__ void k_convert(long long n, const TA* __restrict__ a, TB* __restrict__ b)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = TB(a[i]);
+}
+
+__global__ void k_axpy_add(int n, const double* __restrict__ y, double* __restrict__ x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += y[i];
+}
+
+__global__ void k_to_f32_scaled(int n, const double* __restrict__ a, float* __restrict__ b, double scale)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = float(a[i] * scale);
+}
+
+__global__ void k_add_f32_scaled(int n, const float* __restrict__ y, double scale, double* __restrict__ x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += scale * double(y[i]);
+}
+
+__global__ void k_dirichlet_guess(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                  const int* __restrict__ rowlen, const double* __restrict__ val,
+                                  const double* __restrict__ b, double* __restrict__ x)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int s = r >> 5, lane = r & 31;
+    const int base = sp[s];
+    bool isD = true;
+    double d = 0.0;
+    for (int t = 0; t < rowlen[r]; ++t) {
+        const int k = base + t * 32 + lane;
+        if (col[k] == r) d = val[k];
+        else if (val[k] != 0.0) isD = false;
+    }
+    x[r] = isD ? b[r] / d : 0.0;
+}
+
+template <class T>
+__global__ void __launch_bounds__(RB) k_norm2(int n, const T* __restrict__ x, double* partial, unsigned int* counter,
+                                              double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double v = i < n ? double(x[i]) * double(x[i]) : 0.0;
+    double tot;
+    if (block_reduce_last(v, partial, counter, &tot)) *out = tot;
+}
+
+// ---------------- ILU(0) ----------------
+__device__ __forceinline__ int sell_slot(const int* sp, int r, int t) { return sp[r >> 5] + t * 32 + (r & 31); }
+
+__global__ void k_ilu_factor_level(int nrows, const int* __restrict__ rows, const int* __restrict__ sp,
+                                   const int* __restrict__ col, const int* __restrict__ rowlen,
+                                   const int* __restrict__ diag, double* __restrict__ lu, int* status)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows) return;
+    const int i = rows[q];
+    const int li = rowlen[i];
+    for (int t = 0; t < li; ++t) {
+        const int ij = sell_slot(sp, i, t);
+        const int j = col[ij];
+        if (j >= i) break;
+        const int jj = diag[j];
+        lu[ij] *= lu[jj];                     // L_ij = a_ij * inv(a_jj)
+        const double lij = lu[ij];
+        // a_ik -= L_ij a_jk for k > j present in both rows
+        const int lj = rowlen[j];
+        int tj = 0;
+        while (tj < lj && col[sell_slot(sp, j, tj)] <= j) ++tj;
+        int ti = t + 1;
+        while (ti < li && tj < lj) {
+            const int ik = sell_slot(sp, i, ti), jk = sell_slot(sp, j, tj);
+            const int ci = col[ik], cj = col[jk];
+            if (ci == cj) {
+                lu[ik] -= lij * lu[jk];
+                ++ti;
+                ++tj;
+            } else if (ci < cj) {
+                ++ti;
+            } else {
+                ++tj;
+            }
+        }
+    }
+    const int d = diag[i];
+    const double piv = lu[d];
+    if (!(fabs(piv) > 0.0) || !isfinite(piv)) atomicOr(status, ST_NONFINITE);
+    lu[d] = 1.0 / piv;
+}
+
+__global__ void k_ilu_lower_level(int nrows, const int* __restrict__ rows, const int* __restrict__ sp,
+                                  const int* __restrict__ col, const int* __restrict__ diag,
+                                  const double* __restrict__ lu, const double* __restrict__ r, double* __restrict__ z,
+                                  const int* stop)
+{
+    if (*stop) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows) return;
+    const int i = rows[q];
+    double v = r[i];
+    const int d = diag[i];
+    for (int k = sp[i >> 5] + (i & 31); k < d; k += 32) v -= lu[k] * z[col[k]];
+    z[i] = v;
+}
+
+__global__ void k_ilu_upper_level(int nrows, const int* __restrict__ rows, const int* __restrict__ sp,
+                                  const int* __restrict__ col, const int* __restrict__ rowlen,
+                                  const int* __restrict__ diag, const double* __restrict__ lu, double* __restrict__ z,
+                                  const int* stop)
+{
+    if (*stop) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows) return;
+    const int i = rows[q];
+    const int d = diag[i];
+    const int end = sp[i >> 5] + rowlen[i] * 32 + (i & 31);
+    double v = z[i];
+    for (int k = d + 32; k < end; k += 32) v -= lu[k] * z[col[k]];
+    z[i] = lu[d] * v;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------
+void RedScratch::ensure(int blocks, cudaStream_t s)
+{
+    if (blocks <= max_blocks) return;
+    partial.alloc(blocks);
+    counter.alloc(1);
+    counter.zero(s);
+    max_blocks = blocks;
+}
+
+template <class TV, class TX>
+void spmv(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, TX* y)
+{
+    if (P.n == 0) return;
+    k_spmv<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, y);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+template <class TV, class TX>
+void residual(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, const TX* b, TX* y)
+{
+    if (P.n == 0) return;
+    k_residual<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, b, y);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+template void spmv<double, double>(cudaStream_t, const SellPattern&, const double*, const double*, double*);
+template void spmv<float, float>(cudaStream_t, const SellPattern&, const float*, const float*, float*);
+template void residual<double, double>(cudaStream_t, const SellPattern&, const double*, const double*,
+                                       const double*, double*);
+template void residual<float, float>(cudaStream_t, const SellPattern&, const float*, const float*, const float*,
+                                     float*);
+
+template <class TV, class T>
+void PcgSolver<TV, T>::setup(int n, cudaStream_t s)
+{
+    if (n == n_ && hview_) return;
+    n_ = n;
+    r_.alloc(n);
+    z_.alloc(n);
+    p_.alloc(n);
+    q_.alloc(n);
+    st_.alloc(1);
+    red_.ensure(div_up(std::max(n, 1), RB), s);
+    if (!hview_) {
+        PORSOL_CUDA(cudaHostAlloc((void**)&hview_, sizeof(CgHostView), cudaHostAllocMapped));
+        PORSOL_CUDA(cudaHostGetDevicePointer((void**)&dview_, hview_, 0));
+    }
+    if (ev_.empty()) {
+        ev_.resize(4);
+        for (auto& e : ev_) PORSOL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+}
+
+template <class TV, class T>
+PcgSolver<TV, T>::~PcgSolver()
+{
+    if (hview_) cudaFreeHost(hview_);
+    for (auto& e : ev_) cudaEventDestroy(e);
+}
+
+template <class TV, class T>
+CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV* val, Precond<T>& M, const T* b,
+                                 T* x, double tol, int maxit, Profiler* prof, int prof_kernel)
+{
+    const int n = P.n;
+    CgResult res;
+    if (n == 0) {
+        res.converged = true;
+        return res;
+    }
+    setup(n, s);
+    const int nb = div_up(n, RB);
+    CgDev init{};
+    init.tol = tol;
+    init.maxit = maxit;
+    PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
+    k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p, red_.partial.p,
+                                       red_.counter.p, dview_);
+    PORSOL_CUDA(cudaGetLastError());
+    const int* stop = &st_.p->stop;
+    M.apply(s, r_.p, z_.p, stop);
+    k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
+    k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p);
+    PORSOL_CUDA(cudaGetLastError());
+    // Iterations are queued ahead; the host waits on the event of iteration i - LOOKAHEAD
+    // and reads the mapped stop flag.  Iterations queued after convergence are no-ops.
+    const int LOOKAHEAD = 2;
+    const double spmv_bytes = double(P.nent) * (sizeof(TV) + 4) + 2.0 * n * sizeof(T);
+    int it = 0;
+    bool done = false;
+    while (!done) {
+        if (it < maxit) {
+            if (prof && prof_kernel >= 0) {
+                ProfScope ps(*prof, s, prof_kernel, spmv_bytes);
+                k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                   red_.partial.p, red_.counter.p);
+            } else {
+                k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                   red_.partial.p, red_.counter.p);
+            }
+            k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
+                                             dview_);
+            PORSOL_CUDA(cudaGetLastError());
+            M.apply(s, r_.p, z_.p, stop);
+            k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
+            k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr);
+            k_cg_roll<<<1, 1, 0, s>>>(st_.p);
+            PORSOL_CUDA(cudaGetLastError());
+            PORSOL_CUDA(cudaEventRecord(ev_[it % ev_.size()], s));
+            ++it;
+        }
+        if (it >= LOOKAHEAD || it >= maxit) {
+            const int wait_it = (it >= maxit) ? it - 1 : it - LOOKAHEAD;
+            PORSOL_CUDA(cudaEventSynchronize(ev_[wait_it % ev_.size()]));
+            if (hview_->stop || it >= maxit) {
+                if (it >= maxit) PORSOL_CUDA(cudaStreamSynchronize(s));
+                done = hview_->stop || it >= maxit;
+            }
+        }
+    }
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    res.iterations = hview_->iter;
+    res.def0 = hview_->def0;
+    res.def = hview_->def;
+    res.converged = hview_->converged != 0;
+    res.breakdown = hview_->breakdown != 0;
+    res.reduction = res.def0 > 0 ? res.def / res.def0 : 0.0;
+    return res;
+}
+
+template class PcgSolver<double, double>;
+template class PcgSolver<float, float>;
+
+// ---------------- ILU(0) host side ----------------
+void Ilu0::build_levels(const SellPattern& P, cudaStream_t s)
+{
+    P_ = &P;
+    const int n = P.n;
+    auto slot = [&](int r, int t) { return (long long)P.h_slice_ptr[r / SELL_C] + (long long)t * SELL_C + r % SELL_C; };
+    std::vector<int> lev(n, 0);
+    int nl = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int t = 0; t < P.h_rowlen[i]; ++t) {
+            const int j = P.h_col[slot(i, t)];
+            if (j < i) l = std::max(l, lev[j] + 1);
+        }
+        lev[i] = l;
+        nl = std::max(nl, l + 1);
+    }
+    auto bucket = [&](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows, bool rev) {
+        ptr.assign(nlev + 1, 0);
+        for (int i = 0; i < n; ++i) ptr[lv[i] + 1]++;
+        for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+        rows.assign(n, 0);
+        std::vector<int> f(ptr.begin(), ptr.end() - 1);
+        if (!rev)
+            for (int i = 0; i < n; ++i) rows[f[lv[i]]++] = i;
+        else
+            for (int i = n - 1; i >= 0; --i) rows[f[lv[i]]++] = i;
+    };
+    std::vector<int> lrows, urows;
+    bucket(lev, nl, h_lptr_, lrows, false);
+    std::vector<int> ulev(n, 0);
+    int nu = 0;
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int t = 0; t < P.h_rowlen[i]; ++t) {
+            const int j = P.h_col[slot(i, t)];
+            if (j > i) l = std::max(l, ulev[j] + 1);
+        }
+        ulev[i] = l;
+        nu = std::max(nu, l + 1);
+    }
+    bucket(ulev, nu, h_uptr_, urows, true);
+    lrows_.upload(lrows, s);
+    urows_.upload(urows, s);
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+}
+
+void Ilu0::factor(cudaStream_t s, const SellPattern& P, const double* val)
+{
+    lu_.alloc(P.nent);
+    PORSOL_CUDA(cudaMemcpyAsync(lu_.p, val, P.nent * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    status_.alloc(1);
+    status_.zero(s);
+    DBuf<int>& status = status_;
+    for (size_t l = 0; l + 1 < h_lptr_.size(); ++l) {
+        const int cnt = h_lptr_[l + 1] - h_lptr_[l];
+        k_ilu_factor_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
+                                                            P.rowlen.p, P.diag.p, lu_.p, status.p);
+    }
+    PORSOL_CUDA(cudaGetLastError());
+    int st = 0;
+    PORSOL_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "ILU0: zero or non-finite pivot");
+}
+
+void Ilu0::apply(cudaStream_t s, const double* r, double* z, const int* stop)
+{
+    const SellPattern& P = *P_;
+    for (size_t l = 0; l + 1 < h_lptr_.size(); ++l) {
+        const int cnt = h_lptr_[l + 1] - h_lptr_[l];
+        k_ilu_lower_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
+                                                           P.diag.p, lu_.p, r, z, stop);
+    }
+    for (size_t l = 0; l + 1 < h_uptr_.size(); ++l) {
+        const int cnt = h_uptr_[l + 1] - h_uptr_[l];
+        k_ilu_upper_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, urows_.p + h_uptr_[l], P.slice_ptr.p, P.col.p,
+                                                           P.rowlen.p, P.diag.p, lu_.p, z, stop);
+    }
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+// ---------------- helpers ----------------
+void device_copy(cudaStream_t s, void* dst, const void* src, size_t bytes)
+{
+    if (bytes) PORSOL_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s));
+}
+
+template <class TA, class TB>
+void convert(cudaStream_t s, long long n, const TA* a, TB* b)
+{
+    if (n == 0) return;
+    k_convert<TA, TB><<<div_up(n, RB), RB, 0, s>>>(n, a, b);
+    PORSOL_CUDA(cudaGetLastError());
+}
+template void convert<double, float>(cudaStream_t, long long, const double*, float*);
+template void convert<float, double>(cudaStream_t, long long, const float*, double*);
+
+void axpy_add(cudaStream_t s, int n, const double* y, double* x)
+{
+    if (n == 0) return;
+    k_axpy_add<<<div_up(n, RB), RB, 0, s>>>(n, y, x);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void to_f32_scaled(cudaStream_t s, int n, const double* a, float* b, double scale)
+{
+    if (n == 0) return;
+    k_to_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, a, b, scale);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void add_f32_scaled(cudaStream_t s, int n, const float* y, double scale, double* x)
+{
+    if (n == 0) return;
+    k_add_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, y, scale, x);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void dirichlet_guess(cudaStream_t s, const SellPattern& P, const double* val, const double* b, double* x)
+{
+    if (P.n == 0) return;
+    k_dirichlet_guess<<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, val, b, x);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+template <class T>
+double norm2(cudaStream_t s, int n, const T* x, RedScratch& red)
+{
+    if (n == 0) return 0.0;
+    const int nb = div_up(n, RB);
+    red.ensure(nb + 1, s);
+    k_norm2<T><<<nb, RB, 0, s>>>(n, x, red.partial.p, red.counter.p, red.partial.p + nb);
+    PORSOL_CUDA(cudaGetLastError());
+    double out = 0.0;
+    PORSOL_CUDA(cudaMemcpyAsync(&out, red.partial.p + nb, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    return std::sqrt(out);
+}
+template double norm2<double>(cudaStream_t, int, const double*, RedScratch&);
+template double norm2<float>(cudaStream_t, int, const float*, RedScratch&);
+
+}  // namespace porsol

@@ -1,0 +1,435 @@
+// k_mimetic.cu -- per-cell mimetic kernels: static inner product, local Schur assembly,
+// recipe gathers into the global system, flux recovery and flux post-processing.
+//
+// Thread-per-cell mapping.  Per-cell packed matrices are stored structure-of-arrays
+// ([entry][cell]) so that a warp's loads of one entry are one coalesced transaction; the
+// nf x nf local matrices live in registers (MAXNF is a compile-time bound: 6 for
+// hexahedra, 12 for general cells).
+#include "kernels.h"
+#include "structure.h"
+
+namespace porsol {
+
+namespace {
+
+__device__ __forceinline__ int pk(int r, int s)
+{
+    return r <= s ? s * (s + 1) / 2 + r : r * (r + 1) / 2 + s;
+}
+
+__device__ __forceinline__ void mobilities(const FluidParams& fl, const double* sat, const double* mobdens, int c,
+                                           double& totmob, double& md)
+{
+    if (fl.model == PORSOL_FLUID_COREY2) {
+        const double s = sat[c];
+        const double m1 = (s * s) / fl.mu1;
+        const double m2 = ((1.0 - s) * (1.0 - s)) / fl.mu2;
+        totmob = m1 + m2;                       // MimeticIPEvaluator.hpp:308
+        md = fl.rho1 * m1 + fl.rho2 * m2;       // :309-310
+    } else {
+        totmob = sat[c];
+        md = mobdens ? mobdens[c] : 0.0;
+    }
+}
+
+// MimeticIPEvaluator::buildStaticContrib (MimeticIPEvaluator.hpp:201-270):
+//   W = (N K N^T + t A (I - Q Q^T) A) / |c|,  t = 6 tr(K) / 3,
+//   N = A n (area-weighted normals), Q = orth(A (x_f - x_c)), gflux = N K g.
+// Q is formed by Gram-Schmidt with one re-orthogonalisation pass; Q Q^T does not depend
+// on the orthonormal basis chosen, so this matches the reference's Householder QR.
+template <int MAXNF>
+__global__ void __launch_bounds__(128) k_static_ip(int nc, const int* __restrict__ facepos,
+                                                   const double* __restrict__ area, const double* __restrict__ fcent,
+                                                   const double* __restrict__ fnormal,
+                                                   const double* __restrict__ cvol,
+                                                   const double* __restrict__ ccent,
+                                                   const double* __restrict__ perm, double g0, double g1,
+                                                   double g2, double* __restrict__ W, double* __restrict__ gflux,
+                                                   int* status)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int f0 = facepos[c];
+    const int nf = facepos[c + 1] - f0;
+    if (nf > MAXNF) {
+        atomicOr(status, ST_BAD_INDEX);
+        return;
+    }
+    double K[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) K[k] = perm[9 * (size_t)c + k];
+    const double Kg0 = K[0] * g0 + K[1] * g1 + K[2] * g2;
+    const double Kg1 = K[3] * g0 + K[4] * g1 + K[5] * g2;
+    const double Kg2 = K[6] * g0 + K[7] * g1 + K[8] * g2;
+    const double cc0 = ccent[3 * (size_t)c], cc1 = ccent[3 * (size_t)c + 1], cc2 = ccent[3 * (size_t)c + 2];
+    double N[MAXNF][3], Q[MAXNF][3], a[MAXNF];
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i) {
+        a[i] = 0.0;
+        N[i][0] = N[i][1] = N[i][2] = 0.0;
+        Q[i][0] = Q[i][1] = Q[i][2] = 0.0;
+        if (i < nf) {
+            const size_t hf = f0 + i;
+            a[i] = area[hf];
+            Q[i][0] = (fcent[3 * hf] - cc0) * a[i];
+            Q[i][1] = (fcent[3 * hf + 1] - cc1) * a[i];
+            Q[i][2] = (fcent[3 * hf + 2] - cc2) * a[i];
+            N[i][0] = fnormal[3 * hf] * a[i];
+            N[i][1] = fnormal[3 * hf + 1] * a[i];
+            N[i][2] = fnormal[3 * hf + 2] * a[i];
+            gflux[hf] = N[i][0] * Kg0 + N[i][1] * Kg1 + N[i][2] * Kg2;
+        }
+    }
+    // orthonormalise the three columns of Q (Gram-Schmidt, twice)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+            for (int k = 0; k < j; ++k) {
+                double d = 0.0;
+#pragma unroll
+                for (int i = 0; i < MAXNF; ++i) d += Q[i][k] * Q[i][j];
+#pragma unroll
+                for (int i = 0; i < MAXNF; ++i) Q[i][j] -= d * Q[i][k];
+            }
+        }
+        double nrm = 0.0;
+#pragma unroll
+        for (int i = 0; i < MAXNF; ++i) nrm += Q[i][j] * Q[i][j];
+        nrm = sqrt(nrm);
+        if (!(nrm > 0.0)) {
+            atomicOr(status, ST_NONFINITE);   // degenerate cell: the reference asserts here
+            nrm = 1.0;
+        }
+        const double inv = 1.0 / nrm;
+#pragma unroll
+        for (int i = 0; i < MAXNF; ++i) Q[i][j] *= inv;
+    }
+    // NK = N K (stored back into N's slot after use is not possible; keep separate)
+    double NK[MAXNF][3];
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) NK[i][j] = N[i][0] * K[j] + N[i][1] * K[3 + j] + N[i][2] * K[6 + j];
+    const double t = 6.0 * (K[0] + K[4] + K[8]) / 3.0;
+    const double vol = cvol[c];
+    const double a1 = 1.0 / vol, a2 = t / vol;
+    bool finite = true;
+#pragma unroll
+    for (int j = 0; j < MAXNF; ++j) {
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+            if (j < nf) {
+                const double P = (i == j ? 1.0 : 0.0) - (Q[i][0] * Q[j][0] + Q[i][1] * Q[j][1] + Q[i][2] * Q[j][2]);
+                const double nkn = NK[i][0] * N[j][0] + NK[i][1] * N[j][1] + NK[i][2] * N[j][2];
+                const double w = a2 * (a[i] * P * a[j]) + a1 * nkn;
+                finite = finite && isfinite(w);
+                W[(size_t)pk(i, j) * nc + c] = w;
+            }
+        }
+    }
+    if (!finite) atomicOr(status, ST_NONFINITE);
+}
+
+// assembleDynamic for one cell (IncompFlowSolverHybrid.hpp:1325-1382): dynamic scaling
+// (computeDynamicParams/getInverseMatrix/gravityFlux, MimeticIPEvaluator.hpp:297-350,
+// 540-546), external contributions (setExternalContrib :1736-1779), local Schur
+// complement (buildCellContrib :1785-1811) and the per-row right-hand-side pieces of
+// addCellContrib (:1817-1901).
+template <int MAXNF>
+__global__ void __launch_bounds__(128) k_assemble_cells(AssembleArgs A)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.nc) return;
+    constexpr int NPK = MAXNF * (MAXNF + 1) / 2;
+    const int nc = A.nc;
+    const int f0 = A.facepos[c];
+    const int nf = A.facepos[c + 1] - f0;
+    double totmob, md;
+    mobilities(A.fluid, A.sat, A.mobdens, c, totmob, md);
+    A.totmob[c] = totmob;
+    A.mobdens_out[c] = md;
+    double S[NPK];
+#pragma unroll
+    for (int k = 0; k < NPK; ++k) S[k] = A.W[(size_t)k * nc + c] * totmob;
+    double F[MAXNF], rl[MAXNF];
+    int kd[MAXNF];
+    double bv[MAXNF];
+    double Lc = 0.0, gsum = 0.0;
+#pragma unroll
+    for (int j = 0; j < MAXNF; ++j) {
+        F[j] = 0.0;
+        rl[j] = 0.0;
+        kd[j] = 0;
+        bv[j] = 0.0;
+        if (j < nf) {
+            double s = 0.0;
+#pragma unroll
+            for (int i = 0; i < MAXNF; ++i)
+                if (i < nf) s += S[pk(i, j)];
+            F[j] = s;
+            Lc += s;
+            const double gf = A.gravity_zero ? 0.0 : A.gflux[f0 + j] * md;
+            gsum += gf;
+            kd[j] = A.kind[f0 + j];
+            bv[j] = (kd[j] != HK_INTERNAL) ? A.bcval[f0 + j] : 0.0;
+            const double h = (kd[j] == HK_NEUMANN) ? bv[j] : 0.0;
+            rl[j] = gf - h;
+        }
+    }
+    const double gc = A.src[c] - gsum;
+    const double gl = gc / Lc;
+    const double al = -1.0 / Lc;
+    if (!(Lc > 0.0) || !isfinite(gl)) atomicOr(A.status, ST_NONFINITE);
+#pragma unroll
+    for (int j = 0; j < MAXNF; ++j) {
+        rl[j] = 1.0 * rl[j] + gl * F[j];
+#pragma unroll
+        for (int i = 0; i <= j; ++i) S[pk(i, j)] = S[pk(i, j)] + F[i] * (al * F[j]);
+    }
+#pragma unroll
+    for (int k = 0; k < NPK; ++k) A.sloc[(size_t)k * nc + c] = S[k];
+#pragma unroll
+    for (int r = 0; r < MAXNF; ++r) {
+        if (r < nf) {
+            const size_t hf = f0 + r;
+            double rr, pbv = 0.0;
+            if (kd[r] == HK_DIRICHLET) {
+                rr = S[pk(r, r)] * bv[r];
+            } else {
+                double acc = 0.0;
+#pragma unroll
+                for (int cc = 0; cc < MAXNF; ++cc)
+                    if (cc < nf && (kd[cc] == HK_DIRICHLET || kd[cc] == HK_PERIODIC_LO))
+                        acc -= S[pk(r, cc)] * bv[cc];
+                rr = acc + rl[r];
+                if (kd[r] == HK_PERIODIC_HI || kd[r] == HK_PERIODIC_LO) pbv = S[pk(r, r)] * bv[r];
+            }
+            A.rrow[hf] = rr;
+            A.pb[hf] = pbv;
+            A.F[hf] = F[r];
+        }
+    }
+    A.L[c] = Lc;
+    A.g[c] = gc;
+}
+
+__global__ void k_gather_slots(long long nent, const int* __restrict__ slot_ptr, const int* __restrict__ slot_ent,
+                               const double* __restrict__ sloc, double* __restrict__ val, float* __restrict__ val32)
+{
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= nent) return;
+    const int b = slot_ptr[k], e = slot_ptr[k + 1];
+    double v = 0.0;
+    for (int q = b; q < e; ++q) {
+        const int x = slot_ent[q];
+        v += x >= 0 ? sloc[x] : -sloc[~x];
+    }
+    val[k] = v;
+    if (val32) val32[k] = float(v);
+}
+
+__global__ void k_gather_rhs(int n, const int* __restrict__ rhs_ptr, const int* __restrict__ rhs_ent,
+                             const double* __restrict__ rrow, const double* __restrict__ pb, double* __restrict__ rhs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = 0.0;
+    for (int q = rhs_ptr[i]; q < rhs_ptr[i + 1]; ++q) {
+        const int x = rhs_ent[q];
+        const int hf = x >> 2, kind = x & 3;
+        v += kind == 0 ? rrow[hf] : (kind == 1 ? pb[hf] : -pb[hf]);
+    }
+    rhs[i] = v;
+}
+
+__global__ void k_scale_entry(double* val, const int* diag, int row, double factor, float* val32)
+{
+    const int k = diag[row];
+    val[k] *= factor;
+    if (val32) val32[k] = float(val[k]);
+}
+
+// computePressureAndFluxes (IncompFlowSolverHybrid.hpp:1672-1730):
+//   p_c = (g_c + F . pi_c) / L_c,  v_c = totmob W_c (p_c 1 - pi_c) + mobdens gflux_c.
+template <int MAXNF>
+__global__ void __launch_bounds__(128) k_recover(RecoverArgs A)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.nc) return;
+    const int nc = A.nc;
+    const int f0 = A.facepos[c];
+    const int nf = A.facepos[c + 1] - f0;
+    double pi[MAXNF];
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i) {
+        pi[i] = 0.0;
+        if (i < nf) {
+            pi[i] = A.x[A.cf[f0 + i]];
+            s += A.F[f0 + i] * pi[i];
+        }
+    }
+    const double p = (A.g[c] + s) / A.L[c];
+    A.pressure[c] = p;
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i) pi[i] = p - pi[i];
+    const double tm = A.totmob[c];
+    const double md = A.mobdens[c];
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i) {
+        if (i < nf) {
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < MAXNF; ++j)
+                if (j < nf) v += (A.W[(size_t)pk(i, j) * nc + c] * tm) * pi[j];
+            const double gfl = A.gravity_zero ? 0.0 : A.gflux[f0 + i] * md;
+            A.outflux[f0 + i] = gfl + v;
+        }
+    }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v)
+{
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// postProcessFluxes (IncompFlowSolverHybrid.hpp:754-807): the half-face visited first
+// gets 0.5 (v1 - v2), the second its negative; returns max |v_old - v_new|.
+__global__ void k_post_process(int npairs, const int* __restrict__ pairs, double* __restrict__ outflux,
+                               unsigned long long* maxmod)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double d = 0.0;
+    if (k < npairs) {
+        const int h1 = pairs[2 * k], h2 = pairs[2 * k + 1];
+        const double v1 = outflux[h1], v2 = outflux[h2];
+        const double fl = v1 - v2;
+        const double n1 = 0.5 * fl, n2 = 0.5 * -1.0 * fl;
+        outflux[h1] = n1;
+        outflux[h2] = n2;
+        d = fmax(fabs(v1 - n1), fabs(v2 - n2));
+    }
+    // warp max then one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxmod, d);
+}
+
+__global__ void k_mass_balance(int nc, const int* __restrict__ facepos, const double* __restrict__ outflux,
+                               const double* __restrict__ src, unsigned long long* out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double imb = 0.0, sq = 0.0, vm = 0.0;
+    if (c < nc) {
+        double s = 0.0;
+        for (int hf = facepos[c]; hf < facepos[c + 1]; ++hf) {
+            s += outflux[hf];
+            vm = fmax(vm, fabs(outflux[hf]));
+        }
+        const double q = src ? src[c] : 0.0;
+        imb = fabs(s - q);
+        sq = fabs(q);
+        if (!isfinite(s)) imb = 1e300;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        imb = fmax(imb, __shfl_xor_sync(0xffffffffu, imb, o));
+        sq = fmax(sq, __shfl_xor_sync(0xffffffffu, sq, o));
+        vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_nonneg(&out[0], imb);
+        atomic_max_nonneg(&out[1], sq);
+        atomic_max_nonneg(&out[2], vm);
+    }
+}
+
+__global__ void k_check_finite(long long n, const double* __restrict__ v, int* status)
+{
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        bad |= !isfinite(v[i]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, ST_NONFINITE);
+}
+
+}  // namespace
+
+void launch_static_ip(int maxnf, cudaStream_t s, int nc, const int* facepos, const double* area,
+                      const double* fcent, const double* fnormal, const double* cvol, const double* ccent,
+                      const double* perm, const double grav[3], double* W, double* gflux, int* status)
+{
+    if (nc == 0) return;
+    const int bs = 128;
+    if (maxnf <= 6)
+        k_static_ip<6><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
+                                                     grav[1], grav[2], W, gflux, status);
+    else
+        k_static_ip<12><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
+                                                      grav[1], grav[2], W, gflux, status);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_assemble_cells(int maxnf, cudaStream_t s, const AssembleArgs& a)
+{
+    if (a.nc == 0) return;
+    const int bs = 128;
+    if (maxnf <= 6) k_assemble_cells<6><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    else k_assemble_cells<12><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_gather_slots(cudaStream_t s, long long nent, const int* slot_ptr, const int* slot_ent,
+                         const double* sloc, double* val, float* val32)
+{
+    if (nent == 0) return;
+    k_gather_slots<<<div_up(nent, 256), 256, 0, s>>>(nent, slot_ptr, slot_ent, sloc, val, val32);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_gather_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs_ent, const double* rrow,
+                       const double* pb, double* rhs)
+{
+    if (n == 0) return;
+    k_gather_rhs<<<div_up(n, 256), 256, 0, s>>>(n, rhs_ptr, rhs_ent, rrow, pb, rhs);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_scale_entry(cudaStream_t s, double* val, const int* diag, int row, double factor, float* val32)
+{
+    k_scale_entry<<<1, 1, 0, s>>>(val, diag, row, factor, val32);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_recover(int maxnf, cudaStream_t s, const RecoverArgs& a)
+{
+    if (a.nc == 0) return;
+    const int bs = 128;
+    if (maxnf <= 6) k_recover<6><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    else k_recover<12><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* outflux,
+                         unsigned long long* maxmod_bits)
+{
+    if (npairs == 0) return;
+    k_post_process<<<div_up(npairs, 256), 256, 0, s>>>(npairs, pairs, outflux, maxmod_bits);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const double* outflux, const double* src,
+                         unsigned long long* out3)
+{
+    if (nc == 0) return;
+    k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status)
+{
+    if (n == 0) return;
+    k_check_finite<<<std::min(div_up(n, 256), 152 * 8), 256, 0, s>>>(n, v, status);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+}  // namespace porsol

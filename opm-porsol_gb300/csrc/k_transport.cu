@@ -1,0 +1,569 @@
+// k_transport.cu -- explicit upstream saturation transport (EulerUpstream) on the GPU.
+//
+// Reference: EulerUpstream::transportSolve / computeCflTime / smallTimeStep /
+// checkAndPossiblyClampSat (euler/EulerUpstream_impl.hpp:153-385), the residual of
+// EulerUpstreamResidual (euler/EulerUpstreamResidual_impl.hpp:101-300, 475-547) and the
+// CFL estimates of cfl_calculator (euler/CflCalculator.hpp:55-170), for the scalar
+// two-phase model of ReservoirPropertyCapillary without rock tables (kr1 = s^2,
+// kr2 = (1-s)^2, pc = 1e5 (1-s); ReservoirPropertyCapillary_impl.hpp:118-170,
+// ReservoirPropertyCommon_impl.hpp:466-476).
+//
+// Layout: every face that contributes is one "face entry" (the reference visits each
+// internal/periodic face once, from the lower cell index, and every Dirichlet boundary
+// face).  All saturation-independent per-face factors (gravity driving force G, capillary
+// geometry factor, n.n) are computed once per transportSolve.  A sub-step is two kernels:
+// face entries compute dS, then each cell gathers its entries' dS in a fixed order (no
+// atomics, deterministic) and updates its saturation with the range check.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <sstream>
+
+#include "kernels.h"
+#include "porsol_internal.h"
+#include "structure.h"
+
+using namespace porsol;
+
+namespace {
+
+constexpr int TB = 256;
+
+struct FaceEntry {
+    int c0, c1, hf;     // cells (c1 == c0 on Dirichlet faces) and the half-face of c0
+    int dirichlet;
+    double satbc;       // Dirichlet saturation
+    double G;           // A n . (Kavg g) (rho1 - rho2)
+    double capf;        // A n . (Kavg e) / (d0 + d1), e the unit centre-to-centre direction
+    double nn;          // n . n
+};
+
+__device__ __forceinline__ double mob1(double s, double mu1) { return (s * s) / mu1; }
+__device__ __forceinline__ double mob2(double s, double mu2) { return ((1.0 - s) * (1.0 - s)) / mu2; }
+
+struct TrParams {
+    double mu1, mu2;
+    int visc, grav, cap;
+};
+
+// UpdateForCell::operator() for one face (EulerUpstreamResidual_impl.hpp:101-291), scalar mobilities
+__global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const double* __restrict__ sat,
+                          const double* __restrict__ flux, TrParams p, double* __restrict__ dS,
+                          const int* __restrict__ status)
+{
+    if (*status) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nfe) return;
+    const FaceEntry e = fe[k];
+    const double s0 = sat[e.c0];
+    const double s1 = e.dirichlet ? e.satbc : sat[e.c1];
+    const double q = flux[e.hf];
+    const double G = p.grav ? e.G : 0.0;
+    const int triv = G >= 0.0 ? 0 : 1;
+    const double sup = (q >= 0.0) ? s0 : s1;
+    double m[2];
+    m[triv] = triv == 0 ? mob1(sup, p.mu1) : mob2(sup, p.mu2);
+    const double signG = triv == 0 ? -1.0 : 1.0;
+    const double gnt = signG * m[triv] * G;
+    const double supn = (q + gnt >= 0.0) ? s0 : s1;
+    const int nt = 1 - triv;
+    m[nt] = nt == 0 ? mob1(supn, p.mu1) : mob2(supn, p.mu2);
+    const double mtinv = 1.0 / (m[0] + m[1]);
+    double d = 0.0;
+    if (p.visc) d += m[0] * mtinv * q * e.nn;
+    if (p.grav && !e.dirichlet) d += m[0] * mtinv * m[1] * G;
+    if (p.cap && e.capf != 0.0) {
+        const double as = 0.5 * (s0 + s1);
+        const double a1 = mob1(as, p.mu1), a2 = mob2(as, p.mu2);
+        const double cp0 = 1e5 * (1.0 - s0), cp1 = 1e5 * (1.0 - s1);
+        d += a1 * (1.0 / (a1 + a2)) * a2 * e.capf * (cp1 - cp0);
+    }
+    dS[k] = d;
+}
+
+// residual gather + smallTimeStep update + checkAndPossiblyClampSat
+__global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* __restrict__ cent,
+                              const double* __restrict__ dS, const double* __restrict__ inj,
+                              const double* __restrict__ porevol, TrParams p, double dt, int check, int clamp,
+                              double* __restrict__ sat, int* status)
+{
+    if (*status) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double r = 0.0;
+    for (int q = cptr[c]; q < cptr[c + 1]; ++q) {
+        const int x = cent[q];
+        r += x >= 0 ? dS[x] : -dS[~x];
+    }
+    const double s = sat[c];
+    if (inj) {
+        double rate = inj[c];
+        if (rate < 0.0) {
+            const double l1 = mob1(s, p.mu1), l2 = mob2(s, p.mu2);
+            rate *= l1 / (l1 + l2);
+        }
+        r += rate;
+    }
+    double sn = s + dt * r / porevol[c];
+    if (check || clamp) {
+        if (sn > 1.0 || sn < 0.0) {
+            if (clamp) sn = fmax(fmin(sn, 1.0), 0.0);
+            else if (sn > 1.001 || sn < -0.001) atomicOr(status, ST_SAT_RANGE);
+        }
+    }
+    if (!isfinite(sn)) atomicOr(status, ST_NONFINITE);
+    sat[c] = sn;
+}
+
+__device__ __forceinline__ void atomic_min_pos(unsigned long long* a, double v)
+{
+    atomicMin(a, (unsigned long long)__double_as_longlong(v));
+}
+
+// findCFLtimeVelocity (CflCalculator.hpp:55-88) and findCFLtimeGravity (:91-139) per cell
+__global__ void k_cfl_cells(int nc, const int* __restrict__ facepos, const double* __restrict__ flux,
+                            const double* __restrict__ gflux_hf, const double* __restrict__ vol,
+                            const double* __restrict__ poro, double fac_v, double fac_g, int do_v, int do_g,
+                            unsigned long long* out, int* status)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double dv = 1e100, dg = 1e100;
+    if (c < nc) {
+        double fp = 0.0, fn = 0.0, fg = 0.0;
+        for (int hf = facepos[c]; hf < facepos[c + 1]; ++hf) {
+            const double f = flux[hf];
+            if (f > 0) fp += f;
+            else fn -= f;
+            if (do_g) {
+                const double g = gflux_hf[hf];
+                if (g > 0) fg += g;
+            }
+        }
+        if (do_v) {
+            dv = (fac_v * vol[c] * poro[c]) / fmax(fn, fp);
+            if (dv == 0.0) atomicOr(status, ST_CFL_ZERO);
+        }
+        if (do_g) dg = (fac_g * vol[c] * poro[c]) / fg;
+    }
+    if (!(dv >= 0.0)) dv = 1e300;   // NaN never wins the comparison in the reference
+    if (!(dg >= 0.0)) dg = 1e300;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dv = fmin(dv, __shfl_xor_sync(0xffffffffu, dv, o));
+        dg = fmin(dg, __shfl_xor_sync(0xffffffffu, dg, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_min_pos(&out[0], dv);
+        atomic_min_pos(&out[1], dg);
+    }
+}
+
+}  // namespace
+
+struct porsol_transport {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::string err;
+    bool ready = false;
+    HostGrid g;
+    std::vector<double> perm, poro;
+    std::vector<int> st;
+    std::vector<double> sv;
+    std::vector<int> pbid;
+    porsol_fluid fluid{};
+    porsol_transport_opts o{};
+    double fac[3] = {0, 0, 0};
+    std::vector<int> bid_to_face;   // last periodic half-face with each bid
+    std::vector<int> hf_cell;
+    std::vector<FaceEntry> fe_h;
+    double grav_cached[3] = {NAN, NAN, NAN};
+    DBuf<FaceEntry> fe;
+    DBuf<int> cptr, cent, facepos, status;
+    DBuf<double> porevol, vol, poro_d, dS, sat0, gflux_hf, in_sat, in_flux, in_inj;
+    DBuf<unsigned long long> red;
+
+    void init(const porsol_grid* grid, const double* K, const double* phi, const porsol_fluid* fl, const int* stype,
+              const double* sval, const int* partner, const porsol_transport_opts* opts);
+    void build_entries(const double* grav);
+    void solve(double* sat, double time, const double* grav, const double* flux, const double* inj,
+               porsol_transport_stats* stats, bool dev);
+};
+
+namespace {
+
+// ReservoirPropertyCapillary::computeSingleRockCflFactors(-1, 0, 0)
+// (ReservoirPropertyCapillary_impl.hpp:215-260): 257-point sampling of the fractional
+// flow and the gravity flow function.
+void cfl_factors(double mu1, double mu2, double* out)
+{
+    const int N = 257;
+    const double delta = 1.0 / double(N - 1);
+    auto ff = [&](double s, double& f1, double& fg) {
+        const double l1 = (s * s) / mu1, l2 = ((1 - s) * (1 - s)) / mu2;
+        f1 = l1 / (l1 + l2);
+        fg = l1 * l2 / (l1 + l2);
+    };
+    double last1, lastg, md1 = -1e100, mdg = -1e100;
+    ff(0.0, last1, lastg);
+    double maxffg = lastg;
+    for (int i = 1; i < N; ++i) {
+        const double s = double(i) * delta;
+        double f1, fg;
+        ff(s, f1, fg);
+        md1 = std::max(md1, std::fabs(f1 - last1) / delta);
+        mdg = std::max(mdg, std::fabs(fg - lastg) / delta);
+        maxffg = std::max(maxffg, fg);
+        last1 = f1;
+        lastg = fg;
+    }
+    out[0] = 1.0 / md1;
+    out[1] = 1.0 / mdg;
+    out[2] = maxffg * 0.0;   // no rock table: zero capillary-pressure derivative bound
+}
+
+}  // namespace
+
+void porsol_transport::init(const porsol_grid* grid, const double* K, const double* phi, const porsol_fluid* fl,
+                            const int* stype, const double* sval, const int* partner,
+                            const porsol_transport_opts* opts)
+{
+    ready = false;
+    PORSOL_REQUIRE(K && phi && fl && stype && sval, PORSOL_ERR_BAD_ARG, "transport init: null argument");
+    PORSOL_REQUIRE(fl->model == PORSOL_FLUID_COREY2, PORSOL_ERR_BAD_ARG,
+                   "transport needs the two-phase Corey-2 fluid model");
+    g.copy_from(grid);
+    const int nc = g.nc, nhf = g.nhf;
+    perm.assign(K, K + 9 * size_t(nc));
+    poro.assign(phi, phi + nc);
+    st.assign(stype, stype + nhf);
+    sv.assign(sval, sval + nhf);
+    pbid.assign(nhf, 0);
+    if (partner) pbid.assign(partner, partner + nhf);
+    fluid = *fl;
+    porsol_transport_opts_default(&o);
+    if (opts) o = *opts;
+    cfl_factors(fluid.viscosity1, fluid.viscosity2, fac);
+    hf_cell.resize(nhf);
+    int maxbid = 0;
+    for (int c = 0; c < nc; ++c)
+        for (int hf = g.facepos[c]; hf < g.facepos[c + 1]; ++hf) {
+            hf_cell[hf] = c;
+            maxbid = std::max(maxbid, g.bid[hf]);
+        }
+    bid_to_face.assign(maxbid + 1, -1);
+    for (int hf = 0; hf < nhf; ++hf)
+        if (g.boundary(hf) && st[hf] == PORSOL_BC_PERIODIC) bid_to_face[g.bid[hf]] = hf;
+    for (int hf = 0; hf < nhf; ++hf)
+        if (g.boundary(hf) && st[hf] != PORSOL_BC_PERIODIC)
+            PORSOL_REQUIRE(st[hf] == PORSOL_BC_DIRICHLET, PORSOL_ERR_BAD_ARG,
+                           "saturation boundary conditions must be Dirichlet or periodic");
+    cudaStream_t s = stream;
+    std::vector<double> pv(nc);
+    for (int c = 0; c < nc; ++c) pv[c] = g.cvol[c] * poro[c];   // initObj (EulerUpstream_impl.hpp:120-129)
+    porevol.upload(pv, s);
+    vol.upload(g.cvol, s);
+    poro_d.upload(poro, s);
+    facepos.upload(g.facepos, s);
+    status.alloc(1);
+    status.zero(s);
+    red.alloc(2);
+    grav_cached[0] = grav_cached[1] = grav_cached[2] = NAN;
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    ready = true;
+}
+
+// Build face entries for a gravity vector (G depends on it).  Host work, cached per gravity.
+void porsol_transport::build_entries(const double* grav)
+{
+    const int nc = g.nc, nhf = g.nhf;
+    const double gv[3] = {grav ? grav[0] : 0.0, grav ? grav[1] : 0.0, grav ? grav[2] : 0.0};
+    if (gv[0] == grav_cached[0] && gv[1] == grav_cached[1] && gv[2] == grav_cached[2]) return;
+    const double drho = fluid.density1 - fluid.density2;
+    fe_h.clear();
+    std::vector<std::vector<int>> cl(nc);
+    std::vector<double> ghf(nhf, 0.0);
+    for (int c0 = 0; c0 < nc; ++c0) {
+        for (int f = g.facepos[c0]; f < g.facepos[c0 + 1]; ++f) {
+            // gravity CFL flux per half-face (CflCalculator.hpp:100-131)
+            {
+                const int c1 = g.nb[f];
+                double Kl[9];
+                for (int k = 0; k < 9; ++k)
+                    Kl[k] = g.boundary(f) ? perm[9 * size_t(c0) + k]
+                                          : 0.5 * (perm[9 * size_t(c0) + k] + perm[9 * size_t(c1) + k]);
+                const double* n = &g.fnormal[3 * size_t(f)];
+                double gf = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    for (int q = 0; q < 3; ++q) gf += n[q] * (Kl[3 * q + k] * gv[k] * drho);
+                ghf[f] = gf * g.area[f];
+            }
+            int c1, nbface = f, dir = 0;
+            double sbc = 0.0;
+            if (g.boundary(f)) {
+                if (st[f] == PORSOL_BC_PERIODIC) {
+                    const int pb = pbid[f];
+                    PORSOL_REQUIRE(pb >= 0 && pb < int(bid_to_face.size()) && bid_to_face[pb] >= 0,
+                                   PORSOL_ERR_BAD_ARG, "periodic saturation partner not found");
+                    nbface = bid_to_face[pb];
+                    c1 = hf_cell[nbface];
+                    if (c0 > c1) continue;
+                } else {
+                    c1 = c0;
+                    dir = 1;
+                    sbc = sv[f];
+                }
+            } else {
+                c1 = g.nb[f];
+                if (c0 > c1) continue;
+            }
+            FaceEntry e{};
+            e.c0 = c0;
+            e.c1 = c1;
+            e.hf = f;
+            e.dirichlet = dir;
+            e.satbc = sbc;
+            const double* n = &g.fnormal[3 * size_t(f)];
+            const double A = g.area[f];
+            double Kav[9];
+            for (int k = 0; k < 9; ++k) Kav[k] = 0.5 * (perm[9 * size_t(c0) + k] + perm[9 * size_t(c1) + k]);
+            double gi[3];
+            for (int i = 0; i < 3; ++i)
+                gi[i] = (Kav[3 * i] * gv[0] + Kav[3 * i + 1] * gv[1] + Kav[3 * i + 2] * gv[2]) * drho;
+            e.G = A * (n[0] * gi[0] + n[1] * gi[1] + n[2] * gi[2]);
+            e.nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+            // capillary geometry (estimateCapPressureGradient, EulerUpstreamResidual_impl.hpp:512-547)
+            e.capf = 0.0;
+            if (!(g.boundary(f) && st[f] != PORSOL_BC_PERIODIC)) {
+                const int nb = g.boundary(f) ? hf_cell[nbface] : g.nb[f];
+                double d0 = 0, d1 = 0, r[3], nr = 0;
+                for (int d = 0; d < 3; ++d) {
+                    const double a = g.ccent[3 * size_t(c0) + d] - g.fcent[3 * size_t(f) + d];
+                    const double b = g.ccent[3 * size_t(nb) + d] - g.fcent[3 * size_t(nbface) + d];
+                    d0 += a * a;
+                    d1 += b * b;
+                    r[d] = g.ccent[3 * size_t(nb) + d] - g.fcent[3 * size_t(nbface) + d] + g.fcent[3 * size_t(f) + d] -
+                           g.ccent[3 * size_t(c0) + d];
+                    nr += r[d] * r[d];
+                }
+                nr = std::sqrt(nr);
+                const double inv = 1.0 / (std::sqrt(d0) + std::sqrt(d1));
+                double kr[3];
+                for (int i = 0; i < 3; ++i) kr[i] = Kav[3 * i] * r[0] / nr + Kav[3 * i + 1] * r[1] / nr + Kav[3 * i + 2] * r[2] / nr;
+                e.capf = A * (n[0] * kr[0] + n[1] * kr[1] + n[2] * kr[2]) * inv;
+            }
+            const int k = int(fe_h.size());
+            fe_h.push_back(e);
+            cl[c0].push_back(~k);
+            if (c1 != c0) cl[c1].push_back(k);
+        }
+    }
+    std::vector<int> cp(nc + 1, 0), ce;
+    for (int c = 0; c < nc; ++c) cp[c + 1] = cp[c] + int(cl[c].size());
+    ce.reserve(cp[nc]);
+    for (int c = 0; c < nc; ++c) ce.insert(ce.end(), cl[c].begin(), cl[c].end());
+    cudaStream_t s = stream;
+    fe.upload(fe_h, s);
+    cptr.upload(cp, s);
+    cent.upload(ce, s);
+    gflux_hf.upload(ghf, s);
+    dS.alloc(std::max<size_t>(fe_h.size(), 1));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    grav_cached[0] = gv[0];
+    grav_cached[1] = gv[1];
+    grav_cached[2] = gv[2];
+}
+
+void porsol_transport::solve(double* sat, double time, const double* grav, const double* flux, const double* inj,
+                             porsol_transport_stats* stats, bool dev)
+{
+    PORSOL_REQUIRE(ready, PORSOL_ERR_STATE, "transport solver not initialised");
+    PORSOL_REQUIRE(sat && flux, PORSOL_ERR_BAD_ARG, "transportSolve: null argument");
+    build_entries(grav);
+    const int nc = g.nc, nhf = g.nhf;
+    cudaStream_t s = stream;
+    double* d_sat;
+    const double *d_flux, *d_inj = nullptr;
+    if (dev) {
+        d_sat = sat;
+        d_flux = flux;
+        d_inj = inj;
+    } else {
+        in_sat.upload(sat, nc, s);
+        d_sat = in_sat.p;
+        in_flux.upload(flux, nhf, s);
+        d_flux = in_flux.p;
+        if (inj) {
+            in_inj.upload(inj, nc, s);
+            d_inj = in_inj.p;
+        }
+    }
+    const double gv[3] = {grav ? grav[0] : 0.0, grav ? grav[1] : 0.0, grav ? grav[2] : 0.0};
+    // computeCflTime (EulerUpstream_impl.hpp:265-331)
+    double dtv = 1e99, dtg = 1e99, dtc = 1e99;
+    const int do_v = o.method_viscous && o.use_cfl_viscous;
+    const int do_g = o.method_gravity && o.use_cfl_gravity;
+    const int do_c = o.method_capillary && o.use_cfl_capillary;
+    if (do_v || do_g) {
+        unsigned long long init[2];
+        const double big = 1e100;
+        std::memcpy(&init[0], &big, 8);
+        std::memcpy(&init[1], &big, 8);
+        PORSOL_CUDA(cudaMemcpyAsync(red.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+        k_cfl_cells<<<div_up(nc, TB), TB, 0, s>>>(nc, facepos.p, d_flux, gflux_hf.p, vol.p, poro_d.p, fac[0], fac[1],
+                                                  do_v, do_g, red.p, status.p);
+        PORSOL_CUDA(cudaGetLastError());
+        unsigned long long out[2];
+        int stt = 0;
+        PORSOL_CUDA(cudaMemcpyAsync(out, red.p, sizeof(out), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaMemcpyAsync(&stt, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        if (stt & ST_CFL_ZERO) {
+            status.zero(s);
+            throw Error(PORSOL_ERR_CFL, "Cfl computation gave dt = 0.0");
+        }
+        double v[2];
+        std::memcpy(v, out, sizeof(v));
+        if (do_v) dtv = v[0];
+        if (do_g) dtg = v[1];
+    }
+    if (do_c) {
+        // findCFLtimeCapillary (CflCalculator.hpp:143-170) divides by cflFactorCapillary,
+        // which is zero without rock tables (max_derpc = 0): every local bound is +inf and
+        // the estimate keeps its initial value 1e100.
+        dtc = 1e100;
+    }
+    (void)gv;
+    const double cfl_dt = std::min(std::min(dtv, dtg), dtc) * o.courant_number;
+    int n;
+    if (cfl_dt > time) {
+        n = o.minimum_small_steps;
+    } else {
+        const double steps = std::min<double>(std::ceil(time / cfl_dt), double(std::numeric_limits<int>::max()));
+        n = int(steps);
+        n = std::max(n, o.minimum_small_steps);
+        n = std::min(n, o.maximum_small_steps);
+    }
+    double dt = time / n;
+    sat0.alloc(nc);
+    PORSOL_CUDA(cudaMemcpyAsync(sat0.p, d_sat, nc * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    TrParams p{fluid.viscosity1, fluid.viscosity2, o.method_viscous, o.method_gravity, o.method_capillary};
+    const int nfe = int(fe_h.size());
+    int repeats = 0;
+    const int max_repeats = 10;
+    while (true) {
+        for (int q = 0; q < n; ++q) {
+            if (nfe) k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p, status.p);
+            k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, porevol.p, p, dt, o.check_sat,
+                                                       o.clamp_sat, d_sat, status.p);
+            if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
+        }
+        PORSOL_CUDA(cudaGetLastError());
+        int stt = 0;
+        PORSOL_CUDA(cudaMemcpyAsync(&stt, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        if (stt == 0) break;
+        status.zero(s);
+        if (stt & ST_NONFINITE) throw Error(PORSOL_ERR_NONFINITE, "non-finite saturation in transport");
+        ++repeats;
+        if (repeats > max_repeats) {
+            PORSOL_CUDA(cudaMemcpyAsync(d_sat, sat0.p, nc * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            PORSOL_CUDA(cudaStreamSynchronize(s));
+            throw Error(PORSOL_ERR_SAT_RANGE, "Saturation out of range in EulerUpstream");
+        }
+        n *= 2;   // "Transport failed, retrying with more steps." (EulerUpstream_impl.hpp:200-211)
+        dt = time / n;
+        PORSOL_CUDA(cudaMemcpyAsync(d_sat, sat0.p, nc * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    if (!dev) {
+        PORSOL_CUDA(cudaMemcpyAsync(sat, d_sat, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+    }
+    if (stats) {
+        stats->small_steps = n;
+        stats->repeats = repeats;
+        stats->cfl_dt = cfl_dt;
+    }
+}
+
+namespace {
+template <class F>
+int tguard(porsol_transport* t, F&& f)
+{
+    if (!t) return PORSOL_ERR_BAD_ARG;
+    try {
+        PORSOL_CUDA(cudaSetDevice(t->device));
+        f();
+        t->err.clear();
+        return PORSOL_OK;
+    } catch (const Error& e) {
+        t->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        t->err = e.what();
+        return PORSOL_ERR_BAD_ARG;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+void porsol_transport_opts_default(porsol_transport_opts* o)
+{
+    if (!o) return;
+    o->courant_number = 0.5;
+    o->method_viscous = o->method_gravity = o->method_capillary = 1;
+    o->use_cfl_viscous = o->use_cfl_gravity = o->use_cfl_capillary = 1;
+    o->minimum_small_steps = 1;
+    o->maximum_small_steps = 10000;
+    o->check_sat = 1;
+    o->clamp_sat = 0;
+}
+
+int porsol_transport_create(porsol_transport** out)
+{
+    if (!out) return PORSOL_ERR_BAD_ARG;
+    *out = nullptr;
+    auto* t = new (std::nothrow) porsol_transport();
+    if (!t) return PORSOL_ERR_BAD_ARG;
+    if (cudaGetDevice(&t->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete t;
+        return PORSOL_ERR_CUDA;
+    }
+    *out = t;
+    return PORSOL_OK;
+}
+
+void porsol_transport_destroy(porsol_transport* t)
+{
+    if (!t) return;
+    cudaSetDevice(t->device);
+    cudaStreamSynchronize(t->stream);
+    cudaStream_t s = t->stream;
+    delete t;
+    cudaStreamDestroy(s);
+}
+
+const char* porsol_transport_last_error(const porsol_transport* t) { return t ? t->err.c_str() : "null handle"; }
+
+int porsol_transport_init(porsol_transport* t, const porsol_grid* grid, const double* perm, const double* poro,
+                          const porsol_fluid* fluid, const int* st, const double* sv, const int* partner,
+                          const porsol_transport_opts* opts)
+{
+    return tguard(t, [&] { t->init(grid, perm, poro, fluid, st, sv, partner, opts); });
+}
+
+int porsol_transport_solve(porsol_transport* t, double* sat, double time, const double* grav, const double* outflux,
+                           const double* injection, porsol_transport_stats* stats)
+{
+    return tguard(t, [&] { t->solve(sat, time, grav, outflux, injection, stats, false); });
+}
+
+int porsol_transport_solve_device(porsol_transport* t, double* sat, double time, const double* grav,
+                                  const double* outflux, const double* injection, porsol_transport_stats* stats)
+{
+    return tguard(t, [&] { t->solve(sat, time, grav, outflux, injection, stats, true); });
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// kernels.h -- host launchers of the device kernels (one translation unit per family).
+#pragma once
+
+#include "porsol_internal.h"
+
+namespace porsol {
+
+struct FluidParams {
+    int model;
+    double mu1, mu2, rho1, rho2;
+};
+
+// ---- k_mimetic.cu --------------------------------------------------------------------
+// Static inner products W (packed symmetric, [npk][nc]) and gravity flux per half-face.
+void launch_static_ip(int maxnf, cudaStream_t s, int nc, const int* facepos, const double* area,
+                      const double* fcent, const double* fnormal, const double* cvol, const double* ccent,
+                      const double* perm, const double grav[3], double* W, double* gflux, int* status);
+
+struct AssembleArgs {
+    int nc;
+    const int* facepos;
+    const double* W;
+    const double* gflux;
+    bool gravity_zero;
+    FluidParams fluid;
+    const double* sat;       // saturation (COREY2) or total mobility (CELLWISE)
+    const double* mobdens;   // CELLWISE only, may be null
+    const int* kind;         // HfKind per half-face
+    const double* bcval;     // FlowBC value per half-face
+    const double* src;
+    double* sloc;            // packed local Schur matrices [npk][nc]
+    double* F;               // per half-face
+    double* L;
+    double* g;
+    double* rrow;            // per half-face
+    double* pb;              // per half-face
+    double* totmob;          // per cell (out)
+    double* mobdens_out;     // per cell (out)
+    int* status;
+};
+void launch_assemble_cells(int maxnf, cudaStream_t s, const AssembleArgs& a);
+
+// val[k] = sum of signed recipe entries of SELL slot k; val32 (optional) gets a float copy.
+void launch_gather_slots(cudaStream_t s, long long nent, const int* slot_ptr, const int* slot_ent,
+                         const double* sloc, double* val, float* val32);
+void launch_gather_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs_ent, const double* rrow,
+                       const double* pb, double* rhs);
+void launch_scale_entry(cudaStream_t s, double* val, const int* diag, int row, double factor, float* val32);
+
+struct RecoverArgs {
+    int nc;
+    const int* facepos;
+    const int* cf;
+    const double* x;         // face pressures
+    const double* W;
+    const double* gflux;
+    bool gravity_zero;
+    const double* F;
+    const double* L;
+    const double* g;
+    const double* totmob;
+    const double* mobdens;
+    double* pressure;
+    double* outflux;
+};
+void launch_recover(int maxnf, cudaStream_t s, const RecoverArgs& a);
+
+// postProcessFluxes over precomputed half-face pairs; max |modification| into *maxmod_bits
+// (as the bit pattern of a non-negative double, reduced with atomicMax).
+void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* outflux,
+                         unsigned long long* maxmod_bits);
+// max_c |sum_f v - src_c| -> out[0] bits, max |src| -> out[1], max |v| -> out[2]
+void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const double* outflux, const double* src,
+                         unsigned long long* out3);
+void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status);
+
+}  // namespace porsol

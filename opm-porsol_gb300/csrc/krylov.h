@@ -1,0 +1,105 @@
+// krylov.h -- SELL SpMV, preconditioned CG with device-side scalars, ILU(0).
+#pragma once
+
+#include "porsol_internal.h"
+
+namespace porsol {
+
+// Device-resident CG scalars.  Written by the last block of each reduction kernel; read by
+// the next kernel in stream order, so no host round trip is needed per iteration.
+struct CgDev {
+    double rho, rholast, alpha, def0, def, tol;
+    int iter, maxit, converged, stop, breakdown, pad;
+};
+
+// Mirror of CgDev in mapped pinned host memory, written at the end of every iteration.
+struct CgHostView {
+    volatile double def0, def;
+    volatile int iter, converged, stop, breakdown;
+};
+
+// Reduction scratch: partial sums per block + arrival counter (reset by the last block).
+struct RedScratch {
+    DBuf<double> partial;
+    DBuf<unsigned int> counter;
+    int max_blocks = 0;
+    void ensure(int blocks, cudaStream_t s);
+};
+
+template <class T>
+struct Precond {
+    virtual ~Precond() = default;
+    // z = M^{-1} r; kernels must do nothing when *stop != 0.
+    virtual void apply(cudaStream_t s, const T* r, T* z, const int* stop) = 0;
+};
+
+template <class TV, class TX>
+void spmv(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, TX* y);
+
+// y = b - A x  (residual)
+template <class TV, class TX>
+void residual(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, const TX* b, TX* y);
+
+struct CgResult {
+    int iterations = 0;
+    double reduction = 0.0, def0 = 0.0, def = 0.0;
+    bool converged = false, breakdown = false;
+};
+
+// Preconditioned CG, the algorithm of dune-istl's CGSolver::apply: stop when
+// ||b - A x||_2 < tol ||b - A x0||_2 (or < 1e-30) or after maxit iterations.
+// x holds the initial guess on entry.  TV = matrix value type, T = vector type.
+template <class TV, class T>
+class PcgSolver {
+public:
+    void setup(int n, cudaStream_t s);
+    CgResult solve(cudaStream_t s, const SellPattern& P, const TV* val, Precond<T>& M, const T* b, T* x,
+                   double tol, int maxit, Profiler* prof = nullptr, int prof_kernel = -1);
+    ~PcgSolver();
+
+private:
+    int n_ = 0;
+    DBuf<T> r_, z_, p_, q_;
+    DBuf<CgDev> st_;
+    RedScratch red_;
+    CgHostView* hview_ = nullptr;
+    CgHostView* dview_ = nullptr;
+    std::vector<cudaEvent_t> ev_;
+};
+
+// ILU(0) with the pivots stored inverted, factor and triangular solves level-scheduled
+// (rows of one level are independent).  The algorithm of dune-istl's SeqILU0 with
+// relaxation 1 (IncompFlowSolverHybrid.hpp:1404).
+class Ilu0 : public Precond<double> {
+public:
+    void build_levels(const SellPattern& P, cudaStream_t s);   // structure only
+    void factor(cudaStream_t s, const SellPattern& P, const double* val);
+    void apply(cudaStream_t s, const double* r, double* z, const int* stop) override;
+    int num_levels_lower() const { return int(h_lptr_.size()) - 1; }
+    int num_levels_upper() const { return int(h_uptr_.size()) - 1; }
+
+private:
+    const SellPattern* P_ = nullptr;
+    DBuf<double> lu_;
+    std::vector<int> h_lptr_, h_uptr_;
+    DBuf<int> lrows_, urows_;
+    DBuf<int> status_;
+};
+
+// Helpers used by the solver front end.
+void device_copy(cudaStream_t s, void* dst, const void* src, size_t bytes);
+template <class TA, class TB>
+void convert(cudaStream_t s, long long n, const TA* a, TB* b);
+// x += y (FP64)
+void axpy_add(cudaStream_t s, int n, const double* y, double* x);
+// b = float(a * scale);  x += scale * double(y)
+void to_f32_scaled(cudaStream_t s, int n, const double* a, float* b, double scale);
+void add_f32_scaled(cudaStream_t s, int n, const float* y, double scale, double* x);
+// Dirichlet-row initial guess (IncompFlowSolverHybrid.hpp:1521-1532): x_i = b_i / a_ii
+// where all off-diagonal entries of row i are zero, else 0.
+void dirichlet_guess(cudaStream_t s, const SellPattern& P, const double* val, const double* b, double* x);
+// 2-norm of a vector (synchronous, FP64 accumulation)
+template <class T>
+double norm2(cudaStream_t s, int n, const T* x, RedScratch& red);
+
+}  // namespace porsol

@@ -1,0 +1,159 @@
+// porsol_internal.h -- shared host/device declarations of the GB300 porsol library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "porsol_gpu.h"
+
+namespace porsol {
+
+// ------------------------------------------------------------------ errors
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define PORSOL_CUDA(call)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            throw ::porsol::Error(PORSOL_ERR_CUDA, std::string(#call " failed: ") +          \
+                                                        cudaGetErrorString(e_));            \
+    } while (0)
+
+#define PORSOL_REQUIRE(cond, code, msg)                      \
+    do {                                                     \
+        if (!(cond)) throw ::porsol::Error((code), (msg));    \
+    } while (0)
+
+// Device status bits written by kernels (atomicOr) and mapped to porsol_status on the host.
+enum : int {
+    ST_NONFINITE = 1,     // NaN/Inf or non-positive pivot/mobility sum
+    ST_BREAKDOWN = 2,     // Krylov breakdown (zero curvature)
+    ST_SAT_RANGE = 4,     // saturation outside [-0.001, 1.001]
+    ST_CFL_ZERO = 8,      // CFL step of zero
+    ST_TIMEOUT = 16,      // bounded wait gave up
+    ST_BAD_INDEX = 32,    // index check failed
+};
+
+// ------------------------------------------------------------------ device buffers
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; o.p = nullptr; o.n = 0;
+        }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t cnt)
+    {
+        if (cnt == n && p) return;
+        release();
+        if (cnt == 0) return;
+        PORSOL_CUDA(cudaMalloc(&p, cnt * sizeof(T)));
+        n = cnt;
+    }
+    void upload(const T* h, size_t cnt, cudaStream_t s)
+    {
+        alloc(cnt);
+        if (cnt) PORSOL_CUDA(cudaMemcpyAsync(p, h, cnt * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T>& h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+    void download(T* h, size_t cnt, cudaStream_t s) const
+    {
+        if (cnt) PORSOL_CUDA(cudaMemcpyAsync(h, p, cnt * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    void zero(cudaStream_t s)
+    {
+        if (n) PORSOL_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+// ------------------------------------------------------------------ sparse matrices
+// Sliced ELLPACK with slice height 32 (one warp): row r lives in slice r/32, lane r%32;
+// entry t of row r is at slice_ptr[r/32] + 32*t + r%32.  Entries of a row are sorted by
+// column; padding entries carry col = row and value 0.
+constexpr int SELL_C = 32;
+
+struct SellPattern {
+    int n = 0;          // rows
+    int nslices = 0;
+    long long nent = 0; // stored entries incl. padding
+    std::vector<int> h_slice_ptr, h_col, h_rowlen;
+    DBuf<int> slice_ptr, col, rowlen, diag;   // diag: slot index of the diagonal
+    void upload(cudaStream_t s);
+};
+
+template <class T>
+struct SellMatrix {
+    const SellPattern* pat = nullptr;
+    DBuf<T> val;
+};
+
+// Build a SELL pattern from CSR with sorted columns.  csr2sell[k] = slot of CSR entry k.
+void build_sell(int n, const std::vector<int>& rowptr, const std::vector<int>& col, SellPattern& P,
+                std::vector<long long>* csr2sell);
+
+// ------------------------------------------------------------------ profiling
+enum ProfKernel { PK_SPMV64 = 0, PK_SPMV32 = 1, PK_ASSEMBLE = 2, PK_RECOVER = 3, PK_VCYCLE = 4, PK_COUNT = 5 };
+
+struct Profiler {
+    bool on = false;
+    int launches[PK_COUNT] = {0};
+    double ms[PK_COUNT] = {0};
+    double bytes[PK_COUNT] = {0};
+    struct Pending { cudaEvent_t a, b; int k; double bytes; };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t get();
+    void begin(cudaStream_t s, int k, double bytes, cudaEvent_t* out_a);
+    void end(cudaStream_t s, int k, double bytes, cudaEvent_t a);
+    void collect();    // synchronises on pending events
+    void reset();
+    ~Profiler();
+};
+
+struct ProfScope {
+    Profiler& P;
+    cudaStream_t s;
+    int k;
+    double bytes;
+    cudaEvent_t a = nullptr;
+    ProfScope(Profiler& p, cudaStream_t st, int kern, double b) : P(p), s(st), k(kern), bytes(b)
+    {
+        if (P.on) P.begin(s, k, bytes, &a);
+    }
+    ~ProfScope()
+    {
+        if (P.on && a) P.end(s, k, bytes, a);
+    }
+};
+
+// ------------------------------------------------------------------ launch helpers
+inline int div_up(long long a, int b) { return int((a + b - 1) / b); }
+
+}  // namespace porsol

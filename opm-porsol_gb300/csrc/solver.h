@@ -1,0 +1,71 @@
+// solver.h -- the pressure-solver handle behind the C ABI.
+#pragma once
+
+#include <memory>
+
+#include "amg.h"
+#include "kernels.h"
+#include "krylov.h"
+#include "structure.h"
+
+struct porsol_solver {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::string err;
+
+    bool structure_valid = false, ip_valid = false, solved = false;
+    porsol::Structure S;
+    int maxnf = 6, npk = 21;
+
+    // geometry / topology on the device
+    porsol::DBuf<int> facepos, cf, pairs;
+    porsol::DBuf<double> area, fcent, fnormal, cvol, ccent;
+    // static inner products
+    porsol::DBuf<double> perm, W, gflux;
+    bool gravity_zero = true;
+    porsol::DBuf<int> status;
+    porsol::DBuf<unsigned long long> redbits;
+
+    // assembly
+    porsol::Recipe R;
+    std::vector<int> recipe_types;   // boundary FlowBC types the recipe was built for
+    porsol::DBuf<int> recipe_types_d;
+    porsol::DBuf<double> sloc, F, L, g, rrow, pb, totmob, mobdens, rhs, x;
+    porsol::DBuf<double> val;
+    porsol::DBuf<float> val32;
+    bool reg_applied = false;
+
+    // host-API staging
+    porsol::DBuf<double> in_sat, in_mobdens, in_bcval, in_src;
+    porsol::DBuf<int> in_bctype;
+
+    // results
+    porsol::DBuf<double> pressure, outflux;
+    const double* last_src = nullptr;
+
+    // linear solvers
+    porsol::PcgSolver<double, double> cg64;
+    porsol::PcgSolver<float, float> cg32;
+    porsol::Ilu0 ilu;
+    bool ilu_levels = false;
+    porsol::Amg<double> amg64;
+    porsol::Amg<float> amg32;
+    bool amg_ready = false;
+    int amg_precision = -1;
+    porsol::DBuf<double> ir_r, ir_d;   // iterative refinement
+    porsol::DBuf<float> ir_r32, ir_d32;
+    porsol::RedScratch red;
+
+    porsol::Profiler prof;
+
+    void require_structure() const;
+    void init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
+    void compute_inner_products(const double* perm_h, const double* grav);
+    void solve(const porsol_fluid* fluid, const double* sat, const double* mobdens, const int* bct,
+               const double* bcv, const double* src, const porsol_solve_opts* opts, porsol_solve_stats* stats,
+               bool device_ptrs);
+    double post_process();
+    void check_status(const char* where);
+    void ensure_recipe(const int* bct_host, const int* bct_dev);
+    void linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st);
+};
