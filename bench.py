@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark: pressure solves/s of the mimetic hybrid solver at 1M cells on GB300.
+
+Workload (one step = one IncompFlowSolverHybrid::solve + postProcessFluxes):
+200 x 200 x 25 Cartesian grid (1,000,000 cells, 3,050,000 face unknowns), 25 layers with
+layer means ~ N(ln 100 mD, 1) and ln k ~ N(mean, 2^2) i.i.d. within a layer, Corey-2
+mobilities (viscosity ratio 10) at the initial state s = 0 of the IMPES run, Dirichlet
+p = 1 / p = 0 on x- / x+, AMG-preconditioned CG.  Synthetic inputs from a fixed seed.
+
+  value  = mixed-precision solves/s (FP32 SpMV + FP32 AMG inside FP64 iterative
+           refinement) with inputs resident in HBM, all ranks together;
+  fp64   = the plain FP64 drop-in on the same inputs;
+  e2e    = the same metric through the host-pointer C ABI (inputs copied H2D and the
+           solution D2H inside the timed region);
+  flux error of both against an FP64 solve at a 1e-12 residual reduction.
+
+--impl reference times the reference algorithm's own CPU path restated in the oracle
+(serial FP64 ILU0-CG, the reference's linsolver_type 0) on a bounded sample of the same
+solve and scales it to solves/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Pressure solves/s @1M cells, 1e-8 rel flux err: mixed-prec vs FP64 on GB300"
+UNIT = "pressure solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--dims", default="200,200,25")
+    ap.add_argument("--tol", type=float, default=1e-9, help="residual reduction of the timed solves")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle)
+def cpu_oracle(prob):
+    import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    o = oracle.OraclePressure(prob.grid, prob.bc_type)
+    o.compute_inner_products(prob.perm.ravel())
+    return o
+
+
+def cpu_sample(prob, o=None, sample_iters=6):
+    """Serial FP64 oracle (ILU0-CG, the reference's linsolver_type 0 path) on the full-size
+    system: one assembly + ILU0 factorisation + `sample_iters` CG iterations + recovery,
+    scaled to a complete solve with the recorded iteration count of that solve."""
+    gold = os.path.join(ROOT, "tests", "golden", "oracle_case5_ilu0.json")
+    iters_full = None
+    if os.path.exists(gold) and prob.grid.dims == (200, 200, 25):
+        iters_full = json.load(open(gold))["results"]["1e-08"]["iterations"]
+    o = o if o is not None else cpu_oracle(prob)
+    tm, md = prob.mobilities()
+    rc, t_fix, t_fac, t_cg = o.solve_timed(tm, md, prob.bc_type, prob.bc_value, prob.src, tol=1e-8,
+                                           maxit=sample_iters, dirichlet_guess=True)
+    return dict(t_fixed=t_fix, t_factor=t_fac, t_cg=t_cg, iters=o.iterations, iters_full=iters_full)
+
+
+def cpu_value(s):
+    """solves/s from a sample: assembly + recovery + ILU0 factorisation + iters_full times the
+    measured cost of one CG iteration."""
+    if not s["iters_full"]:
+        return None
+    per_it = s["t_cg"] / max(s["iters"], 1)
+    return 1.0 / (s["t_fixed"] + s["t_factor"] + per_it * s["iters_full"])
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    wl = ge.load_module("workloads")
+    dims = tuple(int(x) for x in args.dims.split(","))
+    prob = wl.case5(dims=dims)
+    o = cpu_oracle(prob)
+    vals = []
+    for k in range(args.warmup + args.steps):
+        s = cpu_sample(prob, o)
+        v = cpu_value(s)
+        if k >= args.warmup:
+            vals.append(v)
+    v = float(np.median(vals)) if vals and vals[0] is not None else None
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "pressure solve, 200x200x25 layered log-normal (1M cells, 3.05M face unknowns)",
+                   "dims": list(dims), "solver": "ILU0-CG (reference linsolver_type 0), serial FP64"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "per step: assembly + ILU0 factorisation + 6 CG iterations + recovery on the "
+                                   "full system, scaled by the recorded full-solve iteration count"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+    rank, world, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    if not os.path.exists(pkg.LIB_PATH):
+        pkg.build()
+    wl = ge.load_module("workloads")
+    dims = tuple(int(x) for x in args.dims.split(","))
+    prob = wl.case5(dims=dims)
+    g = prob.grid
+    nc, nhf = g.num_cells, g.num_half_faces
+    model, mu1, mu2, r1, r2 = prob.fluid
+    fluid = pkg.Fluid(model, mu1, mu2, r1, r2)
+
+    s = pkg.PressureSolver()
+    t0 = time.time()
+    s.init(g, prob.perm.ravel(), (0.0, 0.0, 0.0), prob.bc_type)
+    init_s = time.time() - t0
+    stream = torch.cuda.ExternalStream(s.stream())
+    dev = torch.device("cuda", local)
+    d_sat = torch.from_numpy(prob.sat).to(dev)
+    d_bct = torch.from_numpy(prob.bc_type.astype(np.int32)).to(dev)
+    d_bcv = torch.from_numpy(prob.bc_value).to(dev)
+    d_src = torch.from_numpy(prob.src).to(dev)
+    torch.cuda.synchronize()
+
+    def opts(prec, tol=None):
+        return pkg.default_solve_opts(linsolver_type=1, residual_tolerance=tol or args.tol, precision=prec)
+
+    def step_device(o):
+        st = s.solve_device(fluid, d_sat.data_ptr(), d_bct.data_ptr(), d_bcv.data_ptr(), d_src.data_ptr(), opts=o)
+        s.post_process_fluxes()
+        return st
+
+    # FP64 reference solution for the error figures (not timed)
+    step_device(opts(pkg.FP64, 1e-12))
+    _, v_ref, pi_ref = s.solution()
+    p_ref = s.solution()[0]
+
+    def timed(prec, profile=False):
+        o = opts(prec)
+        for _ in range(args.warmup):
+            step_device(o)
+        s.profile_reset()
+        s.profile_enable(profile)
+        barrier(dist)
+        torch.cuda.synchronize()
+        l0 = pkg.lib().porsol_launch_count()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        st = None
+        for _ in range(args.steps):
+            st = step_device(o)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        launches = pkg.lib().porsol_launch_count() - l0
+        ms = ev0.elapsed_time(ev1)
+        s.profile_enable(False)
+        ms = max_over_ranks(dist, ms)
+        p, v, _ = s.solution()
+        err_v = float(np.linalg.norm(v - v_ref) / np.linalg.norm(v_ref))
+        err_p = float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref))
+        return dict(ms=ms, st=st, launches=launches, err_v=err_v, err_p=err_p)
+
+    clk = ClockSampler(local)
+    clk.start()
+    mixed = timed(pkg.MIXED, profile=True)
+    prof = {k: s.profile_get(k) for k in range(6)}
+    clocks = clk.stop()
+    fp64 = timed(pkg.FP64)
+
+    # end to end through the host-pointer C ABI
+    o = opts(pkg.MIXED)
+    pres = np.empty(nc)
+    flux = np.empty(nhf)
+    for _ in range(max(1, args.warmup // 2)):
+        s.solve(fluid, prob.sat, prob.bc_type, prob.bc_value, prob.src, opts=o)
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.solve(fluid, prob.sat, prob.bc_type, prob.bc_value, prob.src, opts=o)
+        s.post_process_fluxes()
+        pkg.lib().porsol_get_solution(s.h, pres.ctypes.data, flux.ctypes.data, None)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    h2d = prob.sat.nbytes + prob.bc_type.astype(np.int32).nbytes + prob.bc_value.nbytes + prob.src.nbytes
+    d2h = pres.nbytes + flux.nbytes
+
+    # dominant kernel: finest-level Chebyshev smoothing step (FP32)
+    pk = peaks()
+    hbm = pk["hbm_gbs"] if pk else 6800.0
+    n_cheb, ms_cheb, bytes_cheb = prof[5]
+    roof = None
+    if n_cheb:
+        achieved = (bytes_cheb / n_cheb) / (ms_cheb / n_cheb * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_cheb_step<float> (finest AMG level)", "achieved": round(achieved, 1),
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                "traffic": None, "launches": n_cheb, "avg_us": round(ms_cheb / n_cheb * 1e3, 2),
+                "algorithmic_bytes_per_launch": bytes_cheb / n_cheb,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"}
+        tr = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tr):
+            roof["traffic"] = json.load(open(tr)).get("k_cheb_step_float_bytes_per_launch")
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            smp = cpu_sample(prob)
+            v = cpu_value(smp)
+            cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": "serial FP64 oracle ILU0-CG (reference linsolver_type 0) on the full system: "
+                             f"assembly + ILU0 factorisation + {smp['iters']} CG iterations + recovery, scaled "
+                             f"to the recorded {smp['iters_full']} iterations of the full solve"}
+        except Exception as e:  # the baseline must not break the GPU measurement
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+
+    ms_mixed = mixed["ms"] / args.steps
+    value = world * args.steps / (mixed["ms"] * 1e-3)
+    v64 = world * args.steps / (fp64["ms"] * 1e-3)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_mixed, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "pressure solve + postProcessFluxes, 200x200x25 layered log-normal sigma=2 "
+                               "(1M cells, 3.05M face unknowns), Corey-2 mobilities at s=0, AMG-CG",
+                   "dims": list(dims), "cells": nc, "face_unknowns": s.n, "nnz": s.nnz,
+                   "residual_tolerance": args.tol, "precision": "FP32 SpMV/AMG in FP64 iterative refinement",
+                   "l2": "inputs larger than L2 (FP64 matrix 400 MB, FP32 copy 270 MB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "init_s": round(init_s, 3)},
+        "flux_rel_err_vs_fp64": mixed["err_v"], "pressure_rel_err_vs_fp64": mixed["err_p"],
+        "iterations": mixed["st"].iterations, "outer_iterations": mixed["st"].outer_iterations,
+        "amg_levels": mixed["st"].amg_levels, "mass_balance": mixed["st"].mass_balance,
+        "fp64": {"value": round(v64, 3), "ms_per_step": round(fp64["ms"] / args.steps, 3),
+                 "iterations": fp64["st"].iterations, "flux_rel_err_vs_tight": fp64["err_v"]},
+        "speedup_mixed_vs_fp64": round(value / v64, 3),
+        "e2e": {"value": round(world * args.steps / e2e_s, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(mixed["launches"]),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "profile_ms_per_step": {name: round(prof[k][1] / args.steps, 3) for k, name in
+                                enumerate(["spmv64", "spmv32", "assemble", "recover", "vcycle", "cheb_fine"])},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -211,11 +211,14 @@ int porsol_transport_solve_device(porsol_transport* t, double* sat, double time,
 /* Per-kernel CUDA-event timing on the handle's stream (off by default). */
 int porsol_profile_enable(porsol_solver* h, int enable);
 /* Accumulated launches and milliseconds of one kernel class since the last reset.
- * kernel: 0 = SpMV (FP64), 1 = SpMV (FP32), 2 = assembly, 3 = recovery, 4 = V-cycle. */
+ * kernel: 0 = CG SpMV (FP64), 1 = CG SpMV (FP32), 2 = assembly, 3 = recovery,
+ * 4 = whole AMG V-cycle, 5 = finest-level Chebyshev smoothing step. */
 int porsol_profile_get(porsol_solver* h, int kernel, int* launches, double* ms, double* bytes);
 int porsol_profile_reset(porsol_solver* h);
 /* The handle's CUDA stream (cudaStream_t) for callers that time around calls. */
 void* porsol_stream(porsol_solver* h);
+/* Number of kernel launches this library has issued in the process so far. */
+long long porsol_launch_count(void);
 
 #ifdef __cplusplus
 }

@@ -138,6 +138,7 @@ EXPORTS = [
     ("porsol_profile_get", _i, [_vp, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_d)]),
     ("porsol_profile_reset", _i, [_vp]),
     ("porsol_stream", _vp, [_vp]),
+    ("porsol_launch_count", C.c_longlong, []),
 ]
 
 _lib = None

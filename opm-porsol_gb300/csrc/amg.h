@@ -1,16 +1,20 @@
 // amg.h -- aggregation AMG preconditioner on the GPU (replaces dune-istl Amg::AMG).
 //
 // The reference preconditions CG with dune-istl's aggregation AMG (unsmoothed
-// piecewise-constant prolongation, prolongation damping factor `prolongate_factor`,
-// `smooth_steps` pre/post sweeps; IncompFlowSolverHybrid.hpp:1481-1541).  This is a GPU
-// design of the same method class: each level coarsens by two rounds of parallel pairwise
-// matching on the symmetric strength |a_ij| / sqrt(a_ii a_jj) (aggregates of up to 4
-// rows), Galerkin coarse matrices P^T A P computed row-by-row without atomics
-// (deterministic), l1-Jacobi smoothing (symmetric, so the V-cycle is a symmetric
-// preconditioner for CG), the coarse correction scaled by the prolongation damping
-// factor, and an exact FP64 solve on the coarsest level (explicit inverse from a
-// Cholesky factorisation).  The hierarchy values are type T (double or float); the
-// coarsest level is always FP64.
+// piecewise-constant prolongation, coarse correction scaled by `prolongate_factor`,
+// `smooth_steps` pre/post smoothing steps; IncompFlowSolverHybrid.hpp:1481-1541).  This is
+// a GPU design of the same method class:
+//   * rows without off-diagonal couplings (Dirichlet rows) are not aggregated;
+//   * each level coarsens by two rounds of parallel pairwise matching on the strength of
+//     negative couplings -a_ij / sqrt(a_ii a_jj) >= 0.25; a round that stalls (keeps more
+//     than 80% of its rows) is redone on |a_ij| and lets unmatched rows join the aggregate
+//     of their strongest matched neighbour;
+//   * Galerkin coarse matrices P^T A P are merged row by row without atomics
+//     (deterministic, run-to-run reproducible);
+//   * the smoother is a degree-2 Chebyshev polynomial in D^-1 A on [G/30, G], G the
+//     Gershgorin bound of D^-1 A (symmetric, so the V-cycle is a valid CG preconditioner);
+//   * the coarsest level is solved exactly in FP64 (explicit inverse from a Cholesky
+//     factorisation), whatever the precision T of the hierarchy.
 #pragma once
 
 #include "krylov.h"
@@ -18,11 +22,18 @@
 namespace porsol {
 
 struct AmgOpts {
-    int smooth_steps = 1;
-    double prolong = 1.6;
+    int smooth_steps = 1;       // Chebyshev applications before and after the coarse correction
+    double prolong = 1.6;       // coarse-correction damping (dune-istl prolongation damping factor)
     int coarse_target = 128;
     int max_levels = 24;
-    double strength = 0.08;
+    double strength = 0.25;
+    int cheb_degree = 2;
+};
+
+// Device aggregation result: agg (row -> aggregate or -1), members CSR (aggregate -> rows).
+struct Aggregates {
+    int n = 0, nc = 0;
+    DBuf<int> agg, ptr, idx;
 };
 
 template <class T>
@@ -30,52 +41,50 @@ class Amg : public Precond<T> {
 public:
     void setup(cudaStream_t s, const SellPattern& P0, const T* A0, const AmgOpts& o);
     void apply(cudaStream_t s, const T* r, T* z, const int* stop) override;
-    int levels() const { return int(lv_.size()) + 1; }
-    int coarse_n() const { return nc_; }
+    int levels() const { return int(lv_.size()); }
+    void set_profiler(Profiler* p) { prof_ = p; }
     const std::vector<int>& level_sizes() const { return sizes_; }
-    // SELL entries per level (fine level first)
     const std::vector<long long>& level_nnz() const { return nnzs_; }
-    ~Amg();
 
 private:
     struct Level {
-        int n = 0;                       // rows of this level
-        const SellPattern* P = nullptr;  // this level's matrix
+        int n = 0;
+        const SellPattern* P = nullptr;
         const T* A = nullptr;
-        SellPattern own;                 // storage for levels > 0
+        SellPattern own;
         DBuf<T> own_val;
-        DBuf<T> dinv;                    // l1-Jacobi inverse diagonal
-        DBuf<int> agg;                   // row -> coarse row of the next level
-        DBuf<int4> children;             // next-level row -> up to 4 rows of this level
-        DBuf<T> x, b, r;                 // work vectors (level 0 uses the caller's r/z)
+        DBuf<T> dinv;
+        double lmax = 2.0;
+        Aggregates agg;              // to the next level
+        DBuf<T> t, r, d0, d1, b, x;  // work vectors
     };
-    void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, double theta, DBuf<int>& agg,
-                  DBuf<int2>& kids, int& ncoarse);
-    void galerkin_pairs(cudaStream_t s, const SellPattern& P, const T* A, int n, const int* agg, const int2* kids,
-                        int ncoarse, SellPattern& Pc, DBuf<T>& Ac);
+    void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, Aggregates& out);
+    void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
+                  Aggregates& out);
+    void members(cudaStream_t s, Aggregates& a);
+    void galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Aggregates& a, SellPattern& Pc,
+                  DBuf<T>& Ac);
+    void smoother_setup(cudaStream_t s, Level& L);
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);
+    void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
+                   const int* stop);
     void vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop);
 
     AmgOpts o_;
+    Profiler* prof_ = nullptr;
     std::vector<std::unique_ptr<Level>> lv_;
     std::vector<int> sizes_;
     std::vector<long long> nnzs_;
-    // coarsest level: dense FP64 inverse
     int nc_ = 0;
-    const SellPattern* Pc_ = nullptr;
-    const T* Ac_ = nullptr;
     DBuf<double> cinv_;
     DBuf<int> status_;
-    // scratch
-    DBuf<int> best_, state_, flag_, scan_;
-    DBuf<int> tmp_agg_;
-    DBuf<int2> tmp_kids_;
+    DBuf<int> scan_blocks_, iscratch_;
+    DBuf<double> dscratch_;
     SellPattern tmp_pat_;
     DBuf<T> tmp_val_;
-    DBuf<int> scan_blocks_;
 };
 
-// Exclusive prefix sum of n ints on the device; total (if not null) written to *total_dev.
+// Exclusive prefix sum of n ints on the device; the total is written to *total_dev.
 void exclusive_scan(cudaStream_t s, int n, const int* in, int* out, int* total_dev, DBuf<int>& scratch);
 
 }  // namespace porsol

@@ -18,6 +18,8 @@ using namespace porsol;
 // ---------------------------------------------------------------- profiler
 namespace porsol {
 
+std::atomic<long long> g_launches{0};
+
 cudaEvent_t Profiler::get()
 {
     if (!pool.empty()) {
@@ -104,6 +106,8 @@ void porsol_solver::check_status(const char* where)
 
 void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
 {
+    amg64.set_profiler(&prof);
+    amg32.set_profiler(&prof);
     structure_valid = ip_valid = solved = false;
     R.valid = false;
     amg_ready = false;
@@ -646,5 +650,7 @@ int porsol_profile_reset(porsol_solver* h)
 }
 
 void* porsol_stream(porsol_solver* h) { return h ? (void*)h->stream : nullptr; }
+
+long long porsol_launch_count(void) { return porsol::g_launches.load(); }
 
 }  // extern "C"

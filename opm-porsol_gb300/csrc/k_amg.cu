@@ -1,8 +1,9 @@
-// k_amg.cu -- aggregation AMG: pairwise matching, Galerkin products, V-cycle kernels,
-// FP64 dense coarsest-level solve.  Every reduction is ordered (no floating-point
-// atomics), so the hierarchy and the preconditioner are run-to-run reproducible.
+// k_amg.cu -- aggregation AMG: pairwise matching, Galerkin products, Chebyshev V-cycle,
+// FP64 dense coarsest-level solve.  Every floating-point reduction has a fixed order (no
+// floating-point atomics), so hierarchy and preconditioner are run-to-run reproducible.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "amg.h"
 
@@ -11,7 +12,6 @@ namespace porsol {
 namespace {
 
 constexpr int TB = 256;
-constexpr int GAL_CAP = 160;   // max entries of a merged coarse row
 
 __device__ __forceinline__ int slot_of(const int* sp, int r, int t) { return sp[r >> 5] + t * 32 + (r & 31); }
 
@@ -35,7 +35,6 @@ __global__ void k_scan_block(int n, const int* __restrict__ in, int* __restrict_
 
 __global__ void k_scan_sums(int nb, int* bsum, int* total)
 {
-    // single block: sequential chunks, exclusive in place
     __shared__ int sh[1024];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -65,18 +64,36 @@ __global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__
     if (i < n) out[i] += bsum[blockIdx.x];
 }
 
-// ---------------- matching ----------------
+// ---------------- aggregation ----------------
 template <class T>
-__global__ void k_diag_vals(int n, const int* __restrict__ diag, const T* __restrict__ A, double* __restrict__ d)
+__global__ void k_diag_abs(int n, const int* __restrict__ diag, const T* __restrict__ A, double* __restrict__ d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) d[i] = fabs(double(A[diag[i]]));
 }
 
+// state: 0 free, 1 paired, 2 isolated (no off-diagonal coupling: never aggregated)
+template <class T>
+__global__ void k_isolated(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                           const int* __restrict__ rowlen, const T* __restrict__ A, int* __restrict__ state,
+                           int* __restrict__ partner, int* __restrict__ join)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool iso = true;
+    for (int t = 0; t < rowlen[i]; ++t) {
+        const int k = slot_of(sp, i, t);
+        if (col[k] != i && A[k] != T(0)) iso = false;
+    }
+    state[i] = iso ? 2 : 0;
+    partner[i] = -1;
+    join[i] = -1;
+}
+
 template <class T>
 __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
                        const T* __restrict__ A, const double* __restrict__ d, const int* __restrict__ state,
-                       int* __restrict__ best, double theta)
+                       int* __restrict__ best, int neg, double theta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -85,14 +102,15 @@ __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict_
         return;
     }
     const double di = d[i];
-    double bs = -1.0;
+    double bs = 0.0;
     int bj = -1;
     for (int t = 0; t < rowlen[i]; ++t) {
         const int k = slot_of(sp, i, t);
         const int j = col[k];
         if (j == i || state[j] != 0) continue;
-        const double s = fabs(double(A[k])) / sqrt(di * d[j]);
-        if (s >= theta && (s > bs || (s == bs && j < bj))) {
+        const double a = double(A[k]);
+        const double s = (neg ? -a : fabs(a)) / sqrt(di * d[j]);
+        if (s > 0.0 && s >= theta && (s > bs || (s == bs && j < bj))) {
             bs = s;
             bj = j;
         }
@@ -111,53 +129,124 @@ __global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ 
     }
 }
 
-__global__ void k_rep_flag(int n, const int* __restrict__ state, const int* __restrict__ partner, int* __restrict__ flag)
+// unmatched rows pick their strongest paired neighbour (|a_ij| scaled)
+template <class T>
+__global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
+                       const T* __restrict__ A, const double* __restrict__ d, const int* __restrict__ state,
+                       int* __restrict__ join)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || state[i] != 0) return;
+    const double di = d[i];
+    double bs = 0.0;
+    int bj = -1;
+    for (int t = 0; t < rowlen[i]; ++t) {
+        const int k = slot_of(sp, i, t);
+        const int j = col[k];
+        if (j == i || state[j] != 1) continue;
+        const double s = fabs(double(A[k])) / sqrt(di * d[j]);
+        if (s > 0.0 && (s > bs || (s == bs && j < bj))) {
+            bs = s;
+            bj = j;
+        }
+    }
+    join[i] = bj;
+}
+
+__global__ void k_rep_flag(int n, const int* __restrict__ state, const int* __restrict__ partner,
+                           const int* __restrict__ join, int* __restrict__ flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    flag[i] = (state[i] == 0 || i < partner[i]) ? 1 : 0;
+    flag[i] = ((state[i] == 0 && join[i] < 0) || (state[i] == 1 && i < partner[i])) ? 1 : 0;
 }
 
 __global__ void k_assign(int n, const int* __restrict__ state, const int* __restrict__ partner,
-                         const int* __restrict__ flag, const int* __restrict__ cidx, int* __restrict__ agg,
-                         int2* __restrict__ kids)
+                         const int* __restrict__ join, const int* __restrict__ flag, const int* __restrict__ cidx,
+                         int* __restrict__ agg)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (flag[i]) {
-        const int I = cidx[i];
-        agg[i] = I;
-        kids[I] = make_int2(i, state[i] ? partner[i] : -1);
-    } else {
-        agg[i] = cidx[partner[i]];
+    const int st = state[i];
+    int a;
+    if (st == 2) a = -1;
+    else if (flag[i]) a = cidx[i];
+    else if (st == 1) a = cidx[partner[i]];
+    else {
+        const int t = join[i];
+        a = cidx[min(t, partner[t])];
+    }
+    agg[i] = a;
+}
+
+__global__ void k_compose(int n, int* __restrict__ agg1, const int* __restrict__ agg2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int a = agg1[i];
+        agg1[i] = a < 0 ? -1 : agg2[a];
     }
 }
 
-// ---------------- Galerkin products over pairs ----------------
-// Merge the rows of the (<=2) children, mapping columns through agg; sorted unique keys.
-template <class T>
+__global__ void k_count_members(int n, const int* __restrict__ agg, int* __restrict__ cnt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && agg[i] >= 0) atomicAdd(&cnt[agg[i]], 1);
+}
+
+__global__ void k_fill_members(int n, const int* __restrict__ agg, int* __restrict__ pos, int* __restrict__ idx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && agg[i] >= 0) idx[atomicAdd(&pos[agg[i]], 1)] = i;
+}
+
+__global__ void k_sort_members(int nc, const int* __restrict__ ptr, int* __restrict__ idx)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    const int b = ptr[I], e = ptr[I + 1];
+    for (int p = b + 1; p < e; ++p) {
+        const int key = idx[p];
+        int q = p - 1;
+        while (q >= b && idx[q] > key) {
+            idx[q + 1] = idx[q];
+            --q;
+        }
+        idx[q + 1] = key;
+    }
+}
+
+// ---------------- Galerkin products ----------------
+__global__ void k_gal_bound(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
+                            const int* __restrict__ rowlen, int* __restrict__ maxb)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = 0;
+    if (I < nc)
+        for (int q = ptr[I]; q < ptr[I + 1]; ++q) b += rowlen[idx[q]];
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxb, b);
+}
+
+// Merge the member rows of aggregate I, mapping columns through agg (isolated columns,
+// agg < 0, carry no coupling and are skipped): sorted unique keys with summed values.
+template <class T, int CAP>
 __device__ int merge_rows(const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
-                          const T* __restrict__ A, const int* __restrict__ agg, int2 kid, int* kc, double* kv,
-                          bool* overflow)
+                          const T* __restrict__ A, const int* __restrict__ agg, const int* __restrict__ ptr,
+                          const int* __restrict__ idx, int I, int* kc, double* kv)
 {
     int m = 0;
-    const int ch[2] = {kid.x, kid.y};
-    for (int q = 0; q < 2; ++q) {
-        const int r = ch[q];
-        if (r < 0) continue;
+    for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
+        const int r = idx[q];
         for (int t = 0; t < rowlen[r]; ++t) {
             const int k = slot_of(sp, r, t);
             const int c = agg[col[k]];
+            if (c < 0) continue;
             const double v = double(A[k]);
-            // insertion into sorted kc[0..m)
             int pos = m;
             while (pos > 0 && kc[pos - 1] > c) --pos;
             if (pos > 0 && kc[pos - 1] == c) {
                 kv[pos - 1] += v;
-                continue;
-            }
-            if (m >= GAL_CAP) {
-                *overflow = true;
                 continue;
             }
             for (int u = m; u > pos; --u) {
@@ -166,48 +255,35 @@ __device__ int merge_rows(const int* __restrict__ sp, const int* __restrict__ co
             }
             kc[pos] = c;
             kv[pos] = v;
-            ++m;
+            ++m;   // m <= CAP: the host picks CAP >= sum of member row lengths
         }
     }
     return m;
 }
 
-template <class T>
+template <class T, int CAP>
 __global__ void k_gal_count(int nc, const int* __restrict__ sp, const int* __restrict__ col,
                             const int* __restrict__ rowlen, const T* __restrict__ A, const int* __restrict__ agg,
-                            const int2* __restrict__ kids, int* __restrict__ rowlen_c, int* status)
+                            const int* __restrict__ ptr, const int* __restrict__ idx, int* __restrict__ rowlen_c)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= nc) return;
-    int kc[GAL_CAP];
-    double kv[GAL_CAP];
-    bool of = false;
-    const int m = merge_rows(sp, col, rowlen, A, agg, kids[I], kc, kv, &of);
-    if (of) atomicOr(status, ST_BAD_INDEX);
-    rowlen_c[I] = m;
+    int kc[CAP];
+    double kv[CAP];
+    rowlen_c[I] = merge_rows<T, CAP>(sp, col, rowlen, A, agg, ptr, idx, I, kc, kv);
 }
 
-__global__ void k_slice_width(int n, int nslices, const int* __restrict__ rowlen, int* __restrict__ width)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nslices) return;
-    int w = 0;
-    for (int r = s * 32; r < min(n, s * 32 + 32); ++r) w = max(w, rowlen[r]);
-    width[s] = w * 32;
-}
-
-template <class T>
+template <class T, int CAP>
 __global__ void k_gal_fill(int nc, const int* __restrict__ sp, const int* __restrict__ col,
                            const int* __restrict__ rowlen, const T* __restrict__ A, const int* __restrict__ agg,
-                           const int2* __restrict__ kids, const int* __restrict__ sp_c, int* __restrict__ col_c,
-                           T* __restrict__ val_c, int* __restrict__ diag_c)
+                           const int* __restrict__ ptr, const int* __restrict__ idx, const int* __restrict__ sp_c,
+                           int* __restrict__ col_c, T* __restrict__ val_c, int* __restrict__ diag_c)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= nc) return;
-    int kc[GAL_CAP];
-    double kv[GAL_CAP];
-    bool of = false;
-    const int m = merge_rows(sp, col, rowlen, A, agg, kids[I], kc, kv, &of);
+    int kc[CAP];
+    double kv[CAP];
+    const int m = merge_rows<T, CAP>(sp, col, rowlen, A, agg, ptr, idx, I, kc, kv);
     const int s = I >> 5;
     const int w = (sp_c[s + 1] - sp_c[s]) >> 5;
     int dslot = -1;
@@ -225,9 +301,18 @@ __global__ void k_gal_fill(int nc, const int* __restrict__ sp, const int* __rest
     diag_c[I] = dslot;
 }
 
-// padding rows of the last slice beyond nc
+__global__ void k_slice_width(int n, int nslices, const int* __restrict__ rowlen, int* __restrict__ width)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int w = 0;
+    for (int r = s * 32; r < min(n, s * 32 + 32); ++r) w = max(w, rowlen[r]);
+    width[s] = w * 32;
+}
+
+template <class T>
 __global__ void k_pad_tail(int nc, int nslices, const int* __restrict__ sp_c, int* __restrict__ col_c,
-                           void* val_c_raw, int elem)
+                           T* __restrict__ val_c)
 {
     const int lane = threadIdx.x;
     const int s = nslices - 1;
@@ -237,63 +322,132 @@ __global__ void k_pad_tail(int nc, int nslices, const int* __restrict__ sp_c, in
     for (int t = 0; t < w; ++t) {
         const int k = sp_c[s] + t * 32 + lane;
         col_c[k] = 0;
-        if (elem == 8) ((double*)val_c_raw)[k] = 0.0;
-        else ((float*)val_c_raw)[k] = 0.0f;
+        val_c[k] = T(0);
     }
+}
+
+__global__ void k_check_diag(int n, const int* __restrict__ diag, int* status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && diag[i] < 0) atomicOr(status, ST_BAD_INDEX);
+}
+
+// ---------------- Chebyshev smoother ----------------
+// dinv = 1/a_ii and the Gershgorin bound max_i sum_j |a_ij| / a_ii of D^-1 A
+template <class T>
+__global__ void k_cheb_setup(int n, const int* __restrict__ sp, const int* __restrict__ rowlen,
+                             const int* __restrict__ diag, const T* __restrict__ A, T* __restrict__ dinv,
+                             unsigned long long* gmax, int* status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double g = 0.0;
+    if (i < n) {
+        const double a = double(A[diag[i]]);
+        double s = 0.0;
+        for (int t = 0; t < rowlen[i]; ++t) s += fabs(double(A[slot_of(sp, i, t)]));
+        if (!(a > 0.0) || !isfinite(s)) {
+            atomicOr(status, ST_NONFINITE);
+        } else {
+            dinv[i] = T(1.0 / a);
+            g = s / a;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) g = fmax(g, __shfl_xor_sync(0xffffffffu, g, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(gmax, (unsigned long long)__double_as_longlong(g));
+}
+
+// start from x = 0: r = D^-1 b, d = r / theta
+template <class T>
+__global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ r,
+                              T* __restrict__ d, T inv_theta, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T ri = dinv[i] * b[i];
+    r[i] = ri;
+    d[i] = ri * inv_theta;
+}
+
+// start from y = t + w P xc (xc may be null: y = t): x = y, r = D^-1 (b - A y), d = r / theta
+template <class T>
+__global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                             const T* __restrict__ A, const T* __restrict__ dinv, const T* __restrict__ b,
+                             const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg, T wp,
+                             T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, T inv_theta, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = i >> 5, lane = i & 31;
+    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
+    T acc = 0;
+    int k = base + lane;
+    if (xc) {
+        for (int q = 0; q < w; ++q, k += 32) {
+            const int j = col[k];
+            const int aj = agg[j];
+            acc += A[k] * (t[j] + (aj >= 0 ? wp * xc[aj] : T(0)));
+        }
+        const int ai = agg[i];
+        x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
+    } else {
+        for (int q = 0; q < w; ++q, k += 32) acc += A[k] * t[col[k]];
+    }
+    const T ri = dinv[i] * (b[i] - acc);
+    r[i] = ri;
+    d[i] = ri * inv_theta;
+}
+
+// x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
+template <class T>
+__global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
+                            const T* __restrict__ dinv, const T* x_in, const T* __restrict__ d_in, T* __restrict__ r,
+                            T* __restrict__ d_out, T* x_out, T c1, T c2, int final_step, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = i >> 5, lane = i & 31;
+    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
+    T acc = 0;
+    int k = base + lane;
+    for (int q = 0; q < w; ++q, k += 32) acc += A[k] * d_in[col[k]];
+    const T di = d_in[i];
+    T xi = (x_in ? x_in[i] : T(0)) + di;
+    const T ri = r[i] - dinv[i] * acc;
+    const T dn = c1 * di + c2 * ri;
+    if (final_step) xi += dn;
+    r[i] = ri;
+    d_out[i] = dn;
+    x_out[i] = xi;
 }
 
 template <class T>
-__global__ void k_l1_dinv(int n, const int* __restrict__ sp, const int* __restrict__ rowlen, const T* __restrict__ A,
-                          T* __restrict__ dinv, int* status)
+__global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
+                        const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
+    if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double s = 0.0;
-    for (int t = 0; t < rowlen[i]; ++t) s += fabs(double(A[slot_of(sp, i, t)]));
-    if (!(s > 0.0) || !isfinite(s)) {
-        atomicOr(status, ST_NONFINITE);
-        s = 1.0;
-    }
-    dinv[i] = T(1.0 / s);
+    const int s = i >> 5, lane = i & 31;
+    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
+    T acc = 0;
+    int k = base + lane;
+    for (int t = 0; t < w; ++t, k += 32) acc += A[k] * x[col[k]];
+    r[i] = b[i] - acc;
 }
 
-__global__ void k_compose(int n, int* __restrict__ agg1, const int* __restrict__ agg2)
+template <class T>
+__global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __restrict__ idx, const T* __restrict__ r,
+                           T* __restrict__ bc, const int* stop)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) agg1[i] = agg2[agg1[i]];
-}
-
-__global__ void k_kids4(int nc2, const int2* __restrict__ kids2, const int2* __restrict__ kids1, int4* __restrict__ out)
-{
+    if (*stop) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc2) return;
-    int v[4] = {-1, -1, -1, -1};
-    int m = 0;
-    const int2 a = kids2[I];
-    const int mids[2] = {a.x, a.y};
-    for (int q = 0; q < 2; ++q) {
-        if (mids[q] < 0) continue;
-        const int2 b = kids1[mids[q]];
-        if (b.x >= 0) v[m++] = b.x;
-        if (b.y >= 0) v[m++] = b.y;
-    }
-    // sort ascending (m <= 4), -1 last
-    for (int p = 1; p < m; ++p) {
-        const int key = v[p];
-        int q = p - 1;
-        while (q >= 0 && v[q] > key) {
-            v[q + 1] = v[q];
-            --q;
-        }
-        v[q + 1] = key;
-    }
-    out[I] = make_int4(v[0], v[1], v[2], v[3]);
-}
-
-__global__ void k_kids2to4(int nc, const int2* __restrict__ k2, int4* __restrict__ out)
-{
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I < nc) out[I] = make_int4(k2[I].x, k2[I].y, -1, -1);
+    if (I >= nc) return;
+    T s = 0;
+    for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
+    bc[I] = s;
 }
 
 // ---------------- coarsest level ----------------
@@ -331,7 +485,6 @@ __global__ void k_dense_cholesky_inverse(int n, double* __restrict__ D, double* 
         }
         __syncthreads();
     }
-    // Linv: column j by thread j
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
         for (int i = 0; i < n; ++i) Linv[(size_t)i * n + j] = 0.0;
         for (int i = j; i < n; ++i) {
@@ -357,7 +510,6 @@ __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* _
     extern __shared__ double sb[];
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
     __syncthreads();
-    // one warp per row
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int i = warp; i < n; i += nw) {
         double s = 0.0;
@@ -366,104 +518,6 @@ __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* _
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) x[i] = T(s);
     }
-}
-
-// ---------------- V-cycle kernels ----------------
-template <class T>
-__global__ void k_jacobi0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ x,
-                          const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] = dinv[i] * b[i];
-}
-
-// xo = x + dinv (b - A x)
-template <class T>
-__global__ void k_jacobi(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
-                         const T* __restrict__ dinv, const T* __restrict__ b, const T* __restrict__ x,
-                         T* __restrict__ xo, const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
-    for (int t = 0; t < w; ++t, k += 32) acc += A[k] * x[col[k]];
-    xo[i] = x[i] + dinv[i] * (b[i] - acc);
-}
-
-// r = b - A x
-template <class T>
-__global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
-                        const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r, const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
-    for (int t = 0; t < w; ++t, k += 32) acc += A[k] * x[col[k]];
-    r[i] = b[i] - acc;
-}
-
-template <class T>
-__global__ void k_restrict(int nc, const int4* __restrict__ kids, const T* __restrict__ r, T* __restrict__ bc,
-                           const int* stop)
-{
-    if (*stop) return;
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
-    const int4 k = kids[I];
-    T s = r[k.x];
-    if (k.y >= 0) s += r[k.y];
-    if (k.z >= 0) s += r[k.z];
-    if (k.w >= 0) s += r[k.w];
-    bc[I] = s;
-}
-
-// Post-smoothing fused with the prolongation: with y = t + w P xc,
-//   x = y + dinv (b - A y)
-template <class T>
-__global__ void k_prolong_smooth(int n, const int* __restrict__ sp, const int* __restrict__ col,
-                                 const T* __restrict__ A, const T* __restrict__ dinv, const T* __restrict__ b,
-                                 const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
-                                 T wp, T* __restrict__ x, const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
-    for (int q = 0; q < w; ++q, k += 32) {
-        const int j = col[k];
-        acc += A[k] * (t[j] + wp * xc[agg[j]]);
-    }
-    const T yi = t[i] + wp * xc[agg[i]];
-    x[i] = yi + dinv[i] * (b[i] - acc);
-}
-
-template <class T>
-__global__ void k_prolong(int n, const int* __restrict__ agg, const T* __restrict__ xc, T wp, T* __restrict__ x,
-                          const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += wp * xc[agg[i]];
-}
-
-template <class T>
-__global__ void k_copy(int n, const T* __restrict__ a, T* __restrict__ b, const int* stop)
-{
-    if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = a[i];
 }
 
 int read_int(cudaStream_t s, const int* d)
@@ -480,86 +534,160 @@ void exclusive_scan(cudaStream_t s, int n, const int* in, int* out, int* total_d
 {
     const int nb = std::max(1, div_up(n, 1024));
     if ((int)scratch.n < nb) scratch.alloc(nb);
-    if (n > 0) k_scan_block<<<nb, 1024, 0, s>>>(n, in, out, scratch.p);
+    if (n > 0) PORSOL_LAUNCH(k_scan_block<<<nb, 1024, 0, s>>>(n, in, out, scratch.p));
     else PORSOL_CUDA(cudaMemsetAsync(scratch.p, 0, sizeof(int), s));
-    k_scan_sums<<<1, 1024, 0, s>>>(n > 0 ? nb : 1, scratch.p, total_dev);
-    if (n > 0) k_scan_add<<<nb, 1024, 0, s>>>(n, out, scratch.p);
+    PORSOL_LAUNCH(k_scan_sums<<<1, 1024, 0, s>>>(n > 0 ? nb : 1, scratch.p, total_dev));
+    if (n > 0) PORSOL_LAUNCH(k_scan_add<<<nb, 1024, 0, s>>>(n, out, scratch.p));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 template <class T>
-Amg<T>::~Amg() = default;
-
-template <class T>
-void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, double theta, DBuf<int>& agg,
-                      DBuf<int2>& kids, int& ncoarse)
+void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
+                      Aggregates& out)
 {
-    best_.alloc(std::max<size_t>(best_.n, n));
-    state_.alloc(std::max<size_t>(state_.n, n));
-    flag_.alloc(std::max<size_t>(flag_.n, n + 1));
-    scan_.alloc(std::max<size_t>(scan_.n, n + 1));
-    DBuf<double> dval;
-    dval.alloc(n);
-    DBuf<int> partner;
+    DBuf<double> d;
+    DBuf<int> state, partner, jn, best, flag, cidx;
+    d.alloc(n);
+    state.alloc(n);
     partner.alloc(n);
+    jn.alloc(n);
+    best.alloc(n);
+    flag.alloc(n);
+    cidx.alloc(n + 1);
     const int nb = div_up(n, TB);
-    k_diag_vals<T><<<nb, TB, 0, s>>>(n, P.diag.p, A, dval.p);
-    PORSOL_CUDA(cudaMemsetAsync(state_.p, 0, n * sizeof(int), s));
+    PORSOL_LAUNCH(k_diag_abs<T><<<nb, TB, 0, s>>>(n, P.diag.p, A, d.p));
+    PORSOL_LAUNCH(k_isolated<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, state.p, partner.p, jn.p));
     for (int sweep = 0; sweep < 4; ++sweep) {
-        k_pick<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, dval.p, state_.p, best_.p, theta);
-        k_match<<<nb, TB, 0, s>>>(n, state_.p, best_.p, partner.p);
+        PORSOL_LAUNCH(k_pick<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, best.p, neg ? 1 : 0,
+                                    theta));
+        PORSOL_LAUNCH(k_match<<<nb, TB, 0, s>>>(n, state.p, best.p, partner.p));
     }
-    k_rep_flag<<<nb, TB, 0, s>>>(n, state_.p, partner.p, flag_.p);
-    exclusive_scan(s, n, flag_.p, scan_.p, scan_.p + n, scan_blocks_);
-    ncoarse = read_int(s, scan_.p + n);
-    agg.alloc(n);
-    kids.alloc(std::max(ncoarse, 1));
-    k_assign<<<nb, TB, 0, s>>>(n, state_.p, partner.p, flag_.p, scan_.p, agg.p, kids.p);
-    PORSOL_CUDA(cudaGetLastError());
-    PORSOL_CUDA(cudaStreamSynchronize(s));   // temporaries are freed on return
-}
-
-template <class T>
-void Amg<T>::galerkin_pairs(cudaStream_t s, const SellPattern& P, const T* A, int n, const int* agg,
-                            const int2* kids, int nc, SellPattern& Pc, DBuf<T>& Ac)
-{
-    (void)n;
-    Pc.n = nc;
-    Pc.nslices = div_up(nc, 32);
-    Pc.rowlen.alloc(nc);
-    Pc.diag.alloc(nc);
-    Pc.slice_ptr.alloc(Pc.nslices + 1);
-    const int nb = div_up(nc, 128);
-    k_gal_count<T><<<nb, 128, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, agg, kids, Pc.rowlen.p,
-                                      status_.p);
-    DBuf<int> width;
-    width.alloc(Pc.nslices);
-    k_slice_width<<<div_up(Pc.nslices, TB), TB, 0, s>>>(nc, Pc.nslices, Pc.rowlen.p, width.p);
-    exclusive_scan(s, Pc.nslices, width.p, Pc.slice_ptr.p, Pc.slice_ptr.p + Pc.nslices, scan_blocks_);
-    Pc.nent = read_int(s, Pc.slice_ptr.p + Pc.nslices);
-    const int st = read_int(s, status_.p);
-    PORSOL_REQUIRE(st == 0, PORSOL_ERR_BAD_ARG, "AMG: coarse row exceeds the Galerkin merge capacity");
-    Pc.col.alloc(Pc.nent);
-    Ac.alloc(Pc.nent);
-    k_gal_fill<T><<<nb, 128, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, agg, kids, Pc.slice_ptr.p,
-                                     Pc.col.p, Ac.p, Pc.diag.p);
-    k_pad_tail<<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p, int(sizeof(T)));
+    if (join) PORSOL_LAUNCH(k_join<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, jn.p));
+    PORSOL_LAUNCH(k_rep_flag<<<nb, TB, 0, s>>>(n, state.p, partner.p, jn.p, flag.p));
+    exclusive_scan(s, n, flag.p, cidx.p, cidx.p + n, scan_blocks_);
+    out.n = n;
+    out.nc = read_int(s, cidx.p + n);
+    out.agg.alloc(n);
+    PORSOL_LAUNCH(k_assign<<<nb, TB, 0, s>>>(n, state.p, partner.p, jn.p, flag.p, cidx.p, out.agg.p));
     PORSOL_CUDA(cudaGetLastError());
     PORSOL_CUDA(cudaStreamSynchronize(s));
+}
+
+template <class T>
+void Amg<T>::members(cudaStream_t s, Aggregates& a)
+{
+    const int n = a.n, nc = a.nc;
+    DBuf<int> cnt, pos;
+    cnt.alloc(std::max(nc, 1));
+    pos.alloc(std::max(nc, 1));
+    PORSOL_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * std::max(nc, 1), s));
+    a.ptr.alloc(nc + 1);
+    PORSOL_LAUNCH(k_count_members<<<div_up(n, TB), TB, 0, s>>>(n, a.agg.p, cnt.p));
+    exclusive_scan(s, nc, cnt.p, a.ptr.p, a.ptr.p + nc, scan_blocks_);
+    const int total = read_int(s, a.ptr.p + nc);
+    a.idx.alloc(std::max(total, 1));
+    PORSOL_CUDA(cudaMemcpyAsync(pos.p, a.ptr.p, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
+    PORSOL_LAUNCH(k_fill_members<<<div_up(n, TB), TB, 0, s>>>(n, a.agg.p, pos.p, a.idx.p));
+    PORSOL_LAUNCH(k_sort_members<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p));
+    PORSOL_CUDA(cudaGetLastError());
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+}
+
+template <class T>
+void Amg<T>::aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, Aggregates& out)
+{
+    pairwise(s, P, A, n, true, o_.strength, false, out);
+    if (out.nc > 0.8 * n) pairwise(s, P, A, n, false, 0.0, true, out);
+}
+
+template <class T>
+void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Aggregates& a, SellPattern& Pc,
+                      DBuf<T>& Ac)
+{
+    const int nc = a.nc;
+    Pc.n = nc;
+    Pc.nslices = div_up(nc, 32);
+    Pc.rowlen.alloc(std::max(nc, 1));
+    Pc.diag.alloc(std::max(nc, 1));
+    Pc.slice_ptr.alloc(Pc.nslices + 1);
+    iscratch_.alloc(4);
+    PORSOL_CUDA(cudaMemsetAsync(iscratch_.p, 0, sizeof(int), s));
+    PORSOL_LAUNCH(k_gal_bound<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p, P.rowlen.p, iscratch_.p));
+    const int bound = read_int(s, iscratch_.p);
+    PORSOL_REQUIRE(bound <= 2048, PORSOL_ERR_BAD_ARG, "AMG: aggregate rows too long for the Galerkin merge");
+    const int nb = div_up(nc, 64);
+#define PORSOL_GAL(CAP)                                                                                             \
+    PORSOL_COUNT_LAUNCH();                                                                                          \
+    k_gal_count<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,     \
+                                         Pc.rowlen.p)
+    if (bound <= 32) { PORSOL_GAL(32); }
+    else if (bound <= 64) { PORSOL_GAL(64); }
+    else if (bound <= 128) { PORSOL_GAL(128); }
+    else if (bound <= 256) { PORSOL_GAL(256); }
+    else if (bound <= 512) { PORSOL_GAL(512); }
+    else if (bound <= 1024) { PORSOL_GAL(1024); }
+    else { PORSOL_GAL(2048); }
+#undef PORSOL_GAL
+    DBuf<int> width;
+    width.alloc(Pc.nslices);
+    PORSOL_LAUNCH(k_slice_width<<<div_up(Pc.nslices, TB), TB, 0, s>>>(nc, Pc.nslices, Pc.rowlen.p, width.p));
+    exclusive_scan(s, Pc.nslices, width.p, Pc.slice_ptr.p, Pc.slice_ptr.p + Pc.nslices, scan_blocks_);
+    Pc.nent = read_int(s, Pc.slice_ptr.p + Pc.nslices);
+    Pc.col.alloc(std::max<long long>(Pc.nent, 1));
+    Ac.alloc(std::max<long long>(Pc.nent, 1));
+#define PORSOL_GALF(CAP)                                                                                            \
+    PORSOL_COUNT_LAUNCH();                                                                                          \
+    k_gal_fill<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,      \
+                                        Pc.slice_ptr.p, Pc.col.p, Ac.p, Pc.diag.p)
+    if (bound <= 32) { PORSOL_GALF(32); }
+    else if (bound <= 64) { PORSOL_GALF(64); }
+    else if (bound <= 128) { PORSOL_GALF(128); }
+    else if (bound <= 256) { PORSOL_GALF(256); }
+    else if (bound <= 512) { PORSOL_GALF(512); }
+    else if (bound <= 1024) { PORSOL_GALF(1024); }
+    else { PORSOL_GALF(2048); }
+#undef PORSOL_GALF
+    if (nc > 0) PORSOL_LAUNCH(k_pad_tail<T><<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p));
+    PORSOL_LAUNCH(k_check_diag<<<div_up(nc, TB), TB, 0, s>>>(nc, Pc.diag.p, status_.p));
+    PORSOL_CUDA(cudaGetLastError());
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+}
+
+template <class T>
+void Amg<T>::smoother_setup(cudaStream_t s, Level& L)
+{
+    const int n = L.n;
+    L.dinv.alloc(n);
+    DBuf<unsigned long long> g;
+    g.alloc(1);
+    g.zero(s);
+    PORSOL_LAUNCH(k_cheb_setup<T><<<div_up(n, TB), TB, 0, s>>>(n, L.P->slice_ptr.p, L.P->rowlen.p, L.P->diag.p, L.A, L.dinv.p,
+                                                 g.p, status_.p));
+    PORSOL_CUDA(cudaGetLastError());
+    unsigned long long gb = 0;
+    PORSOL_CUDA(cudaMemcpyAsync(&gb, g.p, sizeof(gb), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    double gm;
+    std::memcpy(&gm, &gb, sizeof(gm));
+    L.lmax = gm > 0 ? gm : 1.0;
+    L.t.alloc(n);
+    L.r.alloc(n);
+    L.d0.alloc(n);
+    L.d1.alloc(n);
 }
 
 template <class T>
 void Amg<T>::build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n)
 {
     nc_ = n;
-    Pc_ = &P;
-    Ac_ = A;
     DBuf<double> D, Linv;
-    D.alloc((size_t)n * n);
-    Linv.alloc((size_t)n * n);
-    cinv_.alloc((size_t)n * n);
-    k_dense_from_sell<T><<<div_up(n, 128), 128, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, D.p);
-    k_dense_cholesky_inverse<<<1, 1024, 0, s>>>(n, D.p, Linv.p, cinv_.p, status_.p);
+    D.alloc(std::max<size_t>((size_t)n * n, 1));
+    Linv.alloc(std::max<size_t>((size_t)n * n, 1));
+    cinv_.alloc(std::max<size_t>((size_t)n * n, 1));
+    if (n > 0) {
+        PORSOL_LAUNCH(k_dense_from_sell<T><<<div_up(n, 128), 128, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, D.p));
+        PORSOL_LAUNCH(k_dense_cholesky_inverse<<<1, 1024, 0, s>>>(n, D.p, Linv.p, cinv_.p, status_.p));
+    }
     PORSOL_CUDA(cudaGetLastError());
     const int st = read_int(s, status_.p);
     PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "AMG: coarsest matrix is not positive definite");
@@ -583,31 +711,30 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
     }
     sizes_.push_back(P0.n);
     nnzs_.push_back(P0.nent);
-    const double theta = o.strength;
     while (lv_.back()->n > o.coarse_target && int(lv_.size()) < o.max_levels) {
         Level& L = *lv_.back();
         const int n = L.n;
         const SellPattern& P = *L.P;
-        L.dinv.alloc(n);
-        k_l1_dinv<T><<<div_up(n, TB), TB, 0, s>>>(n, P.slice_ptr.p, P.rowlen.p, L.A, L.dinv.p, status_.p);
+        smoother_setup(s, L);
         // round 1 on this level's matrix
-        int nc1 = 0;
-        DBuf<int2> kids1;
-        pairwise(s, P, L.A, n, theta, L.agg, kids1, nc1);
-        if (nc1 > 0.8 * n) pairwise(s, P, L.A, n, 0.0, L.agg, kids1, nc1);
-        galerkin_pairs(s, P, L.A, n, L.agg.p, kids1.p, nc1, tmp_pat_, tmp_val_);
+        Aggregates a1;
+        aggregate_round(s, P, L.A, n, a1);
+        members(s, a1);
+        galerkin(s, P, L.A, a1, tmp_pat_, tmp_val_);
         auto next = std::make_unique<Level>();
-        if (nc1 > o.coarse_target) {
-            // round 2 on the intermediate matrix: aggregates of up to four rows
-            int nc2 = 0;
-            DBuf<int2> kids2;
-            pairwise(s, tmp_pat_, tmp_val_.p, nc1, theta, tmp_agg_, kids2, nc2);
-            if (nc2 > 0.8 * nc1) pairwise(s, tmp_pat_, tmp_val_.p, nc1, 0.0, tmp_agg_, kids2, nc2);
-            galerkin_pairs(s, tmp_pat_, tmp_val_.p, nc1, tmp_agg_.p, kids2.p, nc2, next->own, next->own_val);
-            k_compose<<<div_up(n, TB), TB, 0, s>>>(n, L.agg.p, tmp_agg_.p);
-            L.children.alloc(nc2);
-            k_kids4<<<div_up(nc2, TB), TB, 0, s>>>(nc2, kids2.p, kids1.p, L.children.p);
-            next->n = nc2;
+        if (a1.nc > o.coarse_target) {
+            // round 2 on the intermediate matrix: aggregates of about four rows
+            Aggregates a2;
+            aggregate_round(s, tmp_pat_, tmp_val_.p, a1.nc, a2);
+            members(s, a2);
+            galerkin(s, tmp_pat_, tmp_val_.p, a2, next->own, next->own_val);
+            PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, a1.agg.p, a2.agg.p));
+            PORSOL_CUDA(cudaGetLastError());
+            L.agg.n = n;
+            L.agg.nc = a2.nc;
+            L.agg.agg = std::move(a1.agg);
+            members(s, L.agg);
+            next->n = a2.nc;
         } else {
             std::swap(next->own.slice_ptr, tmp_pat_.slice_ptr);
             std::swap(next->own.col, tmp_pat_.col);
@@ -617,20 +744,15 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
             next->own.nslices = tmp_pat_.nslices;
             next->own.nent = tmp_pat_.nent;
             std::swap(next->own_val, tmp_val_);
-            L.children.alloc(nc1);
-            k_kids2to4<<<div_up(nc1, TB), TB, 0, s>>>(nc1, kids1.p, L.children.p);
-            next->n = nc1;
+            L.agg = std::move(a1);
+            next->n = L.agg.nc;
         }
-        PORSOL_CUDA(cudaGetLastError());
-        L.x.alloc(n);
-        L.r.alloc(n);
         next->P = &next->own;
         next->A = next->own_val.p;
         next->b.alloc(std::max(next->n, 1));
         next->x.alloc(std::max(next->n, 1));
         sizes_.push_back(next->n);
         nnzs_.push_back(next->own.nent);
-        PORSOL_CUDA(cudaStreamSynchronize(s));
         const bool stalled = next->n > 0.9 * n;
         lv_.push_back(std::move(next));
         if (stalled) break;
@@ -639,15 +761,56 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
     PORSOL_REQUIRE(C.n <= 2048, PORSOL_ERR_BAD_ARG, "AMG: coarsening stalled above the dense-solve limit");
     build_coarse_solver(s, *C.P, C.A, C.n);
     const int st = read_int(s, status_.p);
-    PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "AMG setup: non-finite or non-positive smoother diagonal");
+    PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "AMG setup: non-positive diagonal or missing diagonal entry");
+}
+
+// One Chebyshev application (degree o_.cheb_degree) on [lmax/30, lmax]:
+//   from_zero: x = p(D^-1 A) D^-1 b;  otherwise from y = x0 (+ w P xc when xc is given).
+template <class T>
+void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
+                       const int* stop)
+{
+    const int n = L.n;
+    const int nb = div_up(n, TB);
+    const SellPattern& P = *L.P;
+    const double bmax = L.lmax, amin = L.lmax / 30.0;
+    const double theta = 0.5 * (bmax + amin), delta = 0.5 * (bmax - amin);
+    const double sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    T* d = L.d0.p;
+    T* dn = L.d1.p;
+    if (from_zero) {
+        PORSOL_LAUNCH(k_cheb_start0<T><<<nb, TB, 0, s>>>(n, L.dinv.p, b, L.r.p, d, T(1.0 / theta), stop));
+    } else {
+        // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
+        const T* t = xc ? L.t.p : x;
+        PORSOL_LAUNCH(k_cheb_start<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong),
+                                          x, L.r.p, d, T(1.0 / theta), stop));
+    }
+    const int deg = std::max(1, o_.cheb_degree);
+    for (int k = 1; k <= deg; ++k) {
+        const double rho1 = 1.0 / (2.0 * sigma - rho);
+        const double c1 = rho1 * rho, c2 = 2.0 * rho1 / delta;
+        const T* xin = (from_zero && k == 1) ? nullptr : x;
+        // algorithmic bytes: matrix values + columns, d gathered once, dinv/r/x in, r/d/x out
+        const double bytes = double(P.nent) * (sizeof(T) + 4) + double(n) * sizeof(T) * (xin ? 7 : 6);
+        const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();
+        cudaEvent_t ev = nullptr;
+        if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
+        PORSOL_LAUNCH(k_cheb_step<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
+                                         k == deg ? 1 : 0, stop));
+        if (prof_here) prof_->end(s, PK_CHEB, bytes, ev);
+        rho = rho1;
+        std::swap(d, dn);
+    }
+    PORSOL_CUDA(cudaGetLastError());
 }
 
 template <class T>
 void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
 {
     if (l == int(lv_.size()) - 1) {
-        const int threads = 512;
-        k_dense_apply<T><<<1, threads, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop);
+        if (nc_ > 0) PORSOL_LAUNCH(k_dense_apply<T><<<1, 512, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop));
         return;
     }
     Level& L = *lv_[l];
@@ -655,41 +818,27 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     const int n = L.n;
     const int nb = div_up(n, TB);
     const SellPattern& P = *L.P;
-    const int ncn = Nx.n;
-    T* bc = Nx.b.p;
-    T* xc = Nx.x.p;
-    T* t = L.x.p;   // pre-smoothed iterate
-    T* r = L.r.p;
-    k_jacobi0<T><<<nb, TB, 0, s>>>(n, L.dinv.p, b, t, stop);
-    for (int sw = 1; sw < o_.smooth_steps; ++sw) {
-        k_jacobi<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, b, t, r, stop);
-        std::swap(t, r);
-    }
-    k_resid<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, b, t, r, stop);
-    k_restrict<T><<<div_up(ncn, TB), TB, 0, s>>>(ncn, L.children.p, r, bc, stop);
-    vcycle(s, l + 1, bc, xc, stop);
-    const T wp = T(o_.prolong);
-    if (o_.smooth_steps == 1) {
-        k_prolong_smooth<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, b, t, xc, L.agg.p, wp, x,
-                                              stop);
-    } else {
-        k_prolong<T><<<nb, TB, 0, s>>>(n, L.agg.p, xc, wp, t, stop);
-        T* cur = t;
-        T* nxt = r;
-        for (int sw = 0; sw < o_.smooth_steps; ++sw) {
-            T* dst = (sw == o_.smooth_steps - 1) ? x : nxt;
-            k_jacobi<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, b, cur, dst, stop);
-            nxt = cur;
-            cur = dst;
-        }
-    }
+    // pre-smoothing into t
+    chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
+    for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
+    // restrict the residual
+    PORSOL_LAUNCH(k_resid<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, b, L.t.p, L.r.p, stop));
+    PORSOL_LAUNCH(k_restrict<T><<<div_up(Nx.n, TB), TB, 0, s>>>(Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop));
+    vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
+    // post-smoothing from t + w P xc
+    chebyshev(s, L, b, x, false, Nx.x.p, L.agg.agg.p, stop);
+    for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, x, false, nullptr, nullptr, stop);
     PORSOL_CUDA(cudaGetLastError());
 }
 
 template <class T>
 void Amg<T>::apply(cudaStream_t s, const T* r, T* z, const int* stop)
 {
+    const bool prof_here = prof_ && prof_->on;
+    cudaEvent_t ev = nullptr;
+    if (prof_here) prof_->begin(s, PK_VCYCLE, 0.0, &ev);
     vcycle(s, 0, r, z, stop);
+    if (prof_here) prof_->end(s, PK_VCYCLE, 0.0, ev);
 }
 
 template class Amg<double>;

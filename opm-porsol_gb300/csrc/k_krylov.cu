@@ -360,7 +360,7 @@ template <class TV, class TX>
 void spmv(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, TX* y)
 {
     if (P.n == 0) return;
-    k_spmv<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, y);
+    PORSOL_LAUNCH(k_spmv<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, y));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -368,7 +368,7 @@ template <class TV, class TX>
 void residual(cudaStream_t s, const SellPattern& P, const TV* val, const TX* x, const TX* b, TX* y)
 {
     if (P.n == 0) return;
-    k_residual<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, b, y);
+    PORSOL_LAUNCH(k_residual<TV, TX><<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, val, x, b, y));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -423,13 +423,13 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
     init.tol = tol;
     init.maxit = maxit;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
-    k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p, red_.partial.p,
-                                       red_.counter.p, dview_);
+    PORSOL_LAUNCH(k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p, red_.partial.p,
+                                       red_.counter.p, dview_));
     PORSOL_CUDA(cudaGetLastError());
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
-    k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
-    k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p);
+    PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
+    PORSOL_LAUNCH(k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
     PORSOL_CUDA(cudaGetLastError());
     // Iterations are queued ahead; the host waits on the event of iteration i - LOOKAHEAD
     // and reads the mapped stop flag.  Iterations queued after convergence are no-ops.
@@ -441,19 +441,19 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
         if (it < maxit) {
             if (prof && prof_kernel >= 0) {
                 ProfScope ps(*prof, s, prof_kernel, spmv_bytes);
-                k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                   red_.partial.p, red_.counter.p);
+                PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                   red_.partial.p, red_.counter.p));
             } else {
-                k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                   red_.partial.p, red_.counter.p);
+                PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                   red_.partial.p, red_.counter.p));
             }
-            k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
-                                             dview_);
+            PORSOL_LAUNCH(k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
+                                             dview_));
             PORSOL_CUDA(cudaGetLastError());
             M.apply(s, r_.p, z_.p, stop);
-            k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
-            k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr);
-            k_cg_roll<<<1, 1, 0, s>>>(st_.p);
+            PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
+            PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr));
+            PORSOL_LAUNCH(k_cg_roll<<<1, 1, 0, s>>>(st_.p));
             PORSOL_CUDA(cudaGetLastError());
             PORSOL_CUDA(cudaEventRecord(ev_[it % ev_.size()], s));
             ++it;
@@ -536,8 +536,8 @@ void Ilu0::factor(cudaStream_t s, const SellPattern& P, const double* val)
     DBuf<int>& status = status_;
     for (size_t l = 0; l + 1 < h_lptr_.size(); ++l) {
         const int cnt = h_lptr_[l + 1] - h_lptr_[l];
-        k_ilu_factor_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
-                                                            P.rowlen.p, P.diag.p, lu_.p, status.p);
+        PORSOL_LAUNCH(k_ilu_factor_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
+                                                            P.rowlen.p, P.diag.p, lu_.p, status.p));
     }
     PORSOL_CUDA(cudaGetLastError());
     int st = 0;
@@ -551,13 +551,13 @@ void Ilu0::apply(cudaStream_t s, const double* r, double* z, const int* stop)
     const SellPattern& P = *P_;
     for (size_t l = 0; l + 1 < h_lptr_.size(); ++l) {
         const int cnt = h_lptr_[l + 1] - h_lptr_[l];
-        k_ilu_lower_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
-                                                           P.diag.p, lu_.p, r, z, stop);
+        PORSOL_LAUNCH(k_ilu_lower_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
+                                                           P.diag.p, lu_.p, r, z, stop));
     }
     for (size_t l = 0; l + 1 < h_uptr_.size(); ++l) {
         const int cnt = h_uptr_[l + 1] - h_uptr_[l];
-        k_ilu_upper_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, urows_.p + h_uptr_[l], P.slice_ptr.p, P.col.p,
-                                                           P.rowlen.p, P.diag.p, lu_.p, z, stop);
+        PORSOL_LAUNCH(k_ilu_upper_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, urows_.p + h_uptr_[l], P.slice_ptr.p, P.col.p,
+                                                           P.rowlen.p, P.diag.p, lu_.p, z, stop));
     }
     PORSOL_CUDA(cudaGetLastError());
 }
@@ -572,7 +572,7 @@ template <class TA, class TB>
 void convert(cudaStream_t s, long long n, const TA* a, TB* b)
 {
     if (n == 0) return;
-    k_convert<TA, TB><<<div_up(n, RB), RB, 0, s>>>(n, a, b);
+    PORSOL_LAUNCH(k_convert<TA, TB><<<div_up(n, RB), RB, 0, s>>>(n, a, b));
     PORSOL_CUDA(cudaGetLastError());
 }
 template void convert<double, float>(cudaStream_t, long long, const double*, float*);
@@ -581,28 +581,28 @@ template void convert<float, double>(cudaStream_t, long long, const float*, doub
 void axpy_add(cudaStream_t s, int n, const double* y, double* x)
 {
     if (n == 0) return;
-    k_axpy_add<<<div_up(n, RB), RB, 0, s>>>(n, y, x);
+    PORSOL_LAUNCH(k_axpy_add<<<div_up(n, RB), RB, 0, s>>>(n, y, x));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 void to_f32_scaled(cudaStream_t s, int n, const double* a, float* b, double scale)
 {
     if (n == 0) return;
-    k_to_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, a, b, scale);
+    PORSOL_LAUNCH(k_to_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, a, b, scale));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 void add_f32_scaled(cudaStream_t s, int n, const float* y, double scale, double* x)
 {
     if (n == 0) return;
-    k_add_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, y, scale, x);
+    PORSOL_LAUNCH(k_add_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, y, scale, x));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 void dirichlet_guess(cudaStream_t s, const SellPattern& P, const double* val, const double* b, double* x)
 {
     if (P.n == 0) return;
-    k_dirichlet_guess<<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, val, b, x);
+    PORSOL_LAUNCH(k_dirichlet_guess<<<div_up(P.n, RB), RB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, val, b, x));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -612,7 +612,7 @@ double norm2(cudaStream_t s, int n, const T* x, RedScratch& red)
     if (n == 0) return 0.0;
     const int nb = div_up(n, RB);
     red.ensure(nb + 1, s);
-    k_norm2<T><<<nb, RB, 0, s>>>(n, x, red.partial.p, red.counter.p, red.partial.p + nb);
+    PORSOL_LAUNCH(k_norm2<T><<<nb, RB, 0, s>>>(n, x, red.partial.p, red.counter.p, red.partial.p + nb));
     PORSOL_CUDA(cudaGetLastError());
     double out = 0.0;
     PORSOL_CUDA(cudaMemcpyAsync(&out, red.partial.p + nb, sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -361,11 +361,11 @@ void launch_static_ip(int maxnf, cudaStream_t s, int nc, const int* facepos, con
     if (nc == 0) return;
     const int bs = 128;
     if (maxnf <= 6)
-        k_static_ip<6><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
-                                                     grav[1], grav[2], W, gflux, status);
+        PORSOL_LAUNCH(k_static_ip<6><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
+                                                     grav[1], grav[2], W, gflux, status));
     else
-        k_static_ip<12><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
-                                                      grav[1], grav[2], W, gflux, status);
+        PORSOL_LAUNCH(k_static_ip<12><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
+                                                      grav[1], grav[2], W, gflux, status));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -373,8 +373,8 @@ void launch_assemble_cells(int maxnf, cudaStream_t s, const AssembleArgs& a)
 {
     if (a.nc == 0) return;
     const int bs = 128;
-    if (maxnf <= 6) k_assemble_cells<6><<<div_up(a.nc, bs), bs, 0, s>>>(a);
-    else k_assemble_cells<12><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    if (maxnf <= 6) PORSOL_LAUNCH(k_assemble_cells<6><<<div_up(a.nc, bs), bs, 0, s>>>(a));
+    else PORSOL_LAUNCH(k_assemble_cells<12><<<div_up(a.nc, bs), bs, 0, s>>>(a));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -382,7 +382,7 @@ void launch_gather_slots(cudaStream_t s, long long nent, const int* slot_ptr, co
                          const double* sloc, double* val, float* val32)
 {
     if (nent == 0) return;
-    k_gather_slots<<<div_up(nent, 256), 256, 0, s>>>(nent, slot_ptr, slot_ent, sloc, val, val32);
+    PORSOL_LAUNCH(k_gather_slots<<<div_up(nent, 256), 256, 0, s>>>(nent, slot_ptr, slot_ent, sloc, val, val32));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -390,13 +390,13 @@ void launch_gather_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs
                        const double* pb, double* rhs)
 {
     if (n == 0) return;
-    k_gather_rhs<<<div_up(n, 256), 256, 0, s>>>(n, rhs_ptr, rhs_ent, rrow, pb, rhs);
+    PORSOL_LAUNCH(k_gather_rhs<<<div_up(n, 256), 256, 0, s>>>(n, rhs_ptr, rhs_ent, rrow, pb, rhs));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 void launch_scale_entry(cudaStream_t s, double* val, const int* diag, int row, double factor, float* val32)
 {
-    k_scale_entry<<<1, 1, 0, s>>>(val, diag, row, factor, val32);
+    PORSOL_LAUNCH(k_scale_entry<<<1, 1, 0, s>>>(val, diag, row, factor, val32));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -404,8 +404,8 @@ void launch_recover(int maxnf, cudaStream_t s, const RecoverArgs& a)
 {
     if (a.nc == 0) return;
     const int bs = 128;
-    if (maxnf <= 6) k_recover<6><<<div_up(a.nc, bs), bs, 0, s>>>(a);
-    else k_recover<12><<<div_up(a.nc, bs), bs, 0, s>>>(a);
+    if (maxnf <= 6) PORSOL_LAUNCH(k_recover<6><<<div_up(a.nc, bs), bs, 0, s>>>(a));
+    else PORSOL_LAUNCH(k_recover<12><<<div_up(a.nc, bs), bs, 0, s>>>(a));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -413,7 +413,7 @@ void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* o
                          unsigned long long* maxmod_bits)
 {
     if (npairs == 0) return;
-    k_post_process<<<div_up(npairs, 256), 256, 0, s>>>(npairs, pairs, outflux, maxmod_bits);
+    PORSOL_LAUNCH(k_post_process<<<div_up(npairs, 256), 256, 0, s>>>(npairs, pairs, outflux, maxmod_bits));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -421,14 +421,14 @@ void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const doubl
                          unsigned long long* out3)
 {
     if (nc == 0) return;
-    k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3);
+    PORSOL_LAUNCH(k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3));
     PORSOL_CUDA(cudaGetLastError());
 }
 
 void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status)
 {
     if (n == 0) return;
-    k_check_finite<<<std::min(div_up(n, 256), 152 * 8), 256, 0, s>>>(n, v, status);
+    PORSOL_LAUNCH(k_check_finite<<<std::min(div_up(n, 256), 152 * 8), 256, 0, s>>>(n, v, status));
     PORSOL_CUDA(cudaGetLastError());
 }
 

@@ -410,8 +410,8 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
         std::memcpy(&init[0], &big, 8);
         std::memcpy(&init[1], &big, 8);
         PORSOL_CUDA(cudaMemcpyAsync(red.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
-        k_cfl_cells<<<div_up(nc, TB), TB, 0, s>>>(nc, facepos.p, d_flux, gflux_hf.p, vol.p, poro_d.p, fac[0], fac[1],
-                                                  do_v, do_g, red.p, status.p);
+        PORSOL_LAUNCH(k_cfl_cells<<<div_up(nc, TB), TB, 0, s>>>(nc, facepos.p, d_flux, gflux_hf.p, vol.p, poro_d.p, fac[0], fac[1],
+                                                  do_v, do_g, red.p, status.p));
         PORSOL_CUDA(cudaGetLastError());
         unsigned long long out[2];
         int stt = 0;
@@ -453,9 +453,9 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     const int max_repeats = 10;
     while (true) {
         for (int q = 0; q < n; ++q) {
-            if (nfe) k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p, status.p);
-            k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, porevol.p, p, dt, o.check_sat,
-                                                       o.clamp_sat, d_sat, status.p);
+            if (nfe) PORSOL_LAUNCH(k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p, status.p));
+            PORSOL_LAUNCH(k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, porevol.p, p, dt, o.check_sat,
+                                                       o.clamp_sat, d_sat, status.p));
             if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
         }
         PORSOL_CUDA(cudaGetLastError());

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -119,7 +121,7 @@ void build_sell(int n, const std::vector<int>& rowptr, const std::vector<int>& c
                 std::vector<long long>* csr2sell);
 
 // ------------------------------------------------------------------ profiling
-enum ProfKernel { PK_SPMV64 = 0, PK_SPMV32 = 1, PK_ASSEMBLE = 2, PK_RECOVER = 3, PK_VCYCLE = 4, PK_COUNT = 5 };
+enum ProfKernel { PK_SPMV64 = 0, PK_SPMV32 = 1, PK_ASSEMBLE = 2, PK_RECOVER = 3, PK_VCYCLE = 4, PK_CHEB = 5, PK_COUNT = 6 };
 
 struct Profiler {
     bool on = false;
@@ -155,5 +157,14 @@ struct ProfScope {
 
 // ------------------------------------------------------------------ launch helpers
 inline int div_up(long long a, int b) { return int((a + b - 1) / b); }
+
+// Process-wide count of kernel launches made by this library (porsol_launch_count()).
+extern std::atomic<long long> g_launches;
+#define PORSOL_COUNT_LAUNCH() ::porsol::g_launches.fetch_add(1, std::memory_order_relaxed)
+#define PORSOL_LAUNCH(...)      \
+    do {                        \
+        __VA_ARGS__;            \
+        PORSOL_COUNT_LAUNCH();  \
+    } while (0)
 
 }  // namespace porsol

@@ -93,6 +93,8 @@ def lib():
         L.orc_get_system.argtypes = [vp, dp, dp, dp, dp, dp, ip]
         L.orc_solve.restype = i
         L.orc_solve.argtypes = [vp, dp, dp, ip, dp, dp, d, i, i, ip, dp]
+        L.orc_solve_timed.restype = i
+        L.orc_solve_timed.argtypes = [vp, dp, dp, ip, dp, dp, d, i, i, ip, dp, dp]
         L.orc_get_solution.argtypes = [vp, dp, dp, dp]
         L.orc_post_process_fluxes.restype = d
         L.orc_post_process_fluxes.argtypes = [vp]
@@ -198,6 +200,18 @@ class OraclePressure:
         self.iterations = int(it[0])
         self.reduction = float(red[0])
         return rc
+
+    def solve_timed(self, totmob, mobdens, bc_type, bc_value, src, tol=1e-8, maxit=0, dirichlet_guess=False):
+        """As solve(); returns (rc, seconds of assembly+recovery, of the ILU0 factorisation, of CG)."""
+        args = [_f64(totmob), _f64(mobdens), _i32(bc_type), _f64(bc_value), _f64(src)]
+        it = np.zeros(1, np.int32)
+        red = np.zeros(1)
+        sec = np.zeros(3)
+        rc = lib().orc_solve_timed(self.h, *[_p(a) for a in args], float(tol), int(maxit), int(dirichlet_guess),
+                                   _p(it), _p(red), _p(sec))
+        self.iterations = int(it[0])
+        self.reduction = float(red[0])
+        return rc, float(sec[0]), float(sec[1]), float(sec[2])
 
     def solution(self):
         p = np.empty(self.g.num_cells)

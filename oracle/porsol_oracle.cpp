@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cassert>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -552,10 +553,13 @@ struct Pressure {
     }
 
     // solveLinearSystem / solveLinearSystemAMG (the Krylov part), :1387-1420, :1481-1541
+    double t_factor = 0.0;
     int solve(double tol, int maxit, int dirichlet_guess, int* iters, double* red)
     {
         if (do_reg) S.at(0, 0) *= 2;
+        const auto tf0 = std::chrono::steady_clock::now();
         Ilu0 M(S);
+        t_factor = std::chrono::duration<double>(std::chrono::steady_clock::now() - tf0).count();
         std::fill(soln.begin(), soln.end(), 0.0);
         if (dirichlet_guess) {
             for (int i = 0; i < S.n; ++i) {
@@ -970,14 +974,32 @@ void orc_get_system(void* h, double* Svals, double* rhs, double* F, double* L, d
 int orc_solve(void* h, const double* totmob, const double* mobdens, const int* bct, const double* bcv,
               const double* src, double tol, int maxit, int dirichlet_guess, int* iterations, double* reduction)
 {
+    return orc_solve_timed(h, totmob, mobdens, bct, bcv, src, tol, maxit, dirichlet_guess, iterations, reduction,
+                           nullptr);
+}
+
+int orc_solve_timed(void* h, const double* totmob, const double* mobdens, const int* bct, const double* bcv,
+                    const double* src, double tol, int maxit, int dirichlet_guess, int* iterations,
+                    double* reduction, double* seconds3)
+{
+    using clk = std::chrono::steady_clock;
     Pressure* P = static_cast<Pressure*>(h);
+    const auto t0 = clk::now();
     P->assemble(totmob, mobdens, bct, bcv, src);
+    const auto t1 = clk::now();
     int it = 0;
     double red = 0.0;
     const int rc = P->solve(tol, maxit, dirichlet_guess, &it, &red);
+    const auto t2 = clk::now();
     if (iterations) *iterations = it;
     if (reduction) *reduction = red;
     P->recover();
+    const auto t3 = clk::now();
+    if (seconds3) {
+        seconds3[0] = std::chrono::duration<double>(t1 - t0).count() + std::chrono::duration<double>(t3 - t2).count();
+        seconds3[1] = P->t_factor;
+        seconds3[2] = std::chrono::duration<double>(t2 - t1).count() - P->t_factor;
+    }
     return rc;
 }
 

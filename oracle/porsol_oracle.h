@@ -62,6 +62,12 @@ void  orc_get_system(void* h, double* Svals, double* rhs, double* F, double* L, 
 int   orc_solve(void* h, const double* totmob, const double* mobdens,
                 const int* hf_flow_type, const double* hf_flow_value, const double* src,
                 double tol, int maxit, int dirichlet_guess, int* iterations, double* reduction);
+/* As orc_solve; seconds3[0] = assembly + recovery, seconds3[1] = ILU0 factorisation,
+ * seconds3[2] = CG iterations. */
+int   orc_solve_timed(void* h, const double* totmob, const double* mobdens,
+                      const int* hf_flow_type, const double* hf_flow_value, const double* src,
+                      double tol, int maxit, int dirichlet_guess, int* iterations, double* reduction,
+                      double* seconds3);
 void  orc_get_solution(void* h, double* pressure, double* outflux, double* facepressure);
 double orc_post_process_fluxes(void* h);
 
