@@ -41,7 +41,7 @@ class Amg : public Precond<T> {
 public:
     void setup(cudaStream_t s, const SellPattern& P0, const T* A0, const AmgOpts& o);
     void apply(cudaStream_t s, const T* r, T* z, const int* stop) override;
-    int levels() const { return int(lv_.size()); }
+    int levels() const { return nlev_; }
     void set_profiler(Profiler* p) { prof_ = p; }
     const std::vector<int>& level_sizes() const { return sizes_; }
     const std::vector<long long>& level_nnz() const { return nnzs_; }
@@ -72,7 +72,13 @@ private:
 
     AmgOpts o_;
     Profiler* prof_ = nullptr;
-    std::vector<std::unique_ptr<Level>> lv_;
+    std::vector<std::unique_ptr<Level>> lv_;   // levels are kept and reused by later setups
+    int nlev_ = 0;                              // levels in use
+    // setup scratch (grow-only, reused by every setup)
+    DBuf<double> s_d_, s_D_, s_Linv_;
+    DBuf<int> s_state_, s_partner_, s_join_, s_best_, s_flag_, s_cidx_, s_cnt_, s_pos_, s_width_;
+    DBuf<unsigned long long> s_gmax_;
+    Aggregates agg2_;
     std::vector<int> sizes_;
     std::vector<long long> nnzs_;
     int nc_ = 0;

@@ -545,8 +545,9 @@ template <class T>
 void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
                       Aggregates& out)
 {
-    DBuf<double> d;
-    DBuf<int> state, partner, jn, best, flag, cidx;
+    DBuf<double>& d = s_d_;
+    DBuf<int>&state = s_state_, &partner = s_partner_, &jn = s_join_, &best = s_best_, &flag = s_flag_,
+    &cidx = s_cidx_;
     d.alloc(n);
     state.alloc(n);
     partner.alloc(n);
@@ -577,7 +578,7 @@ template <class T>
 void Amg<T>::members(cudaStream_t s, Aggregates& a)
 {
     const int n = a.n, nc = a.nc;
-    DBuf<int> cnt, pos;
+    DBuf<int>&cnt = s_cnt_, &pos = s_pos_;
     cnt.alloc(std::max(nc, 1));
     pos.alloc(std::max(nc, 1));
     PORSOL_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * std::max(nc, 1), s));
@@ -590,7 +591,6 @@ void Amg<T>::members(cudaStream_t s, Aggregates& a)
     PORSOL_LAUNCH(k_fill_members<<<div_up(n, TB), TB, 0, s>>>(n, a.agg.p, pos.p, a.idx.p));
     PORSOL_LAUNCH(k_sort_members<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p));
     PORSOL_CUDA(cudaGetLastError());
-    PORSOL_CUDA(cudaStreamSynchronize(s));
 }
 
 template <class T>
@@ -628,7 +628,7 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     else if (bound <= 1024) { PORSOL_GAL(1024); }
     else { PORSOL_GAL(2048); }
 #undef PORSOL_GAL
-    DBuf<int> width;
+    DBuf<int>& width = s_width_;
     width.alloc(Pc.nslices);
     PORSOL_LAUNCH(k_slice_width<<<div_up(Pc.nslices, TB), TB, 0, s>>>(nc, Pc.nslices, Pc.rowlen.p, width.p));
     exclusive_scan(s, Pc.nslices, width.p, Pc.slice_ptr.p, Pc.slice_ptr.p + Pc.nslices, scan_blocks_);
@@ -650,7 +650,6 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     if (nc > 0) PORSOL_LAUNCH(k_pad_tail<T><<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p));
     PORSOL_LAUNCH(k_check_diag<<<div_up(nc, TB), TB, 0, s>>>(nc, Pc.diag.p, status_.p));
     PORSOL_CUDA(cudaGetLastError());
-    PORSOL_CUDA(cudaStreamSynchronize(s));
 }
 
 template <class T>
@@ -658,7 +657,7 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L)
 {
     const int n = L.n;
     L.dinv.alloc(n);
-    DBuf<unsigned long long> g;
+    DBuf<unsigned long long>& g = s_gmax_;
     g.alloc(1);
     g.zero(s);
     PORSOL_LAUNCH(k_cheb_setup<T><<<div_up(n, TB), TB, 0, s>>>(n, L.P->slice_ptr.p, L.P->rowlen.p, L.P->diag.p, L.A, L.dinv.p,
@@ -680,7 +679,7 @@ template <class T>
 void Amg<T>::build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n)
 {
     nc_ = n;
-    DBuf<double> D, Linv;
+    DBuf<double>&D = s_D_, &Linv = s_Linv_;
     D.alloc(std::max<size_t>((size_t)n * n, 1));
     Linv.alloc(std::max<size_t>((size_t)n * n, 1));
     cinv_.alloc(std::max<size_t>((size_t)n * n, 1));
@@ -697,67 +696,62 @@ template <class T>
 void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const AmgOpts& o)
 {
     o_ = o;
-    lv_.clear();
     sizes_.clear();
     nnzs_.clear();
     status_.alloc(1);
     status_.zero(s);
+    if (lv_.empty()) lv_.push_back(std::make_unique<Level>());
+    nlev_ = 1;
     {
-        auto L0 = std::make_unique<Level>();
-        L0->n = P0.n;
-        L0->P = &P0;
-        L0->A = A0;
-        lv_.push_back(std::move(L0));
+        Level& L0 = *lv_[0];
+        L0.n = P0.n;
+        L0.P = &P0;
+        L0.A = A0;
     }
     sizes_.push_back(P0.n);
     nnzs_.push_back(P0.nent);
-    while (lv_.back()->n > o.coarse_target && int(lv_.size()) < o.max_levels) {
-        Level& L = *lv_.back();
+    while (lv_[nlev_ - 1]->n > o.coarse_target && nlev_ < o.max_levels) {
+        Level& L = *lv_[nlev_ - 1];
         const int n = L.n;
         const SellPattern& P = *L.P;
         smoother_setup(s, L);
-        // round 1 on this level's matrix
-        Aggregates a1;
-        aggregate_round(s, P, L.A, n, a1);
-        members(s, a1);
-        galerkin(s, P, L.A, a1, tmp_pat_, tmp_val_);
-        auto next = std::make_unique<Level>();
-        if (a1.nc > o.coarse_target) {
+        if (int(lv_.size()) <= nlev_) lv_.push_back(std::make_unique<Level>());
+        Level& next = *lv_[nlev_];
+        // round 1 on this level's matrix; L.agg maps rows to the intermediate level
+        aggregate_round(s, P, L.A, n, L.agg);
+        members(s, L.agg);
+        galerkin(s, P, L.A, L.agg, tmp_pat_, tmp_val_);
+        const int nc1 = L.agg.nc;
+        if (nc1 > o.coarse_target) {
             // round 2 on the intermediate matrix: aggregates of about four rows
-            Aggregates a2;
-            aggregate_round(s, tmp_pat_, tmp_val_.p, a1.nc, a2);
-            members(s, a2);
-            galerkin(s, tmp_pat_, tmp_val_.p, a2, next->own, next->own_val);
-            PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, a1.agg.p, a2.agg.p));
-            PORSOL_CUDA(cudaGetLastError());
-            L.agg.n = n;
-            L.agg.nc = a2.nc;
-            L.agg.agg = std::move(a1.agg);
+            aggregate_round(s, tmp_pat_, tmp_val_.p, nc1, agg2_);
+            members(s, agg2_);
+            galerkin(s, tmp_pat_, tmp_val_.p, agg2_, next.own, next.own_val);
+            PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, L.agg.agg.p, agg2_.agg.p));
+            L.agg.nc = agg2_.nc;
             members(s, L.agg);
-            next->n = a2.nc;
         } else {
-            std::swap(next->own.slice_ptr, tmp_pat_.slice_ptr);
-            std::swap(next->own.col, tmp_pat_.col);
-            std::swap(next->own.rowlen, tmp_pat_.rowlen);
-            std::swap(next->own.diag, tmp_pat_.diag);
-            next->own.n = tmp_pat_.n;
-            next->own.nslices = tmp_pat_.nslices;
-            next->own.nent = tmp_pat_.nent;
-            std::swap(next->own_val, tmp_val_);
-            L.agg = std::move(a1);
-            next->n = L.agg.nc;
+            std::swap(next.own.slice_ptr, tmp_pat_.slice_ptr);
+            std::swap(next.own.col, tmp_pat_.col);
+            std::swap(next.own.rowlen, tmp_pat_.rowlen);
+            std::swap(next.own.diag, tmp_pat_.diag);
+            next.own.n = tmp_pat_.n;
+            next.own.nslices = tmp_pat_.nslices;
+            next.own.nent = tmp_pat_.nent;
+            std::swap(next.own_val, tmp_val_);
         }
-        next->P = &next->own;
-        next->A = next->own_val.p;
-        next->b.alloc(std::max(next->n, 1));
-        next->x.alloc(std::max(next->n, 1));
-        sizes_.push_back(next->n);
-        nnzs_.push_back(next->own.nent);
-        const bool stalled = next->n > 0.9 * n;
-        lv_.push_back(std::move(next));
-        if (stalled) break;
+        PORSOL_CUDA(cudaGetLastError());
+        next.n = L.agg.nc;
+        next.P = &next.own;
+        next.A = next.own_val.p;
+        next.b.alloc(std::max(next.n, 1));
+        next.x.alloc(std::max(next.n, 1));
+        sizes_.push_back(next.n);
+        nnzs_.push_back(next.own.nent);
+        ++nlev_;
+        if (next.n > 0.9 * n) break;   // coarsening stalled
     }
-    Level& C = *lv_.back();
+    Level& C = *lv_[nlev_ - 1];
     PORSOL_REQUIRE(C.n <= 2048, PORSOL_ERR_BAD_ARG, "AMG: coarsening stalled above the dense-solve limit");
     build_coarse_solver(s, *C.P, C.A, C.n);
     const int st = read_int(s, status_.p);
@@ -794,7 +788,7 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         const T* xin = (from_zero && k == 1) ? nullptr : x;
         // algorithmic bytes: matrix values + columns, d gathered once, dinv/r/x in, r/d/x out
         const double bytes = double(P.nent) * (sizeof(T) + 4) + double(n) * sizeof(T) * (xin ? 7 : 6);
-        const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();
+        const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();  // finest level only
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
         PORSOL_LAUNCH(k_cheb_step<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
@@ -809,7 +803,7 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
 template <class T>
 void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
 {
-    if (l == int(lv_.size()) - 1) {
+    if (l == nlev_ - 1) {
         if (nc_ > 0) PORSOL_LAUNCH(k_dense_apply<T><<<1, 512, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop));
         return;
     }

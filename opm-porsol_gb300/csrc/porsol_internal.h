@@ -50,17 +50,21 @@ enum : int {
 // ------------------------------------------------------------------ device buffers
 template <class T>
 struct DBuf {
+    // Grow-only device buffer: alloc() keeps the allocation when it is large enough, so
+    // repeated setups of the same size (every solve) do no cudaMalloc/cudaFree.
     T* p = nullptr;
-    size_t n = 0;
+    size_t n = 0;    // elements in use
+    size_t cap = 0;  // elements allocated
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), cap(o.cap) { o.p = nullptr; o.n = o.cap = 0; }
     DBuf& operator=(DBuf&& o) noexcept
     {
         if (this != &o) {
             release();
-            p = o.p; n = o.n; o.p = nullptr; o.n = 0;
+            p = o.p; n = o.n; cap = o.cap;
+            o.p = nullptr; o.n = o.cap = 0;
         }
         return *this;
     }
@@ -69,15 +73,18 @@ struct DBuf {
     {
         if (p) cudaFree(p);
         p = nullptr;
-        n = 0;
+        n = cap = 0;
     }
     void alloc(size_t cnt)
     {
-        if (cnt == n && p) return;
+        if (cnt <= cap && p) {
+            n = cnt;
+            return;
+        }
         release();
         if (cnt == 0) return;
         PORSOL_CUDA(cudaMalloc(&p, cnt * sizeof(T)));
-        n = cnt;
+        n = cap = cnt;
     }
     void upload(const T* h, size_t cnt, cudaStream_t s)
     {
