@@ -99,6 +99,10 @@ typedef struct porsol_solve_stats {
     double reduction;        /* final ||r||/||r0|| */
     int amg_levels;          /* levels of the AMG hierarchy (0 for ILU0) */
     double mass_balance;     /* max_c |sum_f v - q_c| / max(max_c |q_c|, max_f |v_f|), FP64 */
+    double ms_assemble;      /* wall time of the phases of this solve (host clock, stream synchronised) */
+    double ms_precond_setup;
+    double ms_krylov;
+    double ms_recover;
 } porsol_solve_stats;
 
 void porsol_solve_opts_default(porsol_solve_opts* opts);
@@ -157,6 +161,9 @@ int porsol_get_solution_device(porsol_solver* h, const double** pressure, const 
                                const double** face_pressure);
 
 /* Introspection (printStats, IncompFlowSolverHybrid.hpp:849-871; printSystem :895-905). */
+/* AMG hierarchy of the last type-1..3 solve: rows and stored entries per level (finest
+ * first, at most max_levels written); returns the level count in *levels. */
+int porsol_amg_info(porsol_solver* h, int max_levels, int* levels, int* rows, long long* entries);
 int porsol_num_dofs(porsol_solver* h, int* num_dofs, int* nnz, int* max_ncf, int* num_internal_faces);
 /* cellfaces [nhf], rowptr [ndof+1], colind [nnz] (CSR, sorted), ppartner [ndof] (-1 = none). */
 int porsol_get_structure(porsol_solver* h, int* cellfaces, int* rowptr, int* colind, int* ppartner);

@@ -88,7 +88,8 @@ class SolveOpts(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("reduction", C.c_double),
-                ("amg_levels", C.c_int), ("mass_balance", C.c_double)]
+                ("amg_levels", C.c_int), ("mass_balance", C.c_double), ("ms_assemble", C.c_double),
+                ("ms_precond_setup", C.c_double), ("ms_krylov", C.c_double), ("ms_recover", C.c_double)]
 
 
 class TransportOpts(C.Structure):
@@ -126,6 +127,7 @@ EXPORTS = [
     ("porsol_get_structure", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("porsol_get_inner_products", _i, [_vp, _vp, _vp]),
     ("porsol_get_system", _i, [_vp, _vp, _vp]),
+    ("porsol_amg_info", _i, [_vp, _i, C.POINTER(_i), _vp, _vp]),
     ("porsol_transport_opts_default", None, [C.POINTER(TransportOpts)]),
     ("porsol_transport_create", _i, [C.POINTER(_vp)]),
     ("porsol_transport_destroy", None, [_vp]),
@@ -288,6 +290,13 @@ class PressureSolver:
         gf = np.empty(self.grid.nhf)
         self._check(lib().porsol_get_inner_products(self.h, _p(B), _p(gf)))
         return B, gf
+
+    def amg_info(self):
+        nl = C.c_int()
+        rows = np.zeros(64, np.int32)
+        ent = np.zeros(64, np.int64)
+        self._check(lib().porsol_amg_info(self.h, 64, C.byref(nl), _p(rows), _p(ent)))
+        return rows[:nl.value].tolist(), ent[:nl.value].tolist()
 
     def system(self):
         S = np.empty(self.nnz)

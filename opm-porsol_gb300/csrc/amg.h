@@ -75,7 +75,8 @@ private:
     std::vector<std::unique_ptr<Level>> lv_;   // levels are kept and reused by later setups
     int nlev_ = 0;                              // levels in use
     // setup scratch (grow-only, reused by every setup)
-    DBuf<double> s_d_, s_D_, s_Linv_;
+    DBuf<double> s_D_, s_Linv_;
+    DBuf<float> s_rs_;
     DBuf<int> s_state_, s_partner_, s_join_, s_best_, s_flag_, s_cidx_, s_cnt_, s_pos_, s_width_;
     DBuf<unsigned long long> s_gmax_;
     Aggregates agg2_;

@@ -7,6 +7,7 @@
 //   3. linear solve: ILU0-CG (type 0) or AMG-CG (types 1-3), FP64 or FP32-in-FP64-refinement;
 //   4. computePressureAndFluxes: k_recover.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <sstream>
@@ -176,7 +177,16 @@ void porsol_solver::ensure_recipe(const int* bct_host, const int* bct_dev)
     if (bct_host) {
         for (size_t q = 0; q < bh.size(); ++q) types[q] = bct_host[bh[q]];
     } else {
-        // gather the boundary entries of the device array (boundary faces only)
+        // Compare on the device first; the full array crosses to the host only on a change.
+        if (R.valid) {
+            PORSOL_CUDA(cudaMemsetAsync(redbits.p + 3, 0, sizeof(int), stream));
+            launch_compare_types(stream, int(bh.size()), boundary_hf_d.p, bct_dev, recipe_types_d.p,
+                                 (int*)(redbits.p + 3));
+            int changed = 0;
+            PORSOL_CUDA(cudaMemcpyAsync(&changed, redbits.p + 3, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            PORSOL_CUDA(cudaStreamSynchronize(stream));
+            if (!changed) return;
+        }
         std::vector<int> all(S.g.nhf);
         PORSOL_CUDA(cudaMemcpyAsync(all.data(), bct_dev, sizeof(int) * all.size(), cudaMemcpyDeviceToHost, stream));
         PORSOL_CUDA(cudaStreamSynchronize(stream));
@@ -191,13 +201,23 @@ void porsol_solver::ensure_recipe(const int* bct_host, const int* bct_dev)
     R.slot_ent.upload(R.h_slot_ent, stream);
     R.rhs_ptr.upload(R.h_rhs_ptr, stream);
     R.rhs_ent.upload(R.h_rhs_ent, stream);
+    recipe_types_d.upload(types, stream);
+    boundary_hf_d.upload(bh, stream);
     PORSOL_CUDA(cudaStreamSynchronize(stream));
     recipe_types = types;
     amg_ready = false;   // a different matrix structure of values
 }
 
+namespace {
+double now_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
 void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st)
 {
+    const double t_begin = now_ms();
     const int n = S.N;
     const int maxit = o.linsolver_maxit > 0 ? o.linsolver_maxit : n;
     const SellPattern& P = S.pat;
@@ -216,6 +236,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
             ilu_levels = true;
         }
         ilu.factor(stream, P, val.p);
+        st.ms_precond_setup = now_ms() - t_begin;
         x.zero(stream);
         CgResult r = cg64.solve(stream, P, val.p, ilu, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
         st.iterations = r.iterations;
@@ -236,6 +257,8 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
             amg_ready = true;
             amg_precision = PORSOL_FP64;
         }
+        PORSOL_CUDA(cudaStreamSynchronize(stream));
+        st.ms_precond_setup = now_ms() - t_begin;
         st.amg_levels = amg64.levels();
         CgResult r = cg64.solve(stream, P, val.p, amg64, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
         st.iterations = r.iterations;
@@ -251,6 +274,8 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
     }
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    st.ms_precond_setup = now_ms() - t_begin;
     st.amg_levels = amg32.levels();
     ir_r.alloc(n);
     ir_r32.alloc(n);
@@ -326,6 +351,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     last_src = d_src;
     const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
     if (mixed) val32.alloc(S.pat.nent);
+    const double t_asm = now_ms();
     {
         ProfScope ps(prof, s, PK_ASSEMBLE, double(nc) * (npk * 16.0 + 64) + double(S.pat.nent) * 16.0);
         AssembleArgs a;
@@ -362,7 +388,11 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
         reg_applied = true;
     }
     porsol_solve_stats st{};
+    st.ms_assemble = now_ms() - t_asm;
+    const double t_lin = now_ms();
     linear_solve(o, st);
+    st.ms_krylov = now_ms() - t_lin - st.ms_precond_setup;
+    const double t_rec = now_ms();
     {
         ProfScope ps(prof, s, PK_RECOVER, double(nc) * (npk * 8.0 + 6 * 8 * 4 + 32) + double(S.N) * 8.0);
         RecoverArgs ra;
@@ -391,6 +421,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     double v[3];
     std::memcpy(v, mb, sizeof(v));
     st.mass_balance = v[0] / std::max(std::max(v[1], v[2]), 1e-300);
+    st.ms_recover = now_ms() - t_rec;
     solved = true;
     if (stats) *stats = st;
 }
@@ -625,6 +656,20 @@ int porsol_get_system(porsol_solver* h, double* values, double* rhs)
         }
         if (rhs) h->rhs.download(rhs, S.N, h->stream);
         PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int porsol_amg_info(porsol_solver* h, int max_levels, int* levels, int* rows, long long* entries)
+{
+    return guarded(h, [&] {
+        const bool f32 = h->amg_precision == PORSOL_MIXED;
+        const std::vector<int>& sz = f32 ? h->amg32.level_sizes() : h->amg64.level_sizes();
+        const std::vector<long long>& nz = f32 ? h->amg32.level_nnz() : h->amg64.level_nnz();
+        if (levels) *levels = int(sz.size());
+        for (int l = 0; l < int(sz.size()) && l < max_levels; ++l) {
+            if (rows) rows[l] = sz[l];
+            if (entries) entries[l] = nz[l];
+        }
     });
 }
 

@@ -3,6 +3,9 @@
 // floating-point atomics), so hierarchy and preconditioner are run-to-run reproducible.
 #include <algorithm>
 #include <cmath>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "amg.h"
@@ -65,11 +68,34 @@ __global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__
 }
 
 // ---------------- aggregation ----------------
+// rs_i = 1 / sqrt(|a_ii|): strengths |a_ij| rs_i rs_j are formed in FP32 (a coupling
+// strength needs no more precision, and FP32 keeps the FP64 unit free).
 template <class T>
-__global__ void k_diag_abs(int n, const int* __restrict__ diag, const T* __restrict__ A, double* __restrict__ d)
+__global__ void k_diag_rsqrt(int n, const int* __restrict__ diag, const T* __restrict__ A, float* __restrict__ rs)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) d[i] = fabs(double(A[diag[i]]));
+    if (i < n) rs[i] = rsqrtf(fabsf(float(A[diag[i]])));
+}
+
+// Symmetric 32-bit hash of an edge {i, j}: equal strengths (common on uniform grids) are
+// ordered by this pseudo-random priority, the same from both endpoints, so locally
+// dominant edges are unique and mutual-best matching pairs most rows in a few sweeps.
+__device__ __forceinline__ unsigned edge_hash(int i, int j)
+{
+    const unsigned lo = unsigned(min(i, j)), hi = unsigned(max(i, j));
+    unsigned x = lo * 0x9E3779B1u + hi * 0x85EBCA77u;
+    x ^= x >> 15;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    x *= 0x297A2D39u;
+    x ^= x >> 15;
+    return x;
+}
+
+// (s, hash) lexicographic comparison with the column as the last key
+__device__ __forceinline__ bool stronger(float s, unsigned h, int j, float bs, unsigned bh, int bj)
+{
+    return s > bs || (s == bs && (h > bh || (h == bh && j < bj)));
 }
 
 // state: 0 free, 1 paired, 2 isolated (no off-diagonal coupling: never aggregated)
@@ -92,8 +118,8 @@ __global__ void k_isolated(int n, const int* __restrict__ sp, const int* __restr
 
 template <class T>
 __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
-                       const T* __restrict__ A, const double* __restrict__ d, const int* __restrict__ state,
-                       int* __restrict__ best, int neg, double theta)
+                       const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
+                       int* __restrict__ best, int neg, float theta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -101,17 +127,21 @@ __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict_
         best[i] = -1;
         return;
     }
-    const double di = d[i];
-    double bs = 0.0;
+    const float ri = rs[i];
+    float bs = 0.0f;
+    unsigned bh = 0u;
     int bj = -1;
     for (int t = 0; t < rowlen[i]; ++t) {
         const int k = slot_of(sp, i, t);
         const int j = col[k];
         if (j == i || state[j] != 0) continue;
-        const double a = double(A[k]);
-        const double s = (neg ? -a : fabs(a)) / sqrt(di * d[j]);
-        if (s > 0.0 && s >= theta && (s > bs || (s == bs && j < bj))) {
+        const float a = float(A[k]);
+        const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
+        if (!(s > 0.0f && s >= theta)) continue;
+        const unsigned h = edge_hash(i, j);
+        if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
             bs = s;
+            bh = h;
             bj = j;
         }
     }
@@ -132,21 +162,25 @@ __global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ 
 // unmatched rows pick their strongest paired neighbour (|a_ij| scaled)
 template <class T>
 __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
-                       const T* __restrict__ A, const double* __restrict__ d, const int* __restrict__ state,
+                       const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
                        int* __restrict__ join)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || state[i] != 0) return;
-    const double di = d[i];
-    double bs = 0.0;
+    const float ri = rs[i];
+    float bs = 0.0f;
+    unsigned bh = 0u;
     int bj = -1;
     for (int t = 0; t < rowlen[i]; ++t) {
         const int k = slot_of(sp, i, t);
         const int j = col[k];
         if (j == i || state[j] != 1) continue;
-        const double s = fabs(double(A[k])) / sqrt(di * d[j]);
-        if (s > 0.0 && (s > bs || (s == bs && j < bj))) {
+        const float s = fabsf(float(A[k])) * ri * rs[j];
+        if (!(s > 0.0f)) continue;
+        const unsigned h = edge_hash(i, j);
+        if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
             bs = s;
+            bh = h;
             bj = j;
         }
     }
@@ -299,6 +333,100 @@ __global__ void k_gal_fill(int nc, const int* __restrict__ sp, const int* __rest
         }
     }
     diag_c[I] = dslot;
+}
+
+// Warp-per-coarse-row Galerkin merge: the member rows' entries (column mapped through agg)
+// are loaded into shared memory, bitonic-sorted by column, and duplicates summed (FP64).
+// count: rowlen_c[I] = number of distinct columns; fill: write them into the SELL slots.
+constexpr int GW_WARPS = 4;
+template <class T, int CAP, bool FILL>
+__global__ void __launch_bounds__(GW_WARPS * 32) k_gal_warp(int nc, const int* __restrict__ sp,
+                                                          const int* __restrict__ col, const int* __restrict__ rowlen,
+                                                          const T* __restrict__ A, const int* __restrict__ agg,
+                                                          const int* __restrict__ ptr, const int* __restrict__ idx,
+                                                          int* __restrict__ rowlen_c, const int* __restrict__ sp_c,
+                                                          int* __restrict__ col_c, T* __restrict__ val_c,
+                                                          int* __restrict__ diag_c)
+{
+    __shared__ int sk[GW_WARPS][CAP];
+    __shared__ double sv[GW_WARPS][CAP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I = blockIdx.x * GW_WARPS + w;
+    if (I >= nc) return;   // warp-uniform
+    int* keys = sk[w];
+    double* vals = sv[w];
+    // gather
+    int m = 0;
+    for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
+        const int r = idx[q];
+        const int len = rowlen[r];
+        const int base = sp[r >> 5] + (r & 31);
+        for (int t = lane; t < len; t += 32) {
+            const int k = base + t * 32;
+            const int c = agg[col[k]];
+            keys[m + t] = c < 0 ? INT_MAX : c;
+            vals[m + t] = double(A[k]);
+        }
+        m += len;
+    }
+    int m2 = 1;
+    while (m2 < m) m2 <<= 1;
+    for (int p = m + lane; p < m2; p += 32) {
+        keys[p] = INT_MAX;
+        vals[p] = 0.0;
+    }
+    __syncwarp();
+    // bitonic sort of (key, value) pairs, ascending keys
+    for (int k = 2; k <= m2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int p = lane; p < m2; p += 32) {
+                const int q = p ^ j;
+                if (q > p) {
+                    const bool up = (p & k) == 0;
+                    const int kp = keys[p], kq = keys[q];
+                    if ((kp > kq) == up) {
+                        keys[p] = kq;
+                        keys[q] = kp;
+                        const double t = vals[p];
+                        vals[p] = vals[q];
+                        vals[q] = t;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // distinct keys: heads of runs of equal keys
+    int base = 0, dslot = -1;
+    const int s = I >> 5;
+    const int wdt = FILL ? (sp_c[s + 1] - sp_c[s]) >> 5 : 0;
+    for (int c0 = 0; c0 < m2; c0 += 32) {
+        const int p = c0 + lane;
+        const bool head = p < m2 && keys[p] != INT_MAX && (p == 0 || keys[p] != keys[p - 1]);
+        const unsigned mask = __ballot_sync(0xffffffffu, head);
+        if (FILL && head) {
+            double sum = vals[p];
+            for (int q = p + 1; q < m2 && keys[q] == keys[p]; ++q) sum += vals[q];
+            const int t = base + __popc(mask & ((1u << lane) - 1u));
+            const int kk = sp_c[s] + t * 32 + (I & 31);
+            col_c[kk] = keys[p];
+            val_c[kk] = T(sum);
+            if (keys[p] == I) dslot = kk;
+        }
+        base += __popc(mask);
+    }
+    if (!FILL) {
+        if (lane == 0) rowlen_c[I] = base;
+        return;
+    }
+    for (int t = base + lane; t < wdt; t += 32) {
+        const int kk = sp_c[s] + t * 32 + (I & 31);
+        col_c[kk] = I;
+        val_c[kk] = T(0);
+    }
+    // the diagonal is found by exactly one lane (or none)
+    for (int o = 16; o > 0; o >>= 1) dslot = max(dslot, __shfl_xor_sync(0xffffffffu, dslot, o));
+    if (lane == 0) diag_c[I] = dslot;
 }
 
 __global__ void k_slice_width(int n, int nslices, const int* __restrict__ rowlen, int* __restrict__ width)
@@ -545,7 +673,7 @@ template <class T>
 void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
                       Aggregates& out)
 {
-    DBuf<double>& d = s_d_;
+    DBuf<float>& d = s_rs_;
     DBuf<int>&state = s_state_, &partner = s_partner_, &jn = s_join_, &best = s_best_, &flag = s_flag_,
     &cidx = s_cidx_;
     d.alloc(n);
@@ -556,11 +684,14 @@ void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, b
     flag.alloc(n);
     cidx.alloc(n + 1);
     const int nb = div_up(n, TB);
-    PORSOL_LAUNCH(k_diag_abs<T><<<nb, TB, 0, s>>>(n, P.diag.p, A, d.p));
+    PORSOL_LAUNCH(k_diag_rsqrt<T><<<nb, TB, 0, s>>>(n, P.diag.p, A, d.p));
     PORSOL_LAUNCH(k_isolated<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, state.p, partner.p, jn.p));
-    for (int sweep = 0; sweep < 4; ++sweep) {
+    // Mutual-best matching: each sweep pairs at least the strongest remaining edge; the
+    // stall fallback (join) runs more sweeps so chains and stars also pair up.
+    const int sweeps = join ? 16 : 4;
+    for (int sweep = 0; sweep < sweeps; ++sweep) {
         PORSOL_LAUNCH(k_pick<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, best.p, neg ? 1 : 0,
-                                    theta));
+                                    float(theta)));
         PORSOL_LAUNCH(k_match<<<nb, TB, 0, s>>>(n, state.p, best.p, partner.p));
     }
     if (join) PORSOL_LAUNCH(k_join<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, jn.p));
@@ -597,7 +728,10 @@ template <class T>
 void Amg<T>::aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, Aggregates& out)
 {
     pairwise(s, P, A, n, true, o_.strength, false, out);
+    const int first = out.nc;
     if (out.nc > 0.8 * n) pairwise(s, P, A, n, false, 0.0, true, out);
+    static const bool debug = std::getenv("PORSOL_DEBUG_AMG") != nullptr;
+    if (debug) std::fprintf(stderr, "[amg] round n=%d strong-negative pairs -> %d, final -> %d\n", n, first, out.nc);
 }
 
 template <class T>
@@ -616,17 +750,25 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     const int bound = read_int(s, iscratch_.p);
     PORSOL_REQUIRE(bound <= 2048, PORSOL_ERR_BAD_ARG, "AMG: aggregate rows too long for the Galerkin merge");
     const int nb = div_up(nc, 64);
+    const int nbw = div_up(nc, GW_WARPS);
+    const bool warp = bound <= 1024;
+#define PORSOL_GALW(CAP, FILL)                                                                                      \
+    PORSOL_LAUNCH((k_gal_warp<T, CAP, FILL><<<nbw, GW_WARPS * 32, 0, s>>>(                                          \
+        nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p, Pc.rowlen.p, Pc.slice_ptr.p,          \
+        Pc.col.p, Ac.p, Pc.diag.p)))
 #define PORSOL_GAL(CAP)                                                                                             \
     PORSOL_COUNT_LAUNCH();                                                                                          \
     k_gal_count<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,     \
                                          Pc.rowlen.p)
-    if (bound <= 32) { PORSOL_GAL(32); }
-    else if (bound <= 64) { PORSOL_GAL(64); }
-    else if (bound <= 128) { PORSOL_GAL(128); }
-    else if (bound <= 256) { PORSOL_GAL(256); }
-    else if (bound <= 512) { PORSOL_GAL(512); }
-    else if (bound <= 1024) { PORSOL_GAL(1024); }
-    else { PORSOL_GAL(2048); }
+    if (warp) {
+        if (bound <= 64) { PORSOL_GALW(64, false); }
+        else if (bound <= 128) { PORSOL_GALW(128, false); }
+        else if (bound <= 256) { PORSOL_GALW(256, false); }
+        else if (bound <= 512) { PORSOL_GALW(512, false); }
+        else { PORSOL_GALW(1024, false); }
+    } else {
+        PORSOL_GAL(2048);
+    }
 #undef PORSOL_GAL
     DBuf<int>& width = s_width_;
     width.alloc(Pc.nslices);
@@ -639,14 +781,17 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     PORSOL_COUNT_LAUNCH();                                                                                          \
     k_gal_fill<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,      \
                                         Pc.slice_ptr.p, Pc.col.p, Ac.p, Pc.diag.p)
-    if (bound <= 32) { PORSOL_GALF(32); }
-    else if (bound <= 64) { PORSOL_GALF(64); }
-    else if (bound <= 128) { PORSOL_GALF(128); }
-    else if (bound <= 256) { PORSOL_GALF(256); }
-    else if (bound <= 512) { PORSOL_GALF(512); }
-    else if (bound <= 1024) { PORSOL_GALF(1024); }
-    else { PORSOL_GALF(2048); }
+    if (warp) {
+        if (bound <= 64) { PORSOL_GALW(64, true); }
+        else if (bound <= 128) { PORSOL_GALW(128, true); }
+        else if (bound <= 256) { PORSOL_GALW(256, true); }
+        else if (bound <= 512) { PORSOL_GALW(512, true); }
+        else { PORSOL_GALW(1024, true); }
+    } else {
+        PORSOL_GALF(2048);
+    }
 #undef PORSOL_GALF
+#undef PORSOL_GALW
     if (nc > 0) PORSOL_LAUNCH(k_pad_tail<T><<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p));
     PORSOL_LAUNCH(k_check_diag<<<div_up(nc, TB), TB, 0, s>>>(nc, Pc.diag.p, status_.p));
     PORSOL_CUDA(cudaGetLastError());
@@ -695,6 +840,7 @@ void Amg<T>::build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* 
 template <class T>
 void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const AmgOpts& o)
 {
+    this->bump_generation();
     o_ = o;
     sizes_.clear();
     nnzs_.clear();

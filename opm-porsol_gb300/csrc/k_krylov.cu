@@ -15,7 +15,8 @@ namespace {
 
 constexpr int RB = 256;  // threads per block of the vector kernels
 
-__device__ __forceinline__ double warp_sum(double v)
+template <class V>
+__device__ __forceinline__ V warp_sum(V v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -23,17 +24,20 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // Block reduce + last-block finalisation.  Returns true in thread 0 of the last block,
-// with *total holding the full sum.
-__device__ bool block_reduce_last(double v, double* partial, unsigned int* counter, double* total)
+// with *total holding the full sum.  The per-thread value type V is the vector type: FP32
+// vectors are summed in FP32 within a warp (32 terms) and in FP64 from there on, so the
+// FP64 unit (a small fraction of GB300's FP32 rate) only sees one value per warp.
+template <class V>
+__device__ bool block_reduce_last(V v0, double* partial, unsigned int* counter, double* total)
 {
     __shared__ double ws[RB / 32];
     __shared__ bool amlast;
-    v = warp_sum(v);
+    const double v = double(warp_sum<V>(v0));
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x < 32) {
         double t = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
-        t = warp_sum(t);
+        t = warp_sum<double>(t);
         if (threadIdx.x == 0) {
             partial[blockIdx.x] = t;
             __threadfence();
@@ -48,7 +52,7 @@ __device__ bool block_reduce_last(double v, double* partial, unsigned int* count
     double s = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partial)[b];
     // fixed-order tree over threads
-    s = warp_sum(s);
+    s = warp_sum<double>(s);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -60,15 +64,17 @@ __device__ bool block_reduce_last(double v, double* partial, unsigned int* count
     return threadIdx.x == 0;
 }
 
+// Row r of a SELL matrix times x, accumulated in the vector type TX (FP32 rows stay on the
+// FP32 pipe).
 template <class TV, class TX>
-__device__ __forceinline__ double sell_row(const int* __restrict__ sp, const int* __restrict__ col,
-                                           const TV* __restrict__ val, const TX* __restrict__ x, int r)
+__device__ __forceinline__ TX sell_row(const int* __restrict__ sp, const int* __restrict__ col,
+                                       const TV* __restrict__ val, const TX* __restrict__ x, int r)
 {
     const int s = r >> 5, lane = r & 31;
     const int b = sp[s], w = (sp[s + 1] - b) >> 5;
-    double acc = 0.0;
+    TX acc = 0;
     int k = b + lane;
-    for (int t = 0; t < w; ++t, k += 32) acc += double(val[k]) * double(x[col[k]]);
+    for (int t = 0; t < w; ++t, k += 32) acc += TX(val[k]) * x[col[k]];
     return acc;
 }
 
@@ -88,7 +94,7 @@ __global__ void k_residual(int n, const int* __restrict__ sp, const int* __restr
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    y[r] = TX(double(b[r]) - sell_row(sp, col, val, x, r));
+    y[r] = b[r] - sell_row(sp, col, val, x, r);
 }
 
 // r = b - A x; def0 = ||r||
@@ -99,15 +105,14 @@ __global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ s
                                                 double* partial, unsigned int* counter, CgHostView* hv)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
+    T v = 0;
     if (i < n) {
-        const double ri = double(b[i]) - sell_row(sp, col, val, x, i);
-        r[i] = T(ri);
-        const double rr = double(T(ri));
-        v = rr * rr;
+        const T ri = b[i] - sell_row(sp, col, val, x, i);
+        r[i] = ri;
+        v = ri * ri;
     }
     double tot;
-    if (block_reduce_last(v, partial, counter, &tot)) {
+    if (block_reduce_last<T>(v, partial, counter, &tot)) {
         const double d0 = sqrt(tot);
         st->def0 = d0;
         st->def = d0;
@@ -132,10 +137,13 @@ __global__ void __launch_bounds__(RB) k_dot_zr(int n, const T* __restrict__ z, c
 {
     if (st->stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
-    if (i < n) v = double(z[i]) * double(r[i]);
+    T v = 0;
+    if (i < n) v = z[i] * r[i];
     double tot;
-    if (block_reduce_last(v, partial, counter, &tot)) st->rho = tot;
+    if (block_reduce_last<T>(v, partial, counter, &tot)) {
+        st->rho = tot;
+        st->beta = tot / st->rholast;
+    }
 }
 
 template <class T>
@@ -156,14 +164,17 @@ __global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ s
 {
     if (st->stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
+    T v = 0;
     if (i < n) {
-        const T qi = T(sell_row(sp, col, val, p, i));
+        const T qi = sell_row(sp, col, val, p, i);
         q[i] = qi;
-        v = double(p[i]) * double(qi);
+        v = p[i] * qi;
     }
     double tot;
-    if (block_reduce_last(v, partial, counter, &tot)) st->alpha = tot;
+    if (block_reduce_last<T>(v, partial, counter, &tot)) {
+        st->alpha = tot;
+        st->lambda = st->rholast / tot;
+    }
 }
 
 // lambda = rholast/alpha; x += lambda p; r -= lambda q; def = ||r||; convergence test
@@ -174,17 +185,17 @@ __global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* _
 {
     if (st->stop) return;
     const double alpha = st->alpha;
-    const double lambda = st->rholast / alpha;
+    const T lambda = T(st->lambda);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
+    T v = 0;
     if (i < n) {
-        x[i] = T(double(x[i]) + lambda * double(p[i]));
-        const T ri = T(double(r[i]) - lambda * double(q[i]));
+        x[i] = x[i] + lambda * p[i];
+        const T ri = r[i] - lambda * q[i];
         r[i] = ri;
-        v = double(ri) * double(ri);
+        v = ri * ri;
     }
     double tot;
-    if (block_reduce_last(v, partial, counter, &tot)) {
+    if (block_reduce_last<T>(v, partial, counter, &tot)) {
         const double def = sqrt(tot);
         st->def = def;
         st->iter += 1;
@@ -205,9 +216,9 @@ template <class T>
 __global__ void k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st, int* flip)
 {
     if (st->stop) return;
-    const double beta = st->rho / st->rholast;
+    const T beta = T(st->beta);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = T(double(z[i]) + beta * double(p[i]));
+    if (i < n) p[i] = z[i] + beta * p[i];
     (void)flip;
 }
 
@@ -265,9 +276,9 @@ __global__ void __launch_bounds__(RB) k_norm2(int n, const T* __restrict__ x, do
                                               double* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const double v = i < n ? double(x[i]) * double(x[i]) : 0.0;
+    const T v = i < n ? x[i] * x[i] : T(0);
     double tot;
-    if (block_reduce_last(v, partial, counter, &tot)) *out = tot;
+    if (block_reduce_last<T>(v, partial, counter, &tot)) *out = tot;
 }
 
 // ---------------- ILU(0) ----------------
@@ -403,8 +414,33 @@ void PcgSolver<TV, T>::setup(int n, cudaStream_t s)
 template <class TV, class T>
 PcgSolver<TV, T>::~PcgSolver()
 {
+    if (exec_) cudaGraphExecDestroy(exec_);
     if (hview_) cudaFreeHost(hview_);
     for (auto& e : ev_) cudaEventDestroy(e);
+}
+
+template <class TV, class T>
+void PcgSolver<TV, T>::iteration(cudaStream_t s, const SellPattern& P, const TV* val, Precond<T>& M, T* x,
+                                 Profiler* prof, int prof_kernel)
+{
+    const int n = P.n;
+    const int nb = div_up(n, RB);
+    const int* stop = &st_.p->stop;
+    const double spmv_bytes = double(P.nent) * (sizeof(TV) + 4) + 2.0 * n * sizeof(T);
+    {
+        const bool pf = prof && prof->on && prof_kernel >= 0;
+        cudaEvent_t ev = nullptr;
+        if (pf) prof->begin(s, prof_kernel, spmv_bytes, &ev);
+        PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                         red_.partial.p, red_.counter.p));
+        if (pf) prof->end(s, prof_kernel, spmv_bytes, ev);
+    }
+    PORSOL_LAUNCH(k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
+                                                   dview_));
+    M.apply(s, r_.p, z_.p, stop);
+    PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
+    PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr));
+    PORSOL_LAUNCH(k_cg_roll<<<1, 1, 0, s>>>(st_.p));
 }
 
 template <class TV, class T>
@@ -423,37 +459,52 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
     init.tol = tol;
     init.maxit = maxit;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
-    PORSOL_LAUNCH(k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p, red_.partial.p,
-                                       red_.counter.p, dview_));
+    PORSOL_LAUNCH(k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
+                                                     red_.partial.p, red_.counter.p, dview_));
     PORSOL_CUDA(cudaGetLastError());
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
     PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
     PORSOL_LAUNCH(k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
     PORSOL_CUDA(cudaGetLastError());
+    // One iteration is captured into a CUDA graph (re-captured when the matrix, vectors or
+    // preconditioner change) unless per-kernel profiling is on.
+    const bool graphs = use_graphs_ && !(prof && prof->on);
+    if (graphs) {
+        const void* key[5] = {&P, val, x, (const void*)&M, nullptr};
+        bool same = exec_ && key_gen_ == M.generation();
+        for (int k = 0; k < 4 && same; ++k) same = key_[k] == key[k];
+        if (!same) {
+            if (exec_) {
+                cudaGraphExecDestroy(exec_);
+                exec_ = nullptr;
+            }
+            cudaGraph_t g;
+            const long long l0 = g_launches.load();
+            PORSOL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            iteration(s, P, val, M, x, nullptr, -1);
+            PORSOL_CUDA(cudaStreamEndCapture(s, &g));
+            nodes_ = g_launches.load() - l0;   // captured, not run: counted at each replay
+            g_launches.fetch_sub(nodes_);
+            PORSOL_CUDA(cudaGraphInstantiate(&exec_, g, 0));
+            PORSOL_CUDA(cudaGraphDestroy(g));
+            for (int k = 0; k < 4; ++k) key_[k] = key[k];
+            key_gen_ = M.generation();
+        }
+    }
     // Iterations are queued ahead; the host waits on the event of iteration i - LOOKAHEAD
     // and reads the mapped stop flag.  Iterations queued after convergence are no-ops.
     const int LOOKAHEAD = 2;
-    const double spmv_bytes = double(P.nent) * (sizeof(TV) + 4) + 2.0 * n * sizeof(T);
     int it = 0;
     bool done = false;
     while (!done) {
         if (it < maxit) {
-            if (prof && prof_kernel >= 0) {
-                ProfScope ps(*prof, s, prof_kernel, spmv_bytes);
-                PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                   red_.partial.p, red_.counter.p));
+            if (graphs) {
+                PORSOL_CUDA(cudaGraphLaunch(exec_, s));
+                g_launches.fetch_add(nodes_);
             } else {
-                PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                   red_.partial.p, red_.counter.p));
+                iteration(s, P, val, M, x, prof, prof_kernel);
             }
-            PORSOL_LAUNCH(k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
-                                             dview_));
-            PORSOL_CUDA(cudaGetLastError());
-            M.apply(s, r_.p, z_.p, stop);
-            PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
-            PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr));
-            PORSOL_LAUNCH(k_cg_roll<<<1, 1, 0, s>>>(st_.p));
             PORSOL_CUDA(cudaGetLastError());
             PORSOL_CUDA(cudaEventRecord(ev_[it % ev_.size()], s));
             ++it;
@@ -529,6 +580,7 @@ void Ilu0::build_levels(const SellPattern& P, cudaStream_t s)
 
 void Ilu0::factor(cudaStream_t s, const SellPattern& P, const double* val)
 {
+    bump_generation();
     lu_.alloc(P.nent);
     PORSOL_CUDA(cudaMemcpyAsync(lu_.p, val, P.nent * sizeof(double), cudaMemcpyDeviceToDevice, s));
     status_.alloc(1);

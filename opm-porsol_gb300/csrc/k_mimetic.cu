@@ -344,6 +344,13 @@ __global__ void k_mass_balance(int nc, const int* __restrict__ facepos, const do
     }
 }
 
+__global__ void k_compare_types(int nb, const int* __restrict__ bhf, const int* __restrict__ bct,
+                                const int* __restrict__ cached, int* __restrict__ changed)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nb && bct[bhf[q]] != cached[q]) *changed = 1;
+}
+
 __global__ void k_check_finite(long long n, const double* __restrict__ v, int* status)
 {
     bool bad = false;
@@ -422,6 +429,13 @@ void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const doubl
 {
     if (nc == 0) return;
     PORSOL_LAUNCH(k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_compare_types(cudaStream_t s, int nb, const int* bhf, const int* bct, const int* cached, int* changed)
+{
+    if (nb == 0) return;
+    PORSOL_LAUNCH(k_compare_types<<<div_up(nb, 256), 256, 0, s>>>(nb, bhf, bct, cached, changed));
     PORSOL_CUDA(cudaGetLastError());
 }
 

@@ -73,5 +73,7 @@ void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* o
 void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const double* outflux, const double* src,
                          unsigned long long* out3);
 void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status);
+// changed = 1 if bct[bhf[q]] != cached[q] for some boundary half-face q
+void launch_compare_types(cudaStream_t s, int nb, const int* bhf, const int* bct, const int* cached, int* changed);
 
 }  // namespace porsol

@@ -8,7 +8,7 @@ namespace porsol {
 // Device-resident CG scalars.  Written by the last block of each reduction kernel; read by
 // the next kernel in stream order, so no host round trip is needed per iteration.
 struct CgDev {
-    double rho, rholast, alpha, def0, def, tol;
+    double rho, rholast, alpha, def0, def, tol, lambda, beta;
     int iter, maxit, converged, stop, breakdown, pad;
 };
 
@@ -29,8 +29,15 @@ struct RedScratch {
 template <class T>
 struct Precond {
     virtual ~Precond() = default;
-    // z = M^{-1} r; kernels must do nothing when *stop != 0.
+    // z = M^{-1} r; kernels must do nothing when *stop != 0.  apply() must not synchronise
+    // or allocate: it is captured into a CUDA graph.
     virtual void apply(cudaStream_t s, const T* r, T* z, const int* stop) = 0;
+    // Changes whenever the kernels apply() launches change (new setup/factorisation).
+    long long generation() const { return gen_; }
+    void bump_generation() { ++gen_; }
+
+private:
+    long long gen_ = 0;
 };
 
 template <class TV, class TX>
@@ -55,6 +62,8 @@ public:
     void setup(int n, cudaStream_t s);
     CgResult solve(cudaStream_t s, const SellPattern& P, const TV* val, Precond<T>& M, const T* b, T* x,
                    double tol, int maxit, Profiler* prof = nullptr, int prof_kernel = -1);
+    // Replay one CG iteration (SpMV, updates, preconditioner) as a CUDA graph.
+    void set_graphs(bool on) { use_graphs_ = on; }
     ~PcgSolver();
 
 private:
@@ -65,6 +74,13 @@ private:
     CgHostView* hview_ = nullptr;
     CgHostView* dview_ = nullptr;
     std::vector<cudaEvent_t> ev_;
+    bool use_graphs_ = true;
+    cudaGraphExec_t exec_ = nullptr;
+    const void* key_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    long long key_gen_ = -1;
+    long long nodes_ = 0;   // kernels in one captured iteration
+    void iteration(cudaStream_t s, const SellPattern& P, const TV* val, Precond<T>& M, T* x, Profiler* prof,
+                   int prof_kernel);
 };
 
 // ILU(0) with the pivots stored inverted, factor and triangular solves level-scheduled

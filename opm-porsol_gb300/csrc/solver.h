@@ -29,7 +29,7 @@ struct porsol_solver {
     // assembly
     porsol::Recipe R;
     std::vector<int> recipe_types;   // boundary FlowBC types the recipe was built for
-    porsol::DBuf<int> recipe_types_d;
+    porsol::DBuf<int> recipe_types_d, boundary_hf_d;
     porsol::DBuf<double> sloc, F, L, g, rrow, pb, totmob, mobdens, rhs, x;
     porsol::DBuf<double> val;
     porsol::DBuf<float> val32;
