@@ -293,7 +293,11 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         // O(1) however small the FP64 residual becomes.
         to_f32_scaled(stream, n, ir_r.p, ir_r32.p, 1.0 / rn);
         PORSOL_CUDA(cudaMemsetAsync(ir_d32.p, 0, n * sizeof(float), stream));
-        CgResult r = cg32.solve(stream, P, val32.p, amg32, ir_r32.p, ir_d32.p, inner_tol, maxit - total, &prof,
+        // The last refinement step only needs the remaining reduction (times a safety factor
+        // of 0.3), not the full inner tolerance.
+        const double needed = 0.3 * o.residual_tolerance * r0 / rn;
+        const double tol_k = std::min(0.5, std::max(inner_tol, needed));
+        CgResult r = cg32.solve(stream, P, val32.p, amg32, ir_r32.p, ir_d32.p, tol_k, maxit - total, &prof,
                                 PK_SPMV32);
         total += r.iterations;
         ++outer;

@@ -688,7 +688,7 @@ void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, b
     PORSOL_LAUNCH(k_isolated<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, state.p, partner.p, jn.p));
     // Mutual-best matching: each sweep pairs at least the strongest remaining edge; the
     // stall fallback (join) runs more sweeps so chains and stars also pair up.
-    const int sweeps = join ? 16 : 4;
+    const int sweeps = join ? 8 : 4;
     for (int sweep = 0; sweep < sweeps; ++sweep) {
         PORSOL_LAUNCH(k_pick<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, best.p, neg ? 1 : 0,
                                     float(theta)));
@@ -761,7 +761,8 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     k_gal_count<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,     \
                                          Pc.rowlen.p)
     if (warp) {
-        if (bound <= 64) { PORSOL_GALW(64, false); }
+        if (bound <= 32) { PORSOL_GALW(32, false); }
+        else if (bound <= 64) { PORSOL_GALW(64, false); }
         else if (bound <= 128) { PORSOL_GALW(128, false); }
         else if (bound <= 256) { PORSOL_GALW(256, false); }
         else if (bound <= 512) { PORSOL_GALW(512, false); }
@@ -782,7 +783,8 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     k_gal_fill<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,      \
                                         Pc.slice_ptr.p, Pc.col.p, Ac.p, Pc.diag.p)
     if (warp) {
-        if (bound <= 64) { PORSOL_GALW(64, true); }
+        if (bound <= 32) { PORSOL_GALW(32, true); }
+        else if (bound <= 64) { PORSOL_GALW(64, true); }
         else if (bound <= 128) { PORSOL_GALW(128, true); }
         else if (bound <= 256) { PORSOL_GALW(256, true); }
         else if (bound <= 512) { PORSOL_GALW(512, true); }
