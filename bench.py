@@ -44,11 +44,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--dims", default="200,200,25")
-    ap.add_argument("--tol", type=float, default=1e-10,
+    ap.add_argument("--tol", type=float, default=1e-11,
                     help="residual reduction of the mixed-precision solves (1e-8 flux error)")
     ap.add_argument("--tol64", type=float, default=1e-11,
                     help="residual reduction of the FP64 solves (1e-8 flux error)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", choices=["mixed", "fp64"], default=None,
+                    help="run warmup + steps of one precision and print nothing else (for ncu captures)")
     return ap.parse_args()
 
 
@@ -240,6 +242,15 @@ def run_gpu(args):
         st = s.solve_device(fluid, d_sat.data_ptr(), d_bct.data_ptr(), d_bcv.data_ptr(), d_src.data_ptr(), opts=o)
         s.post_process_fluxes()
         return st
+
+    if args.profile_only:
+        o = opts(pkg.MIXED if args.profile_only == "mixed" else pkg.FP64,
+                 args.tol if args.profile_only == "mixed" else args.tol64)
+        for _ in range(args.warmup + args.steps):
+            step_device(o)
+        torch.cuda.synchronize()
+        s.close()
+        return
 
     # FP64 reference solution for the error figures (not timed)
     step_device(opts(pkg.FP64, 1e-12))

@@ -9,6 +9,7 @@
 #include <cstring>
 
 #include "amg.h"
+#include "sell.cuh"
 
 namespace porsol {
 
@@ -507,20 +508,16 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __res
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
+    T acc;
     if (xc) {
-        for (int q = 0; q < w; ++q, k += 32) {
-            const int j = col[k];
+        acc = sell_dot<T>(sp, col, A, i, [t, xc, agg, wp](int j) {
             const int aj = agg[j];
-            acc += A[k] * (t[j] + (aj >= 0 ? wp * xc[aj] : T(0)));
-        }
+            return t[j] + (aj >= 0 ? wp * xc[aj] : T(0));
+        });
         const int ai = agg[i];
         x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
     } else {
-        for (int q = 0; q < w; ++q, k += 32) acc += A[k] * t[col[k]];
+        acc = sell_dot<T>(sp, col, A, i, [t](int j) { return t[j]; });
     }
     const T ri = dinv[i] * (b[i] - acc);
     r[i] = ri;
@@ -536,11 +533,7 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
-    for (int q = 0; q < w; ++q, k += 32) acc += A[k] * d_in[col[k]];
+    const T acc = sell_dot<T>(sp, col, A, i, [d_in](int j) { return d_in[j]; });
     const T di = d_in[i];
     T xi = (x_in ? x_in[i] : T(0)) + di;
     const T ri = r[i] - dinv[i] * acc;
@@ -558,11 +551,7 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int s = i >> 5, lane = i & 31;
-    const int base = sp[s], w = (sp[s + 1] - base) >> 5;
-    T acc = 0;
-    int k = base + lane;
-    for (int t = 0; t < w; ++t, k += 32) acc += A[k] * x[col[k]];
+    const T acc = sell_dot<T>(sp, col, A, i, [x](int j) { return x[j]; });
     r[i] = b[i] - acc;
 }
 

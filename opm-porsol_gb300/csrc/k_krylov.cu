@@ -8,6 +8,7 @@
 #include <cmath>
 
 #include "krylov.h"
+#include "sell.cuh"
 
 namespace porsol {
 
@@ -70,12 +71,7 @@ template <class TV, class TX>
 __device__ __forceinline__ TX sell_row(const int* __restrict__ sp, const int* __restrict__ col,
                                        const TV* __restrict__ val, const TX* __restrict__ x, int r)
 {
-    const int s = r >> 5, lane = r & 31;
-    const int b = sp[s], w = (sp[s + 1] - b) >> 5;
-    TX acc = 0;
-    int k = b + lane;
-    for (int t = 0; t < w; ++t, k += 32) acc += TX(val[k]) * x[col[k]];
-    return acc;
+    return sell_dot<TX>(sp, col, val, r, [x](int j) { return x[j]; });
 }
 
 template <class TV, class TX>
