@@ -214,6 +214,21 @@ int porsol_transport_solve_device(porsol_transport* t, double* sat, double time,
                                   const double* outflux, const double* injection,
                                   porsol_transport_stats* stats);
 
+/* No counterpart in the reference.  The viscous CFL time step of the transport solver
+ * (the quantity findCFLtimeVelocity bounds, before the Courant factor), for callers that may
+ * not allocate device memory when they need it -- e.g. a simulator whose device memory is
+ * owned by its own pool, or code running while a stream is captured into a CUDA graph.
+ * All arrays are device pointers of the current device (layout of porsol_grid; outflux per
+ * half-face, porosity per cell); *dt is a host double.  No device memory is allocated: the
+ * scratch is a fixed array inside the library (256 KiB, held by every GPU that loads
+ * the library until exit), so num_cells must be <= 4,194,304 (PORSOL_ERR_BAD_ARG beyond).
+ * The first call on a device looks that array up, so make it before any stream capture.
+ * Calls that overlap on the GPU share the array and race.  stream may be NULL.
+ * Returns PORSOL_ERR_CFL (with *dt = 0) when a cell's step is zero. */
+int porsol_transport_cfl_noalloc(int num_cells, const int* cell_facepos, const double* outflux,
+                                 const double* cell_volume, const double* porosity, double cfl_factor,
+                                 double* dt, void* stream);
+
 /* ------------------------------------------------------ profiling */
 /* Per-kernel CUDA-event timing on the handle's stream (off by default). */
 int porsol_profile_enable(porsol_solver* h, int enable);

@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libporsol_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE, "-I", CSRC]
-SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "capi.cu"]
+SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "capi.cu", "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
 FLUID_CELLWISE, FLUID_COREY2 = 0, 1
@@ -141,6 +141,7 @@ EXPORTS = [
     ("porsol_profile_reset", _i, [_vp]),
     ("porsol_stream", _vp, [_vp]),
     ("porsol_launch_count", C.c_longlong, []),
+    ("porsol_transport_cfl_noalloc", _i, [_i, _vp, _vp, _vp, _vp, _d, C.POINTER(_d), _vp]),
 ]
 
 _lib = None
