@@ -277,6 +277,12 @@ class PressureSolver:
         self._check(lib().porsol_get_solution(self.h, _p(p), _p(v), _p(pi)))
         return p, v, pi
 
+    def solution_device(self):
+        """Device addresses of (pressure, outflux, face pressure), valid until the next solve."""
+        p, v, pi = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        self._check(lib().porsol_get_solution_device(self.h, C.byref(p), C.byref(v), C.byref(pi)))
+        return p.value, v.value, pi.value
+
     def structure(self):
         cf = np.empty(self.grid.nhf, np.int32)
         rp = np.empty(self.n + 1, np.int32)
@@ -353,6 +359,15 @@ class TransportSolver:
         o = opts if opts is not None else default_transport_opts()
         self._check(lib().porsol_transport_init(self.h, C.byref(self.grid.s), *[_p(a) for a in self._keep[:2]],
                                                 C.byref(fluid), *[_p(a) for a in self._keep[2:]], C.byref(o)))
+
+    def solve_device(self, d_sat, time, d_outflux, d_injection=0, grav=(0.0, 0.0, 0.0)):
+        """In-place update of the device saturation array (raw device addresses)."""
+        st = TransportStats()
+        g = _f64(grav)
+        self._check(lib().porsol_transport_solve_device(self.h, C.c_void_p(d_sat), float(time), _p(g),
+                                                        C.c_void_p(d_outflux), C.c_void_p(d_injection or None),
+                                                        C.byref(st)))
+        return st
 
     def solve(self, sat, time, outflux, injection=None, grav=(0.0, 0.0, 0.0)):
         s = _f64(sat).copy()

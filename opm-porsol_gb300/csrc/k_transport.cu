@@ -39,11 +39,13 @@ struct FaceEntry {
     double nn;          // n . n
 };
 
-__device__ __forceinline__ double mob1(double s, double mu1) { return (s * s) / mu1; }
-__device__ __forceinline__ double mob2(double s, double mu2) { return ((1.0 - s) * (1.0 - s)) / mu2; }
+// kr_i / mu_i with the reciprocal viscosities precomputed (FP64 division is a multi-FMA
+// sequence on this GPU; the products differ from the quotients by at most one rounding)
+__device__ __forceinline__ double mob1(double s, double imu1) { return (s * s) * imu1; }
+__device__ __forceinline__ double mob2(double s, double imu2) { return ((1.0 - s) * (1.0 - s)) * imu2; }
 
 struct TrParams {
-    double mu1, mu2;
+    double mu1, mu2;   // reciprocal viscosities 1/mu1, 1/mu2
     int visc, grav, cap;
 };
 
@@ -269,6 +271,8 @@ void porsol_transport::init(const porsol_grid* grid, const double* K, const doub
     status.zero(s);
     red.alloc(2);
     grav_cached[0] = grav_cached[1] = grav_cached[2] = NAN;
+    const double zero[3] = {0.0, 0.0, 0.0};
+    build_entries(zero);   // face tables for zero gravity; transportSolve rebuilds only for another vector
     PORSOL_CUDA(cudaStreamSynchronize(s));
     ready = true;
 }
@@ -447,7 +451,8 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     double dt = time / n;
     sat0.alloc(nc);
     PORSOL_CUDA(cudaMemcpyAsync(sat0.p, d_sat, nc * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    TrParams p{fluid.viscosity1, fluid.viscosity2, o.method_viscous, o.method_gravity, o.method_capillary};
+    TrParams p{1.0 / fluid.viscosity1, 1.0 / fluid.viscosity2, o.method_viscous, o.method_gravity,
+               o.method_capillary};
     const int nfe = int(fe_h.size());
     int repeats = 0;
     const int max_repeats = 10;
