@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--impes", type=int, default=0,
                     help="run the 200x200x25 IMPES case for this many steps (50 in the configuration) "
                          "instead of the pressure benchmark and print its own JSON line")
+    ap.add_argument("--upscale", type=int, default=0,
+                    help="batched periodic upscaling of this many sub-grids instead of the pressure bench")
     ap.add_argument("--profile-only", choices=["mixed", "fp64"], default=None,
                     help="run warmup + steps of one precision and print nothing else (for ncu captures)")
     return ap.parse_args()
@@ -433,10 +435,71 @@ def run_impes(args):
     print(json.dumps(out), flush=True)
 
 
+def run_upscale(args):
+    """Configuration 3: effective permeability of N periodic unit-cube sub-grids (side n ~ U{8..32},
+    full log-normal tensors with random axes), three unit pressure-jump solves each, as one
+    block-diagonal system on the GPU.  A step is one porsol_upscale_periodic call with host inputs
+    and host K_eff out (grid, tensors, assembly, AMG setup, 3 solves, side fluxes).  The CPU
+    baseline runs the oracle's per-sub-grid ILU0-CG solves on a seeded uniform sample of the
+    sub-grids and scales the time by N / sample."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    wl = ge.load_module("workloads")
+    union, sizes, K = wl.case3(num=args.upscale)
+    K = np.ascontiguousarray(K)
+    out = {"metric": "upscaled sub-grids/s (3 periodic solves each)", "unit": "sub-grids/s",
+           "config": {"workload": f"{args.upscale} periodic unit cubes, n ~ U{{8..32}}, log-normal full tensors "
+                                  "sigma 1.5, unit pressure jump per axis", "cells": union.num_cells,
+                      "tol": args.tol}}
+    res = {}
+    steps = max(1, min(args.steps, 3))
+    for name, prec, tol in (("mixed", pkg.MIXED, args.tol), ("fp64", pkg.FP64, args.tol64)):
+        s = pkg.PressureSolver()
+        o = pkg.default_solve_opts(residual_tolerance=tol, precision=prec)
+        keff, st = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(), o)   # warm-up
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            keff, st = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(), o)
+            times.append(time.perf_counter() - t0)
+        res[name] = keff
+        t = float(np.median(times))
+        out[name] = {"value": round(args.upscale / t, 3), "seconds": round(t, 4), "cg_iterations": st.iterations,
+                     "amg_levels": st.amg_levels, "ms_precond_setup": round(st.ms_precond_setup, 2),
+                     "ms_krylov": round(st.ms_krylov, 2)}
+        s.close()
+    out["value"] = out["mixed"]["value"]
+    out["speedup_mixed_vs_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    scale = np.abs(res["fp64"]).reshape(len(sizes), 9).max(axis=1)[:, None, None]
+    out["max_rel_diff_mixed_vs_fp64"] = float((np.abs(res["mixed"] - res["fp64"]) / scale).max())
+    if not args.no_cpu_baseline:
+        import oracle
+        if not os.path.exists(oracle.LIB_PATH):
+            oracle.build()
+        pick = np.random.default_rng(7).choice(len(sizes), size=min(16, len(sizes)), replace=False)
+        t0 = time.perf_counter()
+        err = 0.0
+        for g in pick:
+            c0, c1 = union.cellpos[g], union.cellpos[g + 1]
+            ref, _ = oracle.upscale_periodic(union.grids[g], K[c0:c1], args.tol64)
+            err = max(err, float(np.abs(res["fp64"][g] - ref).max() / np.abs(ref).max()))
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(len(pick) / el, 4), "unit": "sub-grids/s", "cores": 1, "kind": "port",
+                               "sample": f"{len(pick)} uniformly sampled sub-grids of the batch, ILU0-CG tol "
+                                         f"{args.tol64}, 3 solves each"}
+        out["max_rel_diff_fp64_vs_oracle_sample"] = err
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impes:
         run_impes(args)
+        return
+    if args.upscale:
+        run_upscale(args)
         return
     if args.impl == "reference":
         run_reference(args)

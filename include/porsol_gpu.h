@@ -173,6 +173,22 @@ int porsol_get_inner_products(porsol_solver* h, double* binv, double* gflux);
  * order of porsol_get_structure, rhs [ndof]. */
 int porsol_get_system(porsol_solver* h, double* values, double* rhs);
 
+/* ------------------------------------------------------ batched periodic upscaling */
+/* Effective permeability of many independent sub-grids (no single-call counterpart in the
+ * reference: each sub-grid and direction is what setupUpscalingConditions(Periodic)
+ * (common/setupBoundaryConditions.hpp:136-157) + IncompFlowSolverHybrid::solve compute).
+ * `grid` is the disjoint union of num_grids sub-grids, sub-grid g owning cells
+ * [grid_cellpos[g], grid_cellpos[g+1]); every boundary half-face is periodic with partner
+ * boundary id hf_partner_bid and canonical side hf_side (1..6 = x-, x+, y-, y+, z-, z+, 0 for
+ * interior).  For d = x, y, z the library solves with a unit pressure drop across d (periodic
+ * jump +1 on side 2d+1, -1 on side 2d+2), unit mobility, each sub-grid regularised as its own
+ * pure-periodic solve, and returns k_eff[9 g + 3 i + d] = L_d * (Q_i / A_i), with Q_i the net
+ * flux through the sub-grid's side 2i+2, A_i that side's area and L_d the sub-grid's extent in d.
+ * The three directions share one AMG hierarchy.  opts may be NULL (AMG-CG, FP64, 1e-8). */
+int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_grids, const int* grid_cellpos,
+                            const int* hf_partner_bid, const int* hf_side, const double* perm,
+                            const porsol_solve_opts* opts, double* k_eff, porsol_solve_stats* stats);
+
 /* ------------------------------------------------------ transport */
 typedef struct porsol_transport porsol_transport;
 

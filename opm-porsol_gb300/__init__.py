@@ -128,6 +128,8 @@ EXPORTS = [
     ("porsol_get_inner_products", _i, [_vp, _vp, _vp]),
     ("porsol_get_system", _i, [_vp, _vp, _vp]),
     ("porsol_amg_info", _i, [_vp, _i, C.POINTER(_i), _vp, _vp]),
+    ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
+                                     C.POINTER(SolveStats)]),
     ("porsol_transport_opts_default", None, [C.POINTER(TransportOpts)]),
     ("porsol_transport_create", _i, [C.POINTER(_vp)]),
     ("porsol_transport_destroy", None, [_vp]),
@@ -264,6 +266,21 @@ class PressureSolver:
                                               C.c_void_p(d_bct), C.c_void_p(d_bcv), C.c_void_p(d_src), C.byref(o),
                                               C.byref(st)))
         return st
+
+    def upscale_periodic(self, grid, cellpos, partner_bid, side, perm, opts=None):
+        """Effective permeability (num_grids, 3, 3) of a batch of periodic sub-grids."""
+        self.grid = _GridArrays(grid)
+        keep = [_i32(cellpos), _i32(partner_bid), _i32(side), _f64(perm)]
+        ng = len(keep[0]) - 1
+        keff = np.zeros(9 * ng)
+        st = SolveStats()
+        o = opts if opts is not None else default_solve_opts()
+        self._check(lib().porsol_upscale_periodic(self.h, C.byref(self.grid.s), ng, *[_p(a) for a in keep],
+                                                  C.byref(o), _p(keff), C.byref(st)))
+        n, nnz, mx, ni = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().porsol_num_dofs(self.h, C.byref(n), C.byref(nnz), C.byref(mx), C.byref(ni)))
+        self.n, self.nnz = n.value, nnz.value
+        return keff.reshape(ng, 3, 3), st
 
     def post_process_fluxes(self):
         m = C.c_double()

@@ -130,3 +130,72 @@ class CartesianGrid:
             volume=np.ascontiguousarray(self.volume, dtype=np.float64),
             ccentroid=np.ascontiguousarray(self.ccentroid, dtype=np.float64),
         )
+
+
+class UnionGrid:
+    """Disjoint union of Cartesian sub-grids with unique boundary ids (batched upscaling).
+
+    Sub-grid g owns cells [cellpos[g], cellpos[g+1]); neighbour indices and boundary ids are
+    offset so that the union is one flattened grid; ``partner`` holds each boundary face's
+    periodic partner id and ``side`` its canonical side (1..6).
+    """
+
+    def __init__(self, grids):
+        self.grids = list(grids)
+        cellpos = [0]
+        nb, bid, side, partner, area, fc, fn, vol, cc, fp = [], [], [], [], [], [], [], [], [], [0]
+        boff = 0
+        for g in self.grids:
+            if not g.unique_bids:
+                raise ValueError("sub-grids need unique boundary ids")
+            off = cellpos[-1]
+            n = g.neighbour.astype(np.int64)
+            nb.append(np.where(n >= 0, n + off, -1))
+            b = g.bid.astype(np.int64)
+            bid.append(np.where(b > 0, b + boff, 0))
+            p = g.periodic_partner_bids().astype(np.int64)
+            partner.append(np.where(p > 0, p + boff, 0))
+            side.append(g.side)
+            area.append(g.area)
+            fc.append(g.fcentroid)
+            fn.append(g.fnormal)
+            vol.append(g.volume)
+            cc.append(g.ccentroid)
+            last = int(fp[-1][-1]) if isinstance(fp[-1], np.ndarray) else int(fp[-1])
+            fp.append(g.facepos[1:].astype(np.int64) + last)
+            boff += int(b.max())
+            cellpos.append(off + g.num_cells)
+        self.cellpos = np.array(cellpos, dtype=np.int32)
+        self.num_cells = int(self.cellpos[-1])
+        self.facepos = np.concatenate([np.zeros(1, np.int64)] + [np.asarray(x, np.int64) for x in fp[1:]]).astype(np.int32)
+        self.neighbour = np.concatenate(nb).astype(np.int32)
+        self.bid = np.concatenate(bid).astype(np.int32)
+        self.partner = np.concatenate(partner).astype(np.int32)
+        self.side = np.concatenate(side).astype(np.int32)
+        self.area = np.concatenate(area)
+        self.fcentroid = np.concatenate(fc)
+        self.fnormal = np.concatenate(fn)
+        self.volume = np.concatenate(vol)
+        self.ccentroid = np.concatenate(cc)
+        self.unique_bids = True
+
+    @property
+    def num_half_faces(self):
+        return int(self.facepos[-1])
+
+    @property
+    def boundary(self):
+        return self.neighbour < 0
+
+    def arrays(self):
+        return dict(
+            num_cells=self.num_cells,
+            facepos=np.ascontiguousarray(self.facepos, dtype=np.int32),
+            neighbour=np.ascontiguousarray(self.neighbour, dtype=np.int32),
+            bid=np.ascontiguousarray(self.bid, dtype=np.int32),
+            area=np.ascontiguousarray(self.area, dtype=np.float64),
+            fcentroid=np.ascontiguousarray(self.fcentroid, dtype=np.float64),
+            fnormal=np.ascontiguousarray(self.fnormal, dtype=np.float64),
+            volume=np.ascontiguousarray(self.volume, dtype=np.float64),
+            ccentroid=np.ascontiguousarray(self.ccentroid, dtype=np.float64),
+        )

@@ -252,7 +252,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     ao.prolong = o.prolongate_factor;
     dirichlet_guess(stream, P, val.p, rhs.p, x.p);
     if (o.precision == PORSOL_FP64) {
-        if (!(o.same_matrix && amg_ready && amg_precision == PORSOL_FP64)) {
+        if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64)) {
             amg64.setup(stream, P, val.p, ao);
             amg_ready = true;
             amg_precision = PORSOL_FP64;
@@ -269,7 +269,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     }
     // Mixed precision: FP32 matrix copy, FP32 AMG hierarchy, FP32 CG on the correction
     // equation; FP64 outer residual r = b - A x and FP64 update x += d.
-    if (!(o.same_matrix && amg_ready && amg_precision == PORSOL_MIXED)) {
+    if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED)) {
         amg32.setup(stream, P, val32.p, ao);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
@@ -387,7 +387,10 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     // Regularisation of pure Neumann/periodic problems: the ILU0 path always applies it
     // (:1398-1400); the AMG paths only when the hierarchy is rebuilt (:1491-1495).
     reg_applied = false;
-    if (R.do_reg && (o.linsolver_type == 0 || !o.same_matrix)) {
+    if (!reg_rows.empty()) {
+        // batched sub-grids: each sub-grid's first DOF, as its own pure-periodic solve would
+        launch_scale_rows(s, int(reg_rows.size()), reg_rows_d.p, val.p, S.pat.diag.p, 2.0, mixed ? val32.p : nullptr);
+    } else if (R.do_reg && (o.linsolver_type == 0 || !o.same_matrix)) {
         launch_scale_entry(s, val.p, S.pat.diag.p, 0, 2.0, mixed ? val32.p : nullptr);
         reg_applied = true;
     }
@@ -441,6 +444,102 @@ double porsol_solver::post_process()
     double d;
     std::memcpy(&d, &b, sizeof(d));
     return d;
+}
+
+// Batched periodic upscaling: one block-diagonal system over the disjoint union of the
+// sub-grids, solved for the three unit pressure drops with one AMG hierarchy.
+void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cellpos, const int* partner,
+                            const int* side, const double* perm_h, const porsol_solve_opts* opts_in, double* keff,
+                            porsol_solve_stats* stats)
+{
+    PORSOL_REQUIRE(grid && cellpos && partner && side && perm_h && keff && ngrids > 0, PORSOL_ERR_BAD_ARG,
+                   "upscale: null argument");
+    const int nc = grid->num_cells;
+    PORSOL_REQUIRE(cellpos[0] == 0 && cellpos[ngrids] == nc, PORSOL_ERR_BAD_ARG, "upscale: grid_cellpos");
+    for (int g = 0; g < ngrids; ++g)
+        PORSOL_REQUIRE(cellpos[g + 1] > cellpos[g], PORSOL_ERR_BAD_ARG, "upscale: empty sub-grid");
+    const int nhf = grid->cell_facepos[nc];
+    std::vector<int> bct(nhf, PORSOL_BC_NEUMANN);
+    for (int hf = 0; hf < nhf; ++hf)
+        if (grid->hf_neighbour[hf] < 0) {
+            PORSOL_REQUIRE(side[hf] >= 1 && side[hf] <= 6, PORSOL_ERR_BAD_ARG, "upscale: boundary side not in 1..6");
+            bct[hf] = PORSOL_BC_PERIODIC;
+        }
+    init_structure(grid, bct.data(), partner);
+    const double zero3[3] = {0.0, 0.0, 0.0};
+    compute_inner_products(perm_h, zero3);
+    // per sub-grid: side areas A_i (high sides), extents L_d, first DOF
+    std::vector<double> A(3 * size_t(ngrids), 0.0), L(3 * size_t(ngrids), 0.0);
+    std::vector<int> dof0(ngrids);
+    const HostGrid& hg = S.g;
+    for (int g = 0; g < ngrids; ++g) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        int d0 = S.N;
+        for (int c = cellpos[g]; c < cellpos[g + 1]; ++c)
+            for (int hf = hg.facepos[c]; hf < hg.facepos[c + 1]; ++hf) {
+                d0 = std::min(d0, S.cf[hf]);
+                const int sd = side[hf];
+                if (!hg.boundary(hf)) continue;
+                const int ax = (sd - 1) / 2;
+                const double x = hg.fcent[3 * size_t(hf) + ax];
+                if (sd % 2 == 1) lo[ax] = std::min(lo[ax], x);
+                else {
+                    hi[ax] = std::max(hi[ax], x);
+                    A[3 * size_t(g) + ax] += hg.area[hf];
+                }
+            }
+        for (int ax = 0; ax < 3; ++ax) {
+            PORSOL_REQUIRE(hi[ax] > lo[ax] && A[3 * size_t(g) + ax] > 0.0, PORSOL_ERR_BAD_ARG,
+                           "upscale: a sub-grid lacks boundary faces on some side");
+            L[3 * size_t(g) + ax] = hi[ax] - lo[ax];
+        }
+        dof0[g] = d0;
+    }
+    reg_rows = dof0;
+    reg_rows_d.upload(reg_rows, stream);
+    DBuf<int> cellpos_d, side_d;
+    cellpos_d.upload(cellpos, ngrids + 1, stream);
+    side_d.upload(side, nhf, stream);
+    DBuf<double> q_d;
+    q_d.alloc(3 * size_t(ngrids));
+    std::vector<double> ones(nc, 1.0), zeros(nc, 0.0), bcv(nhf, 0.0), q(3 * size_t(ngrids));
+    porsol_fluid fl{PORSOL_FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0};
+    porsol_solve_opts o;
+    porsol_solve_opts_default(&o);
+    if (opts_in) o = *opts_in;
+    o.same_matrix = 0;
+    porsol_solve_stats acc{};
+    try {
+        for (int d = 0; d < 3; ++d) {
+            for (int hf = 0; hf < nhf; ++hf)
+                bcv[hf] = side[hf] == 2 * d + 1 ? 1.0 : (side[hf] == 2 * d + 2 ? -1.0 : 0.0);
+            reuse_amg = d > 0;
+            porsol_solve_stats st{};
+            solve(&fl, ones.data(), zeros.data(), bct.data(), bcv.data(), zeros.data(), &o, &st, false);
+            launch_side_fluxes(stream, ngrids, cellpos_d.p, facepos.p, side_d.p, outflux.p, q_d.p);
+            q_d.download(q.data(), q.size(), stream);
+            PORSOL_CUDA(cudaStreamSynchronize(stream));
+            for (int g = 0; g < ngrids; ++g)
+                for (int i = 0; i < 3; ++i)
+                    keff[9 * size_t(g) + 3 * i + d] = L[3 * size_t(g) + d] * q[3 * size_t(g) + i] / A[3 * size_t(g) + i];
+            acc.iterations += st.iterations;
+            acc.outer_iterations += st.outer_iterations;
+            acc.reduction = std::max(acc.reduction, st.reduction);
+            acc.amg_levels = st.amg_levels;
+            acc.mass_balance = std::max(acc.mass_balance, st.mass_balance);
+            acc.ms_assemble += st.ms_assemble;
+            acc.ms_precond_setup += st.ms_precond_setup;
+            acc.ms_krylov += st.ms_krylov;
+            acc.ms_recover += st.ms_recover;
+        }
+    } catch (...) {
+        reuse_amg = false;
+        reg_rows.clear();
+        throw;
+    }
+    reuse_amg = false;
+    reg_rows.clear();
+    if (stats) *stats = acc;
 }
 
 // ---------------------------------------------------------------- C ABI
@@ -562,6 +661,15 @@ int porsol_solve_device(porsol_solver* h, const porsol_fluid* fluid, const doubl
                         porsol_solve_stats* stats)
 {
     return guarded(h, [&] { h->solve(fluid, sat, mobdens, bct, bcv, src, opts, stats, true); });
+}
+
+int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_grids, const int* grid_cellpos,
+                            const int* hf_partner_bid, const int* hf_side, const double* perm,
+                            const porsol_solve_opts* opts, double* k_eff, porsol_solve_stats* stats)
+{
+    return guarded(h, [&] {
+        h->upscale(grid, num_grids, grid_cellpos, hf_partner_bid, hf_side, perm, opts, k_eff, stats);
+    });
 }
 
 int porsol_post_process_fluxes(porsol_solver* h, double* max_modification)

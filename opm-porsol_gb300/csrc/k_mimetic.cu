@@ -344,6 +344,39 @@ __global__ void k_mass_balance(int nc, const int* __restrict__ facepos, const do
     }
 }
 
+__global__ void k_scale_rows(int nrows, const int* __restrict__ rows, double* val, const int* __restrict__ diag,
+                             double factor, float* val32)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows) return;
+    const int k = diag[rows[q]];
+    val[k] *= factor;
+    if (val32) val32[k] = float(val[k]);
+}
+
+// one block per sub-grid: fixed-order sums (deterministic)
+__global__ void k_side_fluxes(int ngrids, const int* __restrict__ cellpos, const int* __restrict__ facepos,
+                              const int* __restrict__ side, const double* __restrict__ outflux, double* __restrict__ q)
+{
+    __shared__ double sh[3][256];
+    const int g = blockIdx.x;
+    if (g >= ngrids) return;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int c = cellpos[g] + threadIdx.x; c < cellpos[g + 1]; c += blockDim.x)
+        for (int hf = facepos[c]; hf < facepos[c + 1]; ++hf) {
+            const int sd = side[hf];
+            if (sd == 2 || sd == 4 || sd == 6) acc[sd / 2 - 1] += outflux[hf];
+        }
+    for (int i = 0; i < 3; ++i) sh[i][threadIdx.x] = acc[i];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int i = 0; i < 3; ++i) sh[i][threadIdx.x] += sh[i][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) q[3 * g + threadIdx.x] = sh[threadIdx.x][0];
+}
+
 __global__ void k_compare_types(int nb, const int* __restrict__ bhf, const int* __restrict__ bct,
                                 const int* __restrict__ cached, int* __restrict__ changed)
 {
@@ -429,6 +462,22 @@ void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const doubl
 {
     if (nc == 0) return;
     PORSOL_LAUNCH(k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_scale_rows(cudaStream_t s, int nrows, const int* rows, double* val, const int* diag, double factor,
+                       float* val32)
+{
+    if (nrows == 0) return;
+    PORSOL_LAUNCH(k_scale_rows<<<div_up(nrows, 256), 256, 0, s>>>(nrows, rows, val, diag, factor, val32));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_side_fluxes(cudaStream_t s, int ngrids, const int* cellpos, const int* facepos, const int* side,
+                        const double* outflux, double* q)
+{
+    if (ngrids == 0) return;
+    PORSOL_LAUNCH(k_side_fluxes<<<ngrids, 256, 0, s>>>(ngrids, cellpos, facepos, side, outflux, q));
     PORSOL_CUDA(cudaGetLastError());
 }
 

@@ -73,6 +73,12 @@ void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* o
 void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const double* outflux, const double* src,
                          unsigned long long* out3);
 void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status);
+// val[diag[rows[q]]] *= factor for q < nrows (and the FP32 copy)
+void launch_scale_rows(cudaStream_t s, int nrows, const int* rows, double* val, const int* diag, double factor,
+                       float* val32);
+// per sub-grid g: q[3 g + i] = sum of outflux over half-faces of side 2 i + 2 (1-based sides)
+void launch_side_fluxes(cudaStream_t s, int ngrids, const int* cellpos, const int* facepos, const int* side,
+                        const double* outflux, double* q);
 // changed = 1 if bct[bhf[q]] != cached[q] for some boundary half-face q
 void launch_compare_types(cudaStream_t s, int nb, const int* bhf, const int* bct, const int* cached, int* changed);
 

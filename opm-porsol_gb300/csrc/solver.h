@@ -58,6 +58,12 @@ struct porsol_solver {
 
     porsol::Profiler prof;
 
+    // batched periodic upscaling: rows regularised in place of row 0 (first DOF of each
+    // sub-grid), and whether the AMG hierarchy of the previous solve is reused
+    std::vector<int> reg_rows;
+    porsol::DBuf<int> reg_rows_d;
+    bool reuse_amg = false;
+
     void require_structure() const;
     void init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
     void compute_inner_products(const double* perm_h, const double* grav);
@@ -68,4 +74,6 @@ struct porsol_solver {
     void check_status(const char* where);
     void ensure_recipe(const int* bct_host, const int* bct_dev);
     void linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st);
+    void upscale(const porsol_grid* grid, int ngrids, const int* cellpos, const int* partner, const int* side,
+                 const double* perm, const porsol_solve_opts* opts, double* keff, porsol_solve_stats* stats);
 };

@@ -25,7 +25,7 @@ import numpy as np
 _here = os.path.dirname(os.path.abspath(__file__))
 if _here not in sys.path:
     sys.path.insert(0, _here)
-from cartesian import CartesianGrid  # noqa: E402
+from cartesian import CartesianGrid, UnionGrid  # noqa: E402
 
 MILLIDARCY = 9.869233e-16
 SEED0 = 20261203
@@ -113,6 +113,30 @@ def case2(dims=(100, 100, 50), seed=None, corr=5.0):
     bct, bcv = x_dirichlet_bc(g)
     return Problem("case2", g, diag_perm(kx, kx, 0.1 * kx), np.full(nc, 0.2), bct, bcv, np.zeros(nc), sat,
                    (1, 1e-3, 5e-3, 1000.0, 850.0))
+
+
+def random_rotations(rng, n):
+    """Uniformly distributed rotation matrices (QR of Gaussian matrices, sign-fixed)."""
+    A = rng.standard_normal((n, 3, 3))
+    Q, R = np.linalg.qr(A)
+    Q = Q * np.sign(np.diagonal(R, axis1=1, axis2=2))[:, None, :]
+    det = np.linalg.det(Q)
+    Q[det < 0, :, 0] *= -1.0
+    return Q
+
+
+def case3(num=512, nmin=8, nmax=32, seed=None, sigma=1.5):
+    """Batched periodic upscaling: `num` unit-cube sub-grids of n^3 cells, n ~ U{nmin..nmax},
+    full SPD tensors K = R diag(exp(g)) R^T per cell, g ~ N(ln 100 mD, sigma^2), R uniform."""
+    rng = np.random.default_rng(SEED0 + 3 if seed is None else seed)
+    sizes = rng.integers(nmin, nmax + 1, size=num)
+    grids = [CartesianGrid(int(n), int(n), int(n), unique_bids=True) for n in sizes]
+    union = UnionGrid(grids)
+    nc = union.num_cells
+    R = random_rotations(rng, nc)
+    lam = np.exp(rng.normal(np.log(100 * MILLIDARCY), sigma, (nc, 3)))
+    K = np.einsum("cij,cj,ckj->cik", R, lam, R)
+    return union, sizes, K.reshape(nc, 9)
 
 
 def case4(dims=(64, 64, 32), seed=None, corr=4.0):

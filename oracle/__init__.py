@@ -224,6 +224,39 @@ class OraclePressure:
         return lib().orc_post_process_fluxes(self.h)
 
 
+def upscale_periodic(grid, K9, tol=1e-13):
+    """Effective permeability (3x3) of one fully periodic Cartesian grid with unique boundary ids.
+
+    Three solves with unit total mobility: periodic pressure jump +1 on the low side and -1 on the
+    high side of axis d (the pattern of setupUpscalingConditions,
+    opm/porsol/common/setupBoundaryConditions.hpp:136-157), Neumann nowhere.  Darcy averaging over
+    the periodic cell gives K_eff[i, d] = L_d Q_i / A_i, Q_i the flux through the high side of axis
+    i, A_i its area, L_d the extent along d.  The reference leaves this step to opm-upscaling; the
+    same formula is what the GPU batch computes.  Returns (keff, total CG iterations)."""
+    pb = grid.periodic_partner_bids()
+    bct = np.where(grid.boundary, BC_PERIODIC, BC_NEUMANN).astype(np.int32)
+    o = OraclePressure(grid, bct, pb)
+    o.compute_inner_products(np.ascontiguousarray(K9, dtype=np.float64).ravel())
+    nc = grid.num_cells
+    keff = np.zeros((3, 3))
+    its = 0
+    for d in range(3):
+        bcv = np.zeros(grid.num_half_faces)
+        bcv[grid.side == 2 * d + 1] = 1.0
+        bcv[grid.side == 2 * d + 2] = -1.0
+        rc = o.solve(np.ones(nc), np.zeros(nc), bct, bcv, np.zeros(nc), tol=tol)
+        if rc != 0:
+            raise RuntimeError(f"oracle periodic solve failed ({rc})")
+        its += o.iterations
+        _, v, _ = o.solution()
+        lo, hi = grid.side == 2 * d + 1, grid.side == 2 * d + 2
+        L = grid.fcentroid[hi, d].max() - grid.fcentroid[lo, d].min()
+        for i in range(3):
+            h = grid.side == 2 * i + 2
+            keff[i, d] = L * v[h].sum() / grid.area[h].sum()
+    return keff, its
+
+
 def ilu0_cg(rowptr, colind, vals, b, x0=None, tol=1e-8, maxit=0):
     rowptr, colind, vals, b = _i32(rowptr), _i32(colind), _f64(vals), _f64(b)
     n = len(b)
