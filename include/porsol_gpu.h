@@ -189,6 +189,33 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
                             const int* hf_partner_bid, const int* hf_side, const double* perm,
                             const porsol_solve_opts* opts, double* k_eff, porsol_solve_stats* stats);
 
+/* ------------------------------------------------------ adjoint permeability sensitivity */
+/* No counterpart in the reference.  Objective of the last solve's solution
+ *     J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf
+ * with p the cell pressures and v the half-face outfluxes of computePressureAndFluxes
+ * (IncompFlowSolverHybrid.hpp:1672-1730, before postProcessFluxes).  Any array may be NULL
+ * (read as zeros).  Supported for solves with zero gravity, no periodic faces and at least one
+ * Dirichlet face (PORSOL_ERR_BAD_ARG otherwise). */
+typedef struct porsol_objective {
+    const double* cell_weight;   /* w_c, num_cells */
+    const double* cell_target;   /* p*_c, num_cells */
+    const double* hf_weight;     /* u_hf, num half-faces */
+} porsol_objective;
+
+/* Gradient modes: d J / d ln s_c for K_c -> s_c K_c (one value per cell, any tensor), or
+ * d J / d ln k_{c,a} for a = x, y, z (three values per cell, grad[3 c + a]; diagonal tensors). */
+enum { PORSOL_GRAD_LOGK = 0, PORSOL_GRAD_LOGK_AXES = 1 };
+
+/* Forward half: J of the last solve (no linear solve). */
+int porsol_objective_value(porsol_solver* h, const porsol_objective* obj, double* value);
+/* Backward half: one adjoint solve with the assembled matrix of the last solve and its
+ * preconditioner (no setup when the hierarchy matches opts->precision; the forward Krylov
+ * iterates are not stored, only the forward solution), then the per-cell gradient.  opts NULL
+ * = the options of the last solve.  grad is a host array of num_cells (mode 0) or
+ * 3 num_cells (mode 1) doubles; value (may be NULL) receives J. */
+int porsol_adjoint_gradient(porsol_solver* h, const porsol_objective* obj, int mode, const porsol_solve_opts* opts,
+                            double* value, double* grad, porsol_solve_stats* stats);
+
 /* ------------------------------------------------------ transport */
 typedef struct porsol_transport porsol_transport;
 

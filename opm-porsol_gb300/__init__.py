@@ -25,11 +25,13 @@ LIB_PATH = os.path.join(LIB_DIR, "libporsol_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE, "-I", CSRC]
-SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "capi.cu", "noalloc_cfl.cu"]
+SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_adjoint.cu", "capi.cu",
+           "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
 FLUID_CELLWISE, FLUID_COREY2 = 0, 1
 FP64, MIXED = 0, 1
+GRAD_LOGK, GRAD_LOGK_AXES = 0, 1
 ERR = {0: "OK", 1: "NOT_CONVERGED", 2: "BAD_ARG", 3: "NONFINITE", 4: "SAT_RANGE", 5: "CUDA", 6: "TIMEOUT",
        7: "STATE", 8: "UNKNOWN_SOLVER", 9: "CFL"}
 
@@ -86,6 +88,10 @@ class SolveOpts(C.Structure):
                 ("inner_tolerance", C.c_double), ("max_outer", C.c_int)]
 
 
+class Objective(C.Structure):
+    _fields_ = [("cell_weight", C.c_void_p), ("cell_target", C.c_void_p), ("hf_weight", C.c_void_p)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("reduction", C.c_double),
                 ("amg_levels", C.c_int), ("mass_balance", C.c_double), ("ms_assemble", C.c_double),
@@ -129,6 +135,9 @@ EXPORTS = [
     ("porsol_get_system", _i, [_vp, _vp, _vp]),
     ("porsol_amg_info", _i, [_vp, _i, C.POINTER(_i), _vp, _vp]),
     ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
+                                     C.POINTER(SolveStats)]),
+    ("porsol_objective_value", _i, [_vp, C.POINTER(Objective), C.POINTER(_d)]),
+    ("porsol_adjoint_gradient", _i, [_vp, C.POINTER(Objective), _i, C.POINTER(SolveOpts), C.POINTER(_d), _vp,
                                      C.POINTER(SolveStats)]),
     ("porsol_transport_opts_default", None, [C.POINTER(TransportOpts)]),
     ("porsol_transport_create", _i, [C.POINTER(_vp)]),
@@ -281,6 +290,30 @@ class PressureSolver:
         self._check(lib().porsol_num_dofs(self.h, C.byref(n), C.byref(nnz), C.byref(mx), C.byref(ni)))
         self.n, self.nnz = n.value, nnz.value
         return keff.reshape(ng, 3, 3), st
+
+    def _objective(self, cell_weight, cell_target, hf_weight):
+        keep = [None if a is None else _f64(a) for a in (cell_weight, cell_target, hf_weight)]
+        obj = Objective(*[None if a is None else a.ctypes.data for a in keep])
+        return obj, keep
+
+    def objective(self, cell_weight=None, cell_target=None, hf_weight=None):
+        """J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf of the last solve."""
+        obj, keep = self._objective(cell_weight, cell_target, hf_weight)
+        J = C.c_double()
+        self._check(lib().porsol_objective_value(self.h, C.byref(obj), C.byref(J)))
+        return J.value
+
+    def adjoint_gradient(self, cell_weight=None, cell_target=None, hf_weight=None, mode=GRAD_LOGK, opts=None):
+        """(J, dJ/d ln k per cell (mode 0) or (nc, 3) per axis (mode 1), stats) of the last solve."""
+        obj, keep = self._objective(cell_weight, cell_target, hf_weight)
+        nc = self.grid.num_cells
+        grad = np.empty(nc * (3 if mode == GRAD_LOGK_AXES else 1))
+        J = C.c_double()
+        st = SolveStats()
+        self._check(lib().porsol_adjoint_gradient(self.h, C.byref(obj), int(mode),
+                                                  None if opts is None else C.byref(opts), C.byref(J), _p(grad),
+                                                  C.byref(st)))
+        return J.value, (grad.reshape(nc, 3) if mode == GRAD_LOGK_AXES else grad), st
 
     def post_process_fluxes(self):
         m = C.c_double()

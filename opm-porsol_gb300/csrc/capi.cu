@@ -331,6 +331,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
                    "unknown fluid model");
     if (o.precision == PORSOL_MIXED && o.linsolver_type == 0)
         o.precision = PORSOL_FP64;   // ILU0 path is FP64 only
+    last_opts = o;
     const int nc = S.g.nc, nhf = S.g.nhf;
     cudaStream_t s = stream;
     ensure_recipe(dev ? nullptr : bct, dev ? bct : nullptr);
@@ -542,6 +543,134 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     if (stats) *stats = acc;
 }
 
+// ---------------------------------------------------------------- adjoint
+namespace {
+const double* upload_or_null(DBuf<double>& b, const double* h, size_t n, cudaStream_t s)
+{
+    if (!h) return nullptr;
+    b.upload(h, n, s);
+    return b.p;
+}
+}  // namespace
+
+double porsol_solver::objective(const porsol_objective* obj)
+{
+    PORSOL_REQUIRE(solved, PORSOL_ERR_STATE, "objective: no solution (call solve first)");
+    PORSOL_REQUIRE(obj, PORSOL_ERR_BAD_ARG, "objective: null argument");
+    PORSOL_REQUIRE(gravity_zero, PORSOL_ERR_BAD_ARG, "adjoint: only zero gravity is supported");
+    PORSOL_REQUIRE(!R.do_reg && reg_rows.empty(), PORSOL_ERR_BAD_ARG,
+                   "adjoint: the problem needs at least one Dirichlet face");
+    for (int k : R.kind)
+        PORSOL_REQUIRE(k != HK_PERIODIC_HI && k != HK_PERIODIC_LO, PORSOL_ERR_BAD_ARG,
+                       "adjoint: periodic faces are not supported");
+    const int nc = S.g.nc, nhf = S.g.nhf;
+    cudaStream_t s = stream;
+    AdjointArgs a{};
+    a.nc = nc;
+    a.facepos = facepos.p;
+    a.cf = cf.p;
+    a.kind = R.kind_d.p;
+    a.sloc = sloc.p;
+    a.W = W.p;
+    a.F = F.p;
+    a.L = L.p;
+    a.g = this->g.p;
+    a.totmob = totmob.p;
+    a.pressure = pressure.p;
+    a.x = x.p;
+    a.wp = upload_or_null(adj_wp, obj->cell_weight, nc, s);
+    a.pstar = upload_or_null(adj_pstar, obj->cell_target, nc, s);
+    a.wv = upload_or_null(adj_wv, obj->hf_weight, nhf, s);
+    adj_y.alloc(nhf);
+    adj_jc.alloc(nc);
+    a.y = adj_y.p;
+    a.jc = adj_jc.p;
+    a.status = status.p;
+    launch_adjoint_source(maxnf, s, a);
+    adj_sum.alloc(sum_scratch_size());
+    launch_sum(s, nc, adj_jc.p, adj_sum.p);
+    double J = 0.0;
+    PORSOL_CUDA(cudaMemcpyAsync(&J, adj_sum.p + sum_result_index(nc), sizeof(double), cudaMemcpyDeviceToHost, s));
+    check_status("objective");
+    return J;
+}
+
+void porsol_solver::adjoint_gradient(const porsol_objective* obj, int mode, const porsol_solve_opts* opts_in,
+                                     double* value, double* grad, porsol_solve_stats* stats)
+{
+    PORSOL_REQUIRE(mode == PORSOL_GRAD_LOGK || mode == PORSOL_GRAD_LOGK_AXES, PORSOL_ERR_BAD_ARG,
+                   "adjoint: unknown gradient mode");
+    PORSOL_REQUIRE(grad, PORSOL_ERR_BAD_ARG, "adjoint: null gradient array");
+    const double J = objective(obj);   // also leaves dJ/dpi in adj_y
+    const int nc = S.g.nc, N = S.N;
+    cudaStream_t s = stream;
+    adj_rhs.alloc(N);
+    adj_x.alloc(N);
+    launch_adjoint_rhs(s, N, R.rhs_ptr.p, R.rhs_ent.p, R.kind_d.p, adj_y.p, adj_rhs.p);
+    // The adjoint system is the assembled (symmetric) matrix of the forward solve: swap the
+    // adjoint vectors in as right-hand side and solution, keep the hierarchy.
+    porsol_solve_opts o = opts_in ? *opts_in : last_opts;
+    if (o.precision == PORSOL_MIXED && o.linsolver_type == 0) o.precision = PORSOL_FP64;
+    o.same_matrix = 1;
+    porsol_solve_stats st{};
+    std::swap(rhs, adj_rhs);
+    std::swap(x, adj_x);
+    const double t0 = now_ms();
+    try {
+        linear_solve(o, st);
+    } catch (...) {
+        std::swap(rhs, adj_rhs);
+        std::swap(x, adj_x);
+        throw;
+    }
+    std::swap(rhs, adj_rhs);
+    std::swap(x, adj_x);
+    st.ms_krylov = now_ms() - t0 - st.ms_precond_setup;
+    const double t1 = now_ms();
+    AdjointArgs a{};
+    a.nc = nc;
+    a.mode = mode;
+    a.facepos = facepos.p;
+    a.cf = cf.p;
+    a.kind = R.kind_d.p;
+    a.W = W.p;
+    a.F = F.p;
+    a.L = L.p;
+    a.g = this->g.p;
+    a.totmob = totmob.p;
+    a.pressure = pressure.p;
+    a.x = x.p;
+    a.mu = adj_x.p;
+    a.wp = obj->cell_weight ? adj_wp.p : nullptr;
+    a.pstar = obj->cell_target ? adj_pstar.p : nullptr;
+    a.wv = obj->hf_weight ? adj_wv.p : nullptr;
+    a.area = area.p;
+    a.fcent = fcent.p;
+    a.fnormal = fnormal.p;
+    a.cvol = cvol.p;
+    a.ccent = ccent.p;
+    a.perm = perm.p;
+    const size_t ng = (mode == PORSOL_GRAD_LOGK ? 1 : 3) * size_t(nc);
+    adj_grad.alloc(ng);
+    a.grad = adj_grad.p;
+    a.status = status.p;
+    launch_adjoint_grad(maxnf, s, a);
+    adj_grad.download(grad, ng, s);
+    {
+        int st_dev = 0;
+        PORSOL_CUDA(cudaMemcpyAsync(&st_dev, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        if (st_dev & ST_BAD_INDEX) {
+            PORSOL_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+            throw Error(PORSOL_ERR_BAD_ARG, "adjoint: axis gradients need diagonal permeability tensors");
+        }
+    }
+    check_status("adjoint gradient");
+    st.ms_recover = now_ms() - t1;
+    if (value) *value = J;
+    if (stats) *stats = st;
+}
+
 // ---------------------------------------------------------------- C ABI
 namespace {
 
@@ -670,6 +799,20 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
     return guarded(h, [&] {
         h->upscale(grid, num_grids, grid_cellpos, hf_partner_bid, hf_side, perm, opts, k_eff, stats);
     });
+}
+
+int porsol_objective_value(porsol_solver* h, const porsol_objective* obj, double* value)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(value, PORSOL_ERR_BAD_ARG, "objective: null value");
+        *value = h->objective(obj);
+    });
+}
+
+int porsol_adjoint_gradient(porsol_solver* h, const porsol_objective* obj, int mode, const porsol_solve_opts* opts,
+                            double* value, double* grad, porsol_solve_stats* stats)
+{
+    return guarded(h, [&] { h->adjoint_gradient(obj, mode, opts, value, grad, stats); });
 }
 
 int porsol_post_process_fluxes(porsol_solver* h, double* max_modification)

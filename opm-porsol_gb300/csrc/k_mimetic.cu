@@ -6,16 +6,12 @@
 // nf x nf local matrices live in registers (MAXNF is a compile-time bound: 6 for
 // hexahedra, 12 for general cells).
 #include "kernels.h"
+#include "mimetic.cuh"
 #include "structure.h"
 
 namespace porsol {
 
 namespace {
-
-__device__ __forceinline__ int pk(int r, int s)
-{
-    return r <= s ? s * (s + 1) / 2 + r : r * (r + 1) / 2 + s;
-}
 
 __device__ __forceinline__ void mobilities(const FluidParams& fl, const double* sat, const double* mobdens, int c,
                                            double& totmob, double& md)
@@ -32,11 +28,8 @@ __device__ __forceinline__ void mobilities(const FluidParams& fl, const double* 
     }
 }
 
-// MimeticIPEvaluator::buildStaticContrib (MimeticIPEvaluator.hpp:201-270):
-//   W = (N K N^T + t A (I - Q Q^T) A) / |c|,  t = 6 tr(K) / 3,
-//   N = A n (area-weighted normals), Q = orth(A (x_f - x_c)), gflux = N K g.
-// Q is formed by Gram-Schmidt with one re-orthogonalisation pass; Q Q^T does not depend
-// on the orthonormal basis chosen, so this matches the reference's Householder QR.
+// MimeticIPEvaluator::buildStaticContrib (MimeticIPEvaluator.hpp:201-270): W of every cell
+// (cell_frame and projected in mimetic.cuh) and the gravity flux gflux = N K g.
 template <int MAXNF>
 __global__ void __launch_bounds__(128) k_static_ip(int nc, const int* __restrict__ facepos,
                                                    const double* __restrict__ area, const double* __restrict__ fcent,
@@ -61,51 +54,12 @@ __global__ void __launch_bounds__(128) k_static_ip(int nc, const int* __restrict
     const double Kg0 = K[0] * g0 + K[1] * g1 + K[2] * g2;
     const double Kg1 = K[3] * g0 + K[4] * g1 + K[5] * g2;
     const double Kg2 = K[6] * g0 + K[7] * g1 + K[8] * g2;
-    const double cc0 = ccent[3 * (size_t)c], cc1 = ccent[3 * (size_t)c + 1], cc2 = ccent[3 * (size_t)c + 2];
     double N[MAXNF][3], Q[MAXNF][3], a[MAXNF];
+    if (!cell_frame<MAXNF>(c, f0, nf, area, fcent, fnormal, ccent, a, N, Q))
+        atomicOr(status, ST_NONFINITE);   // degenerate cell: the reference asserts here
 #pragma unroll
-    for (int i = 0; i < MAXNF; ++i) {
-        a[i] = 0.0;
-        N[i][0] = N[i][1] = N[i][2] = 0.0;
-        Q[i][0] = Q[i][1] = Q[i][2] = 0.0;
-        if (i < nf) {
-            const size_t hf = f0 + i;
-            a[i] = area[hf];
-            Q[i][0] = (fcent[3 * hf] - cc0) * a[i];
-            Q[i][1] = (fcent[3 * hf + 1] - cc1) * a[i];
-            Q[i][2] = (fcent[3 * hf + 2] - cc2) * a[i];
-            N[i][0] = fnormal[3 * hf] * a[i];
-            N[i][1] = fnormal[3 * hf + 1] * a[i];
-            N[i][2] = fnormal[3 * hf + 2] * a[i];
-            gflux[hf] = N[i][0] * Kg0 + N[i][1] * Kg1 + N[i][2] * Kg2;
-        }
-    }
-    // orthonormalise the three columns of Q (Gram-Schmidt, twice)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-#pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {
-#pragma unroll
-            for (int k = 0; k < j; ++k) {
-                double d = 0.0;
-#pragma unroll
-                for (int i = 0; i < MAXNF; ++i) d += Q[i][k] * Q[i][j];
-#pragma unroll
-                for (int i = 0; i < MAXNF; ++i) Q[i][j] -= d * Q[i][k];
-            }
-        }
-        double nrm = 0.0;
-#pragma unroll
-        for (int i = 0; i < MAXNF; ++i) nrm += Q[i][j] * Q[i][j];
-        nrm = sqrt(nrm);
-        if (!(nrm > 0.0)) {
-            atomicOr(status, ST_NONFINITE);   // degenerate cell: the reference asserts here
-            nrm = 1.0;
-        }
-        const double inv = 1.0 / nrm;
-#pragma unroll
-        for (int i = 0; i < MAXNF; ++i) Q[i][j] *= inv;
-    }
+    for (int i = 0; i < MAXNF; ++i)
+        if (i < nf) gflux[f0 + i] = N[i][0] * Kg0 + N[i][1] * Kg1 + N[i][2] * Kg2;
     // NK = N K (stored back into N's slot after use is not possible; keep separate)
     double NK[MAXNF][3];
 #pragma unroll
@@ -121,9 +75,8 @@ __global__ void __launch_bounds__(128) k_static_ip(int nc, const int* __restrict
 #pragma unroll
         for (int i = 0; i <= j; ++i) {
             if (j < nf) {
-                const double P = (i == j ? 1.0 : 0.0) - (Q[i][0] * Q[j][0] + Q[i][1] * Q[j][1] + Q[i][2] * Q[j][2]);
                 const double nkn = NK[i][0] * N[j][0] + NK[i][1] * N[j][1] + NK[i][2] * N[j][2];
-                const double w = a2 * (a[i] * P * a[j]) + a1 * nkn;
+                const double w = a2 * projected<MAXNF>(i, j, a, Q) + a1 * nkn;
                 finite = finite && isfinite(w);
                 W[(size_t)pk(i, j) * nc + c] = w;
             }

@@ -82,4 +82,44 @@ void launch_side_fluxes(cudaStream_t s, int ngrids, const int* cellpos, const in
 // changed = 1 if bct[bhf[q]] != cached[q] for some boundary half-face q
 void launch_compare_types(cudaStream_t s, int nb, const int* bhf, const int* bct, const int* cached, int* changed);
 
+// ---- k_adjoint.cu --------------------------------------------------------------------
+struct AdjointArgs {
+    int nc;
+    int mode;                // 0: d/d ln k (one value per cell); 1: d/d ln k_{x,y,z} (three)
+    const int* facepos;
+    const int* cf;
+    const int* kind;         // HfKind per half-face (Dirichlet faces have zero adjoint)
+    const double* sloc;      // local Schur complements of the last assembly
+    const double* W;
+    const double* F;
+    const double* L;
+    const double* g;
+    const double* totmob;
+    const double* pressure;
+    const double* x;         // forward face pressures
+    const double* mu;        // adjoint face values (gradient kernel only)
+    const double* wp;        // objective: cell weights, targets, half-face flux weights (may be null)
+    const double* pstar;
+    const double* wv;
+    const double* area;      // geometry and permeability (mode 1 only)
+    const double* fcent;
+    const double* fnormal;
+    const double* cvol;
+    const double* ccent;
+    const double* perm;
+    double* y;               // dJ/dpi per half-face (source kernel)
+    double* jc;              // J per cell (source kernel)
+    double* grad;            // gradient (gradient kernel)
+    int* status;
+};
+void launch_adjoint_source(int maxnf, cudaStream_t s, const AdjointArgs& a);
+void launch_adjoint_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs_ent, const int* kind,
+                        const double* y, double* rhs);
+void launch_adjoint_grad(int maxnf, cudaStream_t s, const AdjointArgs& a);
+// Deterministic sum of x[0..n): scratch needs sum_scratch_size() doubles; the result lands
+// in scratch[sum_result_index(n)].
+int sum_scratch_size();
+int sum_result_index(int n);
+void launch_sum(cudaStream_t s, int n, const double* x, double* scratch);
+
 }  // namespace porsol

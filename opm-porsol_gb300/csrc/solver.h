@@ -64,6 +64,10 @@ struct porsol_solver {
     porsol::DBuf<int> reg_rows_d;
     bool reuse_amg = false;
 
+    // adjoint (permeability sensitivity) of the last solve
+    porsol_solve_opts last_opts{};
+    porsol::DBuf<double> adj_wp, adj_pstar, adj_wv, adj_y, adj_jc, adj_rhs, adj_x, adj_grad, adj_sum;
+
     void require_structure() const;
     void init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
     void compute_inner_products(const double* perm_h, const double* grav);
@@ -74,6 +78,10 @@ struct porsol_solver {
     void check_status(const char* where);
     void ensure_recipe(const int* bct_host, const int* bct_dev);
     void linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st);
+    // J of the last solution; leaves dJ/dpi per half-face in adj_y
+    double objective(const porsol_objective* obj);
+    void adjoint_gradient(const porsol_objective* obj, int mode, const porsol_solve_opts* opts, double* value,
+                          double* grad, porsol_solve_stats* stats);
     void upscale(const porsol_grid* grid, int ngrids, const int* cellpos, const int* partner, const int* side,
                  const double* perm, const porsol_solve_opts* opts, double* keff, porsol_solve_stats* stats);
 };

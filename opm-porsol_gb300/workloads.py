@@ -9,7 +9,8 @@ in Pa s, pressure in Pa (the configurations prescribe p = 1 and p = 0).
           mobility 1, Dirichlet p=1 (x-) / p=0 (x+), no-flow elsewhere, ILU0-CG 1e-10.
   case 2  100x100x50, kx=ky log-normal sigma=2 Gaussian-correlated (5 cells),
           kz = 0.1 kx, Corey-2 mobilities with viscosity ratio 5, s ~ U[0,1].
-  case 4  64x64x32, isotropic log-normal sigma=1 correlated over 4 cells.
+  case 4  64x64x32, isotropic log-normal sigma=1 correlated over 4 cells; objective
+          sum of squared pressure mismatches at 50 cells + outflux through x+.
   case 5  200x200x25, 25 layers, layer mean ~ N(ln 100 mD, 1), ln k ~ N(mean, 2^2)
           i.i.d. within a layer, Corey-2 with viscosity ratio 10, initial s = 0,
           water (s = 1) enters through x-.
@@ -147,6 +148,24 @@ def case4(dims=(64, 64, 32), seed=None, corr=4.0):
     bct, bcv = x_dirichlet_bc(g)
     return Problem("case4", g, iso_perm(np.exp(lk)), np.full(nc, 0.2), bct, bcv, np.zeros(nc), np.zeros(nc),
                    (0, 1.0, 1.0, 0.0, 0.0), totmob=np.ones(nc), mobdens=np.zeros(nc))
+
+
+def case4_objective(problem, seed=None, n_obs=50, n_fd=20):
+    """Objective of the adjoint configuration on a case-4 grid: pressure mismatch at `n_obs`
+    seeded cells against targets p* ~ N(0.5, 0.1^2), plus the total outflux through x+ (side 2).
+    Returns (cell_weight, cell_target, hf_weight, fd_cells): fd_cells are the `n_fd` seeded cells
+    at which finite differences check the gradient."""
+    rng = np.random.default_rng(SEED0 + 40 if seed is None else seed)
+    g = problem.grid
+    nc = g.num_cells
+    obs = rng.choice(nc, n_obs, replace=False)
+    w = np.zeros(nc)
+    w[obs] = 1.0
+    target = np.zeros(nc)
+    target[obs] = rng.normal(0.5, 0.1, n_obs)
+    u = np.where(g.side == 2, 1.0, 0.0)
+    fd_cells = rng.choice(nc, n_fd, replace=False)
+    return w, target, u, fd_cells
 
 
 def case5(dims=(200, 200, 25), seed=None, sat=None):

@@ -98,6 +98,8 @@ def lib():
         L.orc_get_solution.argtypes = [vp, dp, dp, dp]
         L.orc_post_process_fluxes.restype = d
         L.orc_post_process_fluxes.argtypes = [vp]
+        L.orc_adjoint_gradient.restype = i
+        L.orc_adjoint_gradient.argtypes = [vp, dp, dp, dp, i, d, dp, dp, ip]
         L.orc_ilu0_cg.restype = i
         L.orc_ilu0_cg.argtypes = [i, ip, ip, dp, dp, dp, d, i, ip, dp]
         L.orc_cfl_factors.argtypes = [C.POINTER(Fluid), dp]
@@ -222,6 +224,19 @@ class OraclePressure:
 
     def post_process_fluxes(self):
         return lib().orc_post_process_fluxes(self.h)
+
+    def adjoint_gradient(self, cell_weight=None, cell_target=None, hf_weight=None, mode=0, tol=1e-12):
+        """(rc, J, gradient) of J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf for the last solve;
+        gradient per cell (mode 0) or (nc, 3) per axis (mode 1)."""
+        keep = [None if a is None else _f64(a) for a in (cell_weight, cell_target, hf_weight)]
+        nc = self.g.num_cells
+        grad = np.zeros(nc * (3 if mode == 1 else 1))
+        J = np.zeros(1)
+        it = np.zeros(1, np.int32)
+        rc = lib().orc_adjoint_gradient(self.h, *[_p(a) for a in keep], int(mode), float(tol), _p(grad), _p(J),
+                                        _p(it))
+        self.adjoint_iterations = int(it[0])
+        return rc, float(J[0]), (grad.reshape(nc, 3) if mode == 1 else grad)
 
 
 def upscale_periodic(grid, K9, tol=1e-13):

@@ -249,6 +249,7 @@ struct Pressure {
     std::vector<double> pressure, outflux;
     std::vector<double> totmob, mobdens;
     bool do_reg = true;
+    std::vector<int> hf_type;       // FaceType per half-face of the last assembly
 
     Pressure(const orc_grid* og, const int* hf_flow_type, const int* partner_bid) : g(og)
     {
@@ -384,16 +385,24 @@ struct Pressure {
     }
 
     // MimeticIPEvaluator::buildStaticContrib, MimeticIPEvaluator.hpp:201-270
+    std::vector<double> perm;
+
     void computeInnerProducts(const double* K9, const double* grav)
     {
+        perm.assign(K9, K9 + 9 * size_t(g.nc));
+        for (int c = 0; c < g.nc; ++c)
+            cellInnerProduct(c, K9 + 9 * c, grav, &Binv[binvpos[c]], &gflux[g.facepos[c]]);
+    }
+
+    // W (column-major nf x nf) and gravity flux of cell c for the row-major tensor K
+    void cellInnerProduct(int c, const double* K, const double* grav, double* W, double* gfl) const
+    {
         const int dim = 3;
-        for (int c = 0; c < g.nc; ++c) {
+        {
             const int nf = g.nf(c), f0 = g.facepos[c];
-            const double* K = K9 + 9 * c;   // row-major K(i,j) = K[3i+j]
             double Kg[3];
             for (int i = 0; i < 3; ++i) Kg[i] = K[3 * i] * grav[0] + K[3 * i + 1] * grav[1] + K[3 * i + 2] * grav[2];
             std::vector<double> T1(nf * dim), T2(nf * dim), fa(nf);
-            double* W = &Binv[binvpos[c]];
             std::fill(W, W + nf * nf, 0.0);
             for (int i = 0; i < nf; ++i) {
                 const int hf = f0 + i;
@@ -404,7 +413,7 @@ struct Pressure {
                     fc[d] = (g.fcent[3 * hf + d] - g.ccent[3 * c + d]) * fa[i];
                     fn[d] = g.fnormal[3 * hf + d] * fa[i];
                 }
-                gflux[hf] = fn[0] * Kg[0] + fn[1] * Kg[1] + fn[2] * Kg[2];
+                gfl[i] = fn[0] * Kg[0] + fn[1] * Kg[1] + fn[2] * Kg[2];
                 for (int d = 0; d < 3; ++d) {
                     T1[i + d * nf] = fn[d];
                     T2[i + d * nf] = fc[d];
@@ -455,6 +464,7 @@ struct Pressure {
         std::fill(L.begin(), L.end(), 0.0);
         totmob.assign(tm, tm + g.nc);
         mobdens.assign(md, md + g.nc);
+        hf_type.assign(g.nhf(), Internal);
         do_reg = true;
         std::vector<double> Sl, r, gfl;
         std::vector<int> ftype, ppart;
@@ -482,6 +492,7 @@ struct Pressure {
                     r[k] = bcv[hf];
                 }
             }
+            for (int k = 0; k < nf; ++k) hf_type[f0 + k] = ftype[k];
             // getInverseMatrix: S = totmob * Binv
             Sl.assign(nf * nf, 0.0);
             const double* W = &Binv[binvpos[c]];
@@ -571,6 +582,110 @@ struct Pressure {
         }
         const bool ok = pcg(S, M, soln, rhs, tol, maxit > 0 ? maxit : S.n, iters, red);
         return ok ? 0 : 1;
+    }
+
+    // Adjoint gradient of J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf (v before
+    // postProcessFluxes) with respect to ln s_c, K_c -> s_c K_c (mode 0), or ln k_{c,a} of a
+    // diagonal tensor (mode 1, grad[3c + a]).  Zero gravity, no periodic faces, at least one
+    // Dirichlet face.  The adjoint mu solves A mu = -dJ/dpi with the assembled matrix of the
+    // last solve (mu = 0 on Dirichlet faces) by ILU0-CG; then per cell
+    //   grad = dJ/dtheta|_pi + mu_c . (dS pi_c - db),  S = B - F F^T / L,  b = F g / L,
+    // with dB = totmob W(K) (mode 0; W is linear in K) or totmob W(k_a e_a e_a^T) (mode 1).
+    int adjoint(const double* wp, const double* pstar, const double* wv, int mode, double tol, double* grad,
+                double* Jout, int* iters)
+    {
+        if (do_reg) return 2;
+        for (int t : hf_type)
+            if (t == Periodic) return 2;
+        const int n = S.n;
+        std::vector<double> b(n, 0.0), Sl, B, dB;
+        std::vector<char> dir(n, 0);
+        double J = 0.0;
+        auto cell_S = [&](int c, std::vector<double>& out) {
+            const int nf = g.nf(c), f0 = g.facepos[c];
+            const double* W = &Binv[binvpos[c]];
+            out.assign(nf * nf, 0.0);
+            for (int j = 0; j < nf; ++j)
+                for (int i = 0; i < nf; ++i)
+                    out[i + j * nf] = W[i + j * nf] * totmob[c] - F[f0 + i] * F[f0 + j] / L[c];
+        };
+        for (int c = 0; c < g.nc; ++c) {
+            const int nf = g.nf(c), f0 = g.facepos[c];
+            cell_S(c, Sl);
+            const double p = pressure[c], ps = pstar ? pstar[c] : 0.0;
+            const double dev = wp ? wp[c] * (p - ps) : 0.0;
+            J += dev * (p - ps);
+            for (int i = 0; i < nf; ++i) {
+                double spi = 0.0, su = 0.0;
+                for (int j = 0; j < nf; ++j) {
+                    spi += Sl[i + j * nf] * soln[cf[f0 + j]];
+                    su += Sl[i + j * nf] * (wv ? wv[f0 + j] : 0.0);
+                }
+                const double u = wv ? wv[f0 + i] : 0.0;
+                J += u * (F[f0 + i] * gv[c] / L[c] - spi);
+                const double y = 2.0 * dev * F[f0 + i] / L[c] - su;
+                if (hf_type[f0 + i] == Dirichlet) dir[cf[f0 + i]] = 1;
+                else b[cf[f0 + i]] -= y;
+            }
+        }
+        for (int i = 0; i < n; ++i)
+            if (dir[i]) b[i] = 0.0;
+        *Jout = J;
+        Ilu0 M(S);
+        std::vector<double> mu(n, 0.0);
+        double red = 0.0;
+        const bool ok = pcg(S, M, mu, b, tol, n, iters, &red);
+        if (!ok) return 1;
+        const double zero3[3] = {0.0, 0.0, 0.0};
+        std::vector<double> gtmp;
+        for (int c = 0; c < g.nc; ++c) {
+            const int nf = g.nf(c), f0 = g.facepos[c];
+            const double Lc = L[c], gc = gv[c], p = pressure[c];
+            const double dev = wp ? wp[c] * (p - (pstar ? pstar[c] : 0.0)) : 0.0;
+            std::vector<double> pi(nf), m(nf), Fc(F.begin() + f0, F.begin() + f0 + nf), u(nf);
+            for (int i = 0; i < nf; ++i) {
+                pi[i] = soln[cf[f0 + i]];
+                m[i] = hf_type[f0 + i] == Dirichlet ? 0.0 : mu[cf[f0 + i]];
+                u[i] = wv ? wv[f0 + i] : 0.0;
+            }
+            const int na = mode == 0 ? 1 : 3;
+            for (int ax = 0; ax < na; ++ax) {
+                dB.assign(nf * nf, 0.0);
+                if (mode == 0) {
+                    const double* W = &Binv[binvpos[c]];
+                    for (int k = 0; k < nf * nf; ++k) dB[k] = W[k] * totmob[c];
+                } else {
+                    const double* K = &perm[9 * size_t(c)];
+                    if (K[1] != 0.0 || K[2] != 0.0 || K[3] != 0.0 || K[5] != 0.0 || K[6] != 0.0 || K[7] != 0.0)
+                        return 2;
+                    double Ka[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    Ka[4 * ax] = K[4 * ax];
+                    gtmp.assign(nf, 0.0);
+                    cellInnerProduct(c, Ka, zero3, dB.data(), gtmp.data());
+                    for (int k = 0; k < nf * nf; ++k) dB[k] *= totmob[c];
+                }
+                std::vector<double> dF(nf, 0.0);
+                double dL = 0.0, Fpi = 0.0, dFpi = 0.0;
+                for (int i = 0; i < nf; ++i) {
+                    for (int j = 0; j < nf; ++j) dF[i] += dB[i + j * nf];
+                    dL += dF[i];
+                    Fpi += Fc[i] * pi[i];
+                    dFpi += dF[i] * pi[i];
+                }
+                const double dp = (dFpi - p * dL) / Lc;
+                double gr = 2.0 * dev * dp;
+                for (int i = 0; i < nf; ++i) {
+                    double dBpi = 0.0;
+                    for (int j = 0; j < nf; ++j) dBpi += dB[i + j * nf] * pi[j];
+                    const double dv = p * dF[i] - dBpi + Fc[i] * dp;
+                    const double dSpi = dBpi - (dF[i] * Fpi + Fc[i] * dFpi) / Lc + Fc[i] * Fpi * dL / (Lc * Lc);
+                    const double db = gc * (dF[i] - Fc[i] * dL / Lc) / Lc;
+                    gr += u[i] * dv + m[i] * (dSpi - db);
+                }
+                grad[na * size_t(c) + ax] = gr;
+            }
+        }
+        return 0;
     }
 
     // computePressureAndFluxes, IncompFlowSolverHybrid.hpp:1672-1730
@@ -1012,6 +1127,13 @@ void orc_get_solution(void* h, double* pressure, double* outflux, double* facepr
 }
 
 double orc_post_process_fluxes(void* h) { return static_cast<Pressure*>(h)->postProcess(); }
+
+int orc_adjoint_gradient(void* h, const double* cell_weight, const double* cell_target, const double* hf_weight,
+                         int mode, double tol, double* grad, double* objective, int* iterations)
+{
+    return static_cast<Pressure*>(h)->adjoint(cell_weight, cell_target, hf_weight, mode, tol, grad, objective,
+                                              iterations);
+}
 
 int orc_ilu0_cg(int n, const int* rowptr, const int* colind, const double* vals, const double* b, double* x,
                 double tol, int maxit, int* iterations, double* reduction)

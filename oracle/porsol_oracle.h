@@ -70,6 +70,11 @@ int   orc_solve_timed(void* h, const double* totmob, const double* mobdens,
                       double* seconds3);
 void  orc_get_solution(void* h, double* pressure, double* outflux, double* facepressure);
 double orc_post_process_fluxes(void* h);
+/* Adjoint gradient of J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf of the last solve with
+ * respect to ln k (mode 0: per cell; mode 1: per cell and axis, diagonal tensors).  0 = ok,
+ * 1 = adjoint CG did not converge, 2 = unsupported problem (periodic, pure Neumann). */
+int orc_adjoint_gradient(void* h, const double* cell_weight, const double* cell_target, const double* hf_weight,
+                         int mode, double tol, double* grad, double* objective, int* iterations);
 
 /* -------- plain CG with ILU0 on a CSR matrix (for solver unit tests) -------- */
 int   orc_ilu0_cg(int n, const int* rowptr, const int* colind, const double* vals,

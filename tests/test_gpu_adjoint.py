@@ -1,0 +1,103 @@
+"""Adjoint permeability gradient on the GPU (porsol_objective_value / porsol_adjoint_gradient)
+against the FP64 CPU adjoint of the oracle and central finite differences.
+
+Tolerances: FP64 gradients agree with the oracle's to 1e-9 (normwise) when both solves run to
+1e-13; the mixed-precision forward + adjoint pair to 1e-8.  Finite differences use ln-k steps of
+1e-6 with forward solves to 1e-14; their round-off (about 1e-15 of J divided by the step)
+limits the check to 1e-6 normwise over the sampled cells."""
+import numpy as np
+import pytest
+
+from adjoint import adjoint_problem, central_differences, objective
+from parity import rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(pkg, prob, ltype=1, precision=0, tol=1e-13):
+    s = pkg.PressureSolver()
+    s.init(prob.grid, prob.perm.ravel(), (0.0, 0.0, 0.0), prob.bc_type)
+    o = pkg.default_solve_opts(linsolver_type=ltype, residual_tolerance=tol, precision=precision)
+    fl = pkg.Fluid(pkg.FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0)
+    s.solve(fl, prob.totmob, prob.bc_type, prob.bc_value, prob.src, mobdens=prob.mobdens, opts=o)
+    return s, fl, o
+
+
+def _oracle(orc, prob, w, target, u, mode=0, tol=1e-13):
+    o = orc.OraclePressure(prob.grid, prob.bc_type)
+    o.compute_inner_products(prob.perm.ravel())
+    assert o.solve(prob.totmob, prob.mobdens, prob.bc_type, prob.bc_value, prob.src, tol=tol) == 0
+    rc, J, g = o.adjoint_gradient(w, target, u, mode=mode, tol=tol)
+    assert rc == 0
+    return J, g
+
+
+@pytest.mark.parametrize("ltype,precision,mode", [(0, 0, 0), (1, 0, 0), (1, 0, 1), (1, 1, 0), (1, 1, 1)])
+def test_adjoint_matches_oracle(pkg, gpulib, orc, workloads, cart, ltype, precision, mode):
+    prob, w, target, u = adjoint_problem(workloads, cart, dims=(12, 10, 8), diagonal=(mode == 1))
+    s, _, _ = _gpu(pkg, prob, ltype, precision)
+    J, g, st = s.adjoint_gradient(w, target, u, mode=mode)
+    Jo, go = _oracle(orc, prob, w, target, u, mode)
+    tol = 1e-9 if precision == 0 else 1e-8
+    assert abs(J - Jo) < tol * abs(Jo)
+    assert rel(g, go) < tol, rel(g, go)
+    assert st.iterations > 0
+
+
+def test_objective_value_matches_solution(pkg, gpulib, workloads, cart):
+    prob, w, target, u = adjoint_problem(workloads, cart, dims=(9, 7, 5))
+    s, _, _ = _gpu(pkg, prob)
+    p, v, _ = s.solution()
+    J = s.objective(w, target, u)
+    assert abs(J - objective(p, v, w, target, u)) < 1e-12 * abs(J)
+    assert s.objective(None, None, None) == 0.0
+
+
+def test_adjoint_rejects_unsupported(pkg, gpulib, cart):
+    g = cart.CartesianGrid(4, 4, 4)
+    s = pkg.PressureSolver()
+    bct = np.full(g.num_half_faces, pkg.BC_NEUMANN, np.int32)   # pure Neumann: regularised
+    s.init(g, np.tile(np.eye(3).ravel(), g.num_cells), (0.0, 0.0, 0.0), bct)
+    src = np.zeros(g.num_cells)
+    src[0], src[-1] = 1.0, -1.0
+    fl = pkg.Fluid(pkg.FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0)
+    s.solve(fl, np.ones(g.num_cells), bct, np.zeros(g.num_half_faces), src,
+            opts=pkg.default_solve_opts(linsolver_type=0, residual_tolerance=1e-10))
+    with pytest.raises(pkg.PorsolError):
+        s.adjoint_gradient(np.ones(g.num_cells))
+
+
+def test_adjoint_config4_against_oracle_and_fd(pkg, gpulib, orc, workloads):
+    """64x64x32 correlated log-normal field: 50 pressure observations + outflux through x+.
+    FP64 AMG-CG forward and adjoint; FD at 20 seeded cells with ln-k step 1e-6."""
+    prob = workloads.case4()
+    w, target, u, cells = workloads.case4_objective(prob)
+    s, fl, o = _gpu(pkg, prob, tol=1e-13)
+    J, g, _ = s.adjoint_gradient(w, target, u)
+    Jo, go = _oracle(orc, prob, w, target, u, tol=1e-13)
+    assert abs(J - Jo) < 1e-10 * abs(Jo)
+    assert rel(g, go) < 1e-8, rel(g, go)
+    # scale identity: the pressure part of J does not change when every k is scaled
+    assert abs(g.sum() - float(np.sum(u * s.solution()[1]))) < 1e-9 * np.abs(g).sum()
+
+    o14 = pkg.default_solve_opts(linsolver_type=1, residual_tolerance=1e-14)
+
+    def J_of(K):
+        s.compute_inner_products(K.ravel())
+        s.solve(fl, prob.totmob, prob.bc_type, prob.bc_value, prob.src, mobdens=prob.mobdens, opts=o14)
+        return s.objective(w, target, u)
+
+    fd = central_differences(J_of, prob.perm, cells, [None])
+    err = np.linalg.norm(g[cells] - fd) / np.linalg.norm(fd)
+    assert err < 1e-6, (err, np.c_[g[cells], fd])
+
+
+def test_adjoint_flux_gradient_sums_to_flux(pkg, gpulib, workloads):
+    """d Q / d ln s for K -> s K summed over cells equals Q (the outflux scales with k)."""
+    prob = workloads.case4(dims=(32, 32, 16))
+    s, _, _ = _gpu(pkg, prob, tol=1e-13)
+    u = np.where(prob.grid.side == 2, 1.0, 0.0)
+    Q, g, _ = s.adjoint_gradient(None, None, u)
+    assert abs(g.sum() - Q) < 1e-9 * abs(Q)
+    g3 = s.adjoint_gradient(None, None, u, mode=pkg.GRAD_LOGK_AXES)[1]
+    assert np.abs(g3.sum(axis=1) - g).max() < 1e-10 * np.abs(g).max()
