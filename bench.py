@@ -54,6 +54,8 @@ def parse():
                          "instead of the pressure benchmark and print its own JSON line")
     ap.add_argument("--upscale", type=int, default=0,
                     help="batched periodic upscaling of this many sub-grids instead of the pressure bench")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="adjoint gradient (forward solve + objective + backward) instead of the pressure bench")
     ap.add_argument("--profile-only", choices=["mixed", "fp64"], default=None,
                     help="run warmup + steps of one precision and print nothing else (for ncu captures)")
     return ap.parse_args()
@@ -435,6 +437,68 @@ def run_impes(args):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args):
+    """Configuration 4: d J / d ln k on the 64x64x32 correlated log-normal grid, J = squared
+    pressure mismatch at 50 cells + outflux through x+.  A step is one forward solve (AMG-CG,
+    host inputs, hierarchy rebuilt) + objective + one adjoint solve + gradient, with the gradient
+    copied to the host.  FP64 and mixed precision; the gradient is compared with the oracle's
+    FP64 CPU adjoint, which is also the CPU baseline (ILU0-CG forward + adjoint, one core)."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    wl = ge.load_module("workloads")
+    prob = wl.case4()
+    w, target, u, _ = wl.case4_objective(prob)
+    g = prob.grid
+    fl = pkg.Fluid(pkg.FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0)
+    tol = 1e-10
+    out = {"metric": "adjoint gradients/s (forward + backward) @131k cells", "unit": "gradients/s",
+           "config": {"workload": "64x64x32 isotropic log-normal sigma 1 correlated 4 cells, 50 pressure "
+                                  "observations + outflux at x+", "tol": tol}}
+    grads = {}
+    steps = max(3, args.steps)
+    for name, prec in (("mixed", pkg.MIXED), ("fp64", pkg.FP64)):
+        s = pkg.PressureSolver()
+        s.init(g, prob.perm.ravel(), (0.0, 0.0, 0.0), prob.bc_type)
+        o = pkg.default_solve_opts(linsolver_type=1, residual_tolerance=tol, precision=prec)
+
+        def step():
+            s.solve(fl, prob.totmob, prob.bc_type, prob.bc_value, prob.src, mobdens=prob.mobdens, opts=o)
+            return s.adjoint_gradient(w, target, u)
+
+        for _ in range(max(3, args.warmup)):
+            step()
+        torch.cuda.synchronize()
+        times, back = [], []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            J, gr, st = step()
+            times.append(time.perf_counter() - t0)
+            back.append(st.ms_krylov + st.ms_recover)
+        grads[name] = gr
+        t = float(np.median(times))
+        out[name] = {"value": round(1.0 / t, 3), "ms_per_gradient": round(1e3 * t, 3),
+                     "ms_backward": round(float(np.median(back)), 3), "adjoint_iterations": st.iterations, "J": J}
+        s.close()
+    out["value"] = out["mixed"]["value"]
+    out["speedup_mixed_vs_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    if not args.no_cpu_baseline:
+        import oracle
+        if not os.path.exists(oracle.LIB_PATH):
+            oracle.build()
+        t0 = time.perf_counter()
+        o = oracle.OraclePressure(g, prob.bc_type)
+        o.compute_inner_products(prob.perm.ravel())
+        assert o.solve(prob.totmob, prob.mobdens, prob.bc_type, prob.bc_value, prob.src, tol=tol) == 0
+        rc, Jo, go = o.adjoint_gradient(w, target, u, tol=tol)
+        el = time.perf_counter() - t0
+        nrm = np.linalg.norm(go)
+        out["rel_err_vs_oracle"] = {k: float(np.linalg.norm(v - go) / nrm) for k, v in grads.items()}
+        out["cpu_baseline"] = {"value": round(1.0 / el, 4), "unit": "gradients/s", "cores": 1, "kind": "port",
+                               "sample": f"one forward + adjoint, ILU0-CG tol {tol}, FP64"}
+    print(json.dumps(out), flush=True)
+
+
 def run_upscale(args):
     """Configuration 3: effective permeability of N periodic unit-cube sub-grids (side n ~ U{8..32},
     full log-normal tensors with random axes), three unit pressure-jump solves each, as one
@@ -500,6 +564,9 @@ def main():
         return
     if args.upscale:
         run_upscale(args)
+        return
+    if args.adjoint:
+        run_adjoint(args)
         return
     if args.impl == "reference":
         run_reference(args)
