@@ -190,7 +190,8 @@ public:
     // PORSOL_FP64 (default, the plain drop-in) or PORSOL_MIXED (FP32 in FP64 refinement).
     void setPrecision(int mode) { extra_.precision = mode; }
     const porsol_solve_stats& lastStats() const { return stats_; }
-    porsol_solver* handle() { return h_; }
+    porsol_solver* handle() const { return h_; }
+    const FlatGrid& flatGrid() const { return grid_; }
 
 private:
     porsol_solver* h_ = nullptr;

@@ -15,6 +15,7 @@
 
 #include "opm/porsol/gpu/EulerUpstream.hpp"
 #include "opm/porsol/gpu/IncompFlowSolverHybrid.hpp"
+#include "opm/porsol/gpu/PermeabilityAdjoint.hpp"
 
 namespace mock {
 
@@ -273,6 +274,55 @@ int main()
     if (water > qin * T * (1 + 1e-9) || water < qin * T * (1 - 1e-3) || smin < -1e-12 || smax > 1 + 1e-12) {
         std::printf("transport mass balance %g vs %g\n", water, qin * T);
         return 1;
+    }
+    // forward/backward pair: J = sum of squared mismatches at three cells + scaled outflux at x+
+    {
+        Rock r2 = r;
+        for (int c = 0; c < nc; ++c) {
+            const double k = 1e-13 * std::exp(0.7 * std::sin(1.3 * c));
+            r2.K[c] = Tensor{{k, 0, 0, 0, 0.5 * k, 0, 0, 0, 0.2 * k}};
+        }
+        Solver sa;
+        sa.init(g, r2, grav, bcx);
+        Opm::gpu::PermeabilityAdjoint<Solver> adj(sa);
+        std::vector<double> w(nc, 0.0), tgt(nc, -0.4), u(sa.flatGrid().numHalfFaces(), 0.0);
+        w[5] = w[77] = w[150] = 1.0;
+        for (CellIterator c = g.cellbegin(); c != g.cellend(); ++c)
+            for (FaceIterator f = c->facebegin(); f != c->faceend(); ++f)
+                if (f->boundary() && f->centroid()[0] > 1.0 - 1e-12) u[sa.flatGrid().halfFace(c->index(), f->localIndex())] = 1e12;
+        adj.setObjective(w, tgt, u);
+        const double J = adj.forward(fl, s0, bcx, src, 1e-14, 0, 1);
+        double Jh = 0.0;
+        for (CellIterator c = g.cellbegin(); c != g.cellend(); ++c) {
+            const double d = sa.getSolution().pressure(c) - tgt[c->index()];
+            Jh += w[c->index()] * d * d;
+            for (FaceIterator f = c->facebegin(); f != c->faceend(); ++f)
+                Jh += u[sa.flatGrid().halfFace(c->index(), f->localIndex())] * sa.getSolution().outflux(f);
+        }
+        if (std::fabs(J - Jh) > 1e-12 * std::fabs(J)) {
+            std::printf("objective %.17g vs %.17g\n", J, Jh);
+            return 1;
+        }
+        const std::vector<double> grad = adj.backward();
+        const std::vector<double> g3 = adj.backward(true);
+        for (int c = 0; c < nc; ++c)
+            if (std::fabs(g3[3 * c] + g3[3 * c + 1] + g3[3 * c + 2] - grad[c]) > 1e-10 * std::fabs(grad[77]) + 1e-300) {
+                std::printf("axis gradients do not sum to the scale gradient at %d\n", c);
+                return 1;
+            }
+        const double h = 1e-4;
+        double Jpm[2];
+        for (int k = 0; k < 2; ++k) {
+            Rock rp = r2;
+            for (int q = 0; q < 9; ++q) rp.K[77].k[q] *= std::exp(k == 0 ? h : -h);
+            sa.computeInnerProducts(rp, grav);
+            Jpm[k] = adj.forward(fl, s0, bcx, src, 1e-14, 0, 1);
+        }
+        const double fd = (Jpm[0] - Jpm[1]) / (2 * h);
+        if (std::fabs(fd - grad[77]) > 1e-6 * std::fabs(fd)) {
+            std::printf("adjoint %.12g vs finite difference %.12g\n", grad[77], fd);
+            return 1;
+        }
     }
     std::printf("OK\n");
     return 0;
