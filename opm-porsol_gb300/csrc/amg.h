@@ -55,6 +55,7 @@ private:
         DBuf<T> own_val;
         DBuf<T> dinv;
         double lmax = 2.0;
+        int lanes = 1;               // threads per row in the smoother/residual kernels
         Aggregates agg;              // to the next level
         DBuf<T> t, r, d0, d1, b, x;  // work vectors
     };

@@ -498,26 +498,53 @@ __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __rest
     d[i] = ri * inv_theta;
 }
 
+// Row r and lane q of the row for K lanes per row (K = 1: one thread per row).
+template <int K>
+__device__ __forceinline__ void row_lane(int& r, int& q)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    r = g / K;
+    q = g % K;
+}
+
+// sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, K lanes otherwise
+template <int K, class T, class XF>
+__device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
+                                     const int* __restrict__ rowlen, int r, int q, bool valid, XF xf)
+{
+    if constexpr (K == 1) {
+        return valid ? sell_dot<T>(sp, col, A, r, xf) : T(0);
+    } else {
+        return sell_dot_lanes<K, T>(sp, col, A, rowlen, r, q, valid, xf);
+    }
+}
+
 // start from y = t + w P xc (xc may be null: y = t): x = y, r = D^-1 (b - A y), d = r / theta
-template <class T>
+template <class T, int K>
 __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __restrict__ col,
-                             const T* __restrict__ A, const T* __restrict__ dinv, const T* __restrict__ b,
-                             const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg, T wp,
-                             T* __restrict__ x, T* __restrict__ r, T* __restrict__ d, T inv_theta, const int* stop)
+                             const int* __restrict__ rowlen, const T* __restrict__ A, const T* __restrict__ dinv,
+                             const T* __restrict__ b, const T* __restrict__ t, const T* __restrict__ xc,
+                             const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
+                             T* __restrict__ d, T inv_theta, const int* stop)
 {
     if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    int i, q;
+    row_lane<K>(i, q);
+    const bool valid = i < n;
+    if (K == 1 && !valid) return;
     T acc;
     if (xc) {
-        acc = sell_dot<T>(sp, col, A, i, [t, xc, agg, wp](int j) {
+        acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [t, xc, agg, wp](int j) {
             const int aj = agg[j];
             return t[j] + (aj >= 0 ? wp * xc[aj] : T(0));
         });
+    } else {
+        acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [t](int j) { return t[j]; });
+    }
+    if (!valid || q != 0) return;
+    if (xc) {
         const int ai = agg[i];
         x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
-    } else {
-        acc = sell_dot<T>(sp, col, A, i, [t](int j) { return t[j]; });
     }
     const T ri = dinv[i] * (b[i] - acc);
     r[i] = ri;
@@ -525,15 +552,19 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __res
 }
 
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
-template <class T>
-__global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
-                            const T* __restrict__ dinv, const T* x_in, const T* __restrict__ d_in, T* __restrict__ r,
-                            T* __restrict__ d_out, T* x_out, T c1, T c2, int final_step, const int* stop)
+template <class T, int K>
+__global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                            const int* __restrict__ rowlen, const T* __restrict__ A, const T* __restrict__ dinv,
+                            const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
+                            T* x_out, T c1, T c2, int final_step, const int* stop)
 {
     if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const T acc = sell_dot<T>(sp, col, A, i, [d_in](int j) { return d_in[j]; });
+    int i, q;
+    row_lane<K>(i, q);
+    const bool valid = i < n;
+    if (K == 1 && !valid) return;
+    const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
+    if (!valid || q != 0) return;
     const T di = d_in[i];
     T xi = (x_in ? x_in[i] : T(0)) + di;
     const T ri = r[i] - dinv[i] * acc;
@@ -544,14 +575,18 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     x_out[i] = xi;
 }
 
-template <class T>
-__global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
-                        const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r, const int* stop)
+template <class T, int K>
+__global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
+                        const T* __restrict__ A, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
+                        const int* stop)
 {
     if (*stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const T acc = sell_dot<T>(sp, col, A, i, [x](int j) { return x[j]; });
+    int i, q;
+    row_lane<K>(i, q);
+    const bool valid = i < n;
+    if (K == 1 && !valid) return;
+    const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
+    if (!valid || q != 0) return;
     r[i] = b[i] - acc;
 }
 
@@ -644,6 +679,28 @@ int read_int(cudaStream_t s, const int* d)
     PORSOL_CUDA(cudaStreamSynchronize(s));
     return v;
 }
+
+// Lanes per row of a level.  Levels with many rows are bandwidth-bound and keep one thread per
+// row (consecutive threads on consecutive rows give fully coalesced SELL loads; more lanes only
+// add instructions).  Small levels (under 20k rows, 30-60 entries per row) are latency-bound:
+// one thread would walk its long row serially, so 3-6 entries per lane are used there.
+int lanes_for(int n, long long nent)
+{
+    const double avg = n > 0 ? double(nent) / n : 0.0;
+    if (n >= 20000 || avg <= 8.0) return 1;
+    int k = 2;
+    while (k < 16 && k * 6 < avg) k *= 2;
+    return k;
+}
+
+#define PORSOL_LANES(K, LAUNCH)                                                                                    \
+    switch (K) {                                                                                                   \
+    case 1: { constexpr int KL = 1; LAUNCH; } break;                                                              \
+    case 2: { constexpr int KL = 2; LAUNCH; } break;                                                              \
+    case 4: { constexpr int KL = 4; LAUNCH; } break;                                                              \
+    case 8: { constexpr int KL = 8; LAUNCH; } break;                                                              \
+    default: { constexpr int KL = 16; LAUNCH; } break;                                                            \
+    }
 
 }  // namespace
 
@@ -805,6 +862,7 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L)
     double gm;
     std::memcpy(&gm, &gb, sizeof(gm));
     L.lmax = gm > 0 ? gm : 1.0;
+    L.lanes = lanes_for(n, L.P->nent);
     L.t.alloc(n);
     L.r.alloc(n);
     L.d0.alloc(n);
@@ -915,8 +973,10 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
     } else {
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
-        PORSOL_LAUNCH(k_cheb_start<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong),
-                                          x, L.r.p, d, T(1.0 / theta), stop));
+        const int nbk = div_up(n * L.lanes, TB);
+        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL><<<nbk, TB, 0, s>>>(
+                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x,
+                                  L.r.p, d, T(1.0 / theta), stop))));
     }
     const int deg = std::max(1, o_.cheb_degree);
     for (int k = 1; k <= deg; ++k) {
@@ -928,8 +988,10 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();  // finest level only
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
-        PORSOL_LAUNCH(k_cheb_step<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
-                                         k == deg ? 1 : 0, stop));
+        const int nbk = div_up(n * L.lanes, TB);
+        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL><<<nbk, TB, 0, s>>>(
+                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1),
+                                  T(c2), k == deg ? 1 : 0, stop))));
         if (prof_here) prof_->end(s, PK_CHEB, bytes, ev);
         rho = rho1;
         std::swap(d, dn);
@@ -953,7 +1015,8 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
     // restrict the residual
-    PORSOL_LAUNCH(k_resid<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, b, L.t.p, L.r.p, stop));
+    PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
+                              n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, b, L.t.p, L.r.p, stop))));
     PORSOL_LAUNCH(k_restrict<T><<<div_up(Nx.n, TB), TB, 0, s>>>(Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop));
     vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
     // post-smoothing from t + w P xc

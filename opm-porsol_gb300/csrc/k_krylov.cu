@@ -16,6 +16,22 @@ namespace {
 
 constexpr int RB = 256;  // threads per block of the vector kernels
 
+// Blocks of the reduction kernels: at most 8 per SM, grid-stride beyond.  The last-block
+// reduction costs one fence + atomic per block, so a grid of one thread per row (12k blocks at
+// 3 M rows) spends more time arriving than summing.  The cap depends only on the device, so
+// the summation order stays fixed.
+int red_blocks(int n)
+{
+    static int cap = 0;
+    if (cap == 0) {
+        int dev = 0, sms = 0;
+        PORSOL_CUDA(cudaGetDevice(&dev));
+        PORSOL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = std::max(1, 8 * sms);
+    }
+    return std::max(1, std::min(div_up(std::max(n, 1), RB), cap));
+}
+
 template <class V>
 __device__ __forceinline__ V warp_sum(V v)
 {
@@ -100,12 +116,11 @@ __global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ s
                                                 const T* __restrict__ b, T* __restrict__ r, CgDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T v = 0;
-    if (i < n) {
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
         const T ri = b[i] - sell_row(sp, col, val, x, i);
         r[i] = ri;
-        v = ri * ri;
+        v += ri * ri;
     }
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) {
@@ -132,9 +147,8 @@ __global__ void __launch_bounds__(RB) k_dot_zr(int n, const T* __restrict__ z, c
                                                double* partial, unsigned int* counter)
 {
     if (st->stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T v = 0;
-    if (i < n) v = z[i] * r[i];
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += z[i] * r[i];
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) {
         st->rho = tot;
@@ -159,12 +173,11 @@ __global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ s
                                                 unsigned int* counter)
 {
     if (st->stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T v = 0;
-    if (i < n) {
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
         const T qi = sell_row(sp, col, val, p, i);
         q[i] = qi;
-        v = p[i] * qi;
+        v += p[i] * qi;
     }
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) {
@@ -182,13 +195,12 @@ __global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* _
     if (st->stop) return;
     const double alpha = st->alpha;
     const T lambda = T(st->lambda);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T v = 0;
-    if (i < n) {
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
         x[i] = x[i] + lambda * p[i];
         const T ri = r[i] - lambda * q[i];
         r[i] = ri;
-        v = ri * ri;
+        v += ri * ri;
     }
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) {
@@ -207,21 +219,16 @@ __global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* _
     }
 }
 
-// beta = rho/rholast; p = z + beta p
+// beta = rho/rholast; p = z + beta p; rholast = rho for the next iteration (no thread of
+// this kernel reads rholast)
 template <class T>
-__global__ void k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st, int* flip)
+__global__ void k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st)
 {
     if (st->stop) return;
     const T beta = T(st->beta);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = z[i] + beta * p[i];
-    (void)flip;
-}
-
-__global__ void k_cg_roll(CgDev* st)
-{
-    if (st->stop) return;
-    st->rholast = st->rho;
+    if (i == 0) st->rholast = st->rho;
 }
 
 template <class TA, class TB>
@@ -271,8 +278,8 @@ template <class T>
 __global__ void __launch_bounds__(RB) k_norm2(int n, const T* __restrict__ x, double* partial, unsigned int* counter,
                                               double* out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const T v = i < n ? x[i] * x[i] : T(0);
+    T v = 0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += x[i] * x[i];
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) *out = tot;
 }
@@ -420,23 +427,22 @@ void PcgSolver<TV, T>::iteration(cudaStream_t s, const SellPattern& P, const TV*
                                  Profiler* prof, int prof_kernel)
 {
     const int n = P.n;
-    const int nb = div_up(n, RB);
+    const int nb = div_up(n, RB), nr = red_blocks(n);
     const int* stop = &st_.p->stop;
     const double spmv_bytes = double(P.nent) * (sizeof(TV) + 4) + 2.0 * n * sizeof(T);
     {
         const bool pf = prof && prof->on && prof_kernel >= 0;
         cudaEvent_t ev = nullptr;
         if (pf) prof->begin(s, prof_kernel, spmv_bytes, &ev);
-        PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+        PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
                                                          red_.partial.p, red_.counter.p));
         if (pf) prof->end(s, prof_kernel, spmv_bytes, ev);
     }
-    PORSOL_LAUNCH(k_cg_update<T><<<nb, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
+    PORSOL_LAUNCH(k_cg_update<T><<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
                                                    dview_));
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
-    PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, nullptr));
-    PORSOL_LAUNCH(k_cg_roll<<<1, 1, 0, s>>>(st_.p));
+    PORSOL_LAUNCH(k_dot_zr<T><<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
+    PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
 }
 
 template <class TV, class T>
@@ -450,17 +456,17 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
         return res;
     }
     setup(n, s);
-    const int nb = div_up(n, RB);
+    const int nb = div_up(n, RB), nr = red_blocks(n);
     CgDev init{};
     init.tol = tol;
     init.maxit = maxit;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
-    PORSOL_LAUNCH(k_cg_init<TV, T><<<nb, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
+    PORSOL_LAUNCH(k_cg_init<TV, T><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
                                                      red_.partial.p, red_.counter.p, dview_));
     PORSOL_CUDA(cudaGetLastError());
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_dot_zr<T><<<nb, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
+    PORSOL_LAUNCH(k_dot_zr<T><<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
     PORSOL_LAUNCH(k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
     PORSOL_CUDA(cudaGetLastError());
     // One iteration is captured into a CUDA graph (re-captured when the matrix, vectors or
@@ -658,7 +664,7 @@ template <class T>
 double norm2(cudaStream_t s, int n, const T* x, RedScratch& red)
 {
     if (n == 0) return 0.0;
-    const int nb = div_up(n, RB);
+    const int nb = red_blocks(n);
     red.ensure(nb + 1, s);
     PORSOL_LAUNCH(k_norm2<T><<<nb, RB, 0, s>>>(n, x, red.partial.p, red.counter.p, red.partial.p + nb));
     PORSOL_CUDA(cudaGetLastError());
