@@ -80,6 +80,8 @@ private:
     DBuf<float> s_rs_;
     DBuf<int> s_state_, s_partner_, s_join_, s_best_, s_flag_, s_cidx_, s_cnt_, s_pos_, s_width_;
     DBuf<unsigned long long> s_gmax_;
+    DBuf<int> s_bnd_, s_goff_, s_tcol_, s_dpos_;   // single-pass Galerkin temporaries
+    DBuf<T> s_tval_;
     Aggregates agg2_;
     std::vector<int> sizes_;
     std::vector<long long> nnzs_;

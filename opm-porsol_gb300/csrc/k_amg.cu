@@ -99,7 +99,10 @@ __device__ __forceinline__ bool stronger(float s, unsigned h, int j, float bs, u
     return s > bs || (s == bs && (h > bh || (h == bh && j < bj)));
 }
 
-// state: 0 free, 1 paired, 2 isolated (no off-diagonal coupling: never aggregated)
+// state: 0 free, 1 paired, 2 isolated (no off-diagonal coupling: never aggregated),
+// 3 free without a free strong neighbour (strengths are symmetric and neighbours only ever
+// become paired, so such a row cannot pair in a later sweep; it is skipped from then on and
+// ends as a singleton or joins a pair)
 template <class T>
 __global__ void k_isolated(int n, const int* __restrict__ sp, const int* __restrict__ col,
                            const int* __restrict__ rowlen, const T* __restrict__ A, int* __restrict__ state,
@@ -157,6 +160,8 @@ __global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ 
     if (j >= 0 && best[j] == i) {
         state[i] = 1;
         partner[i] = j;
+    } else if (j < 0) {
+        state[i] = 3;
     }
 }
 
@@ -167,7 +172,7 @@ __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict_
                        int* __restrict__ join)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || state[i] != 0) return;
+    if (i >= n || (state[i] != 0 && state[i] != 3)) return;
     const float ri = rs[i];
     float bs = 0.0f;
     unsigned bh = 0u;
@@ -193,7 +198,8 @@ __global__ void k_rep_flag(int n, const int* __restrict__ state, const int* __re
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    flag[i] = ((state[i] == 0 && join[i] < 0) || (state[i] == 1 && i < partner[i])) ? 1 : 0;
+    const int st = state[i];
+    flag[i] = (((st == 0 || st == 3) && join[i] < 0) || (st == 1 && i < partner[i])) ? 1 : 0;
 }
 
 __global__ void k_assign(int n, const int* __restrict__ state, const int* __restrict__ partner,
@@ -252,17 +258,6 @@ __global__ void k_sort_members(int nc, const int* __restrict__ ptr, int* __restr
 }
 
 // ---------------- Galerkin products ----------------
-__global__ void k_gal_bound(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
-                            const int* __restrict__ rowlen, int* __restrict__ maxb)
-{
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    int b = 0;
-    if (I < nc)
-        for (int q = ptr[I]; q < ptr[I + 1]; ++q) b += rowlen[idx[q]];
-    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(maxb, b);
-}
-
 // Merge the member rows of aggregate I, mapping columns through agg (isolated columns,
 // agg < 0, carry no coupling and are skipped): sorted unique keys with summed values.
 template <class T, int CAP>
@@ -336,18 +331,35 @@ __global__ void k_gal_fill(int nc, const int* __restrict__ sp, const int* __rest
     diag_c[I] = dslot;
 }
 
-// Warp-per-coarse-row Galerkin merge: the member rows' entries (column mapped through agg)
-// are loaded into shared memory, bitonic-sorted by column, and duplicates summed (FP64).
-// count: rowlen_c[I] = number of distinct columns; fill: write them into the SELL slots.
+// Per coarse row: upper bound of its merged length (sum of the member rows' lengths); the
+// largest bound goes to *maxb.
+__global__ void k_gal_rowbound(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
+                               const int* __restrict__ rowlen, int* __restrict__ bnd, int* __restrict__ maxb)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = 0;
+    if (I < nc) {
+        for (int q = ptr[I]; q < ptr[I + 1]; ++q) b += rowlen[idx[q]];
+        bnd[I] = b;
+    }
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxb, b);
+}
+
+// Warp-per-coarse-row Galerkin merge, one pass: the member rows' entries (column mapped
+// through agg) are loaded into shared memory, bitonic-sorted by column and duplicates summed
+// (FP64); the distinct (column, value) pairs go compactly to off[I] of a temporary buffer,
+// with the row length and the position of the diagonal.  The SELL layout is filled from there
+// once the slice widths are known (k_gal_scatter).
 constexpr int GW_WARPS = 4;
-template <class T, int CAP, bool FILL>
-__global__ void __launch_bounds__(GW_WARPS * 32) k_gal_warp(int nc, const int* __restrict__ sp,
-                                                          const int* __restrict__ col, const int* __restrict__ rowlen,
-                                                          const T* __restrict__ A, const int* __restrict__ agg,
-                                                          const int* __restrict__ ptr, const int* __restrict__ idx,
-                                                          int* __restrict__ rowlen_c, const int* __restrict__ sp_c,
-                                                          int* __restrict__ col_c, T* __restrict__ val_c,
-                                                          int* __restrict__ diag_c)
+template <class T, int CAP>
+__global__ void __launch_bounds__(GW_WARPS * 32) k_gal_merge(int nc, const int* __restrict__ sp,
+                                                           const int* __restrict__ col, const int* __restrict__ rowlen,
+                                                           const T* __restrict__ A, const int* __restrict__ agg,
+                                                           const int* __restrict__ ptr, const int* __restrict__ idx,
+                                                           const int* __restrict__ off, int* __restrict__ tcol,
+                                                           T* __restrict__ tval, int* __restrict__ rowlen_c,
+                                                           int* __restrict__ dpos)
 {
     __shared__ int sk[GW_WARPS][CAP];
     __shared__ double sv[GW_WARPS][CAP];
@@ -356,7 +368,6 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_warp(int nc, const int* _
     if (I >= nc) return;   // warp-uniform
     int* keys = sk[w];
     double* vals = sv[w];
-    // gather
     int m = 0;
     for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
         const int r = idx[q];
@@ -377,7 +388,6 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_warp(int nc, const int* _
         vals[p] = 0.0;
     }
     __syncwarp();
-    // bitonic sort of (key, value) pairs, ascending keys
     for (int k = 2; k <= m2; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int p = lane; p < m2; p += 32) {
@@ -397,37 +407,60 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_warp(int nc, const int* _
             __syncwarp();
         }
     }
-    // distinct keys: heads of runs of equal keys
-    int base = 0, dslot = -1;
-    const int s = I >> 5;
-    const int wdt = FILL ? (sp_c[s + 1] - sp_c[s]) >> 5 : 0;
+    const int o = off[I];
+    int base = 0, dp = -1;
     for (int c0 = 0; c0 < m2; c0 += 32) {
         const int p = c0 + lane;
         const bool head = p < m2 && keys[p] != INT_MAX && (p == 0 || keys[p] != keys[p - 1]);
         const unsigned mask = __ballot_sync(0xffffffffu, head);
-        if (FILL && head) {
+        if (head) {
             double sum = vals[p];
             for (int q = p + 1; q < m2 && keys[q] == keys[p]; ++q) sum += vals[q];
             const int t = base + __popc(mask & ((1u << lane) - 1u));
-            const int kk = sp_c[s] + t * 32 + (I & 31);
-            col_c[kk] = keys[p];
-            val_c[kk] = T(sum);
-            if (keys[p] == I) dslot = kk;
+            tcol[o + t] = keys[p];
+            tval[o + t] = T(sum);
+            if (keys[p] == I) dp = t;
         }
         base += __popc(mask);
     }
-    if (!FILL) {
-        if (lane == 0) rowlen_c[I] = base;
-        return;
+    for (int q = 16; q > 0; q >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, q));
+    if (lane == 0) {
+        rowlen_c[I] = base;
+        dpos[I] = dp;
     }
-    for (int t = base + lane; t < wdt; t += 32) {
-        const int kk = sp_c[s] + t * 32 + (I & 31);
-        col_c[kk] = I;
-        val_c[kk] = T(0);
+}
+
+// One warp per slice of the coarse matrix (lane = row): copy each row from the temporary
+// buffer, pad past the row length (col = row, value 0; rows past nc get col = 0) and record
+// the diagonal's slot (-1 if the row has none; k_check_diag reports it).
+template <class T>
+__global__ void k_gal_scatter(int nc, int nslices, const int* __restrict__ sp_c, const int* __restrict__ off,
+                              const int* __restrict__ tcol, const T* __restrict__ tval,
+                              const int* __restrict__ rowlen_c, const int* __restrict__ dpos, int* __restrict__ col_c,
+                              T* __restrict__ val_c, int* __restrict__ diag_c)
+{
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (s >= nslices) return;
+    const int lane = threadIdx.x & 31;
+    const int I = s * 32 + lane;
+    const int b = sp_c[s], w = (sp_c[s + 1] - b) >> 5;
+    const bool row = I < nc;
+    const int len = row ? rowlen_c[I] : 0;
+    const int o = row ? off[I] : 0;
+    for (int t = 0; t < w; ++t) {
+        const int k = b + t * 32 + lane;
+        if (t < len) {
+            col_c[k] = tcol[o + t];
+            val_c[k] = tval[o + t];
+        } else {
+            col_c[k] = row ? I : 0;
+            val_c[k] = T(0);
+        }
     }
-    // the diagonal is found by exactly one lane (or none)
-    for (int o = 16; o > 0; o >>= 1) dslot = max(dslot, __shfl_xor_sync(0xffffffffu, dslot, o));
-    if (lane == 0) diag_c[I] = dslot;
+    if (row) {
+        const int d = dpos[I];
+        diag_c[I] = d >= 0 ? b + d * 32 + lane : -1;
+    }
 }
 
 __global__ void k_slice_width(int n, int nslices, const int* __restrict__ rowlen, int* __restrict__ width)
@@ -792,31 +825,41 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     Pc.slice_ptr.alloc(Pc.nslices + 1);
     iscratch_.alloc(4);
     PORSOL_CUDA(cudaMemsetAsync(iscratch_.p, 0, sizeof(int), s));
-    PORSOL_LAUNCH(k_gal_bound<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p, P.rowlen.p, iscratch_.p));
-    const int bound = read_int(s, iscratch_.p);
+    s_bnd_.alloc(std::max(nc, 1));
+    s_goff_.alloc(nc + 1);
+    PORSOL_LAUNCH(k_gal_rowbound<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p, P.rowlen.p, s_bnd_.p,
+                                                                iscratch_.p));
+    exclusive_scan(s, nc, s_bnd_.p, s_goff_.p, s_goff_.p + nc, scan_blocks_);
+    int hb[2] = {0, 0};
+    PORSOL_CUDA(cudaMemcpyAsync(&hb[0], iscratch_.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaMemcpyAsync(&hb[1], s_goff_.p + nc, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    const int bound = hb[0], total = hb[1];
     PORSOL_REQUIRE(bound <= 2048, PORSOL_ERR_BAD_ARG, "AMG: aggregate rows too long for the Galerkin merge");
-    const int nb = div_up(nc, 64);
-    const int nbw = div_up(nc, GW_WARPS);
     const bool warp = bound <= 1024;
-#define PORSOL_GALW(CAP, FILL)                                                                                      \
-    PORSOL_LAUNCH((k_gal_warp<T, CAP, FILL><<<nbw, GW_WARPS * 32, 0, s>>>(                                          \
-        nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p, Pc.rowlen.p, Pc.slice_ptr.p,          \
-        Pc.col.p, Ac.p, Pc.diag.p)))
-#define PORSOL_GAL(CAP)                                                                                             \
-    PORSOL_COUNT_LAUNCH();                                                                                          \
-    k_gal_count<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,     \
-                                         Pc.rowlen.p)
     if (warp) {
-        if (bound <= 32) { PORSOL_GALW(32, false); }
-        else if (bound <= 64) { PORSOL_GALW(64, false); }
-        else if (bound <= 128) { PORSOL_GALW(128, false); }
-        else if (bound <= 256) { PORSOL_GALW(256, false); }
-        else if (bound <= 512) { PORSOL_GALW(512, false); }
-        else { PORSOL_GALW(1024, false); }
+        // one merge pass into a compact temporary, then the SELL layout
+        s_tcol_.alloc(std::max(total, 1));
+        s_tval_.alloc(std::max(total, 1));
+        s_dpos_.alloc(std::max(nc, 1));
+        const int nbw = div_up(nc, GW_WARPS);
+#define PORSOL_GALM(CAP)                                                                                            \
+    PORSOL_LAUNCH((k_gal_merge<T, CAP><<<nbw, GW_WARPS * 32, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A,      \
+                                                                      a.agg.p, a.ptr.p, a.idx.p, s_goff_.p,         \
+                                                                      s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p)))
+        if (bound <= 32) { PORSOL_GALM(32); }
+        else if (bound <= 64) { PORSOL_GALM(64); }
+        else if (bound <= 128) { PORSOL_GALM(128); }
+        else if (bound <= 256) { PORSOL_GALM(256); }
+        else if (bound <= 512) { PORSOL_GALM(512); }
+        else { PORSOL_GALM(1024); }
+#undef PORSOL_GALM
     } else {
-        PORSOL_GAL(2048);
+        const int nb = div_up(nc, 64);
+        PORSOL_COUNT_LAUNCH();
+        k_gal_count<T, 2048><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,
+                                               Pc.rowlen.p);
     }
-#undef PORSOL_GAL
     DBuf<int>& width = s_width_;
     width.alloc(Pc.nslices);
     PORSOL_LAUNCH(k_slice_width<<<div_up(Pc.nslices, TB), TB, 0, s>>>(nc, Pc.nslices, Pc.rowlen.p, width.p));
@@ -824,23 +867,17 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     Pc.nent = read_int(s, Pc.slice_ptr.p + Pc.nslices);
     Pc.col.alloc(std::max<long long>(Pc.nent, 1));
     Ac.alloc(std::max<long long>(Pc.nent, 1));
-#define PORSOL_GALF(CAP)                                                                                            \
-    PORSOL_COUNT_LAUNCH();                                                                                          \
-    k_gal_fill<T, CAP><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,      \
-                                        Pc.slice_ptr.p, Pc.col.p, Ac.p, Pc.diag.p)
     if (warp) {
-        if (bound <= 32) { PORSOL_GALW(32, true); }
-        else if (bound <= 64) { PORSOL_GALW(64, true); }
-        else if (bound <= 128) { PORSOL_GALW(128, true); }
-        else if (bound <= 256) { PORSOL_GALW(256, true); }
-        else if (bound <= 512) { PORSOL_GALW(512, true); }
-        else { PORSOL_GALW(1024, true); }
+        PORSOL_LAUNCH(k_gal_scatter<T><<<div_up(Pc.nslices, TB / 32), TB, 0, s>>>(
+            nc, Pc.nslices, Pc.slice_ptr.p, s_goff_.p, s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p, Pc.col.p, Ac.p,
+            Pc.diag.p));
     } else {
-        PORSOL_GALF(2048);
+        const int nb = div_up(nc, 64);
+        PORSOL_COUNT_LAUNCH();
+        k_gal_fill<T, 2048><<<nb, 64, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p,
+                                              Pc.slice_ptr.p, Pc.col.p, Ac.p, Pc.diag.p);
+        if (nc > 0) PORSOL_LAUNCH(k_pad_tail<T><<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p));
     }
-#undef PORSOL_GALF
-#undef PORSOL_GALW
-    if (nc > 0) PORSOL_LAUNCH(k_pad_tail<T><<<1, 32, 0, s>>>(nc, Pc.nslices, Pc.slice_ptr.p, Pc.col.p, Ac.p));
     PORSOL_LAUNCH(k_check_diag<<<div_up(nc, TB), TB, 0, s>>>(nc, Pc.diag.p, status_.p));
     PORSOL_CUDA(cudaGetLastError());
 }
