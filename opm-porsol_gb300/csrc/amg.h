@@ -28,6 +28,9 @@ struct AmgOpts {
     int max_levels = 24;
     double strength = 0.25;
     int cheb_degree = 2;
+    bool round1_negative = true;   // first pairing round of a level on strong negative couplings
+    bool round2_negative = false;  // second round likewise; off: directly |a_ij| with joins (the
+                                   // negative attempt stalls on these systems and is discarded)
 };
 
 // Device aggregation result: agg (row -> aggregate or -1), members CSR (aggregate -> rows).
@@ -59,7 +62,7 @@ private:
         Aggregates agg;              // to the next level
         DBuf<T> t, r, d0, d1, b, x;  // work vectors
     };
-    void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, Aggregates& out);
+    void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg_first, Aggregates& out);
     void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
                   Aggregates& out);
     void members(cudaStream_t s, Aggregates& a);

@@ -111,7 +111,8 @@ __global__ void k_isolated(int n, const int* __restrict__ sp, const int* __restr
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     bool iso = true;
-    for (int t = 0; t < rowlen[i]; ++t) {
+    const int len = rowlen[i];
+    for (int t = 0; t < len && iso; ++t) {
         const int k = slot_of(sp, i, t);
         if (col[k] != i && A[k] != T(0)) iso = false;
     }
@@ -495,27 +496,38 @@ __global__ void k_check_diag(int n, const int* __restrict__ diag, int* status)
 }
 
 // ---------------- Chebyshev smoother ----------------
-// dinv = 1/a_ii and the Gershgorin bound max_i sum_j |a_ij| / a_ii of D^-1 A
+// dinv = 1/a_ii and the Gershgorin bound max_i sum_j |a_ij| / a_ii of D^-1 A.  The bound
+// is an estimate for the Chebyshev interval, so it is summed in FP32 (GB300's FP64 rate is a
+// small fraction of its FP32 rate) and reduced per block before one atomic per block.
 template <class T>
-__global__ void k_cheb_setup(int n, const int* __restrict__ sp, const int* __restrict__ rowlen,
-                             const int* __restrict__ diag, const T* __restrict__ A, T* __restrict__ dinv,
-                             unsigned long long* gmax, int* status)
+__global__ void __launch_bounds__(256) k_cheb_setup(int n, const int* __restrict__ sp, const int* __restrict__ rowlen,
+                                                    const int* __restrict__ diag, const T* __restrict__ A,
+                                                    T* __restrict__ dinv, unsigned long long* gmax, int* status)
 {
+    __shared__ float sg[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double g = 0.0;
+    float g = 0.0f;
     if (i < n) {
-        const double a = double(A[diag[i]]);
-        double s = 0.0;
-        for (int t = 0; t < rowlen[i]; ++t) s += fabs(double(A[slot_of(sp, i, t)]));
-        if (!(a > 0.0) || !isfinite(s)) {
+        const T a = A[diag[i]];
+        float s = 0.0f;
+        const int b = sp[i >> 5] + (i & 31);
+        const int len = rowlen[i];
+        for (int t = 0; t < len; ++t) s += fabsf(float(A[b + 32 * t]));
+        if (!(a > T(0)) || !isfinite(s)) {
             atomicOr(status, ST_NONFINITE);
         } else {
-            dinv[i] = T(1.0 / a);
-            g = s / a;
+            dinv[i] = T(1) / a;
+            g = s / float(a);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) g = fmax(g, __shfl_xor_sync(0xffffffffu, g, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(gmax, (unsigned long long)__double_as_longlong(g));
+    for (int o = 16; o > 0; o >>= 1) g = fmaxf(g, __shfl_xor_sync(0xffffffffu, g, o));
+    if ((threadIdx.x & 31) == 0) sg[threadIdx.x >> 5] = g;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = sg[0];
+        for (int w = 1; w < int(blockDim.x >> 5); ++w) m = fmaxf(m, sg[w]);
+        atomicMax(gmax, (unsigned long long)__double_as_longlong(double(m)));
+    }
 }
 
 // start from x = 0: r = D^-1 b, d = r / theta
@@ -804,11 +816,15 @@ void Amg<T>::members(cudaStream_t s, Aggregates& a)
 }
 
 template <class T>
-void Amg<T>::aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, Aggregates& out)
+void Amg<T>::aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg_first,
+                             Aggregates& out)
 {
-    pairwise(s, P, A, n, true, o_.strength, false, out);
-    const int first = out.nc;
-    if (out.nc > 0.8 * n) pairwise(s, P, A, n, false, 0.0, true, out);
+    int first = -1;
+    if (neg_first) {
+        pairwise(s, P, A, n, true, o_.strength, false, out);
+        first = out.nc;
+    }
+    if (!neg_first || out.nc > 0.8 * n) pairwise(s, P, A, n, false, 0.0, true, out);
     static const bool debug = std::getenv("PORSOL_DEBUG_AMG") != nullptr;
     if (debug) std::fprintf(stderr, "[amg] round n=%d strong-negative pairs -> %d, final -> %d\n", n, first, out.nc);
 }
@@ -950,13 +966,13 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         if (int(lv_.size()) <= nlev_) lv_.push_back(std::make_unique<Level>());
         Level& next = *lv_[nlev_];
         // round 1 on this level's matrix; L.agg maps rows to the intermediate level
-        aggregate_round(s, P, L.A, n, L.agg);
+        aggregate_round(s, P, L.A, n, o_.round1_negative, L.agg);
         members(s, L.agg);
         galerkin(s, P, L.A, L.agg, tmp_pat_, tmp_val_);
         const int nc1 = L.agg.nc;
         if (nc1 > o.coarse_target) {
             // round 2 on the intermediate matrix: aggregates of about four rows
-            aggregate_round(s, tmp_pat_, tmp_val_.p, nc1, agg2_);
+            aggregate_round(s, tmp_pat_, tmp_val_.p, nc1, o_.round2_negative, agg2_);
             members(s, agg2_);
             galerkin(s, tmp_pat_, tmp_val_.p, agg2_, next.own, next.own_val);
             PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, L.agg.agg.p, agg2_.agg.p));
