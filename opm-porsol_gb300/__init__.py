@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libporsol_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE, "-I", CSRC]
-SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_adjoint.cu", "capi.cu",
+SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_adjoint.cu", "k_batch.cu", "capi.cu",
            "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2

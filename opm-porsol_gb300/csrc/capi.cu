@@ -105,10 +105,52 @@ void porsol_solver::check_status(const char* where)
     }
 }
 
+// True when grid topology, initial FlowBC periodicity and partner ids equal those the current
+// structure was built from: the face numbering, sparsity and assembly recipe are then reused.
+bool porsol_solver::same_topology(const porsol_grid* grid, const int* flow_type, const int* partner_bid) const
+{
+    if (!structure_valid || !grid || grid->num_cells != S.g.nc || !grid->cell_facepos) return false;
+    const HostGrid& g = S.g;
+    if (!std::equal(g.facepos.begin(), g.facepos.end(), grid->cell_facepos)) return false;
+    const int nhf = g.nhf;
+    if (!grid->hf_neighbour || !grid->hf_bid) return false;
+    if (!std::equal(g.nb.begin(), g.nb.end(), grid->hf_neighbour)) return false;
+    if (!std::equal(g.bid.begin(), g.bid.end(), grid->hf_bid)) return false;
+    for (int hf = 0; hf < nhf; ++hf) {
+        const int per = (flow_type && g.nb[hf] < 0 && flow_type[hf] == PORSOL_BC_PERIODIC) ? 1 : 0;
+        if (per != S.init_periodic[hf]) return false;
+        if ((partner_bid ? partner_bid[hf] : 0) != S.hf_partner_bid[hf]) return false;
+    }
+    return true;
+}
+
 void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
 {
     amg64.set_profiler(&prof);
     amg32.set_profiler(&prof);
+    if (same_topology(grid, flow_type, partner_bid)) {
+        // geometry may differ: copy and upload it; everything derived from topology is kept
+        HostGrid& g = S.g;
+        const int nc = g.nc, nhf = g.nhf;
+        PORSOL_REQUIRE(grid->hf_area && grid->hf_centroid && grid->hf_normal && grid->cell_volume &&
+                           grid->cell_centroid,
+                       PORSOL_ERR_BAD_ARG, "grid: null array");
+        g.area.assign(grid->hf_area, grid->hf_area + nhf);
+        g.fcent.assign(grid->hf_centroid, grid->hf_centroid + 3 * size_t(nhf));
+        g.fnormal.assign(grid->hf_normal, grid->hf_normal + 3 * size_t(nhf));
+        g.cvol.assign(grid->cell_volume, grid->cell_volume + nc);
+        g.ccent.assign(grid->cell_centroid, grid->cell_centroid + 3 * size_t(nc));
+        cudaStream_t s = stream;
+        area.upload(g.area, s);
+        fcent.upload(g.fcent, s);
+        fnormal.upload(g.fnormal, s);
+        cvol.upload(g.cvol, s);
+        ccent.upload(g.ccent, s);
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        ip_valid = solved = false;
+        amg_ready = false;
+        return;
+    }
     structure_valid = ip_valid = solved = false;
     R.valid = false;
     amg_ready = false;
@@ -229,6 +271,10 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
            << "Residual reduction achieved is " << red << '\n';
         throw Error(PORSOL_ERR_NOT_CONVERGED, os.str());
     };
+    if (batch.nblk > 0) {
+        batched_solve(o, st, maxit);
+        return;
+    }
     if (o.linsolver_type == 0) {
         // solveLinearSystem (:1387-1420): ILU0(S, 1.0), CG, zero initial guess
         if (!ilu_levels) {
@@ -310,6 +356,120 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     st.iterations = total;
     st.outer_iterations = outer;
     st.reduction = r0 > 0 ? rn / r0 : 0.0;
+}
+
+// Block-diagonal systems (batched upscaling): one CG per block (BatchedPcg), each block with
+// the stopping test ||r_g|| < tol ||r_g^0|| that its own solve would use.  FP64: ILU0 or AMG
+// preconditioner; mixed: FP64 per-block residuals around FP32 batched CG + FP32 AMG.
+void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit)
+{
+    const double t_begin = now_ms();
+    const int n = S.N, nb = batch.nblk;
+    const SellPattern& P = S.pat;
+    st.amg_levels = 0;
+    st.outer_iterations = 1;
+    auto fail = [&](int iters, double red) {
+        std::ostringstream os;
+        os << "Linear solver failed to converge in " << iters << " iterations.\n"
+           << "Residual reduction achieved is " << red << '\n';
+        throw Error(PORSOL_ERR_NOT_CONVERGED, os.str());
+    };
+    std::vector<double> h(nb);
+    auto upload = [&](DBuf<double>& d, const std::vector<double>& v) { d.upload(v, stream); };
+    AmgOpts ao;
+    ao.smooth_steps = std::max(1, o.smooth_steps);
+    ao.prolong = o.prolongate_factor;
+    const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
+    if (!mixed) {
+        Precond<double>* M = nullptr;
+        if (o.linsolver_type == 0) {
+            if (!ilu_levels) {
+                ilu.build_levels(P, stream);
+                ilu_levels = true;
+            }
+            ilu.factor(stream, P, val.p);
+            x.zero(stream);
+            M = &ilu;
+        } else {
+            dirichlet_guess(stream, P, val.p, rhs.p, x.p);
+            if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64)) {
+                amg64.setup(stream, P, val.p, ao);
+                amg_ready = true;
+                amg_precision = PORSOL_FP64;
+            }
+            st.amg_levels = amg64.levels();
+            M = &amg64;
+        }
+        PORSOL_CUDA(cudaStreamSynchronize(stream));
+        st.ms_precond_setup = now_ms() - t_begin;
+        std::fill(h.begin(), h.end(), o.residual_tolerance);
+        upload(btol, h);
+        CgResult r = bcg64.solve(stream, P, val.p, *M, batch, rhs.p, x.p, btol.p, maxit);
+        st.iterations = r.iterations;
+        st.reduction = r.reduction;
+        if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+        if (!r.converged) fail(r.iterations, r.reduction);
+        return;
+    }
+    dirichlet_guess(stream, P, val.p, rhs.p, x.p);
+    if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED)) {
+        amg32.setup(stream, P, val32.p, ao);
+        amg_ready = true;
+        amg_precision = PORSOL_MIXED;
+    }
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    st.ms_precond_setup = now_ms() - t_begin;
+    st.amg_levels = amg32.levels();
+    ir_r.alloc(n);
+    ir_r32.alloc(n);
+    ir_d32.alloc(n);
+    bnorm.alloc(nb);
+    std::vector<double> r0(nb), rn(nb), sc(nb);
+    auto norms = [&](std::vector<double>& out) {
+        residual<double, double>(stream, P, val.p, x.p, rhs.p, ir_r.p);
+        batch_norms<double>(stream, batch, ir_r.p, bnorm.p);
+        bnorm.download(out.data(), nb, stream);
+        PORSOL_CUDA(cudaStreamSynchronize(stream));
+    };
+    norms(r0);
+    rn = r0;
+    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3;
+    const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
+    int total = 0, outer = 0;
+    auto worst = [&]() {
+        double w = 0.0;
+        for (int g = 0; g < nb; ++g)
+            if (r0[g] > 0) w = std::max(w, rn[g] / r0[g]);
+        return w;
+    };
+    for (;;) {
+        bool any = false;
+        for (int g = 0; g < nb; ++g) {
+            const bool act = rn[g] >= o.residual_tolerance * r0[g] && rn[g] >= 1e-30;
+            any = any || act;
+            sc[g] = act ? 1.0 / rn[g] : 0.0;
+            // the last refinement step of a block only needs its remaining reduction (x 0.3)
+            h[g] = act ? std::min(0.5, std::max(inner_tol, 0.3 * o.residual_tolerance * r0[g] / rn[g])) : 1.0;
+        }
+        if (!any) break;
+        if (outer >= max_outer || total >= maxit) fail(total, worst());
+        if (!std::isfinite(worst())) throw Error(PORSOL_ERR_NONFINITE, "iterative refinement diverged");
+        upload(bscale, sc);
+        upload(btol, h);
+        batch_to_f32_scaled(stream, batch, ir_r.p, ir_r32.p, bscale.p);
+        PORSOL_CUDA(cudaMemsetAsync(ir_d32.p, 0, n * sizeof(float), stream));
+        CgResult r = bcg32.solve(stream, P, val32.p, amg32, batch, ir_r32.p, ir_d32.p, btol.p, maxit - total);
+        total += r.iterations;
+        ++outer;
+        if (r.breakdown && r.iterations == 0) throw Error(PORSOL_ERR_NONFINITE, "inner CG breakdown");
+        for (int g = 0; g < nb; ++g) sc[g] = sc[g] > 0 ? rn[g] : 0.0;
+        upload(bscale, sc);
+        batch_add_f32_scaled(stream, batch, ir_d32.p, bscale.p, x.p);
+        norms(rn);
+    }
+    st.iterations = total;
+    st.outer_iterations = outer;
+    st.reduction = worst();
 }
 
 void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const double* mobd, const int* bct,
@@ -498,6 +658,31 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     }
     reg_rows = dof0;
     reg_rows_d.upload(reg_rows, stream);
+    // Unknowns of each sub-grid: its internal faces and its boundary faces are each numbered
+    // contiguously (faces are numbered in cell order, internal before boundary).
+    {
+        std::vector<int> rg(4 * size_t(ngrids));
+        for (int g = 0; g < ngrids; ++g) {
+            int lo[2] = {S.N, S.N}, hi[2] = {-1, -1};
+            long long cnt[2] = {0, 0};
+            for (int c = cellpos[g]; c < cellpos[g + 1]; ++c)
+                for (int hf = hg.facepos[c]; hf < hg.facepos[c + 1]; ++hf) {
+                    const int b = hg.boundary(hf) ? 1 : 0;
+                    lo[b] = std::min(lo[b], S.cf[hf]);
+                    hi[b] = std::max(hi[b], S.cf[hf]);
+                    cnt[b] += b ? 2 : 1;   // internal faces are seen from both cells
+                }
+            for (int b = 0; b < 2; ++b) {
+                if (hi[b] < 0) lo[b] = hi[b] = 0;
+                else
+                    PORSOL_REQUIRE(cnt[b] == 2LL * (hi[b] - lo[b] + 1), PORSOL_ERR_BAD_ARG,
+                                   "upscale: face unknowns of a sub-grid are not contiguous");
+                rg[4 * size_t(g) + 2 * b] = lo[b];
+                rg[4 * size_t(g) + 2 * b + 1] = hi[b] < 0 ? 0 : hi[b] + 1;
+            }
+        }
+        batch.build(rg, S.N, stream);
+    }
     DBuf<int> cellpos_d, side_d;
     cellpos_d.upload(cellpos, ngrids + 1, stream);
     side_d.upload(side, nhf, stream);
@@ -536,10 +721,12 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     } catch (...) {
         reuse_amg = false;
         reg_rows.clear();
+        batch.nblk = 0;
         throw;
     }
     reuse_amg = false;
     reg_rows.clear();
+    batch.nblk = 0;
     if (stats) *stats = acc;
 }
 

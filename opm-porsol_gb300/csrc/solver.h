@@ -4,6 +4,7 @@
 #include <memory>
 
 #include "amg.h"
+#include "batch.h"
 #include "kernels.h"
 #include "krylov.h"
 #include "structure.h"
@@ -63,12 +64,19 @@ struct porsol_solver {
     std::vector<int> reg_rows;
     porsol::DBuf<int> reg_rows_d;
     bool reuse_amg = false;
+    // ... and solved with one CG per sub-grid (empty: one CG over the whole system)
+    porsol::BatchRanges batch;
+    porsol::BatchedPcg<double, double> bcg64;
+    porsol::BatchedPcg<float, float> bcg32;
+    porsol::DBuf<double> btol, bscale, bnorm;
+    void batched_solve(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit);
 
     // adjoint (permeability sensitivity) of the last solve
     porsol_solve_opts last_opts{};
     porsol::DBuf<double> adj_wp, adj_pstar, adj_wv, adj_y, adj_jc, adj_rhs, adj_x, adj_grad, adj_sum;
 
     void require_structure() const;
+    bool same_topology(const porsol_grid* grid, const int* flow_type, const int* partner_bid) const;
     void init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
     void compute_inner_products(const double* perm_h, const double* grav);
     void solve(const porsol_fluid* fluid, const double* sat, const double* mobdens, const int* bct,
