@@ -549,8 +549,10 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     // (:1398-1400); the AMG paths only when the hierarchy is rebuilt (:1491-1495).
     reg_applied = false;
     if (!reg_rows.empty()) {
-        // batched sub-grids: each sub-grid's first DOF, as its own pure-periodic solve would
-        launch_scale_rows(s, int(reg_rows.size()), reg_rows_d.p, val.p, S.pat.diag.p, 2.0, mixed ? val32.p : nullptr);
+        // batched sub-grids: each sub-grid's first DOF is pinned to 0, the face pressures its
+        // own pure-periodic solve with S[0][0] *= 2 would give, without the tiny eigenvalue
+        launch_pin_rows(s, int(reg_rows.size()), reg_rows_d.p, S.pat.slice_ptr.p, S.pat.col.p, S.pat.rowlen.p, val.p,
+                        mixed ? val32.p : nullptr, rhs.p);
     } else if (R.do_reg && (o.linsolver_type == 0 || !o.same_matrix)) {
         launch_scale_entry(s, val.p, S.pat.diag.p, 0, 2.0, mixed ? val32.p : nullptr);
         reg_applied = true;

@@ -297,14 +297,35 @@ __global__ void k_mass_balance(int nc, const int* __restrict__ facepos, const do
     }
 }
 
-__global__ void k_scale_rows(int nrows, const int* __restrict__ rows, double* val, const int* __restrict__ diag,
-                             double factor, float* val32)
+// Pin unknown r of a consistent singular block: zero row r and column r except the diagonal
+// and set rhs_r = 0, so the block solves with pi_r = 0.  For a consistent system this is the
+// solution the reference's regularisation S[0][0] *= 2 selects (the doubled row is satisfied
+// only with pi_r = 0); pinning keeps the block well conditioned instead of leaving one tiny
+// eigenvalue.  Rows of different blocks never couple, so the threads do not interfere.
+__global__ void k_pin_rows(int nrows, const int* __restrict__ rows, const int* __restrict__ sp,
+                           const int* __restrict__ col, const int* __restrict__ rowlen, double* val, float* val32,
+                           double* rhs)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nrows) return;
-    const int k = diag[rows[q]];
-    val[k] *= factor;
-    if (val32) val32[k] = float(val[k]);
+    const int r = rows[q];
+    const int br = sp[r >> 5] + (r & 31);
+    for (int t = 0; t < rowlen[r]; ++t) {
+        const int k = br + 32 * t;
+        const int j = col[k];
+        if (j == r) continue;
+        val[k] = 0.0;
+        if (val32) val32[k] = 0.0f;
+        const int bj = sp[j >> 5] + (j & 31);
+        for (int u = 0; u < rowlen[j]; ++u) {
+            const int kj = bj + 32 * u;
+            if (col[kj] == r) {
+                val[kj] = 0.0;
+                if (val32) val32[kj] = 0.0f;
+            }
+        }
+    }
+    rhs[r] = 0.0;
 }
 
 // one block per sub-grid: fixed-order sums (deterministic)
@@ -418,11 +439,11 @@ void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const doubl
     PORSOL_CUDA(cudaGetLastError());
 }
 
-void launch_scale_rows(cudaStream_t s, int nrows, const int* rows, double* val, const int* diag, double factor,
-                       float* val32)
+void launch_pin_rows(cudaStream_t s, int nrows, const int* rows, const int* sp, const int* col, const int* rowlen,
+                     double* val, float* val32, double* rhs)
 {
     if (nrows == 0) return;
-    PORSOL_LAUNCH(k_scale_rows<<<div_up(nrows, 256), 256, 0, s>>>(nrows, rows, val, diag, factor, val32));
+    PORSOL_LAUNCH(k_pin_rows<<<div_up(nrows, 256), 256, 0, s>>>(nrows, rows, sp, col, rowlen, val, val32, rhs));
     PORSOL_CUDA(cudaGetLastError());
 }
 

@@ -73,9 +73,9 @@ void launch_post_process(cudaStream_t s, int npairs, const int* pairs, double* o
 void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const double* outflux, const double* src,
                          unsigned long long* out3);
 void launch_check_finite(cudaStream_t s, long long n, const double* v, int* status);
-// val[diag[rows[q]]] *= factor for q < nrows (and the FP32 copy)
-void launch_scale_rows(cudaStream_t s, int nrows, const int* rows, double* val, const int* diag, double factor,
-                       float* val32);
+// zero row and column rows[q] (diagonal kept), rhs[rows[q]] = 0, for q < nrows (and the FP32 copy)
+void launch_pin_rows(cudaStream_t s, int nrows, const int* rows, const int* sp, const int* col, const int* rowlen,
+                     double* val, float* val32, double* rhs);
 // per sub-grid g: q[3 g + i] = sum of outflux over half-faces of side 2 i + 2 (1-based sides)
 void launch_side_fluxes(cudaStream_t s, int ngrids, const int* cellpos, const int* facepos, const int* side,
                         const double* outflux, double* q);

@@ -59,8 +59,9 @@ struct porsol_solver {
 
     porsol::Profiler prof;
 
-    // batched periodic upscaling: rows regularised in place of row 0 (first DOF of each
-    // sub-grid), and whether the AMG hierarchy of the previous solve is reused
+    // batched periodic upscaling: the pinned row of each sub-grid (its first DOF, the row the
+    // single-grid regularisation acts on), and whether the AMG hierarchy of the previous solve
+    // is reused
     std::vector<int> reg_rows;
     porsol::DBuf<int> reg_rows_d;
     bool reuse_amg = false;
