@@ -64,8 +64,14 @@ typedef struct porsol_grid {
  * PORSOL_FLUID_CELLWISE: the caller passes total mobility and sum(rho_i * mob_i) per cell.
  * PORSOL_FLUID_COREY2: two phases, kr1 = s^2, kr2 = (1-s)^2 (ReservoirPropertyCapillary
  *   without rock tables, ReservoirPropertyCapillary_impl.hpp:118-170), mob_i = kr_i/visc_i,
- *   evaluated on the GPU from the saturation. */
-enum { PORSOL_FLUID_CELLWISE = 0, PORSOL_FLUID_COREY2 = 1 };
+ *   evaluated on the GPU from the saturation.
+ * PORSOL_FLUID_TENSOR: the inner product of MimeticIPAnisoRelpermEvaluator
+ *   (mimetic/MimeticIPAnisoRelpermEvaluator.hpp:207-400): the caller passes per cell the total
+ *   mobility tensor lambda_t = sum_i lambda_i (9 doubles, row-major) as `sat` and
+ *   sum_i rho_i lambda_i (9 doubles, may be NULL) as `mobdens`; every solve rebuilds
+ *   W = (N (lambda_t K) N^T + 2 tr(lambda_t K) A (I - Q Q^T) A) / |c| and the gravity flux
+ *   N (sum_i rho_i lambda_i) K g per cell on the GPU. */
+enum { PORSOL_FLUID_CELLWISE = 0, PORSOL_FLUID_COREY2 = 1, PORSOL_FLUID_TENSOR = 2 };
 typedef struct porsol_fluid {
     int model;
     double viscosity1, viscosity2;
@@ -137,8 +143,8 @@ int porsol_init(porsol_solver* h, const porsol_grid* grid, const double* perm, c
 
 /* IncompFlowSolverHybrid::solve (IncompFlowSolverHybrid.hpp:658-703): assembleDynamic,
  * linear solve of the face-pressure system, computePressureAndFluxes.
- *   sat        [nc]  saturation (COREY2) or total mobility (CELLWISE)
- *   mobdens    [nc]  CELLWISE only: sum_i rho_i mob_i (may be NULL: zero)
+ *   sat        [nc]  saturation (COREY2) or total mobility (CELLWISE); [9 nc] TENSOR: lambda_t
+ *   mobdens    [nc]  CELLWISE: sum_i rho_i mob_i; [9 nc] TENSOR: sum_i rho_i lambda_i (may be NULL: zero)
  *   hf_flow_type/hf_flow_value [nhf]  FlowBC of each boundary half-face
  *   src        [nc]  source rates
  * opts may be NULL (defaults); stats may be NULL. */

@@ -29,7 +29,7 @@ SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transp
            "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
-FLUID_CELLWISE, FLUID_COREY2 = 0, 1
+FLUID_CELLWISE, FLUID_COREY2, FLUID_TENSOR = 0, 1, 2
 FP64, MIXED = 0, 1
 GRAD_LOGK, GRAD_LOGK_AXES = 0, 1
 ERR = {0: "OK", 1: "NOT_CONVERGED", 2: "BAD_ARG", 3: "NONFINITE", 4: "SAT_RANGE", 5: "CUDA", 6: "TIMEOUT",

@@ -204,6 +204,7 @@ void porsol_solver::compute_inner_products(const double* perm_h, const double* g
     PORSOL_REQUIRE(perm_h, PORSOL_ERR_BAD_ARG, "permeability array is null");
     const double g0[3] = {grav ? grav[0] : 0.0, grav ? grav[1] : 0.0, grav ? grav[2] : 0.0};
     gravity_zero = (g0[0] == 0.0 && g0[1] == 0.0 && g0[2] == 0.0);
+    for (int d = 0; d < 3; ++d) grav_[d] = g0[d];
     perm.upload(perm_h, 9 * size_t(S.g.nc), stream);
     launch_static_ip(maxnf, stream, S.g.nc, facepos.p, area.p, fcent.p, fnormal.p, cvol.p, ccent.p, perm.p, g0, W.p,
                      gflux.p, status.p);
@@ -487,8 +488,10 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     }
     PORSOL_REQUIRE(o.precision == PORSOL_FP64 || o.precision == PORSOL_MIXED, PORSOL_ERR_BAD_ARG,
                    "unknown precision mode");
-    PORSOL_REQUIRE(fluid->model == PORSOL_FLUID_CELLWISE || fluid->model == PORSOL_FLUID_COREY2, PORSOL_ERR_BAD_ARG,
-                   "unknown fluid model");
+    PORSOL_REQUIRE(fluid->model == PORSOL_FLUID_CELLWISE || fluid->model == PORSOL_FLUID_COREY2 ||
+                       fluid->model == PORSOL_FLUID_TENSOR,
+                   PORSOL_ERR_BAD_ARG, "unknown fluid model");
+    const bool tensor = fluid->model == PORSOL_FLUID_TENSOR;
     if (o.precision == PORSOL_MIXED && o.linsolver_type == 0)
         o.precision = PORSOL_FP64;   // ILU0 path is FP64 only
     last_opts = o;
@@ -502,10 +505,11 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
         d_bcv = bcv;
         d_src = src;
     } else {
-        in_sat.upload(sat, nc, s);
+        const size_t per = tensor ? 9 : 1;
+        in_sat.upload(sat, per * nc, s);
         d_sat = in_sat.p;
         if (mobd) {
-            in_mobdens.upload(mobd, nc, s);
+            in_mobdens.upload(mobd, per * nc, s);
             d_md = in_mobdens.p;
         }
         in_bcval.upload(bcv, nhf, s);
@@ -517,15 +521,64 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
     if (mixed) val32.alloc(S.pat.nent);
     const double t_asm = now_ms();
+    // Tensor mobilities: this solve's inner products (and gravity fluxes) are rebuilt into Wdyn
+    // (gflux_dyn); the assembly then runs with unit scalar mobility on them.
+    const double* W_use = W.p;
+    const double* gflux_use = gflux.p;
+    bool gzero = gravity_zero;
+    if (tensor) {
+        Wdyn.alloc(size_t(npk) * nc);
+        gflux_dyn.alloc(nhf);
+        if (ones.n != size_t(nc)) {
+            std::vector<double> h1(nc, 1.0);
+            ones.upload(h1, s);
+        }
+        gzero = gravity_zero || d_md == nullptr;
+        TensorIpArgs ta;
+        ta.nc = nc;
+        ta.facepos = facepos.p;
+        ta.area = area.p;
+        ta.fcent = fcent.p;
+        ta.fnormal = fnormal.p;
+        ta.cvol = cvol.p;
+        ta.ccent = ccent.p;
+        ta.perm = perm.p;
+        ta.lam = d_sat;
+        ta.rlam = d_md;
+        ta.gravity = gzero ? 0 : 1;
+        ta.g0 = grav_[0];
+        ta.g1 = grav_[1];
+        ta.g2 = grav_[2];
+        ta.W = Wdyn.p;
+        ta.gflux = gflux_dyn.p;
+        ta.status = status.p;
+        launch_dynamic_ip_tensor(maxnf, s, ta);
+        int st_dev = 0;
+        PORSOL_CUDA(cudaMemcpyAsync(&st_dev, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        if (st_dev & ST_BAD_INDEX) {
+            PORSOL_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+            throw Error(PORSOL_ERR_BAD_ARG, "tensor mobility: lambda_t K must be symmetric (at most 12 faces per cell)");
+        }
+        check_status("tensor inner products");
+        W_use = Wdyn.p;
+        gflux_use = gflux_dyn.p;
+        d_sat = ones.p;
+        d_md = gzero ? nullptr : ones.p;
+    }
+    W_last = W_use;
+    tensor_last = tensor;
     {
         ProfScope ps(prof, s, PK_ASSEMBLE, double(nc) * (npk * 16.0 + 64) + double(S.pat.nent) * 16.0);
         AssembleArgs a;
         a.nc = nc;
         a.facepos = facepos.p;
-        a.W = W.p;
-        a.gflux = gflux.p;
-        a.gravity_zero = gravity_zero;
-        a.fluid = FluidParams{fluid->model, fluid->viscosity1, fluid->viscosity2, fluid->density1, fluid->density2};
+        a.W = W_use;
+        a.gflux = gflux_use;
+        a.gravity_zero = gzero;
+        a.fluid = tensor ? FluidParams{PORSOL_FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0}
+                         : FluidParams{fluid->model, fluid->viscosity1, fluid->viscosity2, fluid->density1,
+                                       fluid->density2};
         a.sat = d_sat;
         a.mobdens = d_md;
         a.kind = R.kind_d.p;
@@ -570,9 +623,9 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
         ra.facepos = facepos.p;
         ra.cf = cf.p;
         ra.x = x.p;
-        ra.W = W.p;
-        ra.gflux = gflux.p;
-        ra.gravity_zero = gravity_zero;
+        ra.W = W_use;
+        ra.gflux = gflux_use;
+        ra.gravity_zero = gzero;
         ra.F = F.p;
         ra.L = L.p;
         ra.g = this->g.p;
@@ -760,7 +813,7 @@ double porsol_solver::objective(const porsol_objective* obj)
     a.cf = cf.p;
     a.kind = R.kind_d.p;
     a.sloc = sloc.p;
-    a.W = W.p;
+    a.W = W_last;
     a.F = F.p;
     a.L = L.p;
     a.g = this->g.p;
@@ -790,6 +843,8 @@ void porsol_solver::adjoint_gradient(const porsol_objective* obj, int mode, cons
     PORSOL_REQUIRE(mode == PORSOL_GRAD_LOGK || mode == PORSOL_GRAD_LOGK_AXES, PORSOL_ERR_BAD_ARG,
                    "adjoint: unknown gradient mode");
     PORSOL_REQUIRE(grad, PORSOL_ERR_BAD_ARG, "adjoint: null gradient array");
+    PORSOL_REQUIRE(!(tensor_last && mode == PORSOL_GRAD_LOGK_AXES), PORSOL_ERR_BAD_ARG,
+                   "adjoint: axis gradients are not available with tensor mobilities");
     const double J = objective(obj);   // also leaves dJ/dpi in adj_y
     const int nc = S.g.nc, N = S.N;
     cudaStream_t s = stream;
@@ -822,7 +877,7 @@ void porsol_solver::adjoint_gradient(const porsol_objective* obj, int mode, cons
     a.facepos = facepos.p;
     a.cf = cf.p;
     a.kind = R.kind_d.p;
-    a.W = W.p;
+    a.W = W_last;
     a.F = F.p;
     a.L = L.p;
     a.g = this->g.p;

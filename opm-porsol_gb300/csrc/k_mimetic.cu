@@ -85,6 +85,73 @@ __global__ void __launch_bounds__(128) k_static_ip(int nc, const int* __restrict
     if (!finite) atomicOr(status, ST_NONFINITE);
 }
 
+// MimeticIPAnisoRelpermEvaluator (MimeticIPAnisoRelpermEvaluator.hpp:207-400), evaluated per
+// solve: W = (N (lambda_t K) N^T + 2 tr(lambda_t K) A (I - Q Q^T) A) / |c| with the cell's total
+// mobility tensor lambda_t, and the gravity flux N (sum_i rho_i lambda_i) K g.  W is stored
+// packed (upper triangle), so lambda_t K must be symmetric (lambda_t commuting with K); a
+// non-symmetric product raises ST_BAD_INDEX.
+template <int MAXNF>
+__global__ void __launch_bounds__(128) k_dynamic_ip_tensor(TensorIpArgs A)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.nc) return;
+    const int nc = A.nc;
+    const int f0 = A.facepos[c];
+    const int nf = A.facepos[c + 1] - f0;
+    if (nf > MAXNF) {
+        atomicOr(A.status, ST_BAD_INDEX);
+        return;
+    }
+    double K[9], Lm[9], LK[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        K[k] = A.perm[9 * (size_t)c + k];
+        Lm[k] = A.lam[9 * (size_t)c + k];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) LK[3 * i + j] = Lm[3 * i] * K[j] + Lm[3 * i + 1] * K[3 + j] + Lm[3 * i + 2] * K[6 + j];
+    const double scale = fabs(LK[0]) + fabs(LK[4]) + fabs(LK[8]);
+    if (fabs(LK[1] - LK[3]) > 1e-12 * scale || fabs(LK[2] - LK[6]) > 1e-12 * scale ||
+        fabs(LK[5] - LK[7]) > 1e-12 * scale)
+        atomicOr(A.status, ST_BAD_INDEX);
+    double N[MAXNF][3], Q[MAXNF][3], a[MAXNF];
+    if (!cell_frame<MAXNF>(c, f0, nf, A.area, A.fcent, A.fnormal, A.ccent, a, N, Q)) atomicOr(A.status, ST_NONFINITE);
+    if (A.gravity) {
+        const double Kg0 = K[0] * A.g0 + K[1] * A.g1 + K[2] * A.g2;
+        const double Kg1 = K[3] * A.g0 + K[4] * A.g1 + K[5] * A.g2;
+        const double Kg2 = K[6] * A.g0 + K[7] * A.g1 + K[8] * A.g2;
+        const double* R = A.rlam + 9 * (size_t)c;
+        const double d0 = R[0] * Kg0 + R[1] * Kg1 + R[2] * Kg2;
+        const double d1 = R[3] * Kg0 + R[4] * Kg1 + R[5] * Kg2;
+        const double d2 = R[6] * Kg0 + R[7] * Kg1 + R[8] * Kg2;
+#pragma unroll
+        for (int i = 0; i < MAXNF; ++i)
+            if (i < nf) A.gflux[f0 + i] = N[i][0] * d0 + N[i][1] * d1 + N[i][2] * d2;
+    }
+    double NK[MAXNF][3];
+#pragma unroll
+    for (int i = 0; i < MAXNF; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) NK[i][j] = N[i][0] * LK[j] + N[i][1] * LK[3 + j] + N[i][2] * LK[6 + j];
+    const double t = 6.0 * (LK[0] + LK[4] + LK[8]) / 3.0;
+    const double vol = A.cvol[c];
+    const double a1 = 1.0 / vol, a2 = t / vol;
+    bool finite = true;
+#pragma unroll
+    for (int j = 0; j < MAXNF; ++j)
+#pragma unroll
+        for (int i = 0; i <= j; ++i)
+            if (j < nf) {
+                const double w = a2 * projected<MAXNF>(i, j, a, Q) +
+                                 a1 * (NK[i][0] * N[j][0] + NK[i][1] * N[j][1] + NK[i][2] * N[j][2]);
+                finite = finite && isfinite(w);
+                A.W[(size_t)pk(i, j) * nc + c] = w;
+            }
+    if (!finite) atomicOr(A.status, ST_NONFINITE);
+}
+
 // assembleDynamic for one cell (IncompFlowSolverHybrid.hpp:1325-1382): dynamic scaling
 // (computeDynamicParams/getInverseMatrix/gravityFlux, MimeticIPEvaluator.hpp:297-350,
 // 540-546), external contributions (setExternalContrib :1736-1779), local Schur
@@ -380,6 +447,15 @@ void launch_static_ip(int maxnf, cudaStream_t s, int nc, const int* facepos, con
     else
         PORSOL_LAUNCH(k_static_ip<12><<<div_up(nc, bs), bs, 0, s>>>(nc, facepos, area, fcent, fnormal, cvol, ccent, perm, grav[0],
                                                       grav[1], grav[2], W, gflux, status));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_dynamic_ip_tensor(int maxnf, cudaStream_t s, const TensorIpArgs& a)
+{
+    if (a.nc == 0) return;
+    const int bs = 128;
+    if (maxnf <= 6) PORSOL_LAUNCH(k_dynamic_ip_tensor<6><<<div_up(a.nc, bs), bs, 0, s>>>(a));
+    else PORSOL_LAUNCH(k_dynamic_ip_tensor<12><<<div_up(a.nc, bs), bs, 0, s>>>(a));
     PORSOL_CUDA(cudaGetLastError());
 }
 

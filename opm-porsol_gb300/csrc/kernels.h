@@ -16,6 +16,21 @@ void launch_static_ip(int maxnf, cudaStream_t s, int nc, const int* facepos, con
                       const double* fcent, const double* fnormal, const double* cvol, const double* ccent,
                       const double* perm, const double grav[3], double* W, double* gflux, int* status);
 
+// Per-solve inner products of the tensor-mobility evaluator (PORSOL_FLUID_TENSOR).
+struct TensorIpArgs {
+    int nc;
+    const int* facepos;
+    const double *area, *fcent, *fnormal, *cvol, *ccent, *perm;
+    const double* lam;     // total mobility tensor per cell (9, row-major)
+    const double* rlam;    // sum_i rho_i lambda_i per cell (9), used when gravity != 0
+    int gravity;
+    double g0, g1, g2;
+    double* W;             // packed [npk][nc] out
+    double* gflux;         // per half-face out (gravity only)
+    int* status;
+};
+void launch_dynamic_ip_tensor(int maxnf, cudaStream_t s, const TensorIpArgs& a);
+
 struct AssembleArgs {
     int nc;
     const int* facepos;

@@ -24,6 +24,11 @@ struct porsol_solver {
     // static inner products
     porsol::DBuf<double> perm, W, gflux;
     bool gravity_zero = true;
+    double grav_[3] = {0.0, 0.0, 0.0};
+    // tensor mobilities (PORSOL_FLUID_TENSOR): per-solve inner products and gravity fluxes
+    porsol::DBuf<double> Wdyn, gflux_dyn, ones;
+    const double* W_last = nullptr;   // inner products of the last assembly
+    bool tensor_last = false;
     porsol::DBuf<int> status;
     porsol::DBuf<unsigned long long> redbits;
 

@@ -98,6 +98,8 @@ def lib():
         L.orc_get_solution.argtypes = [vp, dp, dp, dp]
         L.orc_post_process_fluxes.restype = d
         L.orc_post_process_fluxes.argtypes = [vp]
+        L.orc_solve_tensor.restype = i
+        L.orc_solve_tensor.argtypes = [vp, dp, dp, ip, dp, dp, d, i, ip, dp]
         L.orc_adjoint_gradient.restype = i
         L.orc_adjoint_gradient.argtypes = [vp, dp, dp, dp, i, d, dp, dp, ip]
         L.orc_ilu0_cg.restype = i
@@ -199,6 +201,16 @@ class OraclePressure:
         red = np.zeros(1)
         rc = lib().orc_solve(self.h, *[_p(a) for a in args], float(tol), int(maxit), int(dirichlet_guess),
                              _p(it), _p(red))
+        self.iterations = int(it[0])
+        self.reduction = float(red[0])
+        return rc
+
+    def solve_tensor(self, lam9, rlam9, bc_type, bc_value, src, tol=1e-8, maxit=0):
+        """Solve with per-cell total mobility tensors (MimeticIPAnisoRelpermEvaluator)."""
+        keep = [_f64(lam9), None if rlam9 is None else _f64(rlam9), _i32(bc_type), _f64(bc_value), _f64(src)]
+        it = np.zeros(1, np.int32)
+        red = np.zeros(1)
+        rc = lib().orc_solve_tensor(self.h, *[_p(a) for a in keep], float(tol), int(maxit), _p(it), _p(red))
         self.iterations = int(it[0])
         self.reduction = float(red[0])
         return rc

@@ -387,11 +387,57 @@ struct Pressure {
     // MimeticIPEvaluator::buildStaticContrib, MimeticIPEvaluator.hpp:201-270
     std::vector<double> perm;
 
+    std::vector<double> Binv_static, gflux_static;
+    double grav_[3] = {0.0, 0.0, 0.0};
+    bool tensor_active = false;
+
     void computeInnerProducts(const double* K9, const double* grav)
     {
         perm.assign(K9, K9 + 9 * size_t(g.nc));
+        for (int d = 0; d < 3; ++d) grav_[d] = grav[d];
         for (int c = 0; c < g.nc; ++c)
             cellInnerProduct(c, K9 + 9 * c, grav, &Binv[binvpos[c]], &gflux[g.facepos[c]]);
+        Binv_static = Binv;
+        gflux_static = gflux;
+        tensor_active = false;
+    }
+
+    // Back to the static inner products after a tensor-mobility solve.
+    void useStatic()
+    {
+        if (!tensor_active) return;
+        Binv = Binv_static;
+        gflux = gflux_static;
+        tensor_active = false;
+    }
+
+    // MimeticIPAnisoRelpermEvaluator (MimeticIPAnisoRelpermEvaluator.hpp:207-400): per cell
+    // Binv = W(lambda_t K) and gravity flux N (sum_i rho_i lambda_i) K g; lam, rlam are 9 per
+    // cell row-major (rlam may be null: no gravity flux).  The assembly then uses unit mobility.
+    void tensorInnerProducts(const double* lam, const double* rlam)
+    {
+        std::vector<double> gtmp, wtmp;
+        for (int c = 0; c < g.nc; ++c) {
+            const double* K = &perm[9 * size_t(c)];
+            const double* L = lam + 9 * size_t(c);
+            double LK[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) LK[3 * i + j] = L[3 * i] * K[j] + L[3 * i + 1] * K[3 + j] + L[3 * i + 2] * K[6 + j];
+            const int nf = g.nf(c), f0 = g.facepos[c];
+            gtmp.assign(nf, 0.0);
+            cellInnerProduct(c, LK, grav_, &Binv[binvpos[c]], gtmp.data());
+            if (rlam) {
+                const double* R = rlam + 9 * size_t(c);
+                double RK[9];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) RK[3 * i + j] = R[3 * i] * K[j] + R[3 * i + 1] * K[3 + j] + R[3 * i + 2] * K[6 + j];
+                wtmp.assign(size_t(nf) * nf, 0.0);
+                cellInnerProduct(c, RK, grav_, wtmp.data(), &gflux[f0]);
+            } else {
+                for (int i = 0; i < nf; ++i) gflux[f0 + i] = 0.0;
+            }
+        }
+        tensor_active = true;
     }
 
     // W (column-major nf x nf) and gravity flux of cell c for the row-major tensor K
@@ -594,7 +640,7 @@ struct Pressure {
     int adjoint(const double* wp, const double* pstar, const double* wv, int mode, double tol, double* grad,
                 double* Jout, int* iters)
     {
-        if (do_reg) return 2;
+        if (do_reg || (tensor_active && mode != 0)) return 2;
         for (int t : hf_type)
             if (t == Periodic) return 2;
         const int n = S.n;
@@ -1072,7 +1118,25 @@ void orc_get_inner_products(void* h, double* Binv, double* gflux)
 void orc_assemble(void* h, const double* totmob, const double* mobdens, const int* bct, const double* bcv,
                   const double* src)
 {
+    static_cast<Pressure*>(h)->useStatic();
     static_cast<Pressure*>(h)->assemble(totmob, mobdens, bct, bcv, src);
+}
+
+int orc_solve_tensor(void* h, const double* lam, const double* rlam, const int* bct, const double* bcv,
+                     const double* src, double tol, int maxit, int* iterations, double* reduction)
+{
+    Pressure* P = static_cast<Pressure*>(h);
+    P->tensorInnerProducts(lam, rlam);
+    const int nc = P->g.nc;
+    std::vector<double> one(nc, 1.0), md(nc, rlam ? 1.0 : 0.0);
+    P->assemble(one.data(), md.data(), bct, bcv, src);
+    int it = 0;
+    double red = 0.0;
+    const int rc = P->solve(tol, maxit, 0, &it, &red);
+    if (iterations) *iterations = it;
+    if (reduction) *reduction = red;
+    P->recover();
+    return rc;
 }
 
 void orc_get_system(void* h, double* Svals, double* rhs, double* F, double* L, double* g, int* do_reg)
@@ -1100,6 +1164,7 @@ int orc_solve_timed(void* h, const double* totmob, const double* mobdens, const 
     using clk = std::chrono::steady_clock;
     Pressure* P = static_cast<Pressure*>(h);
     const auto t0 = clk::now();
+    P->useStatic();
     P->assemble(totmob, mobdens, bct, bcv, src);
     const auto t1 = clk::now();
     int it = 0;

@@ -70,6 +70,11 @@ int   orc_solve_timed(void* h, const double* totmob, const double* mobdens,
                       double* seconds3);
 void  orc_get_solution(void* h, double* pressure, double* outflux, double* facepressure);
 double orc_post_process_fluxes(void* h);
+/* Solve with the tensor-mobility inner product of MimeticIPAnisoRelpermEvaluator: lam = total
+ * mobility tensor, rlam = sum_i rho_i lambda_i (may be NULL), 9 doubles per cell row-major.
+ * Later orc_assemble/orc_solve calls return to the static inner products. */
+int orc_solve_tensor(void* h, const double* lam, const double* rlam, const int* bct, const double* bcv,
+                     const double* src, double tol, int maxit, int* iterations, double* reduction);
 /* Adjoint gradient of J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf of the last solve with
  * respect to ln k (mode 0: per cell; mode 1: per cell and axis, diagonal tensors).  0 = ok,
  * 1 = adjoint CG did not converge, 2 = unsupported problem (periodic, pure Neumann). */

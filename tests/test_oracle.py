@@ -4,6 +4,7 @@ import os
 
 import numpy as np
 import pytest
+from tensor_mobility import tensor_problem
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -116,3 +117,19 @@ def test_transport_conserves_mass(orc, cart):
     dv = ((s1 - s0) * poro * g.volume).sum()
     assert s1[g.ccentroid[:, 0] > 0.9].max() == 0.0
     assert abs(dv - inflow * 0.005) < 1e-12
+
+
+def test_oracle_tensor_mobility_scalar_case(orc, workloads, cart):
+    """lambda_t = m I in the tensor evaluator gives the scalar model's solution."""
+    g, K, lam, rlam, bct, bcv, src = tensor_problem(workloads, cart)
+    m = np.random.default_rng(2).uniform(0.5, 2.0, g.num_cells)
+    grav = (0.0, 0.0, -9.81)
+    o = orc.OraclePressure(g, bct)
+    o.compute_inner_products(K.ravel(), grav)
+    eye = np.eye(3).ravel()[None]
+    assert o.solve_tensor(m[:, None] * eye, 900.0 * m[:, None] * eye, bct, bcv, src, tol=1e-14) == 0
+    p1, v1, _ = o.solution()
+    assert o.solve(m, 900.0 * m, bct, bcv, src, tol=1e-14) == 0
+    p2, v2, _ = o.solution()
+    assert np.abs(p1 - p2).max() < 1e-11 * np.abs(p2).max()
+    assert np.abs(v1 - v2).max() < 1e-11 * np.abs(v2).max()
