@@ -20,6 +20,7 @@
 #include <iterator>
 #include <ostream>
 #include <stdexcept>
+#include <type_traits>
 #include <vector>
 
 #include "GridFlattener.hpp"
@@ -27,6 +28,24 @@
 
 namespace Opm {
 namespace gpu {
+
+// InnerProduct tag for the tensor-mobility evaluator (MimeticIPAnisoRelpermEvaluator,
+// mimetic/MimeticIPAnisoRelpermEvaluator.hpp): with it, solve() asks the fluid for phase
+// mobility tensors, fl.phaseMobility(phase, cell, s, m) with m a Mat3, and the GPU rebuilds the
+// inner products from lambda_t K on every solve (PORSOL_FLUID_TENSOR).
+template <class GridIF, class RockIF>
+class MimeticIPAnisoRelpermEvaluator {};
+
+// 3x3 matrix handed to FluidInterface::phaseMobility: m(i, j), column-major storage like the
+// reference's SharedFortranMatrix.
+struct Mat3 {
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double& operator()(int i, int j) { return a[i + 3 * j]; }
+    double operator()(int i, int j) const { return a[i + 3 * j]; }
+    int numRows() const { return 3; }
+    int numCols() const { return 3; }
+    double* data() { return a; }
+};
 
 template <class GridInterface, class RockInterface, class BCInterface,
           template <class GridIF, class RockIF> class InnerProduct>
@@ -128,6 +147,23 @@ public:
                int linsolver_type = 1, bool same_matrix = false, int linsolver_maxit = 0,
                double prolongate_factor = 1.6, int smooth_steps = 1)
     {
+        if constexpr (std::is_same<InnerProduct<GridInterface, RockInterface>,
+                                   MimeticIPAnisoRelpermEvaluator<GridInterface, RockInterface>>::value) {
+            solveTensor(fl, sat, bc, src, residual_tolerance, linsolver_verbosity, linsolver_type, same_matrix,
+                        linsolver_maxit, prolongate_factor, smooth_steps);
+        } else {
+            solveScalar(fl, sat, bc, src, residual_tolerance, linsolver_verbosity, linsolver_type, same_matrix,
+                        linsolver_maxit, prolongate_factor, smooth_steps);
+        }
+    }
+
+private:
+    template <class FluidInterface>
+    void solveScalar(const FluidInterface& fl, const std::vector<double>& sat, const BCInterface& bc,
+                     const std::vector<double>& src, double residual_tolerance, int linsolver_verbosity,
+                     int linsolver_type, bool same_matrix, int linsolver_maxit, double prolongate_factor,
+                     int smooth_steps)
+    {
         const int nc = grid_.numCells();
         // FluidInterface::phaseMobilities / phaseDensities per cell
         // (MimeticIPEvaluator::computeDynamicParams, MimeticIPEvaluator.hpp:297-311)
@@ -161,6 +197,7 @@ public:
         fetchSolution();
     }
 
+public:
     // IncompFlowSolverHybrid.hpp:754-807
     double postProcessFluxes()
     {
@@ -206,6 +243,44 @@ private:
     void check(int rc) const
     {
         if (rc != PORSOL_OK) throw std::runtime_error(porsol_last_error(h_));
+    }
+    // MimeticIPAnisoRelpermEvaluator::computeDynamicParams (MimeticIPAnisoRelpermEvaluator.hpp:
+    // 297-330): lambda_t = sum_i lambda_i and sum_i rho_i lambda_i per cell, row-major.
+    template <class FluidInterface>
+    void solveTensor(const FluidInterface& fl, const std::vector<double>& sat, const BCInterface& bc,
+                     const std::vector<double>& src, double residual_tolerance, int linsolver_verbosity,
+                     int linsolver_type, bool same_matrix, int linsolver_maxit, double prolongate_factor,
+                     int smooth_steps)
+    {
+        const int nc = grid_.numCells();
+        std::vector<double> lam(9 * size_t(nc), 0.0), rlam(9 * size_t(nc), 0.0), srcp(nc);
+        for (int p = 0; p < nc; ++p) {
+            const int ci = grid_.index_of_position[p];
+            std::array<double, FluidInterface::NumberOfPhases> rho;
+            fl.phaseDensities(ci, rho);
+            for (int ph = 0; ph < FluidInterface::NumberOfPhases; ++ph) {
+                Mat3 m;
+                fl.phaseMobility(ph, ci, sat[ci], m);
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        lam[9 * size_t(p) + 3 * i + j] += m(i, j);
+                        rlam[9 * size_t(p) + 3 * i + j] += rho[ph] * m(i, j);
+                    }
+            }
+            srcp[p] = src[ci];
+        }
+        flattenFlowBC(*pgrid_, grid_, bc, bct_, bcv_, partner_);
+        porsol_fluid f{PORSOL_FLUID_TENSOR, 1.0, 1.0, 0.0, 0.0};
+        porsol_solve_opts o = extra_;
+        o.residual_tolerance = residual_tolerance;
+        o.linsolver_verbosity = linsolver_verbosity;
+        o.linsolver_type = linsolver_type;
+        o.same_matrix = same_matrix ? 1 : 0;
+        o.linsolver_maxit = linsolver_maxit;
+        o.prolongate_factor = prolongate_factor;
+        o.smooth_steps = smooth_steps;
+        check(porsol_solve(h_, &f, lam.data(), rlam.data(), bct_.data(), bcv_.data(), srcp.data(), &o, &stats_));
+        fetchSolution();
     }
     void fetchSolution()
     {
