@@ -195,6 +195,22 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
                             const int* hf_partner_bid, const int* hf_side, const double* perm,
                             const porsol_solve_opts* opts, double* k_eff, porsol_solve_stats* stats);
 
+/* ------------------------------------------------------ output fields */
+/* The cell fields writeVtkOutput gathers (common/SimulatorUtilities.hpp:54-297), computed on the
+ * GPU from the current solution (after postProcessFluxes when it was called):
+ *   velocity [3 nc]  estimateCellVelocity: sum_f outflux_f (x_f - x_c) / |c|
+ *   water_velocity, oil_velocity [3 nc]  computePhaseVelocities: f_w v, (1 - f_w) v
+ *   fractional_flow [nc]  f_w = lambda_1 / (lambda_1 + lambda_2), Corey-2 model of `fluid`
+ *   cap_pressure [nc]  computeCapPressure without rock tables: 1e5 (1 - s)
+ * Host output arrays, each may be NULL; sat (host, [nc]) and fluid are needed only for the
+ * saturation-dependent fields (fluid->model must then be PORSOL_FLUID_COREY2). */
+int porsol_cell_fields(porsol_solver* h, const porsol_fluid* fluid, const double* sat, double* velocity,
+                       double* water_velocity, double* oil_velocity, double* fractional_flow, double* cap_pressure);
+/* writeField (SimulatorUtilities.hpp:290-297): the count on the first line, then one value per
+ * line in the default ostream format (%g, 6 significant digits), as the reference writes it.
+ * Host only; returns PORSOL_ERR_BAD_ARG if the file cannot be written. */
+int porsol_write_field(const double* field, int n, const char* filename);
+
 /* ------------------------------------------------------ adjoint permeability sensitivity */
 /* No counterpart in the reference.  Objective of the last solve's solution
  *     J = sum_c w_c (p_c - p*_c)^2 + sum_hf u_hf v_hf

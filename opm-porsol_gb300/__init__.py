@@ -136,6 +136,8 @@ EXPORTS = [
     ("porsol_amg_info", _i, [_vp, _i, C.POINTER(_i), _vp, _vp]),
     ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
                                      C.POINTER(SolveStats)]),
+    ("porsol_cell_fields", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("porsol_write_field", _i, [_vp, _i, C.c_char_p]),
     ("porsol_objective_value", _i, [_vp, C.POINTER(Objective), C.POINTER(_d)]),
     ("porsol_adjoint_gradient", _i, [_vp, C.POINTER(Objective), _i, C.POINTER(SolveOpts), C.POINTER(_d), _vp,
                                      C.POINTER(SolveStats)]),
@@ -200,6 +202,14 @@ class _GridArrays:
         self.s = Grid(a["num_cells"], _p(a["facepos"]).value, _p(a["neighbour"]).value, _p(a["bid"]).value,
                       _p(a["area"]).value, _p(a["fcentroid"]).value, _p(a["fnormal"]).value,
                       _p(a["volume"]).value, _p(a["ccentroid"]).value)
+
+
+def write_field(field, filename):
+    """writeField: count, then one value per line (%g), written by the library."""
+    f = _f64(field)
+    rc = lib().porsol_write_field(_p(f), len(f), str(filename).encode())
+    if rc != 0:
+        raise PorsolError(rc, f"cannot write {filename}")
 
 
 def default_solve_opts(**kw) -> SolveOpts:
@@ -314,6 +324,21 @@ class PressureSolver:
                                                   None if opts is None else C.byref(opts), C.byref(J), _p(grad),
                                                   C.byref(st)))
         return J.value, (grad.reshape(nc, 3) if mode == GRAD_LOGK_AXES else grad), st
+
+    def cell_fields(self, fluid=None, sat=None):
+        """Cell velocity (nc, 3) and, with a Corey-2 fluid and saturations, water/oil velocities,
+        fractional flow and capillary pressure (the fields of writeVtkOutput)."""
+        nc = self.grid.num_cells
+        out = {"velocity": np.empty((nc, 3))}
+        satf = sat is not None
+        if satf:
+            out.update(water_velocity=np.empty((nc, 3)), oil_velocity=np.empty((nc, 3)),
+                       fractional_flow=np.empty(nc), cap_pressure=np.empty(nc))
+        s = None if not satf else _f64(sat)
+        ptrs = [_p(out.get(k)) for k in ("velocity", "water_velocity", "oil_velocity", "fractional_flow",
+                                          "cap_pressure")]
+        self._check(lib().porsol_cell_fields(self.h, None if fluid is None else C.byref(fluid), _p(s), *ptrs))
+        return out
 
     def post_process_fluxes(self):
         m = C.c_double()

@@ -1045,6 +1045,61 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
     });
 }
 
+int porsol_cell_fields(porsol_solver* h, const porsol_fluid* fluid, const double* sat, double* velocity,
+                       double* water_velocity, double* oil_velocity, double* fractional_flow, double* cap_pressure)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "cell fields: no solution (call solve first)");
+        const bool satf = water_velocity || oil_velocity || fractional_flow || cap_pressure;
+        PORSOL_REQUIRE(!satf || (sat && fluid && fluid->model == PORSOL_FLUID_COREY2), PORSOL_ERR_BAD_ARG,
+                       "cell fields: saturation fields need sat and a Corey-2 fluid");
+        const int nc = h->S.g.nc;
+        cudaStream_t s = h->stream;
+        DBuf<double> d_sat, out;
+        const size_t o_v = 0, o_w = 3 * size_t(nc), o_o = 6 * size_t(nc), o_f = 9 * size_t(nc), o_p = 10 * size_t(nc);
+        out.alloc(11 * size_t(nc));
+        CellFieldArgs a{};
+        a.nc = nc;
+        a.facepos = h->facepos.p;
+        a.fcent = h->fcent.p;
+        a.ccent = h->ccent.p;
+        a.cvol = h->cvol.p;
+        a.outflux = h->outflux.p;
+        if (satf) {
+            d_sat.upload(sat, nc, s);
+            a.sat = d_sat.p;
+            a.mu1 = fluid->viscosity1;
+            a.mu2 = fluid->viscosity2;
+        }
+        a.vel = velocity ? out.p + o_v : nullptr;
+        a.vw = water_velocity ? out.p + o_w : nullptr;
+        a.vo = oil_velocity ? out.p + o_o : nullptr;
+        a.fw = fractional_flow ? out.p + o_f : nullptr;
+        a.pc = cap_pressure ? out.p + o_p : nullptr;
+        launch_cell_fields(s, a);
+        auto get = [&](double* dst, size_t off, size_t n) {
+            if (dst) PORSOL_CUDA(cudaMemcpyAsync(dst, out.p + off, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        };
+        get(velocity, o_v, 3 * size_t(nc));
+        get(water_velocity, o_w, 3 * size_t(nc));
+        get(oil_velocity, o_o, 3 * size_t(nc));
+        get(fractional_flow, o_f, nc);
+        get(cap_pressure, o_p, nc);
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int porsol_write_field(const double* field, int n, const char* filename)
+{
+    if (!filename || n < 0 || (n > 0 && !field)) return PORSOL_ERR_BAD_ARG;
+    FILE* f = std::fopen(filename, "w");
+    if (!f) return PORSOL_ERR_BAD_ARG;
+    // the reference streams with the default ostream format (6 significant digits, %g)
+    std::fprintf(f, "%d\n", n);
+    for (int i = 0; i < n; ++i) std::fprintf(f, "%g\n", field[i]);
+    return std::fclose(f) == 0 ? PORSOL_OK : PORSOL_ERR_BAD_ARG;
+}
+
 int porsol_objective_value(porsol_solver* h, const porsol_objective* obj, double* value)
 {
     return guarded(h, [&] {

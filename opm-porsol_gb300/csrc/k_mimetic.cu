@@ -336,6 +336,51 @@ __global__ void k_post_process(int npairs, const int* __restrict__ pairs, double
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(maxmod, d);
 }
 
+// Output fields of SimulatorUtilities.hpp from the solver's own buffers, one thread per cell:
+//   velocity  v_c = sum_f outflux_f (x_f - x_c) / |c|         (estimateCellVelocity, :54-82)
+//   phase velocities f_w v_c and (1 - f_w) v_c                 (computePhaseVelocities, :144-160)
+//   fractional flow f_w = lambda_1 / (lambda_1 + lambda_2)      (Corey-2 model)
+//   capillary pressure 1e5 (1 - s)                             (computeCapPressure, :214-225, with
+//     ReservoirPropertyCommon_impl.hpp:466-476 when no rock table is given)
+__global__ void k_cell_fields(CellFieldArgs A)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.nc) return;
+    const double x0 = A.ccent[3 * (size_t)c], x1 = A.ccent[3 * (size_t)c + 1], x2 = A.ccent[3 * (size_t)c + 2];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    for (int hf = A.facepos[c]; hf < A.facepos[c + 1]; ++hf) {
+        const double f = A.outflux[hf];
+        v0 += f * (A.fcent[3 * (size_t)hf] - x0);
+        v1 += f * (A.fcent[3 * (size_t)hf + 1] - x1);
+        v2 += f * (A.fcent[3 * (size_t)hf + 2] - x2);
+    }
+    const double iv = 1.0 / A.cvol[c];
+    v0 *= iv;
+    v1 *= iv;
+    v2 *= iv;
+    if (A.vel) {
+        A.vel[3 * (size_t)c] = v0;
+        A.vel[3 * (size_t)c + 1] = v1;
+        A.vel[3 * (size_t)c + 2] = v2;
+    }
+    if (!A.sat) return;
+    const double sw = A.sat[c];
+    const double m1 = sw * sw / A.mu1, m2 = (1.0 - sw) * (1.0 - sw) / A.mu2;
+    const double fw = m1 / (m1 + m2);
+    if (A.fw) A.fw[c] = fw;
+    if (A.pc) A.pc[c] = 1e5 * (1.0 - sw);
+    if (A.vw) {
+        A.vw[3 * (size_t)c] = fw * v0;
+        A.vw[3 * (size_t)c + 1] = fw * v1;
+        A.vw[3 * (size_t)c + 2] = fw * v2;
+    }
+    if (A.vo) {
+        A.vo[3 * (size_t)c] = (1.0 - fw) * v0;
+        A.vo[3 * (size_t)c + 1] = (1.0 - fw) * v1;
+        A.vo[3 * (size_t)c + 2] = (1.0 - fw) * v2;
+    }
+}
+
 __global__ void k_mass_balance(int nc, const int* __restrict__ facepos, const double* __restrict__ outflux,
                                const double* __restrict__ src, unsigned long long* out)
 {
@@ -512,6 +557,13 @@ void launch_mass_balance(cudaStream_t s, int nc, const int* facepos, const doubl
 {
     if (nc == 0) return;
     PORSOL_LAUNCH(k_mass_balance<<<div_up(nc, 256), 256, 0, s>>>(nc, facepos, outflux, src, out3));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_cell_fields(cudaStream_t s, const CellFieldArgs& a)
+{
+    if (a.nc == 0) return;
+    PORSOL_LAUNCH(k_cell_fields<<<div_up(a.nc, 256), 256, 0, s>>>(a));
     PORSOL_CUDA(cudaGetLastError());
 }
 

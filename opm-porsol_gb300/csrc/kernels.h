@@ -97,6 +97,18 @@ void launch_side_fluxes(cudaStream_t s, int ngrids, const int* cellpos, const in
 // changed = 1 if bct[bhf[q]] != cached[q] for some boundary half-face q
 void launch_compare_types(cudaStream_t s, int nb, const int* bhf, const int* bct, const int* cached, int* changed);
 
+// Output fields (cell velocity, phase velocities, fractional flow, capillary pressure); any
+// output pointer may be null; sat null: velocity only.
+struct CellFieldArgs {
+    int nc;
+    const int* facepos;
+    const double *fcent, *ccent, *cvol, *outflux;
+    const double* sat;
+    double mu1, mu2;
+    double *vel, *vw, *vo, *fw, *pc;
+};
+void launch_cell_fields(cudaStream_t s, const CellFieldArgs& a);
+
 // ---- k_adjoint.cu --------------------------------------------------------------------
 struct AdjointArgs {
     int nc;

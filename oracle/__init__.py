@@ -284,6 +284,26 @@ def upscale_periodic(grid, K9, tol=1e-13):
     return keff, its
 
 
+def cell_fields(grid, outflux, sat=None, mu1=1.0, mu2=1.0):
+    """Output fields of common/SimulatorUtilities.hpp restated with numpy: estimateCellVelocity
+    (:54-82), computePhaseVelocities (:144-160) with the Corey-2 fractional flow, and
+    computeCapPressure (:214-225) with the no-rock-table curve 1e5 (1 - s)
+    (ReservoirPropertyCommon_impl.hpp:466-476)."""
+    cell = np.repeat(np.arange(grid.num_cells), np.diff(grid.facepos))
+    d = (grid.fcentroid - grid.ccentroid[cell]) * outflux[:, None]
+    vel = np.zeros((grid.num_cells, 3))
+    np.add.at(vel, cell, d)
+    vel /= grid.volume[:, None]
+    out = {"velocity": vel}
+    if sat is not None:
+        m1 = sat * sat / mu1
+        m2 = (1.0 - sat) ** 2 / mu2
+        fw = m1 / (m1 + m2)
+        out.update(fractional_flow=fw, water_velocity=fw[:, None] * vel, oil_velocity=(1 - fw)[:, None] * vel,
+                   cap_pressure=1e5 * (1.0 - sat))
+    return out
+
+
 def ilu0_cg(rowptr, colind, vals, b, x0=None, tol=1e-8, maxit=0):
     rowptr, colind, vals, b = _i32(rowptr), _i32(colind), _f64(vals), _f64(b)
     n = len(b)
