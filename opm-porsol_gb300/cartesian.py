@@ -199,3 +199,71 @@ class UnionGrid:
             volume=np.ascontiguousarray(self.volume, dtype=np.float64),
             ccentroid=np.ascontiguousarray(self.ccentroid, dtype=np.float64),
         )
+
+
+class HexGrid(CartesianGrid):
+    """Logically Cartesian hexahedral grid with vertices moved by `mapping` (a function of an
+    (m, 3) array of reference points in the unit cube, returning (m, 3)).  Same cell/face order,
+    neighbours and boundary ids as CartesianGrid; the geometry is computed from the 8 corners:
+    each quadrilateral face is split into four triangles around its vertex average (area-weighted
+    normal = sum of triangle normals, centroid = area-weighted triangle centroids), and the cell
+    volume and centroid follow from the tetrahedra formed by those triangles and the cell's
+    vertex average.  For an affine mapping the faces are planar parallelograms and the geometry
+    is exact."""
+
+    # local vertices (di, dj, dk) of each local face, ordered so the normal points outwards
+    _FACE_VERTS = [
+        [(0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)],   # x-
+        [(1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1)],   # x+
+        [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)],   # y-
+        [(0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)],   # y+
+        [(0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0)],   # z-
+        [(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)],   # z+
+    ]
+
+    def __init__(self, nx, ny, nz, mapping, unique_bids=False):
+        super().__init__(nx, ny, nz, unique_bids=unique_bids)
+        k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+        ref = np.stack([i.ravel() / nx, j.ravel() / ny, k.ravel() / nz], axis=1)
+        V = np.asarray(mapping(ref), dtype=np.float64).reshape(nz + 1, ny + 1, nx + 1, 3)
+        nc = self.num_cells
+        kk, jj, ii = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        ii, jj, kk = ii.ravel(), jj.ravel(), kk.ravel()
+        corners = {}
+        for dk in (0, 1):
+            for dj in (0, 1):
+                for di in (0, 1):
+                    corners[(di, dj, dk)] = V[kk + dk, jj + dj, ii + di]
+        xc0 = sum(corners.values()) / 8.0
+        area = np.empty((nc, 6))
+        fcent = np.empty((nc, 6, 3))
+        fnorm = np.empty((nc, 6, 3))
+        vol = np.zeros(nc)
+        mom = np.zeros((nc, 3))
+        for lf, fv in enumerate(self._FACE_VERTS):
+            P = [corners[v] for v in fv]
+            m = sum(P) / 4.0
+            nsum = np.zeros((nc, 3))
+            csum = np.zeros((nc, 3))
+            asum = np.zeros(nc)
+            for q in range(4):
+                a, b = P[q], P[(q + 1) % 4]
+                tn = 0.5 * np.cross(a - m, b - m)
+                ta = np.linalg.norm(tn, axis=1)
+                tc = (a + b + m) / 3.0
+                nsum += tn
+                csum += tc * ta[:, None]
+                asum += ta
+                # tetrahedron (xc0, m, a, b): signed volume and centroid
+                tv = np.einsum("ij,ij->i", tn, m - xc0) / 3.0
+                vol += tv
+                mom += tv[:, None] * (xc0 + m + a + b) / 4.0
+            A = np.linalg.norm(nsum, axis=1)
+            area[:, lf] = A
+            fnorm[:, lf] = nsum / A[:, None]
+            fcent[:, lf] = csum / asum[:, None]
+        self.area = area.ravel()
+        self.fcentroid = fcent.reshape(-1, 3)
+        self.fnormal = fnorm.reshape(-1, 3)
+        self.volume = vol
+        self.ccentroid = mom / vol[:, None]

@@ -4,6 +4,7 @@ import os
 
 import numpy as np
 import pytest
+from hexgrids import linear_field_problem, sheared
 from tensor_mobility import tensor_problem
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -133,3 +134,14 @@ def test_oracle_tensor_mobility_scalar_case(orc, workloads, cart):
     p2, v2, _ = o.solution()
     assert np.abs(p1 - p2).max() < 1e-11 * np.abs(p2).max()
     assert np.abs(v1 - v2).max() < 1e-11 * np.abs(v2).max()
+
+
+def test_oracle_linear_field_on_sheared_grid(orc, workloads, cart):
+    """Parallelepiped cells (affine map of a Cartesian grid): linear fields are exact."""
+    g = sheared(cart)
+    prob = linear_field_problem(workloads, g)
+    o = orc.OraclePressure(g, prob.bc_type)
+    o.compute_inner_products(prob.perm.ravel())
+    assert o.solve(prob.totmob, prob.mobdens, prob.bc_type, prob.bc_value, prob.src, tol=1e-14) == 0
+    p, _, _ = o.solution()
+    assert np.abs(p - g.ccentroid @ np.array([1.5, -0.7, 0.4])).max() < 1e-10
