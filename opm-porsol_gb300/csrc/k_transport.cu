@@ -84,11 +84,44 @@ __global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const doubl
     dS[k] = d;
 }
 
+// Fractional flow lambda_1 / (lambda_1 + lambda_2), evaluated with the same operations as the
+// viscous term of k_face_dS (m1 * (1 / (m1 + m2))), so the fast path below is bitwise equal.
+__device__ __forceinline__ double frac1(double s, const TrParams& p)
+{
+    const double m0 = mob1(s, p.mu1), m1 = mob2(s, p.mu2);
+    return m0 * (1.0 / (m0 + m1));
+}
+
+__global__ void k_frac_init(int nc, const double* __restrict__ sat, TrParams p, double* __restrict__ frac)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nc) frac[c] = frac1(sat[c], p);
+}
+
+// Viscous-only sub-step (no gravity driving force, no capillary term): both phase mobilities
+// come from the same upstream cell, so the face term is f(s_up) q n.n with f precomputed per
+// cell (one FP64 division per cell instead of one per face; GB300's FP64 rate makes the
+// per-face form compute-bound).
+__global__ void k_face_dS_visc(int nfe, const FaceEntry* __restrict__ fe, const double* __restrict__ frac,
+                               const double* __restrict__ flux, TrParams p, double* __restrict__ dS,
+                               const int* __restrict__ status)
+{
+    if (*status) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nfe) return;
+    const int c0 = fe[k].c0, c1 = fe[k].c1, hf = fe[k].hf, dir = fe[k].dirichlet;
+    const double q = flux[hf];
+    double f;
+    if (q >= 0.0) f = frac[c0];
+    else f = dir ? frac1(fe[k].satbc, p) : frac[c1];
+    dS[k] = f * q * fe[k].nn;
+}
+
 // residual gather + smallTimeStep update + checkAndPossiblyClampSat
 __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* __restrict__ cent,
                               const double* __restrict__ dS, const double* __restrict__ inj,
-                              const double* __restrict__ porevol, TrParams p, double dt, int check, int clamp,
-                              double* __restrict__ sat, int* status)
+                              const double* __restrict__ ipv, TrParams p, double dt, int check, int clamp,
+                              double* __restrict__ sat, double* __restrict__ frac, int* status)
 {
     if (*status) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -107,7 +140,9 @@ __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* _
         }
         r += rate;
     }
-    double sn = s + dt * r / porevol[c];
+    // ipv = 1 / pore volume, precomputed at init: one FP64 division per cell and sub-step saved
+    // (the update differs from s + dt r / pv by at most one rounding of the increment)
+    double sn = s + (dt * r) * ipv[c];
     if (check || clamp) {
         if (sn > 1.0 || sn < 0.0) {
             if (clamp) sn = fmax(fmin(sn, 1.0), 0.0);
@@ -116,6 +151,7 @@ __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* _
     }
     if (!isfinite(sn)) atomicOr(status, ST_NONFINITE);
     sat[c] = sn;
+    if (frac) frac[c] = frac1(sn, p);   // for the next viscous-only sub-step
 }
 
 __device__ __forceinline__ void atomic_min_pos(unsigned long long* a, double v)
@@ -182,7 +218,8 @@ struct porsol_transport {
     double grav_cached[3] = {NAN, NAN, NAN};
     DBuf<FaceEntry> fe;
     DBuf<int> cptr, cent, facepos, status;
-    DBuf<double> porevol, vol, poro_d, dS, sat0, gflux_hf, in_sat, in_flux, in_inj;
+    DBuf<double> ipv, vol, poro_d, dS, sat0, gflux_hf, in_sat, in_flux, in_inj, frac;
+    bool any_gravity = false;   // some face entry has a non-zero gravity driving force
     DBuf<unsigned long long> red;
 
     void init(const porsol_grid* grid, const double* K, const double* phi, const porsol_fluid* fl, const int* stype,
@@ -263,7 +300,9 @@ void porsol_transport::init(const porsol_grid* grid, const double* K, const doub
     cudaStream_t s = stream;
     std::vector<double> pv(nc);
     for (int c = 0; c < nc; ++c) pv[c] = g.cvol[c] * poro[c];   // initObj (EulerUpstream_impl.hpp:120-129)
-    porevol.upload(pv, s);
+    std::vector<double> ip(nc);
+    for (int c = 0; c < nc; ++c) ip[c] = 1.0 / pv[c];
+    ipv.upload(ip, s);
     vol.upload(g.cvol, s);
     poro_d.upload(poro, s);
     facepos.upload(g.facepos, s);
@@ -366,6 +405,8 @@ void porsol_transport::build_entries(const double* grav)
     for (int c = 0; c < nc; ++c) cp[c + 1] = cp[c] + int(cl[c].size());
     ce.reserve(cp[nc]);
     for (int c = 0; c < nc; ++c) ce.insert(ce.end(), cl[c].begin(), cl[c].end());
+    any_gravity = false;
+    for (const FaceEntry& e : fe_h) any_gravity = any_gravity || e.G != 0.0;
     cudaStream_t s = stream;
     fe.upload(fe_h, s);
     cptr.upload(cp, s);
@@ -454,13 +495,25 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     TrParams p{1.0 / fluid.viscosity1, 1.0 / fluid.viscosity2, o.method_viscous, o.method_gravity,
                o.method_capillary};
     const int nfe = int(fe_h.size());
+    // viscous-only sub-steps use the per-cell fractional flow (same arithmetic, fewer FP64 ops)
+    const bool visc_only = o.method_viscous && !o.method_capillary && (!o.method_gravity || !any_gravity);
+    if (visc_only) frac.alloc(nc);
     int repeats = 0;
     const int max_repeats = 10;
     while (true) {
+        if (visc_only) PORSOL_LAUNCH(k_frac_init<<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, frac.p));
         for (int q = 0; q < n; ++q) {
-            if (nfe) PORSOL_LAUNCH(k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p, status.p));
-            PORSOL_LAUNCH(k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, porevol.p, p, dt, o.check_sat,
-                                                       o.clamp_sat, d_sat, status.p));
+            if (nfe) {
+                if (visc_only)
+                    PORSOL_LAUNCH(k_face_dS_visc<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p, dS.p,
+                                                                              status.p));
+                else
+                    PORSOL_LAUNCH(k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p,
+                                                                         status.p));
+            }
+            PORSOL_LAUNCH(k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, dt,
+                                                                    o.check_sat, o.clamp_sat, d_sat,
+                                                                    visc_only ? frac.p : nullptr, status.p));
             if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
         }
         PORSOL_CUDA(cudaGetLastError());
