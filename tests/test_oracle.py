@@ -4,7 +4,7 @@ import os
 
 import numpy as np
 import pytest
-from hexgrids import linear_field_problem, sheared
+from hexgrids import linear_field_problem, refined_top, sheared
 from tensor_mobility import tensor_problem
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -139,6 +139,18 @@ def test_oracle_tensor_mobility_scalar_case(orc, workloads, cart):
 def test_oracle_linear_field_on_sheared_grid(orc, workloads, cart):
     """Parallelepiped cells (affine map of a Cartesian grid): linear fields are exact."""
     g = sheared(cart)
+    prob = linear_field_problem(workloads, g)
+    o = orc.OraclePressure(g, prob.bc_type)
+    o.compute_inner_products(prob.perm.ravel())
+    assert o.solve(prob.totmob, prob.mobdens, prob.bc_type, prob.bc_value, prob.src, tol=1e-14) == 0
+    p, _, _ = o.solution()
+    assert np.abs(p - g.ccentroid @ np.array([1.5, -0.7, 0.4])).max() < 1e-10
+
+
+def test_oracle_linear_field_with_nine_face_cells(orc, workloads):
+    """A 2x2-refined layer over coarse cells: the coarse top cells have 9 faces."""
+    g = refined_top()
+    assert np.diff(g.facepos).max() == 9
     prob = linear_field_problem(workloads, g)
     o = orc.OraclePressure(g, prob.bc_type)
     o.compute_inner_products(prob.perm.ravel())
