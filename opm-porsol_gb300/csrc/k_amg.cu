@@ -707,14 +707,16 @@ __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* _
     extern __shared__ double sb[];
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
     __syncthreads();
+    // one warp per row, blockDim/32 rows per block: a large coarsest level (up to 2048 rows
+    // when coarsening stalls) spreads over many SMs instead of one
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int i = warp; i < n; i += nw) {
-        double s = 0.0;
-        for (int j = lane; j < n; j += 32) s += Dinv[(size_t)i * n + j] * sb[j];
+    const int i = blockIdx.x * nw + warp;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s += Dinv[(size_t)i * n + j] * sb[j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) x[i] = T(s);
-    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[i] = T(s);
 }
 
 int read_int(cudaStream_t s, const int* d)
@@ -1056,7 +1058,8 @@ template <class T>
 void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
 {
     if (l == nlev_ - 1) {
-        if (nc_ > 0) PORSOL_LAUNCH(k_dense_apply<T><<<1, 512, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop));
+        if (nc_ > 0)
+            PORSOL_LAUNCH(k_dense_apply<T><<<div_up(nc_, 8), 256, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop));
         return;
     }
     Level& L = *lv_[l];
