@@ -17,6 +17,8 @@
 //     factorisation), whatever the precision T of the hierarchy.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "krylov.h"
 
 namespace porsol {
@@ -31,6 +33,7 @@ struct AmgOpts {
     bool round1_negative = true;   // first pairing round of a level on strong negative couplings
     bool round2_negative = false;  // second round likewise; off: directly |a_ij| with joins (the
                                    // negative attempt stalls on these systems and is discarded)
+    bool half_smoother = true;     // FP32 hierarchies: smoother/residual read D^-1 A stored in FP16
 };
 
 // Device aggregation result: agg (row -> aggregate or -1), members CSR (aggregate -> rows).
@@ -57,6 +60,11 @@ private:
         SellPattern own;
         DBuf<T> own_val;
         DBuf<T> dinv;
+        // FP16 copy of D^-1 A (row-scaled, so entries are O(1) whatever the units) and the
+        // diagonal, read by the smoother and residual kernels of FP32 hierarchies
+        DBuf<__half> ah;
+        DBuf<T> diagv;
+        bool half = false;
         double lmax = 2.0;
         int lanes = 1;               // threads per row in the smoother/residual kernels
         Aggregates agg;              // to the next level

@@ -8,6 +8,8 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <type_traits>
+
 #include "amg.h"
 #include "sell.cuh"
 
@@ -553,8 +555,8 @@ __device__ __forceinline__ void row_lane(int& r, int& q)
 }
 
 // sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, K lanes otherwise
-template <int K, class T, class XF>
-__device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
+template <int K, class T, class V, class XF>
+__device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __restrict__ col, const V* __restrict__ A,
                                      const int* __restrict__ rowlen, int r, int q, bool valid, XF xf)
 {
     if constexpr (K == 1) {
@@ -564,10 +566,13 @@ __device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __re
     }
 }
 
+// Scaled form (SCALED, FP32 hierarchies): the matrix read is D^-1 A in FP16 (V = __half), so the
+// row dot already carries the 1/a_ii factor; the unscaled residual multiplies it back by a_ii.
+
 // start from y = t + w P xc (xc may be null: y = t): x = y, r = D^-1 (b - A y), d = r / theta
-template <class T, int K>
+template <class T, int K, class V, bool SCALED>
 __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __restrict__ col,
-                             const int* __restrict__ rowlen, const T* __restrict__ A, const T* __restrict__ dinv,
+                             const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                              const T* __restrict__ b, const T* __restrict__ t, const T* __restrict__ xc,
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
                              T* __restrict__ d, T inv_theta, const int* stop)
@@ -591,15 +596,15 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __res
         const int ai = agg[i];
         x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
     }
-    const T ri = dinv[i] * (b[i] - acc);
+    const T ri = SCALED ? dinv[i] * b[i] - acc : dinv[i] * (b[i] - acc);
     r[i] = ri;
     d[i] = ri * inv_theta;
 }
 
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
-template <class T, int K>
+template <class T, int K, class V, bool SCALED>
 __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col,
-                            const int* __restrict__ rowlen, const T* __restrict__ A, const T* __restrict__ dinv,
+                            const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
                             T* x_out, T c1, T c2, int final_step, const int* stop)
 {
@@ -612,7 +617,7 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     if (!valid || q != 0) return;
     const T di = d_in[i];
     T xi = (x_in ? x_in[i] : T(0)) + di;
-    const T ri = r[i] - dinv[i] * acc;
+    const T ri = SCALED ? r[i] - acc : r[i] - dinv[i] * acc;
     const T dn = c1 * di + c2 * ri;
     if (final_step) xi += dn;
     r[i] = ri;
@@ -620,10 +625,10 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     x_out[i] = xi;
 }
 
-template <class T, int K>
+template <class T, int K, class V, bool SCALED>
 __global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
-                        const T* __restrict__ A, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
-                        const int* stop)
+                        const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
+                        const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
     if (*stop) return;
     int i, q;
@@ -632,7 +637,27 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict
     if (K == 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
     if (!valid || q != 0) return;
-    r[i] = b[i] - acc;
+    r[i] = SCALED ? b[i] - diagv[i] * acc : b[i] - acc;
+}
+
+// D^-1 A in FP16 (padding slots stay 0) and the diagonal, for the scaled smoother
+template <class T>
+__global__ void k_scale_half(int n, const int* __restrict__ sp, const int* __restrict__ rowlen,
+                             const int* __restrict__ diag, const T* __restrict__ A, const T* __restrict__ dinv,
+                             __half* __restrict__ ah, T* __restrict__ diagv)
+{
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nslices = (n + 31) >> 5;
+    if (s >= nslices) return;
+    const int lane = threadIdx.x & 31, r = s * 32 + lane;
+    const int b = sp[s], w = (sp[s + 1] - b) >> 5;
+    const bool row = r < n;
+    const T di = row ? dinv[r] : T(0);
+    for (int t = 0; t < w; ++t) {
+        const int k = b + 32 * t + lane;
+        ah[k] = __float2half_rn(row ? float(A[k] * di) : 0.0f);
+    }
+    if (row) diagv[r] = A[diag[r]];
 }
 
 template <class T>
@@ -918,6 +943,14 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L)
     std::memcpy(&gm, &gb, sizeof(gm));
     L.lmax = gm > 0 ? gm : 1.0;
     L.lanes = lanes_for(n, L.P->nent);
+    L.half = o_.half_smoother && std::is_same<T, float>::value;
+    if (L.half) {
+        L.ah.alloc(size_t(L.P->nent));
+        L.diagv.alloc(n);
+        PORSOL_LAUNCH(k_scale_half<T><<<div_up(L.P->nslices, TB / 32), TB, 0, s>>>(
+            n, L.P->slice_ptr.p, L.P->rowlen.p, L.P->diag.p, L.A, L.dinv.p, L.ah.p, L.diagv.p));
+        PORSOL_CUDA(cudaGetLastError());
+    }
     L.t.alloc(n);
     L.r.alloc(n);
     L.d0.alloc(n);
@@ -1029,24 +1062,38 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
         const int nbk = div_up(n * L.lanes, TB);
-        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL><<<nbk, TB, 0, s>>>(
-                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x,
-                                  L.r.p, d, T(1.0 / theta), stop))));
+        if (L.half) {
+            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, __half, true><<<nbk, TB, 0, s>>>(
+                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg,
+                                      T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop))));
+        } else {
+            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, T, false><<<nbk, TB, 0, s>>>(
+                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg,
+                                      T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop))));
+        }
     }
     const int deg = std::max(1, o_.cheb_degree);
     for (int k = 1; k <= deg; ++k) {
         const double rho1 = 1.0 / (2.0 * sigma - rho);
         const double c1 = rho1 * rho, c2 = 2.0 * rho1 / delta;
         const T* xin = (from_zero && k == 1) ? nullptr : x;
-        // algorithmic bytes: matrix values + columns, d gathered once, dinv/r/x in, r/d/x out
-        const double bytes = double(P.nent) * (sizeof(T) + 4) + double(n) * sizeof(T) * (xin ? 7 : 6);
+        // algorithmic bytes: matrix values + columns, d gathered once, dinv (unscaled form only),
+        // r and x in, r/d/x out
+        const double bytes = double(P.nent) * ((L.half ? 2 : sizeof(T)) + 4) +
+                             double(n) * sizeof(T) * ((xin ? 7 : 6) - (L.half ? 1 : 0));
         const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();  // finest level only
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
         const int nbk = div_up(n * L.lanes, TB);
-        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL><<<nbk, TB, 0, s>>>(
-                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1),
-                                  T(c2), k == deg ? 1 : 0, stop))));
+        if (L.half) {
+            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, __half, true><<<nbk, TB, 0, s>>>(
+                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x,
+                                      T(c1), T(c2), k == deg ? 1 : 0, stop))));
+        } else {
+            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, T, false><<<nbk, TB, 0, s>>>(
+                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x,
+                                      T(c1), T(c2), k == deg ? 1 : 0, stop))));
+        }
         if (prof_here) prof_->end(s, PK_CHEB, bytes, ev);
         rho = rho1;
         std::swap(d, dn);
@@ -1071,8 +1118,13 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
     // restrict the residual
-    PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
-                              n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, b, L.t.p, L.r.p, stop))));
+    if (L.half) {
+        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL, __half, true><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
+                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop))));
+    } else {
+        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL, T, false><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
+                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop))));
+    }
     PORSOL_LAUNCH(k_restrict<T><<<div_up(Nx.n, TB), TB, 0, s>>>(Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop));
     vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
     // post-smoothing from t + w P xc
