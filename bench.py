@@ -143,12 +143,19 @@ def barrier(dist):
 
 
 def max_over_ranks(dist, v):
+    """Largest value over the ranks (the job's time is its slowest replica's)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_throughput(dist, world, units_per_rank, seconds):
+    """Whole-job throughput of independent replicas: all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / max_over_ranks(dist, seconds)
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle)
