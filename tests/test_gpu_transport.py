@@ -78,3 +78,38 @@ def test_transport_retry_and_failure(pkg, gpulib, orc, workloads, cart):
     with pytest.raises(pkg.PorsolError) as e:
         T2.solve(prob.sat, 1e4 * t, flux)
     assert e.value.code == 4
+
+
+def test_transport_periodic_and_wells(pkg, gpulib, orc, workloads, cart):
+    """Periodic in y (pressure and saturation), Dirichlet x-/x+, plus an injector and a producer
+    (injection rates: positive injects water, negative produces with the cell's fractional flow)."""
+    g = cart.CartesianGrid(8, 6, 3, unique_bids=True)
+    nc = g.num_cells
+    rng = np.random.default_rng(12)
+    K = workloads.iso_perm(np.exp(rng.normal(np.log(100 * workloads.MILLIDARCY), 1.0, nc)))
+    poro = np.full(nc, 0.2)
+    pb = g.periodic_partner_bids()
+    ybnd = (g.side == 3) | (g.side == 4)
+    bct, bcv = workloads.x_dirichlet_bc(g)
+    bct[ybnd] = workloads.BC_PERIODIC
+    bcv[ybnd] = 0.0
+    partner = np.where(ybnd, pb, 0).astype(np.int32)
+    src = np.zeros(nc)
+    src[5], src[nc - 7] = 2e-14, -2e-14
+    sat = rng.uniform(0.0, 0.3, nc)
+    prob = workloads.Problem("per", g, K, poro, bct, bcv, src, sat, (1, 1e-3, 1e-2, 1000.0, 850.0))
+    r = gpu_solve(pkg, prob, ltype=1, tol=1e-13, post=True, partner=partner)
+    flux = r["v"]
+    st_t = np.where(ybnd, workloads.BC_PERIODIC, workloads.BC_DIRICHLET).astype(np.int32)
+    sv = np.ones(g.num_half_faces)
+    fl = pkg.Fluid(pkg.FLUID_COREY2, 1e-3, 1e-2, 1000.0, 850.0)
+    T = pkg.TransportSolver()
+    T.init(g, K.ravel(), poro, fl, st_t, sv, partner_bid=partner, opts=pkg.default_transport_opts(method_capillary=0))
+    O = orc.OracleTransport(g, K.ravel(), poro, orc.Fluid(1e-3, 1e-2, 1000.0, 850.0), st_t, sv, partner_bid=partner,
+                            opts=orc.TransportOpts.defaults(method_capillary=0))
+    pv = (poro * g.volume).sum()
+    t = 0.02 * pv / np.abs(flux[g.side == 1]).sum()
+    s_gpu, st = T.solve(sat, t, flux, injection=src)
+    rc, s_orc, ns, rep = O.solve(sat, t, flux, injection=src)
+    assert rc == 0 and st.small_steps == ns and st.repeats == rep
+    assert relmax(s_gpu, s_orc) < 1e-11
