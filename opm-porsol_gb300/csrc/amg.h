@@ -76,7 +76,7 @@ private:
     void members(cudaStream_t s, Aggregates& a);
     void galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Aggregates& a, SellPattern& Pc,
                   DBuf<T>& Ac);
-    void smoother_setup(cudaStream_t s, Level& L);
+    void smoother_setup(cudaStream_t s, Level& L, int level);
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);
     void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
                    const int* stop);

@@ -820,7 +820,6 @@ void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, b
     out.agg.alloc(n);
     PORSOL_LAUNCH(k_assign<<<nb, TB, 0, s>>>(n, state.p, partner.p, jn.p, flag.p, cidx.p, out.agg.p));
     PORSOL_CUDA(cudaGetLastError());
-    PORSOL_CUDA(cudaStreamSynchronize(s));
 }
 
 template <class T>
@@ -834,8 +833,7 @@ void Amg<T>::members(cudaStream_t s, Aggregates& a)
     a.ptr.alloc(nc + 1);
     PORSOL_LAUNCH(k_count_members<<<div_up(n, TB), TB, 0, s>>>(n, a.agg.p, cnt.p));
     exclusive_scan(s, nc, cnt.p, a.ptr.p, a.ptr.p + nc, scan_blocks_);
-    const int total = read_int(s, a.ptr.p + nc);
-    a.idx.alloc(std::max(total, 1));
+    a.idx.alloc(std::max(n, 1));   // members <= rows; no host read of the exact count
     PORSOL_CUDA(cudaMemcpyAsync(pos.p, a.ptr.p, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
     PORSOL_LAUNCH(k_fill_members<<<div_up(n, TB), TB, 0, s>>>(n, a.agg.p, pos.p, a.idx.p));
     PORSOL_LAUNCH(k_sort_members<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p));
@@ -926,22 +924,14 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
 }
 
 template <class T>
-void Amg<T>::smoother_setup(cudaStream_t s, Level& L)
+void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
 {
     const int n = L.n;
     L.dinv.alloc(n);
-    DBuf<unsigned long long>& g = s_gmax_;
-    g.alloc(1);
-    g.zero(s);
+    // the Gershgorin bound stays on the device; setup() reads all levels' bounds in one copy
     PORSOL_LAUNCH(k_cheb_setup<T><<<div_up(n, TB), TB, 0, s>>>(n, L.P->slice_ptr.p, L.P->rowlen.p, L.P->diag.p, L.A, L.dinv.p,
-                                                 g.p, status_.p));
+                                                 s_gmax_.p + level, status_.p));
     PORSOL_CUDA(cudaGetLastError());
-    unsigned long long gb = 0;
-    PORSOL_CUDA(cudaMemcpyAsync(&gb, g.p, sizeof(gb), cudaMemcpyDeviceToHost, s));
-    PORSOL_CUDA(cudaStreamSynchronize(s));
-    double gm;
-    std::memcpy(&gm, &gb, sizeof(gm));
-    L.lmax = gm > 0 ? gm : 1.0;
     L.lanes = lanes_for(n, L.P->nent);
     L.half = o_.half_smoother && std::is_same<T, float>::value;
     if (L.half) {
@@ -983,6 +973,8 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
     nnzs_.clear();
     status_.alloc(1);
     status_.zero(s);
+    s_gmax_.alloc(size_t(std::max(o.max_levels, 1)));
+    s_gmax_.zero(s);
     if (lv_.empty()) lv_.push_back(std::make_unique<Level>());
     nlev_ = 1;
     {
@@ -997,7 +989,7 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         Level& L = *lv_[nlev_ - 1];
         const int n = L.n;
         const SellPattern& P = *L.P;
-        smoother_setup(s, L);
+        smoother_setup(s, L, nlev_ - 1);
         if (int(lv_.size()) <= nlev_) lv_.push_back(std::make_unique<Level>());
         Level& next = *lv_[nlev_];
         // round 1 on this level's matrix; L.agg maps rows to the intermediate level
@@ -1033,6 +1025,18 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         nnzs_.push_back(next.own.nent);
         ++nlev_;
         if (next.n > 0.9 * n) break;   // coarsening stalled
+    }
+    // Chebyshev intervals of the smoothed levels (one copy for all levels)
+    {
+        std::vector<unsigned long long> gb(size_t(nlev_), 0ULL);
+        PORSOL_CUDA(cudaMemcpyAsync(gb.data(), s_gmax_.p, sizeof(unsigned long long) * gb.size(),
+                                    cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaStreamSynchronize(s));
+        for (int l = 0; l + 1 < nlev_; ++l) {
+            double gm;
+            std::memcpy(&gm, &gb[size_t(l)], sizeof(gm));
+            lv_[l]->lmax = gm > 0 ? gm : 1.0;
+        }
     }
     Level& C = *lv_[nlev_ - 1];
     PORSOL_REQUIRE(C.n <= 2048, PORSOL_ERR_BAD_ARG, "AMG: coarsening stalled above the dense-solve limit");
