@@ -50,7 +50,7 @@ def parse():
                     help="residual reduction of the FP64 solves (1e-8 flux error)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--impes", type=int, default=0,
-                    help="run the 200x200x25 IMPES case for this many steps (50 in the configuration) "
+                    help="run the 200x200x25 IMPES workload for this many steps (50 in the headline IMPES run) "
                          "instead of the pressure benchmark and print its own JSON line")
     ap.add_argument("--upscale", type=int, default=0,
                     help="batched periodic upscaling of this many sub-grids instead of the pressure bench")
@@ -172,7 +172,7 @@ def cpu_sample(prob, o=None, sample_iters=6):
     """Serial FP64 oracle (ILU0-CG, the reference's linsolver_type 0 path) on the full-size
     system: one assembly + ILU0 factorisation + `sample_iters` CG iterations + recovery,
     scaled to a complete solve with the recorded iteration count of that solve."""
-    gold = os.path.join(ROOT, "tests", "golden", "oracle_case5_ilu0.json")
+    gold = os.path.join(ROOT, "tests", "golden", "oracle_layered_1m_ilu0.json")
     iters_full = None
     if os.path.exists(gold) and prob.grid.dims == (200, 200, 25):
         iters_full = json.load(open(gold))["results"]["1e-08"]["iterations"]
@@ -199,7 +199,7 @@ def run_reference(args):
     import __graft_entry__ as ge
     wl = ge.load_module("workloads")
     dims = tuple(int(x) for x in args.dims.split(","))
-    prob = wl.case5(dims=dims)
+    prob = wl.layered_lognormal(dims=dims)
     o = cpu_oracle(prob)
     vals = []
     for k in range(args.warmup + args.steps):
@@ -233,7 +233,7 @@ def run_gpu(args):
         pkg.build()
     wl = ge.load_module("workloads")
     dims = tuple(int(x) for x in args.dims.split(","))
-    prob = wl.case5(dims=dims)
+    prob = wl.layered_lognormal(dims=dims)
     g = prob.grid
     nc, nhf = g.num_cells, g.num_half_faces
     model, mu1, mu2, r1, r2 = prob.fluid
@@ -392,7 +392,7 @@ def run_gpu(args):
 
 
 def run_impes(args):
-    """Configuration 5: pressure solve every step, then EulerUpstream::transportSolve with
+    """IMPES on the 200x200x25 layered grid: pressure solve every step, then EulerUpstream::transportSolve with
     CFL-limited sub-steps; water (s = 1) enters through x- at Dirichlet p = 1, p = 0 at x+;
     step length 0.1 PV / (nsteps Q_in) with Q_in the inflow of the first pressure solve.
     Mixed precision and FP64 runs on the same inputs, everything device-resident."""
@@ -401,7 +401,7 @@ def run_impes(args):
     pkg = ge.load_package()
     wl = ge.load_module("workloads")
     dims = tuple(int(x) for x in args.dims.split(","))
-    prob = wl.case5(dims=dims)
+    prob = wl.layered_lognormal(dims=dims)
     g = prob.grid
     _, mu1, mu2, r1, r2 = prob.fluid
     fluid = pkg.Fluid(pkg.FLUID_COREY2, mu1, mu2, r1, r2)
@@ -460,7 +460,7 @@ def run_tensor(args):
     pkg = ge.load_package()
     wl = ge.load_module("workloads")
     dims = tuple(int(x) for x in args.dims.split(","))
-    prob = wl.case2(dims=dims)   # diagonal anisotropic K, Corey-2, s ~ U[0, 1]
+    prob = wl.anisotropic_corey(dims=dims)   # diagonal anisotropic K, Corey-2, s ~ U[0, 1]
     g = prob.grid
     nc = g.num_cells
     _, mu1, mu2, r1, r2 = prob.fluid
@@ -498,7 +498,7 @@ def run_tensor(args):
 
 
 def run_adjoint(args):
-    """Configuration 4: d J / d ln k on the 64x64x32 correlated log-normal grid, J = squared
+    """Adjoint gradient: d J / d ln k on the 64x64x32 correlated log-normal grid, J = squared
     pressure mismatch at 50 cells + outflux through x+.  A step is one forward solve (AMG-CG,
     host inputs, hierarchy rebuilt) + objective + one adjoint solve + gradient, with the gradient
     copied to the host.  FP64 and mixed precision; the gradient is compared with the oracle's
@@ -507,8 +507,8 @@ def run_adjoint(args):
     import __graft_entry__ as ge
     pkg = ge.load_package()
     wl = ge.load_module("workloads")
-    prob = wl.case4()
-    w, target, u, _ = wl.case4_objective(prob)
+    prob = wl.correlated_lognormal()
+    w, target, u, _ = wl.pressure_mismatch_objective(prob)
     g = prob.grid
     fl = pkg.Fluid(pkg.FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0)
     tol = 1e-10
@@ -560,7 +560,7 @@ def run_adjoint(args):
 
 
 def run_upscale(args):
-    """Configuration 3: effective permeability of N periodic unit-cube sub-grids (side n ~ U{8..32},
+    """Batched upscaling: effective permeability of N periodic unit-cube sub-grids (side n ~ U{8..32},
     full log-normal tensors with random axes), three unit pressure-jump solves each, as one
     block-diagonal system on the GPU.  A step is one porsol_upscale_periodic call with host inputs
     and host K_eff out (grid, tensors, assembly, AMG setup, 3 solves, side fluxes).  The CPU
@@ -570,7 +570,7 @@ def run_upscale(args):
     import __graft_entry__ as ge
     pkg = ge.load_package()
     wl = ge.load_module("workloads")
-    union, sizes, K = wl.case3(num=args.upscale)
+    union, sizes, K = wl.periodic_subgrids(num=args.upscale)
     K = np.ascontiguousarray(K)
     out = {"metric": "upscaled sub-grids/s (3 periodic solves each)", "unit": "sub-grids/s",
            "config": {"workload": f"{args.upscale} periodic unit cubes, n ~ U{{8..32}}, log-normal full tensors "

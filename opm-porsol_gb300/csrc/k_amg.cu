@@ -992,7 +992,7 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         smoother_setup(s, L, nlev_ - 1);
         if (int(lv_.size()) <= nlev_) lv_.push_back(std::make_unique<Level>());
         Level& next = *lv_[nlev_];
-        // round 1 on this level's matrix; L.agg maps rows to the intermediate level
+        // first pairing round on this level's matrix; L.agg maps rows to the intermediate level
         aggregate_round(s, P, L.A, n, o_.round1_negative, L.agg);
         members(s, L.agg);
         galerkin(s, P, L.A, L.agg, tmp_pat_, tmp_val_);

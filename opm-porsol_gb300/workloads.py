@@ -1,19 +1,24 @@
-"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+"""Seeded synthetic workloads for the tests and the benchmark.
 
 There is no public dataset for this path; every input is generated here from a
-documented seed (20261203 + config index, numpy PCG64).  Units are SI as in the
-reference (Opm::unit): permeability in m^2 (1 mD = 9.869233e-16 m^2), viscosity
-in Pa s, pressure in Pa (the configurations prescribe p = 1 and p = 0).
+documented seed (20261203 + k, numpy PCG64).  Units are SI as in the reference
+(Opm::unit): permeability in m^2 (1 mD = 9.869233e-16 m^2), viscosity in Pa s,
+pressure in Pa (the workloads prescribe p = 1 and p = 0).
 
-  case 1  10x10x10 unit cube, isotropic ln k ~ N(ln 100 mD, 1) i.i.d., total
-          mobility 1, Dirichlet p=1 (x-) / p=0 (x+), no-flow elsewhere, ILU0-CG 1e-10.
-  case 2  100x100x50, kx=ky log-normal sigma=2 Gaussian-correlated (5 cells),
-          kz = 0.1 kx, Corey-2 mobilities with viscosity ratio 5, s ~ U[0,1].
-  case 4  64x64x32, isotropic log-normal sigma=1 correlated over 4 cells; objective
-          sum of squared pressure mismatches at 50 cells + outflux through x+.
-  case 5  200x200x25, 25 layers, layer mean ~ N(ln 100 mD, 1), ln k ~ N(mean, 2^2)
-          i.i.d. within a layer, Corey-2 with viscosity ratio 10, initial s = 0,
-          water (s = 1) enters through x-.
+  unit_cube_lognormal    10x10x10 unit cube, isotropic ln k ~ N(ln 100 mD, 1) i.i.d.,
+                         total mobility 1, Dirichlet p=1 (x-) / p=0 (x+), no-flow elsewhere,
+                         ILU0-CG 1e-10 (seed + 1).
+  anisotropic_corey      100x100x50, kx=ky log-normal sigma=2 Gaussian-correlated (5 cells),
+                         kz = 0.1 kx, Corey-2 mobilities with viscosity ratio 5, s ~ U[0,1]
+                         (seed + 2).
+  periodic_subgrids      512 periodic unit cubes n^3, n ~ U{8..32}, full log-normal tensors
+                         sigma=1.5 with random principal axes (seed + 3).
+  correlated_lognormal   64x64x32, isotropic log-normal sigma=1 correlated over 4 cells
+                         (seed + 4); pressure_mismatch_objective: squared pressure mismatches
+                         at 50 cells + outflux through x+.
+  layered_lognormal      200x200x25, 25 layers, layer mean ~ N(ln 100 mD, 1),
+                         ln k ~ N(mean, 2^2) i.i.d. within a layer, Corey-2 with viscosity
+                         ratio 10, initial s = 0, water (s = 1) enters through x- (seed + 5).
 """
 from __future__ import annotations
 
@@ -94,17 +99,17 @@ def correlated_normal(rng, dims, corr_cells, sigma=1.0):
     return f.ravel()   # x fastest, matching the grid's cell order
 
 
-def case1(n=10, seed=None):
+def unit_cube_lognormal(n=10, seed=None):
     rng = np.random.default_rng(SEED0 + 1 if seed is None else seed)
     g = CartesianGrid(n, n, n)
     nc = g.num_cells
     k = np.exp(rng.normal(np.log(100 * MILLIDARCY), 1.0, nc))
     bct, bcv = x_dirichlet_bc(g)
-    return Problem("case1", g, iso_perm(k), np.full(nc, 0.2), bct, bcv, np.zeros(nc), np.zeros(nc),
+    return Problem("unit_cube_lognormal", g, iso_perm(k), np.full(nc, 0.2), bct, bcv, np.zeros(nc), np.zeros(nc),
                    (0, 1.0, 1.0, 0.0, 0.0), totmob=np.ones(nc), mobdens=np.zeros(nc))
 
 
-def case2(dims=(100, 100, 50), seed=None, corr=5.0):
+def anisotropic_corey(dims=(100, 100, 50), seed=None, corr=5.0):
     rng = np.random.default_rng(SEED0 + 2 if seed is None else seed)
     g = CartesianGrid(*dims)
     nc = g.num_cells
@@ -112,7 +117,7 @@ def case2(dims=(100, 100, 50), seed=None, corr=5.0):
     kx = np.exp(lk)
     sat = rng.uniform(0.0, 1.0, nc)
     bct, bcv = x_dirichlet_bc(g)
-    return Problem("case2", g, diag_perm(kx, kx, 0.1 * kx), np.full(nc, 0.2), bct, bcv, np.zeros(nc), sat,
+    return Problem("anisotropic_corey", g, diag_perm(kx, kx, 0.1 * kx), np.full(nc, 0.2), bct, bcv, np.zeros(nc), sat,
                    (1, 1e-3, 5e-3, 1000.0, 850.0))
 
 
@@ -126,7 +131,7 @@ def random_rotations(rng, n):
     return Q
 
 
-def case3(num=512, nmin=8, nmax=32, seed=None, sigma=1.5):
+def periodic_subgrids(num=512, nmin=8, nmax=32, seed=None, sigma=1.5):
     """Batched periodic upscaling: `num` unit-cube sub-grids of n^3 cells, n ~ U{nmin..nmax},
     full SPD tensors K = R diag(exp(g)) R^T per cell, g ~ N(ln 100 mD, sigma^2), R uniform."""
     rng = np.random.default_rng(SEED0 + 3 if seed is None else seed)
@@ -140,18 +145,18 @@ def case3(num=512, nmin=8, nmax=32, seed=None, sigma=1.5):
     return union, sizes, K.reshape(nc, 9)
 
 
-def case4(dims=(64, 64, 32), seed=None, corr=4.0):
+def correlated_lognormal(dims=(64, 64, 32), seed=None, corr=4.0):
     rng = np.random.default_rng(SEED0 + 4 if seed is None else seed)
     g = CartesianGrid(*dims)
     nc = g.num_cells
     lk = np.log(100 * MILLIDARCY) + correlated_normal(rng, dims, corr, 1.0)
     bct, bcv = x_dirichlet_bc(g)
-    return Problem("case4", g, iso_perm(np.exp(lk)), np.full(nc, 0.2), bct, bcv, np.zeros(nc), np.zeros(nc),
+    return Problem("correlated_lognormal", g, iso_perm(np.exp(lk)), np.full(nc, 0.2), bct, bcv, np.zeros(nc), np.zeros(nc),
                    (0, 1.0, 1.0, 0.0, 0.0), totmob=np.ones(nc), mobdens=np.zeros(nc))
 
 
-def case4_objective(problem, seed=None, n_obs=50, n_fd=20):
-    """Objective of the adjoint configuration on a case-4 grid: pressure mismatch at `n_obs`
+def pressure_mismatch_objective(problem, seed=None, n_obs=50, n_fd=20):
+    """Objective of the adjoint workload on a correlated_lognormal grid: pressure mismatch at `n_obs`
     seeded cells against targets p* ~ N(0.5, 0.1^2), plus the total outflux through x+ (side 2).
     Returns (cell_weight, cell_target, hf_weight, fd_cells): fd_cells are the `n_fd` seeded cells
     at which finite differences check the gradient."""
@@ -168,7 +173,7 @@ def case4_objective(problem, seed=None, n_obs=50, n_fd=20):
     return w, target, u, fd_cells
 
 
-def case5(dims=(200, 200, 25), seed=None, sat=None):
+def layered_lognormal(dims=(200, 200, 25), seed=None, sat=None):
     rng = np.random.default_rng(SEED0 + 5 if seed is None else seed)
     nx, ny, nz = dims
     g = CartesianGrid(*dims)
@@ -180,7 +185,7 @@ def case5(dims=(200, 200, 25), seed=None, sat=None):
     s = np.zeros(nc) if sat is None else sat
     st = np.full(g.num_half_faces, BC_DIRICHLET, np.int32)   # SatBC default: Dirichlet s = 1
     sv = np.ones(g.num_half_faces)
-    return Problem("case5", g, iso_perm(np.exp(lk)), np.full(nc, 0.2), bct, bcv, np.zeros(nc), s,
+    return Problem("layered_lognormal", g, iso_perm(np.exp(lk)), np.full(nc, 0.2), bct, bcv, np.zeros(nc), s,
                    (1, 1e-3, 1e-2, 1000.0, 850.0), sat_type=st, sat_value=sv)
 
 

@@ -4,7 +4,7 @@ ctypes binding of ``oracle/porsol_oracle.cpp``, the serial C++ restatement of
 OPM/opm-porsol's mimetic pressure solver (IncompFlowSolverHybrid +
 MimeticIPEvaluator) and explicit upstream transport (EulerUpstream).  Only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this package, and only as the checker; the GPU product
+``bench.py`` import this package, and only to check results; the GPU product
 library never calls it.
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 // porsol_oracle.cpp -- FP64 CPU oracle for the mimetic pressure / upstream transport path.
 //
 // TEST INFRASTRUCTURE ONLY.  A plain, serial C++ restatement of the reference algorithms
-// of OPM/opm-porsol, used as the checker for the GPU library.  Nothing in the product
+// of OPM/opm-porsol, used to check the GPU library.  Nothing in the product
 // path links, loads or calls this file.  Each function cites the reference lines it
 // restates.  Dense local algebra that the reference delegates to BLAS/LAPACK is written
 // out here (Householder QR as in LAPACK xGEQR2/xORG2R, plain loops for SYRK/TRMM/GEMM).

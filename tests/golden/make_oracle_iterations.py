@@ -18,7 +18,7 @@ import oracle  # noqa: E402
 wl = ge.load_module("workloads")
 out = {}
 for tol in (1e-8,):
-    p = wl.case5()
+    p = wl.layered_lognormal()
     o = oracle.OraclePressure(p.grid, p.bc_type)
     o.compute_inner_products(p.perm.ravel())
     tm, md = p.mobilities()
@@ -29,4 +29,4 @@ for tol in (1e-8,):
     print(tol, out[f"{tol:g}"], flush=True)
 json.dump(dict(case="200x200x25 layered log-normal (seed 20261208), s=0, Dirichlet p=1/p=0 on x-/x+",
                solver="oracle ILU0-CG with the Dirichlet-row initial guess", results=out),
-          open(os.path.join(HERE, "oracle_case5_ilu0.json"), "w"), indent=2)
+          open(os.path.join(HERE, "oracle_layered_1m_ilu0.json"), "w"), indent=2)

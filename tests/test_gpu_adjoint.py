@@ -76,8 +76,8 @@ def test_adjoint_rejects_unsupported(pkg, gpulib, cart):
 def test_adjoint_config4_against_oracle_and_fd(pkg, gpulib, orc, workloads):
     """64x64x32 correlated log-normal field: 50 pressure observations + outflux through x+.
     FP64 AMG-CG forward and adjoint; FD at 20 seeded cells with ln-k step 1e-6."""
-    prob = workloads.case4()
-    w, target, u, cells = workloads.case4_objective(prob)
+    prob = workloads.correlated_lognormal()
+    w, target, u, cells = workloads.pressure_mismatch_objective(prob)
     s, fl, o = _gpu(pkg, prob, tol=1e-13)
     J, g, _ = s.adjoint_gradient(w, target, u)
     Jo, go = _oracle(orc, prob, w, target, u, tol=1e-13)
@@ -113,7 +113,7 @@ def test_adjoint_config4_against_oracle_and_fd(pkg, gpulib, orc, workloads):
 
 def test_adjoint_flux_gradient_sums_to_flux(pkg, gpulib, workloads):
     """d Q / d ln s for K -> s K summed over cells equals Q (the outflux scales with k)."""
-    prob = workloads.case4(dims=(32, 32, 16))
+    prob = workloads.correlated_lognormal(dims=(32, 32, 16))
     s, _, _ = _gpu(pkg, prob, tol=1e-13)
     u = np.where(prob.grid.side == 2, 1.0, 0.0)
     Q, g, _ = s.adjoint_gradient(None, None, u)

@@ -110,9 +110,9 @@ def test_solve_matches_oracle(pkg, gpulib, orc, workloads, cart, ltype):
     assert g["stats"].mass_balance < 1e-9
 
 
-def test_case1_ilu0(pkg, gpulib, orc, workloads):
-    """Configuration 1: 10^3 cells, CG + ILU0 to 1e-10, plain FP64."""
-    prob = workloads.case1()
+def test_unit_cube_ilu0(pkg, gpulib, orc, workloads):
+    """10^3 cells, CG + ILU0 to 1e-10, plain FP64."""
+    prob = workloads.unit_cube_lognormal()
     g = gpu_solve(pkg, prob, ltype=0, tol=1e-10)
     o = oracle_solve(orc, prob, tol=1e-10)
     assert g["stats"].iterations == o["iterations"]
@@ -185,7 +185,7 @@ def test_post_process_antisymmetric(pkg, gpulib, workloads, cart):
 
 def test_mixed_precision_flux_error(pkg, gpulib, orc, workloads):
     """FP32 SpMV/AMG inside FP64 refinement reaches 1e-8 relative flux error (sigma=2 field)."""
-    prob = workloads.case2(dims=(24, 20, 10))
+    prob = workloads.anisotropic_corey(dims=(24, 20, 10))
     o = oracle_solve(orc, prob, tol=1e-13, dirichlet_guess=True)
     g = gpu_solve(pkg, prob, ltype=1, tol=1e-11, precision=pkg.MIXED)
     assert rel(g["v"], o["v"]) < 1e-8

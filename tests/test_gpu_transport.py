@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 def _setup(pkg, orc, workloads, cart, dims=(10, 8, 4), grav=(0.0, 0.0, 0.0), capillary=False, seed=3):
     rng = np.random.default_rng(seed)
-    prob = workloads.case5(dims=dims, seed=seed, sat=rng.uniform(0.0, 0.4, int(np.prod(dims))))
+    prob = workloads.layered_lognormal(dims=dims, seed=seed, sat=rng.uniform(0.0, 0.4, int(np.prod(dims))))
     if capillary:
         # The no-rock capillary pressure is 1e5 (1 - s) Pa; with a 1 Pa drop it swamps the
         # viscous flux and the explicit scheme (which has no capillary CFL bound without rock

@@ -26,7 +26,7 @@ def test_write_field_format(pkg, tmp_path):
 
 @pytest.mark.gpu
 def test_cell_fields_match_restatement(pkg, gpulib, orc, workloads):
-    prob = workloads.case2(dims=(12, 10, 6))
+    prob = workloads.anisotropic_corey(dims=(12, 10, 6))
     r = gpu_solve(pkg, prob, ltype=1, tol=1e-12, post=True)
     s = r["solver"]
     _, mu1, mu2, r1, r2 = prob.fluid

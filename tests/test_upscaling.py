@@ -1,4 +1,4 @@
-"""Batched periodic upscaling (configuration 3): the GPU batch against per-sub-grid FP64 oracle
+"""Batched periodic upscaling (512-sub-grid workload shape): the GPU batch against per-sub-grid FP64 oracle
 solves, and analytic effective permeabilities."""
 import numpy as np
 import pytest
@@ -29,7 +29,7 @@ def test_oracle_layered_medium_means(orc, cart):
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_matches_per_subgrid_oracle(pkg, gpulib, orc, workloads, precision):
-    union, sizes, K = workloads.case3(num=5, nmin=3, nmax=6, seed=21)
+    union, sizes, K = workloads.periodic_subgrids(num=5, nmin=3, nmax=6, seed=21)
     s = pkg.PressureSolver()
     opts = pkg.default_solve_opts(residual_tolerance=1e-12, precision=precision)
     keff, st = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(), opts)

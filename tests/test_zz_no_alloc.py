@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 def test_noalloc_cfl_matches_transport_entry_point(pkg, gpulib, orc, workloads):
     import torch
     from parity import gpu_solve
-    prob = workloads.case5(dims=(12, 9, 5), seed=17)
+    prob = workloads.layered_lognormal(dims=(12, 9, 5), seed=17)
     flux = gpu_solve(pkg, prob, ltype=1, tol=1e-12, post=True)["v"]
     g = prob.grid
     _, mu1, mu2, r1, r2 = prob.fluid
