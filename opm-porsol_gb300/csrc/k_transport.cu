@@ -191,7 +191,18 @@ __global__ void k_cfl_cells(int nc, const int* __restrict__ facepos, const doubl
         dv = fmin(dv, __shfl_xor_sync(0xffffffffu, dv, o));
         dg = fmin(dg, __shfl_xor_sync(0xffffffffu, dg, o));
     }
+    // block minimum first: one atomic per block and quantity instead of one per warp
+    __shared__ double sv[TB / 32], sg[TB / 32];
     if ((threadIdx.x & 31) == 0) {
+        sv[threadIdx.x >> 5] = dv;
+        sg[threadIdx.x >> 5] = dg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < TB / 32; ++w) {
+            dv = fmin(dv, sv[w]);
+            dg = fmin(dg, sg[w]);
+        }
         atomic_min_pos(&out[0], dv);
         atomic_min_pos(&out[1], dg);
     }
