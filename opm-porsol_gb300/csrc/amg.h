@@ -34,6 +34,9 @@ struct AmgOpts {
     bool round2_negative = false;  // second round likewise; off: directly |a_ij| with joins (the
                                    // negative attempt stalls on these systems and is discarded)
     bool half_smoother = true;     // FP32 hierarchies: smoother/residual read D^-1 A stored in FP16
+    bool autotune = false;         // time the lane schedules of each new level shape once (the
+                                   // choice then depends on timing: off where runs must be
+                                   // bitwise reproducible)
 };
 
 // Device aggregation result: agg (row -> aggregate or -1), members CSR (aggregate -> rows).
@@ -77,6 +80,8 @@ private:
     void galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Aggregates& a, SellPattern& Pc,
                   DBuf<T>& Ac);
     void smoother_setup(cudaStream_t s, Level& L, int level);
+    int tune_lanes(cudaStream_t s, Level& L);
+    DBuf<int> tune_stop_;
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);
     void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
                    const int* stop);

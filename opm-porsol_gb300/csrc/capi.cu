@@ -380,6 +380,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     AmgOpts ao;
     ao.smooth_steps = std::max(1, o.smooth_steps);
     ao.prolong = o.prolongate_factor;
+    ao.autotune = true;   // the sub-grid union's level shapes are unlike a single grid's
     const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
     if (!mixed) {
         Precond<double>* M = nullptr;

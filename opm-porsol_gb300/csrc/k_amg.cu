@@ -8,7 +8,9 @@
 #include <cstdlib>
 #include <cstring>
 
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 
 #include "amg.h"
 #include "sell.cuh"
@@ -774,6 +776,18 @@ int lanes_for(int n, long long nent)
     default: { constexpr int KL = 16; LAUNCH; } break;                                                            \
     }
 
+// Process-wide cache of autotuned lanes per row, keyed by level shape.
+std::mutex& tune_mutex()
+{
+    static std::mutex m;
+    return m;
+}
+std::unordered_map<long long, int>& tune_cache()
+{
+    static std::unordered_map<long long, int> c;
+    return c;
+}
+
 }  // namespace
 
 void exclusive_scan(cudaStream_t s, int n, const int* in, int* out, int* total_dev, DBuf<int>& scratch)
@@ -932,7 +946,6 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     PORSOL_LAUNCH(k_cheb_setup<T><<<div_up(n, TB), TB, 0, s>>>(n, L.P->slice_ptr.p, L.P->rowlen.p, L.P->diag.p, L.A, L.dinv.p,
                                                  s_gmax_.p + level, status_.p));
     PORSOL_CUDA(cudaGetLastError());
-    L.lanes = lanes_for(n, L.P->nent);
     L.half = o_.half_smoother && std::is_same<T, float>::value;
     if (L.half) {
         L.ah.alloc(size_t(L.P->nent));
@@ -945,6 +958,72 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.r.alloc(n);
     L.d0.alloc(n);
     L.d1.alloc(n);
+    L.lanes = tune_lanes(s, L);
+}
+
+// Lane schedule autotuner: for a level shape not seen before, time one smoother step with 1, 2,
+// 4, 8 and 16 lanes per row and keep the fastest.  Shapes are bucketed by value width, log2 of
+// the row count and the mean padded row length, so nearby hierarchies (the next solve of an
+// IMPES run, the next batch of sub-grids) reuse the choice without timing again.
+template <class T>
+int Amg<T>::tune_lanes(cudaStream_t s, Level& L)
+{
+    const int n = L.n;
+    const int rule = lanes_for(n, L.P->nent);
+    if (!o_.autotune || n < 1024) return rule;
+    const int avg = int(std::lround(double(L.P->nent) / n));
+    int lg = 0;
+    while ((2LL << lg) <= n) ++lg;
+    const long long key = ((long long)(L.half ? 2 : sizeof(T)) << 40) | ((long long)lg << 20) | (long long)avg;
+    {
+        std::lock_guard<std::mutex> lk(tune_mutex());
+        auto it = tune_cache().find(key);
+        if (it != tune_cache().end()) return it->second;
+    }
+    tune_stop_.alloc(1);
+    tune_stop_.zero(s);
+    L.d0.zero(s);
+    L.r.zero(s);
+    cudaEvent_t a, b;
+    PORSOL_CUDA(cudaEventCreate(&a));
+    PORSOL_CUDA(cudaEventCreate(&b));
+    const SellPattern& P = *L.P;
+    auto step = [&](int lanes) {
+        const int nbk = div_up(n * lanes, TB);
+        if (L.half) {
+            PORSOL_LANES(lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, __half, true><<<nbk, TB, 0, s>>>(
+                                    n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, nullptr, L.d0.p, L.r.p,
+                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p))));
+        } else {
+            PORSOL_LANES(lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, T, false><<<nbk, TB, 0, s>>>(
+                                    n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, nullptr, L.d0.p, L.r.p,
+                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p))));
+        }
+    };
+    int best = rule;
+    float best_ms = 1e30f;
+    float rule_ms = 1e30f;
+    for (int lanes : {1, 2, 4, 8, 16}) {
+        step(lanes);   // warm-up
+        PORSOL_CUDA(cudaEventRecord(a, s));
+        for (int r = 0; r < 3; ++r) step(lanes);
+        PORSOL_CUDA(cudaEventRecord(b, s));
+        PORSOL_CUDA(cudaEventSynchronize(b));
+        float ms = 0.f;
+        PORSOL_CUDA(cudaEventElapsedTime(&ms, a, b));
+        if (lanes == rule) rule_ms = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = lanes;
+        }
+    }
+    if (best_ms > 0.9f * rule_ms) best = rule;   // keep the rule unless another schedule is clearly faster
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    PORSOL_CUDA(cudaGetLastError());
+    std::lock_guard<std::mutex> lk(tune_mutex());
+    tune_cache()[key] = best;
+    return best;
 }
 
 template <class T>
