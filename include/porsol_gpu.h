@@ -95,7 +95,7 @@ typedef struct porsol_solve_opts {
     double prolongate_factor;   /* 1.6    (:667) coarse-correction damping */
     int smooth_steps;           /* 1      (:668) pre/post smoothing sweeps */
     int precision;              /* PORSOL_FP64 */
-    double inner_tolerance;     /* mixed only: residual reduction per FP32 inner solve (1e-2) */
+    double inner_tolerance;     /* mixed only: residual drop that triggers an FP64 residual replacement (3e-3) */
     int max_outer;              /* mixed only: refinement steps before giving up (30) */
 } porsol_solve_opts;
 

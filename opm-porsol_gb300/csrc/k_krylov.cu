@@ -244,18 +244,6 @@ __global__ void k_axpy_add(int n, const double* __restrict__ y, double* __restri
     if (i < n) x[i] += y[i];
 }
 
-__global__ void k_to_f32_scaled(int n, const double* __restrict__ a, float* __restrict__ b, double scale)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = float(a[i] * scale);
-}
-
-__global__ void k_add_f32_scaled(int n, const float* __restrict__ y, double scale, double* __restrict__ x)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += scale * double(y[i]);
-}
-
 __global__ void k_dirichlet_guess(int n, const int* __restrict__ sp, const int* __restrict__ col,
                                   const int* __restrict__ rowlen, const double* __restrict__ val,
                                   const double* __restrict__ b, double* __restrict__ x)
@@ -282,6 +270,175 @@ __global__ void __launch_bounds__(RB) k_norm2(int n, const T* __restrict__ x, do
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += x[i] * x[i];
     double tot;
     if (block_reduce_last<T>(v, partial, counter, &tot)) *out = tot;
+}
+
+// ---------------- mixed-precision CG with reliable updates ----------------
+__device__ __forceinline__ void rc_publish(const RcDev* st, CgHostView* hv)
+{
+    hv->def0 = st->def0;
+    hv->def = st->true_def;
+    hv->iter = st->iter;
+    hv->converged = st->converged;
+    hv->breakdown = st->breakdown;
+    hv->stop = st->stop;
+    __threadfence_system();
+}
+
+// r64 = b - A x (FP64); def0 = sigma = ||r64||
+__global__ void __launch_bounds__(RB) k_rc_init(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                                const double* __restrict__ val, const double* __restrict__ x,
+                                                const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
+                                                double* partial, unsigned int* counter, CgHostView* hv)
+{
+    double v = 0.0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        const double ri = b[i] - sell_row(sp, col, val, x, i);
+        r64[i] = ri;
+        v += ri * ri;
+    }
+    double tot;
+    if (block_reduce_last<double>(v, partial, counter, &tot)) {
+        const double d = sqrt(tot);
+        st->def0 = st->true_def = st->sigma = d;
+        st->isig = d > 0.0 ? 1.0 / d : 0.0;
+        st->factor = 1.0;
+        st->iter = st->nrep = st->replace = st->breakdown = 0;
+        st->converged = (d < 1e-30) ? 1 : 0;
+        st->stop = st->converged || !isfinite(d);
+        st->breakdown = !isfinite(d);
+        rc_publish(st, hv);
+    }
+}
+
+// r32 = r64 / sigma; p *= factor (after a replacement, or at the start when p is unused)
+__global__ void k_rc_rescale(int n, const double* __restrict__ r64, float* __restrict__ r, float* __restrict__ p,
+                             const RcDev* st, int init)
+{
+    if (st->stop || !(init || st->replace)) return;
+    const double is = st->isig;
+    const float f = float(st->factor);
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        r[i] = float(r64[i] * is);
+        if (!init) p[i] *= f;
+    }
+}
+
+// q = A32 p; alpha = rho / (p . q)
+__global__ void __launch_bounds__(RB) k_rc_pq(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                              const float* __restrict__ val, const float* __restrict__ p,
+                                              float* __restrict__ q, RcDev* st, double* partial,
+                                              unsigned int* counter, CgHostView* hv)
+{
+    if (st->stop) return;
+    float v = 0.0f;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        const float qi = sell_row(sp, col, val, p, i);
+        q[i] = qi;
+        v += p[i] * qi;
+    }
+    double tot;
+    if (block_reduce_last<float>(v, partial, counter, &tot)) {
+        if (!(tot > 0.0) || !isfinite(tot)) {
+            st->alpha = 0.0;
+            st->breakdown = 1;
+            st->stop = 1;
+            rc_publish(st, hv);
+        } else {
+            st->alpha = st->rho / tot;
+        }
+    }
+}
+
+// x += sigma alpha p (FP64); r -= alpha q; decide on a replacement
+__global__ void __launch_bounds__(RB) k_rc_update(int n, double* __restrict__ x, float* __restrict__ r,
+                                                  const float* __restrict__ p, const float* __restrict__ q,
+                                                  RcDev* st, double* partial, unsigned int* counter,
+                                                  CgHostView* hv)
+{
+    if (st->stop) return;
+    const double sa = st->sigma * st->alpha;
+    const float a = float(st->alpha);
+    float v = 0.0f;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        x[i] += sa * double(p[i]);
+        const float ri = r[i] - a * q[i];
+        r[i] = ri;
+        v += ri * ri;
+    }
+    double tot;
+    if (block_reduce_last<float>(v, partial, counter, &tot)) {
+        const double defs = sqrt(tot);
+        st->defs = defs;
+        st->iter += 1;
+        const double est = defs * st->sigma;
+        st->replace = (defs < st->delta || est < st->tol * st->def0 || est < 1e-30 || !isfinite(defs) ||
+                       st->iter >= st->maxit)
+                          ? 1
+                          : 0;
+        hv->iter = st->iter;
+        __threadfence_system();
+    }
+}
+
+// Replacement: r64 = b - A x in FP64; convergence is decided on this true residual only
+__global__ void __launch_bounds__(RB) k_rc_true(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                                                const double* __restrict__ val, const double* __restrict__ x,
+                                                const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
+                                                double* partial, unsigned int* counter, CgHostView* hv)
+{
+    if (st->stop || !st->replace) return;
+    double v = 0.0;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
+        const double ri = b[i] - sell_row(sp, col, val, x, i);
+        r64[i] = ri;
+        v += ri * ri;
+    }
+    double tot;
+    if (block_reduce_last<double>(v, partial, counter, &tot)) {
+        const double d = sqrt(tot);
+        st->true_def = d;
+        st->nrep += 1;
+        if (!isfinite(d)) {
+            st->breakdown = 1;
+            st->stop = 1;
+        } else if (d < st->tol * st->def0 || d < 1e-30) {
+            st->converged = 1;
+            st->stop = 1;
+        } else if (st->iter >= st->maxit) {
+            st->stop = 1;
+        } else {
+            // continue on the rescaled system: r and p in units of the new sigma
+            st->factor = st->sigma / d;
+            st->rho *= st->factor * st->factor;
+            st->sigma = d;
+            st->isig = 1.0 / d;
+        }
+        rc_publish(st, hv);
+    }
+}
+
+// rho_new = z . r; beta = rho_new / rho
+__global__ void __launch_bounds__(RB) k_rc_zr(int n, const float* __restrict__ z, const float* __restrict__ r,
+                                              RcDev* st, double* partial, unsigned int* counter, int init)
+{
+    if (st->stop) return;
+    float v = 0.0f;
+    for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += z[i] * r[i];
+    double tot;
+    if (block_reduce_last<float>(v, partial, counter, &tot)) {
+        st->beta = init ? 0.0 : tot / st->rho;
+        st->rho = tot;
+        st->replace = 0;
+    }
+}
+
+// p = z + beta p (beta = 0 at the start)
+__global__ void k_rc_direction(int n, const float* __restrict__ z, float* __restrict__ p, const RcDev* st, int init)
+{
+    if (st->stop) return;
+    const float beta = float(st->beta);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = init ? z[i] : z[i] + beta * p[i];
 }
 
 // ---------------- ILU(0) ----------------
@@ -531,7 +688,129 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
 }
 
 template class PcgSolver<double, double>;
-template class PcgSolver<float, float>;
+
+// ---------------- ReliableCg host side ----------------
+void ReliableCg::setup(int n, cudaStream_t s)
+{
+    if (n != n_) {
+        r_.alloc(n);
+        z_.alloc(n);
+        p_.alloc(n);
+        q_.alloc(n);
+        r64_.alloc(n);
+        n_ = n;
+    }
+    st_.alloc(1);
+    red_.ensure(div_up(std::max(n, 1), RB), s);
+    if (!hview_) {
+        PORSOL_CUDA(cudaHostAlloc((void**)&hview_, sizeof(CgHostView), cudaHostAllocMapped));
+        PORSOL_CUDA(cudaHostGetDevicePointer((void**)&dview_, hview_, 0));
+    }
+    if (ev_.empty()) {
+        ev_.resize(4);
+        for (auto& e : ev_) PORSOL_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+}
+
+ReliableCg::~ReliableCg()
+{
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (hview_) cudaFreeHost(hview_);
+    for (auto& e : ev_) cudaEventDestroy(e);
+}
+
+void ReliableCg::iteration(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
+                           Precond<float>& M, const double* b, double* x)
+{
+    const int n = P.n, nb = div_up(n, RB), nr = red_blocks(n);
+    const int* stop = &st_.p->stop;
+    PORSOL_LAUNCH(k_rc_pq<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
+                                            red_.counter.p, dview_));
+    PORSOL_LAUNCH(k_rc_update<<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_));
+    PORSOL_LAUNCH(k_rc_true<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
+                                              red_.counter.p, dview_));
+    PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 0));
+    M.apply(s, r_.p, z_.p, stop);
+    PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 0));
+    PORSOL_LAUNCH(k_rc_direction<<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, 0));
+}
+
+CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
+                           Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta)
+{
+    const int n = P.n;
+    CgResult res;
+    if (n == 0) {
+        res.converged = true;
+        return res;
+    }
+    setup(n, s);
+    const int nb = div_up(n, RB), nr = red_blocks(n);
+    RcDev init{};
+    init.tol = tol;
+    init.maxit = maxit;
+    init.delta = delta;
+    PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(RcDev), cudaMemcpyHostToDevice, s));
+    PORSOL_LAUNCH(k_rc_init<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
+                                              red_.partial.p, red_.counter.p, dview_));
+    PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 1));
+    const int* stop = &st_.p->stop;
+    M.apply(s, r_.p, z_.p, stop);
+    PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 1));
+    PORSOL_LAUNCH(k_rc_direction<<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, 1));
+    PORSOL_CUDA(cudaGetLastError());
+    const void* key[5] = {&P, val64, val32, (const void*)&M, x};
+    bool same = exec_ && key_gen_ == M.generation() && key_[4] == (const void*)b;
+    for (int k = 0; k < 4 && same; ++k) same = key_[k] == key[k];
+    if (!same) {
+        if (exec_) {
+            cudaGraphExecDestroy(exec_);
+            exec_ = nullptr;
+        }
+        cudaGraph_t g;
+        const long long l0 = g_launches.load();
+        PORSOL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        iteration(s, P, val64, val32, M, b, x);
+        PORSOL_CUDA(cudaStreamEndCapture(s, &g));
+        nodes_ = g_launches.load() - l0;
+        g_launches.fetch_sub(nodes_);
+        PORSOL_CUDA(cudaGraphInstantiate(&exec_, g, 0));
+        PORSOL_CUDA(cudaGraphDestroy(g));
+        for (int k = 0; k < 4; ++k) key_[k] = key[k];
+        key_[4] = b;
+        key_gen_ = M.generation();
+    }
+    const int LOOKAHEAD = 2;
+    int it = 0;
+    bool done = false;
+    while (!done) {
+        if (it < maxit) {
+            PORSOL_CUDA(cudaGraphLaunch(exec_, s));
+            g_launches.fetch_add(nodes_);
+            PORSOL_CUDA(cudaEventRecord(ev_[it % ev_.size()], s));
+            ++it;
+        }
+        if (it >= LOOKAHEAD || it >= maxit) {
+            const int wait_it = (it >= maxit) ? it - 1 : it - LOOKAHEAD;
+            PORSOL_CUDA(cudaEventSynchronize(ev_[wait_it % ev_.size()]));
+            if (hview_->stop || it >= maxit) {
+                if (it >= maxit) PORSOL_CUDA(cudaStreamSynchronize(s));
+                done = hview_->stop || it >= maxit;
+            }
+        }
+    }
+    RcDev fin{};
+    PORSOL_CUDA(cudaMemcpyAsync(&fin, st_.p, sizeof(RcDev), cudaMemcpyDeviceToHost, s));
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    nrep_ = fin.nrep;
+    res.iterations = fin.iter;
+    res.def0 = fin.def0;
+    res.def = fin.true_def;
+    res.converged = fin.converged != 0;
+    res.breakdown = fin.breakdown != 0;
+    res.reduction = fin.def0 > 0 ? fin.true_def / fin.def0 : 0.0;
+    return res;
+}
 
 // ---------------- ILU(0) host side ----------------
 void Ilu0::build_levels(const SellPattern& P, cudaStream_t s)
@@ -639,19 +918,6 @@ void axpy_add(cudaStream_t s, int n, const double* y, double* x)
     PORSOL_CUDA(cudaGetLastError());
 }
 
-void to_f32_scaled(cudaStream_t s, int n, const double* a, float* b, double scale)
-{
-    if (n == 0) return;
-    PORSOL_LAUNCH(k_to_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, a, b, scale));
-    PORSOL_CUDA(cudaGetLastError());
-}
-
-void add_f32_scaled(cudaStream_t s, int n, const float* y, double scale, double* x)
-{
-    if (n == 0) return;
-    PORSOL_LAUNCH(k_add_f32_scaled<<<div_up(n, RB), RB, 0, s>>>(n, y, scale, x));
-    PORSOL_CUDA(cudaGetLastError());
-}
 
 void dirichlet_guess(cudaStream_t s, const SellPattern& P, const double* val, const double* b, double* x)
 {

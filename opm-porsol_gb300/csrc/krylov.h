@@ -83,6 +83,45 @@ private:
                    int prof_kernel);
 };
 
+// Mixed-precision CG with reliable updates (residual replacement; Sleijpen and van der Vorst,
+// "Reliable updated residuals in hybrid Bi-CG methods", Computing 56, 1996): one FP32 CG
+// recurrence (FP32 matrix copy, FP32 preconditioner) on the system scaled by sigma, the
+// solution accumulated in FP64 (x += sigma alpha p), and the iterated residual replaced by the
+// true FP64 residual b - A x whenever it has dropped by `delta` since the last replacement or
+// the estimate reaches the tolerance.  Unlike restarted iterative refinement the search
+// direction is kept across replacements (rescaled), so no Krylov information and no extra
+// preconditioner application is lost.  Stops when the true residual satisfies
+// ||b - A x|| < tol ||b - A x0|| (or < 1e-30).
+struct RcDev {
+    double rho, alpha, beta, sigma, isig, factor, def0, defs, tol, delta, true_def;
+    int iter, maxit, stop, converged, breakdown, replace, nrep, pad;
+};
+
+class ReliableCg {
+public:
+    CgResult solve(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
+                   Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta);
+    int replacements() const { return nrep_; }
+    ~ReliableCg();
+
+private:
+    int n_ = 0, nrep_ = 0;
+    DBuf<float> r_, z_, p_, q_;
+    DBuf<double> r64_;
+    DBuf<RcDev> st_;
+    RedScratch red_;
+    CgHostView* hview_ = nullptr;
+    CgHostView* dview_ = nullptr;
+    std::vector<cudaEvent_t> ev_;
+    cudaGraphExec_t exec_ = nullptr;
+    const void* key_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    long long key_gen_ = -1;
+    long long nodes_ = 0;
+    void setup(int n, cudaStream_t s);
+    void iteration(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32, Precond<float>& M,
+                   const double* b, double* x);
+};
+
 // ILU(0) with the pivots stored inverted, factor and triangular solves level-scheduled
 // (rows of one level are independent).  The algorithm of dune-istl's SeqILU0 with
 // relaxation 1 (IncompFlowSolverHybrid.hpp:1404).
@@ -108,9 +147,6 @@ template <class TA, class TB>
 void convert(cudaStream_t s, long long n, const TA* a, TB* b);
 // x += y (FP64)
 void axpy_add(cudaStream_t s, int n, const double* y, double* x);
-// b = float(a * scale);  x += scale * double(y)
-void to_f32_scaled(cudaStream_t s, int n, const double* a, float* b, double scale);
-void add_f32_scaled(cudaStream_t s, int n, const float* y, double scale, double* x);
 // Dirichlet-row initial guess (IncompFlowSolverHybrid.hpp:1521-1532): x_i = b_i / a_ii
 // where all off-diagonal entries of row i are zero, else 0.
 void dirichlet_guess(cudaStream_t s, const SellPattern& P, const double* val, const double* b, double* x);

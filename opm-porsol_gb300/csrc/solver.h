@@ -51,14 +51,14 @@ struct porsol_solver {
 
     // linear solvers
     porsol::PcgSolver<double, double> cg64;
-    porsol::PcgSolver<float, float> cg32;
+    porsol::ReliableCg rcg;
     porsol::Ilu0 ilu;
     bool ilu_levels = false;
     porsol::Amg<double> amg64;
     porsol::Amg<float> amg32;
     bool amg_ready = false;
     int amg_precision = -1;
-    porsol::DBuf<double> ir_r, ir_d;   // iterative refinement
+    porsol::DBuf<double> ir_r;   // batched iterative refinement
     porsol::DBuf<float> ir_r32, ir_d32;
     porsol::RedScratch red;
 
