@@ -96,7 +96,7 @@ typedef struct porsol_solve_opts {
     int smooth_steps;           /* 1      (:668) pre/post smoothing sweeps */
     int precision;              /* PORSOL_FP64 */
     double inner_tolerance;     /* mixed only: residual drop that triggers an FP64 residual replacement (3e-3) */
-    int max_outer;              /* mixed only: refinement steps before giving up (30) */
+    int max_outer;              /* mixed batched upscaling only: refinement steps before giving up (30) */
 } porsol_solve_opts;
 
 typedef struct porsol_solve_stats {
