@@ -326,7 +326,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     st.ms_precond_setup = now_ms() - t_begin;
     st.amg_levels = amg32.levels();
     const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 3e-3;
-    CgResult r = rcg.solve(stream, P, val.p, val32.p, amg32, rhs.p, x.p, o.residual_tolerance, maxit, inner_tol);
+    CgResult r = rcg.solve(stream, P, val.p, val32.p, amg32, rhs.p, x.p, o.residual_tolerance, maxit, inner_tol, &prof);
     st.iterations = r.iterations;
     st.outer_iterations = rcg.replacements();
     st.reduction = r.reduction;
@@ -410,7 +410,8 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     };
     norms(r0);
     rn = r0;
-    const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 3e-3;
+    // restarted per-block refinement: each restart needs a 1e-3 drop to pay for itself
+    const double inner_tol = std::min(o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3, 1e-3);
     const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
     int total = 0, outer = 0;
     auto worst = [&]() {

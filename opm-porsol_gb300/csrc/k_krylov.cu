@@ -720,12 +720,19 @@ ReliableCg::~ReliableCg()
 }
 
 void ReliableCg::iteration(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
-                           Precond<float>& M, const double* b, double* x)
+                           Precond<float>& M, const double* b, double* x, Profiler* prof)
 {
     const int n = P.n, nb = div_up(n, RB), nr = red_blocks(n);
     const int* stop = &st_.p->stop;
-    PORSOL_LAUNCH(k_rc_pq<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
-                                            red_.counter.p, dview_));
+    {
+        const bool pf = prof && prof->on;
+        const double bytes = double(P.nent) * 8.0 + 2.0 * n * 4.0;
+        cudaEvent_t ev = nullptr;
+        if (pf) prof->begin(s, PK_SPMV32, bytes, &ev);
+        PORSOL_LAUNCH(k_rc_pq<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
+                                                red_.counter.p, dview_));
+        if (pf) prof->end(s, PK_SPMV32, bytes, ev);
+    }
     PORSOL_LAUNCH(k_rc_update<<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_));
     PORSOL_LAUNCH(k_rc_true<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
                                               red_.counter.p, dview_));
@@ -736,7 +743,8 @@ void ReliableCg::iteration(cudaStream_t s, const SellPattern& P, const double* v
 }
 
 CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
-                           Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta)
+                           Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta,
+                           Profiler* prof)
 {
     const int n = P.n;
     CgResult res;
@@ -759,10 +767,12 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
     PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 1));
     PORSOL_LAUNCH(k_rc_direction<<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, 1));
     PORSOL_CUDA(cudaGetLastError());
+    // per-kernel event timing records events inside the V-cycle: no graph capture then
+    const bool graphs = !(prof && prof->on);
     const void* key[5] = {&P, val64, val32, (const void*)&M, x};
     bool same = exec_ && key_gen_ == M.generation() && key_[4] == (const void*)b;
     for (int k = 0; k < 4 && same; ++k) same = key_[k] == key[k];
-    if (!same) {
+    if (graphs && !same) {
         if (exec_) {
             cudaGraphExecDestroy(exec_);
             exec_ = nullptr;
@@ -770,7 +780,7 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
         cudaGraph_t g;
         const long long l0 = g_launches.load();
         PORSOL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        iteration(s, P, val64, val32, M, b, x);
+        iteration(s, P, val64, val32, M, b, x, nullptr);
         PORSOL_CUDA(cudaStreamEndCapture(s, &g));
         nodes_ = g_launches.load() - l0;
         g_launches.fetch_sub(nodes_);
@@ -785,8 +795,12 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
     bool done = false;
     while (!done) {
         if (it < maxit) {
-            PORSOL_CUDA(cudaGraphLaunch(exec_, s));
-            g_launches.fetch_add(nodes_);
+            if (graphs) {
+                PORSOL_CUDA(cudaGraphLaunch(exec_, s));
+                g_launches.fetch_add(nodes_);
+            } else {
+                iteration(s, P, val64, val32, M, b, x, prof);
+            }
             PORSOL_CUDA(cudaEventRecord(ev_[it % ev_.size()], s));
             ++it;
         }

@@ -99,8 +99,10 @@ struct RcDev {
 
 class ReliableCg {
 public:
+    // prof (may be null): when per-kernel event timing is on, iterations run uncaptured
     CgResult solve(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
-                   Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta);
+                   Precond<float>& M, const double* b, double* x, double tol, int maxit, double delta,
+                   Profiler* prof = nullptr);
     int replacements() const { return nrep_; }
     ~ReliableCg();
 
@@ -119,7 +121,7 @@ private:
     long long nodes_ = 0;
     void setup(int n, cudaStream_t s);
     void iteration(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32, Precond<float>& M,
-                   const double* b, double* x);
+                   const double* b, double* x, Profiler* prof);
 };
 
 // ILU(0) with the pivots stored inverted, factor and triangular solves level-scheduled
