@@ -279,6 +279,81 @@ int porsol_transport_solve_device(porsol_transport* t, double* sat, double time,
                                   const double* outflux, const double* injection,
                                   porsol_transport_stats* stats);
 
+/* Rock tables (RockJfunc, common/RockJfunc.hpp:63-216, read by
+ * ReservoirPropertyCommon::readRocks, ReservoirPropertyCommon_impl.hpp:785-805): rows
+ * table_pos[r] .. table_pos[r+1]-1 of the columns (s, krw, kro, jfunc) are the table of rock
+ * r, s non-decreasing and jfunc monotone within a rock; cell_rock[c] is the rock of cell c
+ * (cell_to_rock_, 0-based).  As the reader does, krw is set to 0 at the first row and kro
+ * to 0 at the last row of each table.  With use_jfunction_scaling the capillary pressure
+ * is J(s) sigma_cos_theta / sqrt(tr K / (3 phi)), else the jfunc column itself.  The
+ * tables are piecewise linear with the end value outside the table. */
+typedef struct porsol_rock_tables {
+    int num_rocks;
+    const int* table_pos;       /* [num_rocks + 1] */
+    const double* s;
+    const double* krw;
+    const double* kro;
+    const double* jfunc;
+    const int* cell_rock;       /* [num_cells] */
+    int use_jfunction_scaling;  /* 1 */
+    double sigma_cos_theta;     /* 1.0 (RockJfunc::setSigmaAndTheta: sigma cos(theta)) */
+} porsol_rock_tables;
+
+/* ReservoirPropertyCapillary with rock tables (ReservoirPropertyCapillary_impl.hpp:118-282,
+ * ReservoirPropertyCommon_impl.hpp:466-528): from now on the transport solver's phase
+ * mobilities are krw/visc1 and kro/visc2 from the tables, the capillary pressure is the
+ * table's, and the CFL factors (incl. the capillary one) are recomputed per rock.
+ * NULL returns to kr1 = s^2, kr2 = (1-s)^2, pc = 1e5 (1-s).  PORSOL_ERR_BAD_ARG for
+ * malformed tables. */
+int porsol_transport_set_rock_tables(porsol_transport* t, const porsol_rock_tables* rocks);
+
+/* ImplicitCapillarity parameters (euler/ImplicitCapillarity_impl.hpp:57-68, 91-101). */
+typedef struct porsol_capillary_opts {
+    int method_viscous, method_gravity;   /* 1, 1 */
+    int check_sat, clamp_sat;             /* 1, 0 */
+    double residual_tolerance;            /* 1e-8 */
+    int linsolver_verbosity;              /* 1 */
+    int linsolver_type;                   /* 1 */
+    double update_relaxation;             /* 1.0 */
+    int precision;                        /* PORSOL_FP64 (PORSOL_MIXED for the capillary pressure solve) */
+} porsol_capillary_opts;
+
+typedef struct porsol_capillary_stats {
+    double shift;                  /* constant added to the capillary pressure (mod_correct) */
+    int root_iterations;           /* regula falsi iterations */
+    int evaluations;               /* saturation-volume evaluations (bracket search included) */
+    porsol_solve_stats pressure;   /* the capillary pressure solve */
+} porsol_capillary_stats;
+
+void porsol_capillary_opts_default(porsol_capillary_opts* opts);
+
+/* ImplicitCapillarity::transportSolve (euler/ImplicitCapillarity_impl.hpp:138-226): capillary
+ * mobilities lambda_1 lambda_2 / (lambda_1 + lambda_2) (at least 1e-10), the viscous/gravity
+ * upstream residual of the transport solver t as source, a pressure solve on p with those
+ * fixed mobilities and the flow BCs (periodic jumps set to 0) for the capillary pressure, then
+ * the constant shift of the capillary pressure that keeps the pore-volume-weighted saturation
+ * (MatchSaturatedVolumeFunctor.hpp:49-112), found by a bracket search from 0 with step
+ * max(pc) - min(pc) and regula falsi (40 iterations, |residual| <= 1e-12); the new
+ * saturation is the inverse capillary-pressure curve at the shifted pressure, relaxed by
+ * update_relaxation, then checked/clamped as transportSolve does.
+ * p: a pressure solver initialised on the same grid and flow-BC topology with zero gravity
+ * (the reference's inner solver, :80-83).  t: a transport solver on that grid, normally with
+ * rock tables (without them the inverse curve is 0 everywhere, as in the reference).
+ * sat [nc] in/out (unchanged on failure), outflux [nhf] half-face fluxes of the pressure
+ * solution, injection [nc] (may be NULL), hf_flow_type/value the flow BCs.
+ * PORSOL_ERR_NOT_CONVERGED if no shift is bracketed or regula falsi runs out of iterations
+ * (or the pressure solve fails); PORSOL_ERR_SAT_RANGE when the saturation leaves
+ * [-0.001, 1.001] without clamp_sat. */
+int porsol_capillary_solve(porsol_transport* t, porsol_solver* p, double* sat, const double* grav,
+                           const double* outflux, const double* injection, const int* hf_flow_type,
+                           const double* hf_flow_value, const porsol_capillary_opts* opts,
+                           porsol_capillary_stats* stats);
+/* As porsol_capillary_solve with device pointers for every array (grav stays a host [3]). */
+int porsol_capillary_solve_device(porsol_transport* t, porsol_solver* p, double* sat, const double* grav,
+                                  const double* outflux, const double* injection, const int* hf_flow_type,
+                                  const double* hf_flow_value, const porsol_capillary_opts* opts,
+                                  porsol_capillary_stats* stats);
+
 /* No counterpart in the reference.  The viscous CFL time step of the transport solver
  * (the quantity findCFLtimeVelocity bounds, before the Courant factor), for callers that may
  * not allocate device memory when they need it -- e.g. a simulator whose device memory is

@@ -25,8 +25,8 @@ LIB_PATH = os.path.join(LIB_DIR, "libporsol_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE, "-I", CSRC]
-SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_adjoint.cu", "k_batch.cu", "capi.cu",
-           "noalloc_cfl.cu"]
+SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_capillary.cu", "k_adjoint.cu",
+           "k_batch.cu", "capi.cu", "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
 FLUID_CELLWISE, FLUID_COREY2, FLUID_TENSOR = 0, 1, 2
@@ -110,6 +110,23 @@ class TransportStats(C.Structure):
     _fields_ = [("small_steps", C.c_int), ("repeats", C.c_int), ("cfl_dt", C.c_double)]
 
 
+class RockTablesStruct(C.Structure):
+    _fields_ = [("num_rocks", C.c_int), ("table_pos", C.c_void_p), ("s", C.c_void_p), ("krw", C.c_void_p),
+                ("kro", C.c_void_p), ("jfunc", C.c_void_p), ("cell_rock", C.c_void_p),
+                ("use_jfunction_scaling", C.c_int), ("sigma_cos_theta", C.c_double)]
+
+
+class CapillaryOpts(C.Structure):
+    _fields_ = [("method_viscous", C.c_int), ("method_gravity", C.c_int), ("check_sat", C.c_int),
+                ("clamp_sat", C.c_int), ("residual_tolerance", C.c_double), ("linsolver_verbosity", C.c_int),
+                ("linsolver_type", C.c_int), ("update_relaxation", C.c_double), ("precision", C.c_int)]
+
+
+class CapillaryStats(C.Structure):
+    _fields_ = [("shift", C.c_double), ("root_iterations", C.c_int), ("evaluations", C.c_int),
+                ("pressure", SolveStats)]
+
+
 # (name, restype, argtypes) of every exported entry point of include/porsol_gpu.h
 _vp, _i, _d = C.c_void_p, C.c_int, C.c_double
 EXPORTS = [
@@ -149,6 +166,12 @@ EXPORTS = [
                                    C.POINTER(TransportOpts)]),
     ("porsol_transport_solve", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
     ("porsol_transport_solve_device", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
+    ("porsol_transport_set_rock_tables", _i, [_vp, C.POINTER(RockTablesStruct)]),
+    ("porsol_capillary_opts_default", None, [C.POINTER(CapillaryOpts)]),
+    ("porsol_capillary_solve", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(CapillaryOpts),
+                                    C.POINTER(CapillaryStats)]),
+    ("porsol_capillary_solve_device", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(CapillaryOpts),
+                                           C.POINTER(CapillaryStats)]),
     ("porsol_profile_enable", _i, [_vp, _i]),
     ("porsol_profile_get", _i, [_vp, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_d)]),
     ("porsol_profile_reset", _i, [_vp]),
@@ -215,6 +238,14 @@ def write_field(field, filename):
 def default_solve_opts(**kw) -> SolveOpts:
     o = SolveOpts()
     lib().porsol_solve_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def default_capillary_opts(**kw) -> CapillaryOpts:
+    o = CapillaryOpts()
+    lib().porsol_capillary_opts_default(C.byref(o))
     for k, v in kw.items():
         setattr(o, k, v)
     return o
@@ -450,5 +481,32 @@ class TransportSolver:
         g = _f64(grav)
         inj = None if injection is None else _f64(injection)
         self._check(lib().porsol_transport_solve(self.h, _p(s), float(time), _p(g), _p(_f64(outflux)), _p(inj),
+                                                 C.byref(st)))
+        return s, st
+
+    def set_rock_tables(self, tables, cell_rock, use_jfunction_scaling=True, sigma_cos_theta=1.0):
+        """RockJfunc tables: ``tables`` a list of (n, 4) arrays (columns s, krw, kro, J), one per rock;
+        ``cell_rock`` the rock of every cell.  ``tables=None`` returns to Corey-2."""
+        if tables is None:
+            self._check(lib().porsol_transport_set_rock_tables(self.h, None))
+            return
+        arrs = [np.asarray(x, np.float64).reshape(-1, 4) for x in tables]
+        cat = np.concatenate(arrs)
+        pos = np.cumsum([0] + [len(a) for a in arrs]).astype(np.int32)
+        cols = [np.ascontiguousarray(cat[:, k]) for k in range(4)]
+        cell = _i32(cell_rock)
+        rt = RockTablesStruct(len(arrs), _p(pos), *(_p(c) for c in cols), _p(cell),
+                              1 if use_jfunction_scaling else 0, float(sigma_cos_theta))
+        self._check(lib().porsol_transport_set_rock_tables(self.h, C.byref(rt)))
+
+    def capillary_solve(self, pressure: "PressureSolver", sat, outflux, bc_type, bc_value, injection=None,
+                        grav=(0.0, 0.0, 0.0), opts=None):
+        """ImplicitCapillarity::transportSolve: returns (new saturation, CapillaryStats)."""
+        s = _f64(sat).copy()
+        st = CapillaryStats()
+        o = opts if opts is not None else default_capillary_opts()
+        inj = None if injection is None else _f64(injection)
+        self._check(lib().porsol_capillary_solve(self.h, pressure.h, _p(s), _p(_f64(grav)), _p(_f64(outflux)),
+                                                 _p(inj), _p(_i32(bc_type)), _p(_f64(bc_value)), C.byref(o),
                                                  C.byref(st)))
         return s, st

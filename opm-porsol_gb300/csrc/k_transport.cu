@@ -4,9 +4,10 @@
 // checkAndPossiblyClampSat (euler/EulerUpstream_impl.hpp:153-385), the residual of
 // EulerUpstreamResidual (euler/EulerUpstreamResidual_impl.hpp:101-300, 475-547) and the
 // CFL estimates of cfl_calculator (euler/CflCalculator.hpp:55-170), for the scalar
-// two-phase model of ReservoirPropertyCapillary without rock tables (kr1 = s^2,
-// kr2 = (1-s)^2, pc = 1e5 (1-s); ReservoirPropertyCapillary_impl.hpp:118-170,
-// ReservoirPropertyCommon_impl.hpp:466-476).
+// two-phase model of ReservoirPropertyCapillary: with rock tables (RockJfunc, rock.cuh) or
+// without (kr1 = s^2, kr2 = (1-s)^2, pc = 1e5 (1-s); ReservoirPropertyCapillary_impl.hpp:
+// 118-170, ReservoirPropertyCommon_impl.hpp:466-476).  Kernels are instantiated for both
+// (template flag TAB), so the table-free path keeps its closed-form arithmetic.
 //
 // Layout: every face that contributes is one "face entry" (the reference visits each
 // internal/periodic face once, from the lower cell index, and every Dirichlet boundary
@@ -23,6 +24,7 @@
 #include "kernels.h"
 #include "porsol_internal.h"
 #include "structure.h"
+#include "transport.h"
 
 using namespace porsol;
 
@@ -30,28 +32,11 @@ namespace {
 
 constexpr int TB = 256;
 
-struct FaceEntry {
-    int c0, c1, hf;     // cells (c1 == c0 on Dirichlet faces) and the half-face of c0
-    int dirichlet;
-    double satbc;       // Dirichlet saturation
-    double G;           // A n . (Kavg g) (rho1 - rho2)
-    double capf;        // A n . (Kavg e) / (d0 + d1), e the unit centre-to-centre direction
-    double nn;          // n . n
-};
-
-// kr_i / mu_i with the reciprocal viscosities precomputed (FP64 division is a multi-FMA
-// sequence on this GPU; the products differ from the quotients by at most one rounding)
-__device__ __forceinline__ double mob1(double s, double imu1) { return (s * s) * imu1; }
-__device__ __forceinline__ double mob2(double s, double imu2) { return ((1.0 - s) * (1.0 - s)) * imu2; }
-
-struct TrParams {
-    double mu1, mu2;   // reciprocal viscosities 1/mu1, 1/mu2
-    int visc, grav, cap;
-};
-
-// UpdateForCell::operator() for one face (EulerUpstreamResidual_impl.hpp:101-291), scalar mobilities
+// UpdateForCell::operator() for one face (EulerUpstreamResidual_impl.hpp:101-291), scalar
+// mobilities evaluated in the upstream cell (the boundary cell on Dirichlet faces)
+template <bool TAB>
 __global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const double* __restrict__ sat,
-                          const double* __restrict__ flux, TrParams p, double* __restrict__ dS,
+                          const double* __restrict__ flux, TrParams p, RockView R, double* __restrict__ dS,
                           const int* __restrict__ status)
 {
     if (*status) return;
@@ -64,21 +49,34 @@ __global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const doubl
     const double G = p.grav ? e.G : 0.0;
     const int triv = G >= 0.0 ? 0 : 1;
     const double sup = (q >= 0.0) ? s0 : s1;
+    const int cup = (q >= 0.0) ? e.c0 : e.c1;
     double m[2];
-    m[triv] = triv == 0 ? mob1(sup, p.mu1) : mob2(sup, p.mu2);
+    m[triv] = mobp<TAB>(triv, cup, sup, p, R);
     const double signG = triv == 0 ? -1.0 : 1.0;
     const double gnt = signG * m[triv] * G;
     const double supn = (q + gnt >= 0.0) ? s0 : s1;
+    const int cupn = (q + gnt >= 0.0) ? e.c0 : e.c1;
     const int nt = 1 - triv;
-    m[nt] = nt == 0 ? mob1(supn, p.mu1) : mob2(supn, p.mu2);
+    m[nt] = mobp<TAB>(nt, cupn, supn, p, R);
     const double mtinv = 1.0 / (m[0] + m[1]);
     double d = 0.0;
     if (p.visc) d += m[0] * mtinv * q * e.nn;
     if (p.grav && !e.dirichlet) d += m[0] * mtinv * m[1] * G;
     if (p.cap && e.capf != 0.0) {
         const double as = 0.5 * (s0 + s1);
-        const double a1 = mob1(as, p.mu1), a2 = mob2(as, p.mu2);
-        const double cp0 = 1e5 * (1.0 - s0), cp1 = 1e5 * (1.0 - s1);
+        double a1, a2, cp0, cp1;
+        if (TAB) {
+            // mobilities at the mean saturation averaged over both cells' rocks (:226-236)
+            a1 = 0.5 * (mobp<TAB>(0, e.c0, as, p, R) + mobp<TAB>(0, e.c1, as, p, R));
+            a2 = 0.5 * (mobp<TAB>(1, e.c0, as, p, R) + mobp<TAB>(1, e.c1, as, p, R));
+            cp0 = rock_pc(R, e.c0, s0);
+            cp1 = rock_pc(R, e.c1, s1);
+        } else {
+            a1 = mob1(as, p.mu1);
+            a2 = mob2(as, p.mu2);
+            cp0 = 1e5 * (1.0 - s0);
+            cp1 = 1e5 * (1.0 - s1);
+        }
         d += a1 * (1.0 / (a1 + a2)) * a2 * e.capf * (cp1 - cp0);
     }
     dS[k] = d;
@@ -86,24 +84,27 @@ __global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const doubl
 
 // Fractional flow lambda_1 / (lambda_1 + lambda_2), evaluated with the same operations as the
 // viscous term of k_face_dS (m1 * (1 / (m1 + m2))), so the fast path below is bitwise equal.
-__device__ __forceinline__ double frac1(double s, const TrParams& p)
+template <bool TAB>
+__device__ __forceinline__ double frac1(int c, double s, const TrParams& p, const RockView& R)
 {
-    const double m0 = mob1(s, p.mu1), m1 = mob2(s, p.mu2);
+    const double m0 = mobp<TAB>(0, c, s, p, R), m1 = mobp<TAB>(1, c, s, p, R);
     return m0 * (1.0 / (m0 + m1));
 }
 
-__global__ void k_frac_init(int nc, const double* __restrict__ sat, TrParams p, double* __restrict__ frac)
+template <bool TAB>
+__global__ void k_frac_init(int nc, const double* __restrict__ sat, TrParams p, RockView R, double* __restrict__ frac)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < nc) frac[c] = frac1(sat[c], p);
+    if (c < nc) frac[c] = frac1<TAB>(c, sat[c], p, R);
 }
 
 // Viscous-only sub-step (no gravity driving force, no capillary term): both phase mobilities
 // come from the same upstream cell, so the face term is f(s_up) q n.n with f precomputed per
 // cell (one FP64 division per cell instead of one per face; GB300's FP64 rate makes the
 // per-face form compute-bound).
+template <bool TAB>
 __global__ void k_face_dS_visc(int nfe, const FaceEntry* __restrict__ fe, const double* __restrict__ frac,
-                               const double* __restrict__ flux, TrParams p, double* __restrict__ dS,
+                               const double* __restrict__ flux, TrParams p, RockView R, double* __restrict__ dS,
                                const int* __restrict__ status)
 {
     if (*status) return;
@@ -113,15 +114,16 @@ __global__ void k_face_dS_visc(int nfe, const FaceEntry* __restrict__ fe, const 
     const double q = flux[hf];
     double f;
     if (q >= 0.0) f = frac[c0];
-    else f = dir ? frac1(fe[k].satbc, p) : frac[c1];
+    else f = dir ? frac1<TAB>(c0, fe[k].satbc, p, R) : frac[c1];
     dS[k] = f * q * fe[k].nn;
 }
 
 // residual gather + smallTimeStep update + checkAndPossiblyClampSat
+template <bool TAB>
 __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* __restrict__ cent,
                               const double* __restrict__ dS, const double* __restrict__ inj,
-                              const double* __restrict__ ipv, TrParams p, double dt, int check, int clamp,
-                              double* __restrict__ sat, double* __restrict__ frac, int* status)
+                              const double* __restrict__ ipv, TrParams p, RockView R, double dt, int check,
+                              int clamp, double* __restrict__ sat, double* __restrict__ frac, int* status)
 {
     if (*status) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -135,7 +137,7 @@ __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* _
     if (inj) {
         double rate = inj[c];
         if (rate < 0.0) {
-            const double l1 = mob1(s, p.mu1), l2 = mob2(s, p.mu2);
+            const double l1 = mobp<TAB>(0, c, s, p, R), l2 = mobp<TAB>(1, c, s, p, R);
             rate *= l1 / (l1 + l2);
         }
         r += rate;
@@ -151,7 +153,7 @@ __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* _
     }
     if (!isfinite(sn)) atomicOr(status, ST_NONFINITE);
     sat[c] = sn;
-    if (frac) frac[c] = frac1(sn, p);   // for the next viscous-only sub-step
+    if (frac) frac[c] = frac1<TAB>(c, sn, p, R);   // for the next viscous-only sub-step
 }
 
 __device__ __forceinline__ void atomic_min_pos(unsigned long long* a, double v)
@@ -210,53 +212,42 @@ __global__ void k_cfl_cells(int nc, const int* __restrict__ facepos, const doubl
 
 }  // namespace
 
-struct porsol_transport {
-    cudaStream_t stream = nullptr;
-    int device = 0;
-    std::string err;
-    bool ready = false;
-    HostGrid g;
-    std::vector<double> perm, poro;
-    std::vector<int> st;
-    std::vector<double> sv;
-    std::vector<int> pbid;
-    porsol_fluid fluid{};
-    porsol_transport_opts o{};
-    double fac[3] = {0, 0, 0};
-    std::vector<int> bid_to_face;   // last periodic half-face with each bid
-    std::vector<int> hf_cell;
-    std::vector<FaceEntry> fe_h;
-    double grav_cached[3] = {NAN, NAN, NAN};
-    DBuf<FaceEntry> fe;
-    DBuf<int> cptr, cent, facepos, status;
-    DBuf<double> ipv, vol, poro_d, dS, sat0, gflux_hf, in_sat, in_flux, in_inj, frac;
-    bool any_gravity = false;   // some face entry has a non-zero gravity driving force
-    DBuf<unsigned long long> red;
-
-    void init(const porsol_grid* grid, const double* K, const double* phi, const porsol_fluid* fl, const int* stype,
-              const double* sval, const int* partner, const porsol_transport_opts* opts);
-    void build_entries(const double* grav);
-    void solve(double* sat, double time, const double* grav, const double* flux, const double* inj,
-               porsol_transport_stats* stats, bool dev);
-};
-
 namespace {
 
-// ReservoirPropertyCapillary::computeSingleRockCflFactors(-1, 0, 0)
-// (ReservoirPropertyCapillary_impl.hpp:215-260): 257-point sampling of the fractional
-// flow and the gravity flow function.
-void cfl_factors(double mu1, double mu2, double* out)
+// ReservoirPropertyCapillary::computeSingleRockCflFactors (ReservoirPropertyCapillary_impl.hpp:
+// 213-250): 257-point sampling of the fractional flow, the gravity flow function and, with a
+// rock table (rock >= 0), the capillary-pressure derivative at min_perm I and max_poro.
+void single_rock_cfl(double mu1, double mu2, const RockView* R, int rock, double min_perm, double max_poro,
+                     double* out)
 {
     const int N = 257;
     const double delta = 1.0 / double(N - 1);
+    int a = 0, n = 0;
+    if (rock >= 0) {
+        a = R->pos[rock];
+        n = R->pos[rock + 1] - a;
+    }
     auto ff = [&](double s, double& f1, double& fg) {
-        const double l1 = (s * s) / mu1, l2 = ((1 - s) * (1 - s)) / mu2;
+        double l1, l2;
+        if (rock < 0) {
+            l1 = (s * s) / mu1;
+            l2 = ((1 - s) * (1 - s)) / mu2;
+        } else {
+            l1 = tab_value(R->s + a, R->krw + a, n, s) / mu1;
+            l2 = tab_value(R->s + a, R->kro + a, n, s) / mu2;
+        }
         f1 = l1 / (l1 + l2);
         fg = l1 * l2 / (l1 + l2);
+    };
+    // RockJfunc::capPressDeriv (common/RockJfunc.hpp:110-123) for perm = min_perm I
+    auto dpc = [&](double s) {
+        const double d = tab_slope(R->s + a, R->J + a, n, s);
+        return R->jscale ? d * R->sct / std::sqrt(3 * min_perm / (3 * max_poro)) : d;
     };
     double last1, lastg, md1 = -1e100, mdg = -1e100;
     ff(0.0, last1, lastg);
     double maxffg = lastg;
+    double mdpc = rock < 0 ? 0.0 : std::fabs(dpc(0.0));
     for (int i = 1; i < N; ++i) {
         const double s = double(i) * delta;
         double f1, fg;
@@ -264,15 +255,173 @@ void cfl_factors(double mu1, double mu2, double* out)
         md1 = std::max(md1, std::fabs(f1 - last1) / delta);
         mdg = std::max(mdg, std::fabs(fg - lastg) / delta);
         maxffg = std::max(maxffg, fg);
+        if (rock >= 0) mdpc = std::max(mdpc, std::fabs(dpc(s)));
         last1 = f1;
         lastg = fg;
     }
     out[0] = 1.0 / md1;
     out[1] = 1.0 / mdg;
-    out[2] = maxffg * 0.0;   // no rock table: zero capillary-pressure derivative bound
+    out[2] = maxffg * mdpc;   // 0 without a rock table
 }
 
 }  // namespace
+
+namespace porsol {
+
+void launch_face_dS(cudaStream_t s, int nfe, const FaceEntry* fe, const double* sat, const double* flux,
+                    const TrParams& p, const RockView& R, double* dS, const int* status)
+{
+    if (R.nrock > 0) PORSOL_LAUNCH(k_face_dS<true><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe, sat, flux, p, R, dS, status));
+    else PORSOL_LAUNCH(k_face_dS<false><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe, sat, flux, p, R, dS, status));
+}
+
+}  // namespace porsol
+
+// ReservoirPropertyCapillary::computeCflFactors (ReservoirPropertyCapillary_impl.hpp:255-282):
+// per rock the smallest mean diagonal permeability and the largest porosity of its cells, the
+// most restrictive factors over the rocks; then findCFLtimeCapillary (CflCalculator.hpp:
+// 143-170), which depends on geometry, permeability and that factor only.
+void porsol_transport::compute_cfl_factors()
+{
+    const double mu1 = fluid.viscosity1, mu2 = fluid.viscosity2;
+    dt_capillary = 1e100;
+    if (rock_h.nrock == 0) {
+        single_rock_cfl(mu1, mu2, nullptr, -1, 0.0, 0.0, fac);
+        return;
+    }
+    const int nr = rock_h.nrock, nc = g.nc;
+    std::vector<double> min_perm(nr, 1e100), max_poro(nr, 0.0);
+    for (int c = 0; c < nc; ++c) {
+        const int r = rk_cell_h[c];
+        const double* K = &perm[9 * size_t(c)];
+        min_perm[r] = std::min(min_perm[r], (K[0] + K[4] + K[8]) / 3.0);
+        max_poro[r] = std::max(max_poro[r], poro[c]);
+    }
+    fac[0] = 1e100;
+    fac[1] = 1e100;
+    fac[2] = 0.0;
+    for (int r = 0; r < nr; ++r) {
+        double f[3];
+        single_rock_cfl(mu1, mu2, &rock_h, r, min_perm[r], max_poro[r], f);
+        fac[0] = std::min(fac[0], f[0]);
+        fac[1] = std::min(fac[1], f[1]);
+        fac[2] = std::max(fac[2], f[2]);
+    }
+    double dt = 1e100;
+    for (int c = 0; c < nc; ++c)
+        for (int f = g.facepos[c]; f < g.facepos[c + 1]; ++f) {
+            double Kl[9];
+            const int c1 = g.nb[f];
+            for (int k = 0; k < 9; ++k)
+                Kl[k] = g.boundary(f) ? perm[9 * size_t(c) + k]
+                                      : 0.5 * (perm[9 * size_t(c) + k] + perm[9 * size_t(c1) + k]);
+            // inverse3x3 (MatrixInverse.hpp:85) by cofactors
+            const double det = Kl[0] * (Kl[4] * Kl[8] - Kl[5] * Kl[7]) - Kl[1] * (Kl[3] * Kl[8] - Kl[5] * Kl[6]) +
+                               Kl[2] * (Kl[3] * Kl[7] - Kl[4] * Kl[6]);
+            double Ki[9];
+            Ki[0] = (Kl[4] * Kl[8] - Kl[5] * Kl[7]) / det;
+            Ki[1] = (Kl[2] * Kl[7] - Kl[1] * Kl[8]) / det;
+            Ki[2] = (Kl[1] * Kl[5] - Kl[2] * Kl[4]) / det;
+            Ki[3] = (Kl[5] * Kl[6] - Kl[3] * Kl[8]) / det;
+            Ki[4] = (Kl[0] * Kl[8] - Kl[2] * Kl[6]) / det;
+            Ki[5] = (Kl[2] * Kl[3] - Kl[0] * Kl[5]) / det;
+            Ki[6] = (Kl[3] * Kl[7] - Kl[4] * Kl[6]) / det;
+            Ki[7] = (Kl[1] * Kl[6] - Kl[0] * Kl[7]) / det;
+            Ki[8] = (Kl[0] * Kl[4] - Kl[1] * Kl[3]) / det;
+            double x[3];
+            for (int d = 0; d < 3; ++d) x[d] = g.fcent[3 * size_t(f) + d] - g.ccent[3 * size_t(c) + d];
+            double sc = 0.0;
+            for (int i = 0; i < 3; ++i) sc += x[i] * (Ki[3 * i] * x[0] + Ki[3 * i + 1] * x[1] + Ki[3 * i + 2] * x[2]);
+            dt = std::min(dt, sc / fac[2]);
+        }
+    dt_capillary = dt;
+}
+
+void porsol_transport::set_rock_tables(const porsol_rock_tables* rt)
+{
+    PORSOL_REQUIRE(ready, PORSOL_ERR_STATE, "transport solver not initialised");
+    if (!rt) {
+        rock = RockView{};
+        rock_h = RockView{};
+        compute_cfl_factors();
+        return;
+    }
+    const int nr = rt->num_rocks, nc = g.nc;
+    PORSOL_REQUIRE(nr >= 1 && rt->table_pos && rt->s && rt->krw && rt->kro && rt->jfunc && rt->cell_rock,
+                   PORSOL_ERR_BAD_ARG, "rock tables: no rock or null array");
+    PORSOL_REQUIRE(rt->table_pos[0] == 0, PORSOL_ERR_BAD_ARG, "rock tables: table_pos[0] must be 0");
+    for (int r = 0; r < nr; ++r)
+        PORSOL_REQUIRE(rt->table_pos[r + 1] > rt->table_pos[r], PORSOL_ERR_BAD_ARG, "rock tables: empty table");
+    PORSOL_REQUIRE(!rt->use_jfunction_scaling || (std::isfinite(rt->sigma_cos_theta) && rt->sigma_cos_theta != 0.0),
+                   PORSOL_ERR_BAD_ARG, "rock tables: sigma cos(theta) must be finite and non-zero");
+    const int m = rt->table_pos[nr];
+    rk_pos_h.assign(rt->table_pos, rt->table_pos + nr + 1);
+    rk_s_h.assign(rt->s, rt->s + m);
+    rk_krw_h.assign(rt->krw, rt->krw + m);
+    rk_kro_h.assign(rt->kro, rt->kro + m);
+    rk_J_h.assign(rt->jfunc, rt->jfunc + m);
+    rk_Jx_h.resize(m);
+    rk_sy_h.resize(m);
+    for (int r = 0; r < nr; ++r) {
+        const int a = rk_pos_h[r], b = rk_pos_h[r + 1];
+        for (int k = a; k < b; ++k)
+            PORSOL_REQUIRE(std::isfinite(rk_s_h[k]) && std::isfinite(rk_krw_h[k]) && std::isfinite(rk_kro_h[k]) &&
+                               std::isfinite(rk_J_h[k]),
+                           PORSOL_ERR_BAD_ARG, "rock tables: non-finite entry");
+        for (int k = a + 1; k < b; ++k)
+            PORSOL_REQUIRE(rk_s_h[k] >= rk_s_h[k - 1], PORSOL_ERR_BAD_ARG, "rock tables: saturations must increase");
+        // the reader's fix-ups (RockJfunc.hpp:200-207)
+        rk_krw_h[a] = 0.0;
+        rk_kro_h[b - 1] = 0.0;
+        const bool inc = rk_J_h[b - 1] >= rk_J_h[a];
+        for (int k = a + 1; k < b; ++k)
+            PORSOL_REQUIRE(inc ? rk_J_h[k] >= rk_J_h[k - 1] : rk_J_h[k] <= rk_J_h[k - 1], PORSOL_ERR_BAD_ARG,
+                           "rock tables: J must be monotone");
+        for (int k = 0; k < b - a; ++k) {
+            const int src = inc ? a + k : b - 1 - k;
+            rk_Jx_h[a + k] = rk_J_h[src];
+            rk_sy_h[a + k] = rk_s_h[src];
+        }
+    }
+    rk_cell_h.assign(rt->cell_rock, rt->cell_rock + nc);
+    for (int c = 0; c < nc; ++c)
+        PORSOL_REQUIRE(rk_cell_h[c] >= 0 && rk_cell_h[c] < nr, PORSOL_ERR_BAD_ARG, "rock tables: rock index out of range");
+    rk_skp_h.resize(nc);
+    for (int c = 0; c < nc; ++c) {
+        const double* K = &perm[9 * size_t(c)];
+        rk_skp_h[c] = std::sqrt((K[0] + K[4] + K[8]) / (3 * poro[c]));
+    }
+    cudaStream_t s = stream;
+    rk_pos.upload(rk_pos_h, s);
+    rk_s.upload(rk_s_h, s);
+    rk_krw.upload(rk_krw_h, s);
+    rk_kro.upload(rk_kro_h, s);
+    rk_J.upload(rk_J_h, s);
+    rk_Jx.upload(rk_Jx_h, s);
+    rk_sy.upload(rk_sy_h, s);
+    rk_cell.upload(rk_cell_h, s);
+    rk_skp.upload(rk_skp_h, s);
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    auto view = [&](bool dev) {
+        RockView v;
+        v.nrock = nr;
+        v.pos = dev ? rk_pos.p : rk_pos_h.data();
+        v.s = dev ? rk_s.p : rk_s_h.data();
+        v.krw = dev ? rk_krw.p : rk_krw_h.data();
+        v.kro = dev ? rk_kro.p : rk_kro_h.data();
+        v.J = dev ? rk_J.p : rk_J_h.data();
+        v.Jx = dev ? rk_Jx.p : rk_Jx_h.data();
+        v.sy = dev ? rk_sy.p : rk_sy_h.data();
+        v.cell = dev ? rk_cell.p : rk_cell_h.data();
+        v.skp = dev ? rk_skp.p : rk_skp_h.data();
+        v.jscale = rt->use_jfunction_scaling ? 1 : 0;
+        v.sct = rt->sigma_cos_theta;
+        return v;
+    };
+    rock = view(true);
+    rock_h = view(false);
+    compute_cfl_factors();
+}
 
 void porsol_transport::init(const porsol_grid* grid, const double* K, const double* phi, const porsol_fluid* fl,
                             const int* stype, const double* sval, const int* partner,
@@ -293,7 +442,9 @@ void porsol_transport::init(const porsol_grid* grid, const double* K, const doub
     fluid = *fl;
     porsol_transport_opts_default(&o);
     if (opts) o = *opts;
-    cfl_factors(fluid.viscosity1, fluid.viscosity2, fac);
+    rock = RockView{};   // a new grid drops earlier rock tables
+    rock_h = RockView{};
+    compute_cfl_factors();
     hf_cell.resize(nhf);
     int maxbid = 0;
     for (int c = 0; c < nc; ++c)
@@ -484,10 +635,10 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
         if (do_g) dtg = v[1];
     }
     if (do_c) {
-        // findCFLtimeCapillary (CflCalculator.hpp:143-170) divides by cflFactorCapillary,
-        // which is zero without rock tables (max_derpc = 0): every local bound is +inf and
-        // the estimate keeps its initial value 1e100.
-        dtc = 1e100;
+        // findCFLtimeCapillary (CflCalculator.hpp:143-170) depends on the geometry and the rock
+        // tables only (computed when they are set); without tables cflFactorCapillary is zero,
+        // every local bound is +inf and the estimate keeps its initial value 1e100.
+        dtc = dt_capillary;
     }
     (void)gv;
     const double cfl_dt = std::min(std::min(dtv, dtg), dtc) * o.courant_number;
@@ -503,8 +654,8 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     double dt = time / n;
     sat0.alloc(nc);
     PORSOL_CUDA(cudaMemcpyAsync(sat0.p, d_sat, nc * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    TrParams p{1.0 / fluid.viscosity1, 1.0 / fluid.viscosity2, o.method_viscous, o.method_gravity,
-               o.method_capillary};
+    const TrParams p = params(o.method_viscous, o.method_gravity, o.method_capillary);
+    const bool tab = rock.nrock > 0;
     const int nfe = int(fe_h.size());
     // viscous-only sub-steps use the per-cell fractional flow (same arithmetic, fewer FP64 ops)
     const bool visc_only = o.method_viscous && !o.method_capillary && (!o.method_gravity || !any_gravity);
@@ -512,19 +663,31 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     int repeats = 0;
     const int max_repeats = 10;
     while (true) {
-        if (visc_only) PORSOL_LAUNCH(k_frac_init<<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, frac.p));
+        if (visc_only) {
+            if (tab) PORSOL_LAUNCH(k_frac_init<true><<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, rock, frac.p));
+            else PORSOL_LAUNCH(k_frac_init<false><<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, rock, frac.p));
+        }
         for (int q = 0; q < n; ++q) {
             if (nfe) {
-                if (visc_only)
-                    PORSOL_LAUNCH(k_face_dS_visc<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p, dS.p,
-                                                                              status.p));
-                else
-                    PORSOL_LAUNCH(k_face_dS<<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, d_sat, d_flux, p, dS.p,
-                                                                         status.p));
+                if (visc_only) {
+                    if (tab)
+                        PORSOL_LAUNCH(k_face_dS_visc<true><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p,
+                                                                                        rock, dS.p, status.p));
+                    else
+                        PORSOL_LAUNCH(k_face_dS_visc<false><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p,
+                                                                                         rock, dS.p, status.p));
+                } else {
+                    launch_face_dS(s, nfe, fe.p, d_sat, d_flux, p, rock, dS.p, status.p);
+                }
             }
-            PORSOL_LAUNCH(k_cell_update<<<div_up(nc, TB), TB, 0, s>>>(nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, dt,
-                                                                    o.check_sat, o.clamp_sat, d_sat,
-                                                                    visc_only ? frac.p : nullptr, status.p));
+            if (tab)
+                PORSOL_LAUNCH(k_cell_update<true><<<div_up(nc, TB), TB, 0, s>>>(
+                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat,
+                    visc_only ? frac.p : nullptr, status.p));
+            else
+                PORSOL_LAUNCH(k_cell_update<false><<<div_up(nc, TB), TB, 0, s>>>(
+                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat,
+                    visc_only ? frac.p : nullptr, status.p));
             if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
         }
         PORSOL_CUDA(cudaGetLastError());
@@ -555,25 +718,6 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     }
 }
 
-namespace {
-template <class F>
-int tguard(porsol_transport* t, F&& f)
-{
-    if (!t) return PORSOL_ERR_BAD_ARG;
-    try {
-        PORSOL_CUDA(cudaSetDevice(t->device));
-        f();
-        t->err.clear();
-        return PORSOL_OK;
-    } catch (const Error& e) {
-        t->err = e.what();
-        return e.code;
-    } catch (const std::exception& e) {
-        t->err = e.what();
-        return PORSOL_ERR_BAD_ARG;
-    }
-}
-}  // namespace
 
 extern "C" {
 
@@ -633,6 +777,11 @@ int porsol_transport_solve_device(porsol_transport* t, double* sat, double time,
                                   const double* outflux, const double* injection, porsol_transport_stats* stats)
 {
     return tguard(t, [&] { t->solve(sat, time, grav, outflux, injection, stats, true); });
+}
+
+int porsol_transport_set_rock_tables(porsol_transport* t, const porsol_rock_tables* rocks)
+{
+    return tguard(t, [&] { t->set_rock_tables(rocks); });
 }
 
 }  // extern "C"

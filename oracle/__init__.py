@@ -67,7 +67,46 @@ class TransportOpts(C.Structure):
 
 class Fluid(C.Structure):
     _fields_ = [("viscosity1", C.c_double), ("viscosity2", C.c_double),
-                ("density1", C.c_double), ("density2", C.c_double)]
+                ("density1", C.c_double), ("density2", C.c_double),
+                ("rocks", C.c_void_p)]
+
+
+class _RockTables(C.Structure):
+    _fields_ = [("num_rocks", C.c_int), ("table_pos", C.c_void_p), ("s", C.c_void_p), ("krw", C.c_void_p),
+                ("kro", C.c_void_p), ("jfunc", C.c_void_p), ("cell_rock", C.c_void_p),
+                ("use_jfunction_scaling", C.c_int), ("sigma_cos_theta", C.c_double)]
+
+
+class RockTables:
+    """RockJfunc tables (common/RockJfunc.hpp:63-216): ``tables`` is a list of (n, 4) arrays with
+    the columns s, krw, kro, J of each rock; ``cell_rock`` the rock of every cell."""
+
+    def __init__(self, tables, cell_rock, use_jfunction_scaling=True, sigma_cos_theta=1.0):
+        cat = np.concatenate([np.asarray(t, np.float64).reshape(-1, 4) for t in tables])
+        self.pos = np.cumsum([0] + [len(np.asarray(t).reshape(-1, 4)) for t in tables]).astype(np.int32)
+        self.cols = [np.ascontiguousarray(cat[:, k]) for k in range(4)]
+        self.cell = _i32(cell_rock)
+        self.s = _RockTables(len(tables), _p(self.pos), *(_p(c) for c in self.cols), _p(self.cell),
+                             1 if use_jfunction_scaling else 0, float(sigma_cos_theta))
+
+    def fluid(self, mu1, mu2, rho1=0.0, rho2=0.0) -> Fluid:
+        f = Fluid(mu1, mu2, rho1, rho2, C.addressof(self.s))
+        f._rocks_ref = self   # keep the tables alive with the fluid
+        return f
+
+
+class CapillaryOpts(C.Structure):
+    _fields_ = [("method_viscous", C.c_int), ("method_gravity", C.c_int), ("check_sat", C.c_int),
+                ("clamp_sat", C.c_int), ("residual_tolerance", C.c_double), ("linsolver_type", C.c_int),
+                ("update_relaxation", C.c_double)]
+
+    @classmethod
+    def defaults(cls, **kw):
+        """ImplicitCapillarity defaults (euler/ImplicitCapillarity_impl.hpp:59-68)."""
+        o = cls(1, 1, 1, 0, 1e-8, 1, 1.0)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
 
 
 _lib = None
@@ -104,11 +143,14 @@ def lib():
         L.orc_adjoint_gradient.argtypes = [vp, dp, dp, dp, i, d, dp, dp, ip]
         L.orc_ilu0_cg.restype = i
         L.orc_ilu0_cg.argtypes = [i, ip, ip, dp, dp, dp, d, i, ip, dp]
-        L.orc_cfl_factors.argtypes = [C.POINTER(Fluid), dp]
+        L.orc_cfl_factors.argtypes = [C.POINTER(Fluid), i, dp, dp, dp]
         L.orc_transport_cfl.restype = d
         L.orc_transport_cfl.argtypes = [C.POINTER(_Grid), dp, dp, C.POINTER(Fluid), C.POINTER(TransportOpts), dp, dp]
-        L.orc_transport_residual.argtypes = [C.POINTER(_Grid), dp, C.POINTER(Fluid), C.POINTER(TransportOpts),
+        L.orc_transport_residual.argtypes = [C.POINTER(_Grid), dp, dp, C.POINTER(Fluid), C.POINTER(TransportOpts),
                                              ip, dp, ip, dp, dp, dp, dp, dp]
+        L.orc_capillary_solve.restype = i
+        L.orc_capillary_solve.argtypes = [vp, C.POINTER(_Grid), dp, dp, C.POINTER(Fluid), C.POINTER(CapillaryOpts),
+                                          ip, dp, ip, ip, dp, dp, dp, dp, dp, dp, ip, ip]
         L.orc_transport_solve.restype = i
         L.orc_transport_solve.argtypes = [C.POINTER(_Grid), dp, dp, C.POINTER(Fluid), C.POINTER(TransportOpts),
                                           ip, dp, ip, dp, dp, dp, d, dp, ip, ip]
@@ -314,14 +356,17 @@ def ilu0_cg(rowptr, colind, vals, b, x0=None, tol=1e-8, maxit=0):
     return rc, x, int(it[0]), float(red[0])
 
 
-def cfl_factors(fluid: Fluid):
+def cfl_factors(fluid: Fluid, K9=None, poro=None):
     out = np.zeros(3)
-    lib().orc_cfl_factors(C.byref(fluid), _p(out))
+    K = None if K9 is None else _f64(K9)
+    ph = None if poro is None else _f64(poro)
+    lib().orc_cfl_factors(C.byref(fluid), 0 if ph is None else len(ph), _p(K), _p(ph), _p(out))
     return out
 
 
 class OracleTransport:
-    """EulerUpstream restated on the CPU (FP64), scalar Corey-2 mobilities."""
+    """EulerUpstream restated on the CPU (FP64), scalar mobilities: Corey-2, or the rock tables
+    the fluid carries (RockTables.fluid)."""
 
     def __init__(self, grid, K9, poro, fluid: Fluid, sat_type, sat_value, partner_bid=None, opts=None):
         self.g = GridRef(grid)
@@ -340,7 +385,8 @@ class OracleTransport:
     def residual(self, sat, outflux, injection=None, grav=(0.0, 0.0, 0.0)):
         inj = np.zeros(self.g.num_cells) if injection is None else _f64(injection)
         res = np.empty(self.g.num_cells)
-        lib().orc_transport_residual(C.byref(self.g.s), _p(self.K), C.byref(self.fluid), C.byref(self.opts),
+        lib().orc_transport_residual(C.byref(self.g.s), _p(self.K), _p(self.poro), C.byref(self.fluid),
+                                     C.byref(self.opts),
                                      _p(self.st), _p(self.sv), _p(self.pb), _p(_f64(outflux)), _p(inj),
                                      _p(_f64(sat)), _p(_f64(grav)), _p(res))
         return res
@@ -355,3 +401,21 @@ class OracleTransport:
                                        _p(_f64(outflux)), _p(inj), _p(s), float(time), _p(_f64(grav)),
                                        _p(ns), _p(rp))
         return rc, s, int(ns[0]), int(rp[0])
+
+
+def capillary_solve(pressure: OraclePressure, transport: OracleTransport, sat, outflux, bc_type, bc_value,
+                    injection=None, grav=(0.0, 0.0, 0.0), opts=None):
+    """ImplicitCapillarity::transportSolve restated (euler/ImplicitCapillarity_impl.hpp:138-226).
+    ``pressure`` must hold the inner products for zero gravity.  Returns (rc, sat, shift,
+    root_iterations, cg_iterations); rc as orc_capillary_solve."""
+    T = transport
+    s = _f64(sat).copy()
+    inj = np.zeros(T.g.num_cells) if injection is None else _f64(injection)
+    o = opts if opts is not None else CapillaryOpts.defaults()
+    shift = np.zeros(1)
+    rit = np.zeros(1, np.int32)
+    cit = np.zeros(1, np.int32)
+    rc = lib().orc_capillary_solve(pressure.h, C.byref(T.g.s), _p(T.K), _p(T.poro), C.byref(T.fluid), C.byref(o),
+                                   _p(T.st), _p(T.sv), _p(T.pb), _p(_i32(bc_type)), _p(_f64(bc_value)),
+                                   _p(_f64(outflux)), _p(inj), _p(s), _p(_f64(grav)), _p(shift), _p(rit), _p(cit))
+    return rc, s, float(shift[0]), int(rit[0]), int(cit[0])

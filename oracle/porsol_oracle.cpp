@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <numeric>
 #include <stdexcept>
 #include <unordered_map>
@@ -808,19 +809,137 @@ struct Pressure {
 };
 
 // ---------------------------------------------------------------------------
+// Rock tables of RockJfunc (common/RockJfunc.hpp:63-216) with the cell -> rock map and the
+// capillary functions of ReservoirPropertyCommon (common/ReservoirPropertyCommon_impl.hpp:
+// 466-528, 740-781).  The reader's fix-ups are applied: krw starts at 0 and kro ends at 0
+// (RockJfunc.hpp:200-207); s_min / s_max are the first / last saturation of the table.
+// The table functions restate opm-core's NonuniformTableLinear, which is not part of the
+// reference tree (unpinned): piecewise-linear interpolation with the end value outside the
+// table; the derivative is the slope of the interval that holds the point (0 outside); the
+// inverse interpolates the abscissa in the ordinate, read in increasing ordinate order.
+double tab_value(const double* x, const double* y, int n, double v)
+{
+    if (v <= x[0]) return y[0];
+    if (v >= x[n - 1]) return y[n - 1];
+    int lo = 0, hi = n - 1;   // x[lo] <= v < x[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (x[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    const double w = (v - x[lo]) / (x[hi] - x[lo]);
+    return (1.0 - w) * y[lo] + w * y[hi];
+}
+
+double tab_slope(const double* x, const double* y, int n, double v)
+{
+    if (n < 2 || v < x[0] || v > x[n - 1]) return 0.0;
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (x[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    return x[hi] > x[lo] ? (y[hi] - y[lo]) / (x[hi] - x[lo]) : 0.0;
+}
+
+struct Rocks {
+    int nrock = 0;
+    std::vector<int> pos, cell;
+    std::vector<double> s, krw, kro, J, Jx, sy;   // Jx/sy: the J table in increasing J order
+    std::vector<double> skp;                      // per cell sqrt(tr K / (3 phi)) (J scaling)
+    bool jscale = true;
+    double sct = 1.0;
+
+    // throws std::invalid_argument on malformed tables
+    void set(const orc_rock_tables* rt, int nc, const double* K9, const double* poro)
+    {
+        nrock = rt->num_rocks;
+        if (nrock < 1) throw std::invalid_argument("rock tables: no rock");
+        pos.assign(rt->table_pos, rt->table_pos + nrock + 1);
+        const int m = pos[nrock];
+        s.assign(rt->s, rt->s + m);
+        krw.assign(rt->krw, rt->krw + m);
+        kro.assign(rt->kro, rt->kro + m);
+        J.assign(rt->jfunc, rt->jfunc + m);
+        Jx.resize(m);
+        sy.resize(m);
+        for (int r = 0; r < nrock; ++r) {
+            const int a = pos[r], b = pos[r + 1];
+            if (b - a < 1) throw std::invalid_argument("rock tables: empty table");
+            for (int k = a + 1; k < b; ++k)
+                if (!(s[k] >= s[k - 1])) throw std::invalid_argument("rock tables: saturations must increase");
+            krw[a] = 0.0;
+            kro[b - 1] = 0.0;
+            const bool inc = J[b - 1] >= J[a];
+            for (int k = a + 1; k < b; ++k)
+                if (inc ? J[k] < J[k - 1] : J[k] > J[k - 1])
+                    throw std::invalid_argument("rock tables: J must be monotone");
+            for (int k = 0; k < b - a; ++k) {
+                const int src = inc ? a + k : b - 1 - k;
+                Jx[a + k] = J[src];
+                sy[a + k] = s[src];
+            }
+        }
+        cell.assign(rt->cell_rock, rt->cell_rock + nc);
+        for (int c = 0; c < nc; ++c)
+            if (cell[c] < 0 || cell[c] >= nrock) throw std::invalid_argument("rock tables: rock index out of range");
+        jscale = rt->use_jfunction_scaling != 0;
+        sct = rt->sigma_cos_theta;
+        skp.assign(nc, 1.0);
+        if (K9 && poro)
+            for (int c = 0; c < nc; ++c)
+                skp[c] = std::sqrt((K9[9 * c] + K9[9 * c + 4] + K9[9 * c + 8]) / (3 * poro[c]));
+    }
+    int n(int r) const { return pos[r + 1] - pos[r]; }
+    double kr(int phase, int c, double sat) const
+    {
+        const int r = cell[c], a = pos[r];
+        return tab_value(&s[a], phase == 0 ? &krw[a] : &kro[a], n(r), sat);
+    }
+    // RockJfunc::capPress (RockJfunc.hpp:94-107)
+    double capPress(int c, double sat) const
+    {
+        const int r = cell[c], a = pos[r];
+        const double j = tab_value(&s[a], &J[a], n(r), sat);
+        return jscale ? j * sct / skp[c] : j;
+    }
+    // RockJfunc::capPressDeriv for perm = min_perm I and porosity max_poro (:110-123)
+    double capPressDeriv(int r, double min_perm, double max_poro, double sat) const
+    {
+        const int a = pos[r];
+        const double d = tab_slope(&s[a], &J[a], n(r), sat);
+        return jscale ? d * sct / std::sqrt(3 * min_perm / (3 * max_poro)) : d;
+    }
+    // RockJfunc::satFromCapPress (:126-141)
+    double satFromCapPress(int c, double pc) const
+    {
+        const int r = cell[c], a = pos[r];
+        const double v = jscale ? pc * skp[c] / sct : pc;
+        const double sat = tab_value(&Jx[a], &sy[a], n(r), v);
+        return std::min(s[pos[r + 1] - 1], std::max(s[a], sat));
+    }
+};
+
 // Transport restatement (EulerUpstream / EulerUpstreamResidual / cfl_calculator) for the
-// scalar-mobility ReservoirPropertyCapillary without rock tables: kr1 = s^2, kr2 = (1-s)^2
-// (ReservoirPropertyCapillary_impl.hpp:118-170), pc = 1e5 (1-s)
+// scalar-mobility ReservoirPropertyCapillary: with rock tables the relative permeabilities
+// and capillary pressure come from the tables above; without, kr1 = s^2, kr2 = (1-s)^2
+// (ReservoirPropertyCapillary_impl.hpp:118-170) and pc = 1e5 (1-s)
 // (ReservoirPropertyCommon_impl.hpp:466-476).
 struct Fluid {
     double mu1, mu2, rho1, rho2;
-    double mob(int phase, double s) const { return phase == 0 ? (s * s) / mu1 : ((1 - s) * (1 - s)) / mu2; }
-    double fracflow(double s) const
+    const Rocks* rk = nullptr;
+    double mob(int phase, int c, double s) const
     {
-        const double l1 = mob(0, s), l2 = mob(1, s);
+        if (rk) return rk->kr(phase, c, s) / (phase == 0 ? mu1 : mu2);
+        return phase == 0 ? (s * s) / mu1 : ((1 - s) * (1 - s)) / mu2;
+    }
+    double fracflow(int c, double s) const
+    {
+        const double l1 = mob(0, c, s), l2 = mob(1, c, s);
         return l1 / (l1 + l2);
     }
-    double capPress(double s) const { return 1e5 * (1 - s); }
+    double capPress(int c, double s) const { return rk ? rk->capPress(c, s) : 1e5 * (1 - s); }
 };
 
 struct TransportCtx {
@@ -834,11 +953,16 @@ struct TransportCtx {
     std::vector<int> bid_to_face;   // last periodic half-face seen with this bid
     std::vector<int> hf_cell;
     std::vector<double> cap;
-    TransportCtx(const orc_grid* og, const double* K, const orc_fluid* f, const orc_transport_opts* opts,
-                 const int* sat_type, const double* sat_value, const int* partner)
+    Rocks rocks;
+    TransportCtx(const orc_grid* og, const double* K, const double* poro, const orc_fluid* f,
+                 const orc_transport_opts* opts, const int* sat_type, const double* sat_value, const int* partner)
         : g(og), K9(K), st(sat_type), sv(sat_value), pbid(partner)
     {
         fl = Fluid{f->viscosity1, f->viscosity2, f->density1, f->density2};
+        if (f->rocks) {
+            rocks.set(f->rocks, g.nc, K, poro);
+            fl.rk = &rocks;
+        }
         o = *opts;
         int maxbid = 0;
         for (int hf = 0; hf < g.nhf(); ++hf) maxbid = std::max(maxbid, g.bid[hf]);
@@ -884,7 +1008,7 @@ struct TransportCtx {
         const double delta_rho = fl.rho1 - fl.rho2;
         if (o.method_capillary) {
             cap.resize(g.nc);
-            for (int c = 0; c < g.nc; ++c) cap[c] = fl.capPress(sat[c]);
+            for (int c = 0; c < g.nc; ++c) cap[c] = fl.capPress(c, sat[c]);
         }
         std::fill(res, res + g.nc, 0.0);
         for (int c0 = 0; c0 < g.nc; ++c0) {
@@ -922,17 +1046,17 @@ struct TransportCtx {
                 const int triv = G >= 0.0 ? 0 : 1;
                 const int ups = q >= 0.0 ? 0 : 1;
                 double mu[2];
-                mu[triv] = fl.mob(triv, cs[ups]);
+                mu[triv] = fl.mob(triv, cell[ups], cs[ups]);
                 const double signG[2] = {-1.0, 1.0};
                 const double gnt = signG[triv] * A * (n[0] * (mu[triv] * gi[0]) + n[1] * (mu[triv] * gi[1]) + n[2] * (mu[triv] * gi[2]));
                 const int ups_nt = (q + gnt >= 0.0) ? 0 : 1;
                 const int nontriv = (triv + 1) % 2;
-                mu[nontriv] = fl.mob(nontriv, cs[ups_nt]);
+                mu[nontriv] = fl.mob(nontriv, cell[ups_nt], cs[ups_nt]);
                 const double mtot = mu[0] + mu[1];
                 const double mtinv = 1.0 / mtot;
                 const double asat = 0.5 * (cs[0] + cs[1]);
-                const double m1 = 0.5 * (fl.mob(0, asat) + fl.mob(0, asat));
-                const double m2 = 0.5 * (fl.mob(1, asat) + fl.mob(1, asat));
+                const double m1 = 0.5 * (fl.mob(0, cell[0], asat) + fl.mob(0, cell[1], asat));
+                const double m2 = 0.5 * (fl.mob(1, cell[0], asat) + fl.mob(1, cell[1], asat));
                 const double matinv = 1.0 / (m1 + m2);
                 if (o.method_viscous) {
                     double s = 0.0;
@@ -960,24 +1084,37 @@ struct TransportCtx {
                 }
             }
             double rate = inj ? inj[c0] : 0.0;
-            if (rate < 0.0) rate *= fl.fracflow(cs[0]);
+            if (rate < 0.0) rate *= fl.fracflow(c0, cs[0]);
             res[c0] += rate;
         }
     }
 };
 
-void cfl_factors(const Fluid& fl, double* out)
+// ReservoirPropertyCapillary::computeSingleRockCflFactors (ReservoirPropertyCapillary_impl.hpp:
+// 213-250): 257-point sampling of the fractional flow, the gravity flow function and (with a
+// rock table) the capillary-pressure derivative; rock -1 = no table.
+void single_rock_cfl(const Fluid& fl, int rock, double min_perm, double max_poro, double* out)
 {
     const int N = 257;
     const double delta = 1.0 / double(N - 1);
     auto ff = [&](double s, double& f1, double& fg) {
-        const double l1 = fl.mob(0, s), l2 = fl.mob(1, s);
+        double l1, l2;
+        if (rock < 0) {
+            l1 = (s * s) / fl.mu1;
+            l2 = ((1 - s) * (1 - s)) / fl.mu2;
+        } else {
+            const Rocks& R = *fl.rk;
+            const int a = R.pos[rock], n = R.n(rock);
+            l1 = tab_value(&R.s[a], &R.krw[a], n, s) / fl.mu1;
+            l2 = tab_value(&R.s[a], &R.kro[a], n, s) / fl.mu2;
+        }
         f1 = l1 / (l1 + l2);
         fg = l1 * l2 / (l1 + l2);
     };
     double last1, lastg, md1 = -1e100, mdg = -1e100;
     ff(0.0, last1, lastg);
     double maxffg = lastg;
+    double mdpc = rock < 0 ? 0.0 : std::fabs(fl.rk->capPressDeriv(rock, min_perm, max_poro, 0.0));
     for (int i = 1; i < N; ++i) {
         const double s = double(i) * delta;
         double f1, fg;
@@ -985,12 +1122,40 @@ void cfl_factors(const Fluid& fl, double* out)
         md1 = std::max(md1, std::fabs(f1 - last1) / delta);
         mdg = std::max(mdg, std::fabs(fg - lastg) / delta);
         maxffg = std::max(maxffg, fg);
+        if (rock >= 0) mdpc = std::max(mdpc, std::fabs(fl.rk->capPressDeriv(rock, min_perm, max_poro, s)));
         last1 = f1;
         lastg = fg;
     }
     out[0] = 1.0 / md1;
     out[1] = 1.0 / mdg;
-    out[2] = maxffg * 0.0;   // max_derpc = 0 without a rock table
+    out[2] = maxffg * mdpc;
+}
+
+// ReservoirPropertyCapillary::computeCflFactors (:255-282): per rock the smallest mean diagonal
+// permeability and the largest porosity of its cells; the most restrictive factors win.
+void cfl_factors(const Fluid& fl, int nc, const double* K9, const double* poro, double* out)
+{
+    if (!fl.rk) {
+        single_rock_cfl(fl, -1, 0.0, 0.0, out);
+        return;
+    }
+    const Rocks& R = *fl.rk;
+    std::vector<double> min_perm(R.nrock, 1e100), max_poro(R.nrock, 0.0);
+    for (int c = 0; c < nc; ++c) {
+        const int r = R.cell[c];
+        min_perm[r] = std::min(min_perm[r], (K9[9 * c] + K9[9 * c + 4] + K9[9 * c + 8]) / 3.0);
+        max_poro[r] = std::max(max_poro[r], poro[c]);
+    }
+    out[0] = 1e100;
+    out[1] = 1e100;
+    out[2] = 0.0;
+    for (int r = 0; r < R.nrock; ++r) {
+        double f[3];
+        single_rock_cfl(fl, r, min_perm[r], max_poro[r], f);
+        out[0] = std::min(out[0], f[0]);
+        out[1] = std::min(out[1], f[1]);
+        out[2] = std::max(out[2], f[2]);
+    }
 }
 
 // computeCflTime, EulerUpstream_impl.hpp:265-331, and cfl_calculator, CflCalculator.hpp:55-170
@@ -998,7 +1163,7 @@ double cfl_time(const Grid& g, const double* K9, const double* poro, const Fluid
                 const orc_transport_opts& o, const double* flux, const double* grav)
 {
     double fac[3];
-    cfl_factors(fl, fac);
+    cfl_factors(fl, g.nc, K9, poro, fac);
     double dtv = 1e99, dtg = 1e99, dtc = 1e99;
     if (o.method_viscous && o.use_cfl_viscous) {
         double dt = 1e100;
@@ -1071,6 +1236,59 @@ double cfl_time(const Grid& g, const double* K9, const double* poro, const Fluid
 }
 
 struct SatRangeError {};
+
+// Root bracketing and regula falsi as ImplicitCapillarity uses them from opm-core's
+// RootFinders (not part of the reference tree; unpinned), restated from the published
+// methods.  bracket_zero steps away from x0 by dx, alternating sides and doubling the step,
+// until the sign of f changes (at most 100 trials); regula_falsi is false position with the
+// Pegasus modification (Dowell & Jarratt, BIT 12 (1972) 503-508) and stops at |f| <= tol.
+// Error codes: 4 = no sign change found, 5 = more than max_iter iterations.
+struct RootError {
+    int code;
+};
+
+template <class F>
+void bracket_zero(F& f, double x0, double dx, double& a, double& b)
+{
+    const double f0 = f(x0);
+    double step = dx;
+    for (int i = 0; i < 100; ++i) {
+        const double x = x0 + step;
+        if (f0 * f(x) <= 0.0) {
+            a = std::min(x0, x);
+            b = std::max(x0, x);
+            return;
+        }
+        step = -2.0 * step;
+    }
+    throw RootError{4};
+}
+
+template <class F>
+double regula_falsi(F& f, double a, double b, int max_iter, double tol, int* iters)
+{
+    *iters = 0;
+    double x0 = a, f0 = f(x0);
+    if (std::fabs(f0) <= tol) return x0;
+    double x1 = b, f1 = f(x1);
+    if (std::fabs(f1) <= tol) return x1;
+    if (f0 * f1 > 0.0) throw RootError{4};
+    for (int it = 1; it <= max_iter; ++it) {
+        const double x = x1 - f1 * (x1 - x0) / (f1 - f0);
+        const double fx = f(x);
+        *iters = it;
+        if (std::fabs(fx) <= tol) return x;
+        if ((fx < 0.0) != (f1 < 0.0)) {
+            x0 = x1;
+            f0 = f1;
+        } else {
+            f0 *= f1 / (f1 + fx);
+        }
+        x1 = x;
+        f1 = fx;
+    }
+    throw RootError{5};
+}
 
 }  // namespace
 
@@ -1219,10 +1437,15 @@ int orc_ilu0_cg(int n, const int* rowptr, const int* colind, const double* vals,
     return ok ? 0 : 1;
 }
 
-void orc_cfl_factors(const orc_fluid* f, double* out3)
+void orc_cfl_factors(const orc_fluid* f, int nc, const double* K9, const double* poro, double* out3)
 {
     Fluid fl{f->viscosity1, f->viscosity2, f->density1, f->density2};
-    cfl_factors(fl, out3);
+    Rocks R;
+    if (f->rocks) {
+        R.set(f->rocks, nc, K9, poro);
+        fl.rk = &R;
+    }
+    cfl_factors(fl, nc, K9, poro, out3);
 }
 
 double orc_transport_cfl(const orc_grid* og, const double* K9, const double* poro, const orc_fluid* f,
@@ -1230,6 +1453,11 @@ double orc_transport_cfl(const orc_grid* og, const double* K9, const double* por
 {
     Grid g(og);
     Fluid fl{f->viscosity1, f->viscosity2, f->density1, f->density2};
+    Rocks R;
+    if (f->rocks) {
+        R.set(f->rocks, g.nc, K9, poro);
+        fl.rk = &R;
+    }
     try {
         return cfl_time(g, K9, poro, fl, *opts, flux, grav);
     } catch (...) {
@@ -1237,11 +1465,12 @@ double orc_transport_cfl(const orc_grid* og, const double* K9, const double* por
     }
 }
 
-void orc_transport_residual(const orc_grid* g, const double* K9, const orc_fluid* fl, const orc_transport_opts* opts,
-                            const int* st, const double* sv, const int* pbid, const double* flux,
-                            const double* inj, const double* sat, const double* grav, double* residual)
+void orc_transport_residual(const orc_grid* g, const double* K9, const double* poro, const orc_fluid* fl,
+                            const orc_transport_opts* opts, const int* st, const double* sv, const int* pbid,
+                            const double* flux, const double* inj, const double* sat, const double* grav,
+                            double* residual)
 {
-    TransportCtx T(g, K9, fl, opts, st, sv, pbid);
+    TransportCtx T(g, K9, poro, fl, opts, st, sv, pbid);
     T.residual(sat, grav, flux, inj, residual);
 }
 
@@ -1253,11 +1482,17 @@ int orc_transport_solve(const orc_grid* og, const double* K9, const double* poro
                         int* nsteps, int* repeats)
 {
     Grid g(og);
-    Fluid fl{f->viscosity1, f->viscosity2, f->density1, f->density2};
+    std::unique_ptr<TransportCtx> Tp;
+    try {
+        Tp.reset(new TransportCtx(og, K9, poro, f, opts, st, sv, pbid));
+    } catch (const std::invalid_argument&) {
+        return 6;
+    }
+    TransportCtx& T = *Tp;
     const orc_transport_opts& o = *opts;
     double cfl_dt;
     try {
-        cfl_dt = cfl_time(g, K9, poro, fl, o, flux, grav);
+        cfl_dt = cfl_time(g, K9, poro, T.fl, o, flux, grav);
     } catch (...) {
         return 3;
     }
@@ -1273,7 +1508,6 @@ int orc_transport_solve(const orc_grid* og, const double* K9, const double* poro
     double dt = time / n;
     std::vector<double> porevol(g.nc), s0(sat, sat + g.nc), res(g.nc);
     for (int c = 0; c < g.nc; ++c) porevol[c] = g.cvol[c] * poro[c];
-    TransportCtx T(og, K9, f, opts, st, sv, pbid);
     int rep = 0;
     const int max_repeats = 10;
     while (true) {
@@ -1306,6 +1540,99 @@ int orc_transport_solve(const orc_grid* og, const double* K9, const double* poro
     }
     if (nsteps) *nsteps = n;
     if (repeats) *repeats = rep;
+    return 0;
+}
+
+// ImplicitCapillarity::transportSolve (euler/ImplicitCapillarity_impl.hpp:138-226) with
+// MatchSaturatedVolumeFunctor (euler/MatchSaturatedVolumeFunctor.hpp:49-112).  The pressure
+// handle must hold the grid, the flow-BC topology and the inner products for zero gravity
+// (the reference's psolver_ is initialised with zero gravity, :80-83).  Without rock tables
+// saturationFromCapillaryPressure is 0 (ReservoirPropertyCommon_impl.hpp:518-528).
+int orc_capillary_solve(void* ph, const orc_grid* og, const double* K9, const double* poro, const orc_fluid* f,
+                        const orc_capillary_opts* co, const int* st, const double* sv, const int* pbid,
+                        const int* bct, const double* bcv, const double* flux, const double* inj, double* sat,
+                        const double* grav, double* shift, int* root_iterations, int* cg_iterations)
+{
+    Pressure* P = static_cast<Pressure*>(ph);
+    Grid g(og);
+    const int nc = g.nc, nhf = g.nhf();
+    orc_transport_opts to{};
+    to.method_viscous = co->method_viscous;
+    to.method_gravity = co->method_gravity;
+    to.method_capillary = 0;
+    std::unique_ptr<TransportCtx> Tp;
+    try {
+        Tp.reset(new TransportCtx(og, K9, poro, f, &to, st, sv, pbid));
+    } catch (const std::invalid_argument&) {
+        return 6;
+    }
+    TransportCtx& T = *Tp;
+    // capillary mobilities lambda_1 lambda_2 / (lambda_1 + lambda_2), threshold 1e-10 (:148-165)
+    std::vector<double> capmob(nc);
+    for (int c = 0; c < nc; ++c) {
+        const double m1 = T.fl.mob(0, c, sat[c]), m2 = T.fl.mob(1, c, sat[c]);
+        const double mtinv = 1.0 / (m1 + m2);
+        capmob[c] = std::max((m1 * mtinv) * m2, 1e-10);
+    }
+    // periodic flow conditions get a zero jump (:168-174)
+    std::vector<double> bv(bcv, bcv + nhf);
+    for (int hf = 0; hf < nhf; ++hf)
+        if (g.boundary(hf) && bct[hf] == ORC_BC_PERIODIC) bv[hf] = 0.0;
+    // injection rates from the viscous/gravity residual (:176-183)
+    std::vector<double> res(nc);
+    T.residual(sat, grav, flux, inj, res.data());
+    for (int c = 0; c < nc; ++c) res[c] = -res[c];
+    // capillary pressure: a pressure solve with the fixed mobilities, phase densities (1, 0) (:186-193,
+    // ReservoirPropertyFixedMobility.hpp:55-74)
+    P->useStatic();
+    P->assemble(capmob.data(), capmob.data(), bct, bv.data(), res.data());
+    int it = 0;
+    double red = 0.0;
+    if (P->solve(co->residual_tolerance, 0, co->linsolver_type != 0, &it, &red) != 0) return 1;
+    P->recover();
+    if (cg_iterations) *cg_iterations = it;
+    const std::vector<double> cp = P->pressure;
+    // MatchSaturatedVolumeFunctor
+    std::vector<double> snew(nc);
+    double pv_sum = 0.0, sv0 = 0.0;
+    for (int c = 0; c < nc; ++c) {
+        const double pv = g.cvol[c] * poro[c];
+        pv_sum += pv;
+        sv0 += pv * sat[c];
+    }
+    auto fun = [&](double dp) {
+        double pvs = 0.0, svs = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            snew[c] = T.fl.rk ? T.fl.rk->satFromCapPress(c, cp[c] + dp) : 0.0;
+            const double pv = g.cvol[c] * poro[c];
+            pvs += pv;
+            svs += pv * snew[c];
+        }
+        return (svs - sv0) / pvs;
+    };
+    (void)pv_sum;
+    const double lo = *std::min_element(cp.begin(), cp.end()), hi = *std::max_element(cp.begin(), cp.end());
+    double a = 1e100, b = -1e100, x;
+    int rit = 0;
+    try {
+        bracket_zero(fun, 0.0, hi - lo, a, b);
+        x = regula_falsi(fun, a, b, 40, 1e-12, &rit);
+    } catch (const RootError& e) {
+        return e.code;
+    }
+    if (shift) *shift = x;
+    if (root_iterations) *root_iterations = rit;
+    const double w = co->update_relaxation;
+    for (int c = 0; c < nc; ++c) sat[c] = (1.0 - w) * sat[c] + w * snew[c];
+    // relaxation (:213-217), checkAndPossiblyClampSat (:234-247)
+    if (co->check_sat || co->clamp_sat) {
+        for (int c = 0; c < nc; ++c) {
+            if (sat[c] > 1.0 || sat[c] < 0.0) {
+                if (co->clamp_sat) sat[c] = std::max(std::min(sat[c], 1.0), 0.0);
+                else if (sat[c] > 1.001 || sat[c] < -0.001) return 2;
+            }
+        }
+    }
     return 0;
 }
 

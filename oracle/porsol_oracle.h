@@ -4,7 +4,8 @@
  * TEST INFRASTRUCTURE ONLY.  This library is a plain C++ restatement of the
  * reference algorithms (OPM/opm-porsol, mimetic/IncompFlowSolverHybrid.hpp,
  * mimetic/MimeticIPEvaluator.hpp, euler/EulerUpstream_impl.hpp,
- * euler/EulerUpstreamResidual_impl.hpp, euler/CflCalculator.hpp).  It is the
+ * euler/EulerUpstreamResidual_impl.hpp, euler/CflCalculator.hpp,
+ * euler/ImplicitCapillarity_impl.hpp, common/RockJfunc.hpp).  It is the
  * checker that the GPU product path is compared against; only the test-suite,
  * the smoke check and the CPU-baseline leg of the benchmark may load it.  The
  * product library never links, loads or calls it.
@@ -94,17 +95,36 @@ typedef struct orc_transport_opts {
     int check_sat, clamp_sat;                                /* 1, 0 */
 } orc_transport_opts;
 
+/* Rock tables of RockJfunc (common/RockJfunc.hpp:63-216): rows table_pos[r] ..
+ * table_pos[r+1]-1 of (s, krw, kro, jfunc) belong to rock r; cell_rock[c] is the rock of
+ * cell c (cell_to_rock_, ReservoirPropertyCommon_impl.hpp:740-781).  With J scaling the
+ * capillary pressure is J(s) sigma_cos_theta / sqrt(tr K / (3 phi)). */
+typedef struct orc_rock_tables {
+    int num_rocks;
+    const int* table_pos;
+    const double* s;
+    const double* krw;
+    const double* kro;
+    const double* jfunc;
+    const int* cell_rock;
+    int use_jfunction_scaling;
+    double sigma_cos_theta;
+} orc_rock_tables;
+
 typedef struct orc_fluid {
     double viscosity1, viscosity2;   /* mobility_i = kr_i / viscosity_i */
     double density1, density2;
+    const orc_rock_tables* rocks;    /* NULL: kr1 = s^2, kr2 = (1-s)^2, pc = 1e5 (1-s) */
 } orc_fluid;
 
-/* CFL factors of ReservoirPropertyCapillary::computeSingleRockCflFactors(-1, 0, 0)
- * (ReservoirPropertyCapillary_impl.hpp:215-260): out[0]=cfl_factor,
- * out[1]=cfl_factor_gravity, out[2]=cfl_factor_capillary. */
-void orc_cfl_factors(const orc_fluid* fl, double* out3);
+/* CFL factors of ReservoirPropertyCapillary::computeCflFactors
+ * (ReservoirPropertyCapillary_impl.hpp:213-282): out[0]=cfl_factor,
+ * out[1]=cfl_factor_gravity, out[2]=cfl_factor_capillary.  K9/poro are used with rock
+ * tables only (may be NULL otherwise). */
+void orc_cfl_factors(const orc_fluid* fl, int num_cells, const double* K9, const double* poro, double* out3);
 
-/* EulerUpstream::transportSolve.  Returns 0 on success, 2 if the retry loop gave up.
+/* EulerUpstream::transportSolve.  Returns 0 on success, 2 if the retry loop gave up,
+ * 3 if a CFL step is zero, 6 for malformed rock tables.
  * sat is updated in place.  nsteps/repeats report the small-step count used. */
 int orc_transport_solve(const orc_grid* g, const double* K9, const double* poro,
                         const orc_fluid* fl, const orc_transport_opts* opts,
@@ -113,7 +133,7 @@ int orc_transport_solve(const orc_grid* g, const double* K9, const double* poro,
                         double* sat, double time, const double* grav,
                         int* nsteps, int* repeats);
 /* One computeResidual (EulerUpstreamResidual_impl.hpp:475-505), for kernel unit tests. */
-void orc_transport_residual(const orc_grid* g, const double* K9, const orc_fluid* fl,
+void orc_transport_residual(const orc_grid* g, const double* K9, const double* poro, const orc_fluid* fl,
                             const orc_transport_opts* opts,
                             const int* hf_sat_type, const double* hf_sat_value, const int* hf_partner_bid,
                             const double* outflux_hf, const double* injection,
@@ -122,6 +142,28 @@ void orc_transport_residual(const orc_grid* g, const double* K9, const orc_fluid
 double orc_transport_cfl(const orc_grid* g, const double* K9, const double* poro,
                          const orc_fluid* fl, const orc_transport_opts* opts,
                          const double* outflux_hf, const double* grav);
+
+/* ---------------- ImplicitCapillarity ---------------- */
+typedef struct orc_capillary_opts {
+    int method_viscous, method_gravity;   /* 1, 1 */
+    int check_sat, clamp_sat;             /* 1, 0 */
+    double residual_tolerance;            /* 1e-8 */
+    int linsolver_type;                   /* 1: Dirichlet rows pre-solved in the initial guess */
+    double update_relaxation;             /* 1.0 */
+} orc_capillary_opts;
+
+/* ImplicitCapillarity::transportSolve (euler/ImplicitCapillarity_impl.hpp:138-226).
+ * pressure: an orc_create handle for the same grid and flow-BC topology whose inner products
+ * were computed with zero gravity.  hf_flow_type/value: the flow BCs (periodic values are
+ * replaced by 0).  sat is updated in place.  Returns 0 = ok, 1 = pressure CG did not
+ * converge, 2 = saturation out of range, 4 = no bracket of the volume-matching shift,
+ * 5 = root iterations exhausted (40), 6 = malformed rock tables. */
+int orc_capillary_solve(void* pressure, const orc_grid* g, const double* K9, const double* poro,
+                        const orc_fluid* fl, const orc_capillary_opts* opts,
+                        const int* hf_sat_type, const double* hf_sat_value, const int* hf_partner_bid,
+                        const int* hf_flow_type, const double* hf_flow_value,
+                        const double* outflux_hf, const double* injection, double* sat, const double* grav,
+                        double* shift, int* root_iterations, int* cg_iterations);
 
 #ifdef __cplusplus
 }
