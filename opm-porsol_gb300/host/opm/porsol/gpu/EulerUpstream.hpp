@@ -6,10 +6,10 @@
 // Opm::parameter::ParameterGroup works unchanged, and so does the plain Params struct
 // below.  The transport runs on the GPU through porsol_transport_* (include/porsol_gpu.h).
 //
-// The reservoir-properties concept consumed is that of ReservoirPropertyCapillary without
-// rock tables (kr1 = s^2, kr2 = (1-s)^2; ReservoirPropertyCapillary_impl.hpp:118-170):
-// permeability(c), porosity(c), viscosityFirstPhase/SecondPhase(), densityFirstPhase/
-// SecondPhase() (ReservoirPropertyCommon.hpp).
+// The reservoir-properties concept consumed is that of ReservoirPropertyCapillary
+// (ReservoirPropertyCapillary_impl.hpp:118-170): permeability(c), porosity(c),
+// viscosityFirstPhase/SecondPhase(), densityFirstPhase/SecondPhase() (ReservoirPropertyCommon.hpp),
+// with kr1 = s^2, kr2 = (1-s)^2 until setRockTables() hands over the RockJfunc tables.
 #ifndef OPM_PORSOL_GPU_EULERUPSTREAM_HPP
 #define OPM_PORSOL_GPU_EULERUPSTREAM_HPP
 
@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "GridFlattener.hpp"
+#include "RockTables.hpp"
 #include "porsol_gpu.h"
 
 namespace Opm {
@@ -126,6 +127,17 @@ public:
     }
 
     void setCourantNumber(double cn) { o_.courant_number = cn; }
+
+    // ReservoirPropertyCapillary with rock tables: table mobilities and capillary pressure,
+    // per-rock CFL factors (call after initObj; an empty table list returns to Corey-2)
+    void setRockTables(const RockTables& rt)
+    {
+        if (rt.rocks.empty()) check(porsol_transport_set_rock_tables(t_, nullptr));
+        else check(Opm::gpu::setRockTables(t_, grid_, rt));
+    }
+
+    porsol_transport* handle() const { return t_; }
+    const FlatGrid& flatGrid() const { return grid_; }
 
     // EulerUpstream_impl.hpp:153-218.  PressureSolution is any type with outflux(face);
     // a FlowSolution of Opm::gpu::IncompFlowSolverHybrid is read straight from device memory.

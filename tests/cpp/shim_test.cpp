@@ -6,7 +6,8 @@
 //
 // Checks: a linear pressure field is reproduced exactly (mimetic consistency), for both
 // linsolver_type 0 (ILU0-CG) and 1 (AMG-CG); postProcessFluxes leaves antisymmetric twin
-// fluxes; transportSolve conserves water volume.  Prints "OK" on success.
+// fluxes; transportSolve conserves water volume; the ImplicitCapillarity step conserves the
+// saturation volume.  Prints "OK" on success.
 #include <cmath>
 #include <cstdio>
 #include <iostream>
@@ -14,6 +15,7 @@
 #include <vector>
 
 #include "opm/porsol/gpu/EulerUpstream.hpp"
+#include "opm/porsol/gpu/ImplicitCapillarity.hpp"
 #include "opm/porsol/gpu/IncompFlowSolverHybrid.hpp"
 #include "opm/porsol/gpu/PermeabilityAdjoint.hpp"
 
@@ -310,6 +312,41 @@ int main()
     if (water > qin * T * (1 + 1e-9) || water < qin * T * (1 - 1e-3) || smin < -1e-12 || smax > 1 + 1e-12) {
         std::printf("transport mass balance %g vs %g\n", water, qin * T);
         return 1;
+    }
+    // ImplicitCapillarity with one RockJfunc table: the step keeps the saturation volume and
+    // stays inside the table's [s_min, s_max]
+    {
+        Opm::gpu::RockTables rt;
+        Opm::gpu::RockTable tab;
+        for (int i = 0; i <= 16; ++i) {
+            const double s = 0.1 + 0.05 * i, se = (s - 0.1) / 0.8;
+            tab.s.push_back(s);
+            tab.krw.push_back(se * se);
+            tab.kro.push_back((1 - se) * (1 - se));
+            tab.J.push_back(2.0 * (1 - se) * (1 - se) + 0.05 * (1 - se));
+        }
+        rt.rocks.push_back(tab);
+        rt.cell_rock.assign(nc, 0);
+        rt.sigma_cos_theta = 1e-6;
+        Opm::gpu::ImplicitCapillarity<GridInterface, Rock, LinearBC, NoInnerProduct> cap(g, r, bcx);
+        cap.setRockTables(rt);
+        std::vector<double> sc(nc);
+        double v0 = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            sc[c] = 0.3 + 0.4 * sw[c];
+            v0 += sc[c];
+        }
+        cap.transportSolve(sc, T, grav, s.getSolution(), inj);
+        double v1 = 0.0, lo = 1, hi = 0;
+        for (int c = 0; c < nc; ++c) {
+            v1 += sc[c];
+            lo = std::fmin(lo, sc[c]);
+            hi = std::fmax(hi, sc[c]);
+        }
+        if (std::fabs(v1 - v0) > 1e-10 * v0 || lo < 0.1 || hi > 0.9 || cap.lastStats().root_iterations <= 0) {
+            std::printf("capillary step: volume %g vs %g, range [%g, %g]\n", v1, v0, lo, hi);
+            return 1;
+        }
     }
     // forward/backward pair: J = sum of squared mismatches at three cells + scaled outflux at x+
     {
