@@ -58,6 +58,9 @@ def parse():
                     help="pressure solve with tensor mobilities (MimeticIPAnisoRelpermEvaluator inner product)")
     ap.add_argument("--adjoint", action="store_true",
                     help="adjoint gradient (forward solve + objective + backward) instead of the pressure bench")
+    ap.add_argument("--capillary", action="store_true",
+                    help="ImplicitCapillarity steps on the layered 1M-cell grid with rock tables instead of the "
+                         "pressure bench")
     ap.add_argument("--profile-only", choices=["mixed", "fp64"], default=None,
                     help="run warmup + steps of one precision and print nothing else (for ncu captures)")
     return ap.parse_args()
@@ -449,6 +452,93 @@ def run_impes(args):
     print(json.dumps(out), flush=True)
 
 
+def run_capillary(args):
+    """ImplicitCapillarity::transportSolve on the layered grid with two RockJfunc rocks: a step is one
+    porsol_capillary_solve with host inputs and output (capillary mobilities, viscous upstream residual,
+    the capillary-pressure solve with AMG-CG, the volume-matching root search, the relaxed update).
+    The flux comes from one pressure solve with the tables' mobilities.  The CPU baseline runs the
+    oracle's step (ILU0-CG) on a 50x50x25 box of the same workload and scales it by the cell ratio
+    (its CG iteration count grows with the grid, so the scaled figure flatters the CPU)."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    wl = ge.load_module("workloads")
+    dims = tuple(int(x) for x in args.dims.split(","))
+
+    def setup(dims_):
+        prob = wl.layered_capillary(dims=dims_)
+        g = prob.grid
+        _, mu1, mu2, r1, r2 = prob.fluid
+        tabs, cr = prob.extra["tables"], prob.extra["cell_rock"]
+        m1, m2 = wl.table_mobilities(tabs, cr, prob.sat, mu1, mu2)
+        return prob, g, (mu1, mu2, r1, r2), tabs, cr, m1, m2
+
+    prob, g, (mu1, mu2, r1, r2), tabs, cr, m1, m2 = setup(dims)
+    nc = g.num_cells
+    sct = prob.extra["sigma_cos_theta"]
+    P = pkg.PressureSolver()
+    P.init(g, prob.perm.ravel(), (0.0, 0.0, 0.0), prob.bc_type)
+    P.solve(pkg.Fluid(pkg.FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0), m1 + m2, prob.bc_type, prob.bc_value, prob.src,
+            mobdens=r1 * m1 + r2 * m2, opts=pkg.default_solve_opts(residual_tolerance=1e-12))
+    P.post_process_fluxes()
+    flux = P.solution()[1].copy()
+    T = pkg.TransportSolver()
+    T.init(g, prob.perm.ravel(), prob.poro, pkg.Fluid(pkg.FLUID_COREY2, mu1, mu2, r1, r2), prob.sat_type,
+           prob.sat_value)
+    T.set_rock_tables(tabs, cr, True, sct)
+    out = {"metric": "ImplicitCapillarity steps/s @1M cells", "unit": "capillary steps/s",
+           "config": {"workload": f"{'x'.join(map(str, dims))} layered log-normal, two RockJfunc rocks by layer, "
+                                  "s ~ U[0.3, 0.6], capillary pressure solve AMG-CG", "cells": nc, "tol": args.tol},
+           "data": "synthetic"}
+    pv = prob.poro * g.volume
+    res = {}
+    for name, prec, tol in (("mixed", pkg.MIXED, args.tol), ("fp64", pkg.FP64, args.tol64)):
+        o = pkg.default_capillary_opts(residual_tolerance=tol, precision=prec)
+        for _ in range(max(3, args.warmup)):
+            s_new, st = T.capillary_solve(P, prob.sat, flux, prob.bc_type, prob.bc_value, opts=o)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            s_new, st = T.capillary_solve(P, prob.sat, flux, prob.bc_type, prob.bc_value, opts=o)
+            times.append(time.perf_counter() - t0)
+        t = float(np.median(times))
+        res[name] = s_new
+        out[name] = {"value": round(1.0 / t, 3), "ms_per_step": round(1e3 * t, 3),
+                     "cg_iterations": st.pressure.iterations, "root_iterations": st.root_iterations,
+                     "evaluations": st.evaluations, "shift": st.shift,
+                     "volume_change": float(abs((pv * s_new).sum() - (pv * prob.sat).sum()) / pv.sum())}
+    out["value"] = out["mixed"]["value"]
+    out["speedup_mixed_vs_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    out["max_abs_diff_mixed_vs_fp64"] = float(np.abs(res["mixed"] - res["fp64"]).max())
+    if not args.no_cpu_baseline:
+        import oracle
+        if not os.path.exists(oracle.LIB_PATH):
+            oracle.build()
+        sdims = (50, 50, 25)
+        sp, sg, _, stabs, scr, sm1, sm2 = setup(sdims)
+        o = oracle.OraclePressure(sg, sp.bc_type)
+        o.compute_inner_products(sp.perm.ravel())
+        assert o.solve(sm1 + sm2, r1 * sm1 + r2 * sm2, sp.bc_type, sp.bc_value, sp.src, tol=1e-12) == 0
+        o.post_process_fluxes()
+        sflux = o.solution()[1]
+        rt = oracle.RockTables(stabs, scr, True, sct)
+        OT = oracle.OracleTransport(sg, sp.perm.ravel(), sp.poro, rt.fluid(mu1, mu2, r1, r2), sp.sat_type,
+                                    sp.sat_value)
+        OP = oracle.OraclePressure(sg, sp.bc_type)
+        OP.compute_inner_products(sp.perm.ravel())
+        t0 = time.perf_counter()
+        rc, _, _, _, cit = oracle.capillary_solve(OP, OT, sp.sat, sflux, sp.bc_type, sp.bc_value,
+                                                  opts=oracle.CapillaryOpts.defaults(residual_tolerance=args.tol64))
+        el = time.perf_counter() - t0
+        assert rc == 0
+        scale = sg.num_cells / nc
+        out["cpu_baseline"] = {"value": round(scale / el, 5), "unit": "capillary steps/s", "cores": 1, "kind": "port",
+                               "sample": f"oracle step (ILU0-CG, {cit} its) on the 50x50x25 box of the workload, "
+                                         f"{el:.2f} s, scaled by the cell ratio {scale:.4f}"}
+    print(json.dumps(out), flush=True)
+
+
 def run_tensor(args):
     """The 1M-cell pressure solve of the headline with tensor mobilities: per cell the total mobility
     tensor diag(m, m/2, 2m), m the Corey-2 total mobility at the cell's saturation (lambda_t commutes
@@ -637,6 +727,9 @@ def main():
         return
     if args.tensor:
         run_tensor(args)
+        return
+    if args.capillary:
+        run_capillary(args)
         return
     if args.impl == "reference":
         run_reference(args)

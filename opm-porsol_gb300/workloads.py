@@ -19,6 +19,10 @@ pressure in Pa (the workloads prescribe p = 1 and p = 0).
   layered_lognormal      200x200x25, 25 layers, layer mean ~ N(ln 100 mD, 1),
                          ln k ~ N(mean, 2^2) i.i.d. within a layer, Corey-2 with viscosity
                          ratio 10, initial s = 0, water (s = 1) enters through x- (seed + 5).
+  layered_capillary      the layered_lognormal grid and permeability with two RockJfunc
+                         rocks by layer parity (s in [0.1, 0.9] / [0.15, 0.85], power-law
+                         relperms, decreasing J), porosity ~ U[0.15, 0.3], s ~ U[0.3, 0.6],
+                         J scaling sigma cos(theta) = 1e-6 (seed + 6).
 """
 from __future__ import annotations
 
@@ -219,3 +223,40 @@ def error_norms(problem, pressure):
     v = g.volume
     totv = v.sum()
     return (np.sum(np.abs(diff * v)) / totv, np.sqrt(np.sum(diff * diff * v)) / totv, np.abs(diff).max())
+
+
+def rock_table(smin, smax, n=17, jmax=2.0, ew=2.0, eo=2.0):
+    """A RockJfunc table (columns s, krw, kro, J): power-law relative permeabilities in the
+    normalised saturation and a decreasing J-function that reaches 0 at s_max."""
+    s = np.linspace(smin, smax, n)
+    se = (s - smin) / (smax - smin)
+    J = jmax * (1.0 - se) ** 2 + 0.05 * (1.0 - se)
+    return np.column_stack([s, se ** ew, (1.0 - se) ** eo, J])
+
+
+def layered_capillary(dims=(200, 200, 25), seed=None):
+    """The ImplicitCapillarity workload: layered_lognormal's grid, permeability and x-Dirichlet
+    pressure BCs with two rocks (by layer parity) and a heterogeneous initial saturation."""
+    base = layered_lognormal(dims=dims, seed=SEED0 + 5 if seed is None else seed)
+    rng = np.random.default_rng(SEED0 + 6 if seed is None else seed + 1)
+    nc = base.grid.num_cells
+    nx, ny, _ = dims
+    tables = [rock_table(0.1, 0.9), rock_table(0.15, 0.85, n=11, jmax=3.0, ew=3.0, eo=1.5)]
+    cell_rock = ((np.arange(nc) // (nx * ny)) % 2).astype(np.int32)
+    base.poro = rng.uniform(0.15, 0.3, nc)
+    base.sat = rng.uniform(0.3, 0.6, nc)
+    base.sat_value = np.full(base.grid.num_half_faces, 0.85)
+    base.name = "layered_capillary"
+    base.extra.update(tables=tables, cell_rock=cell_rock, sigma_cos_theta=1e-6)
+    return base
+
+
+def table_mobilities(tables, cell_rock, s, mu1, mu2):
+    """kr / mu per cell from the rock tables (piecewise linear, end values outside)."""
+    m1 = np.empty_like(s)
+    m2 = np.empty_like(s)
+    for r, t in enumerate(tables):
+        c = cell_rock == r
+        m1[c] = np.interp(s[c], t[:, 0], t[:, 1]) / mu1
+        m2[c] = np.interp(s[c], t[:, 0], t[:, 2]) / mu2
+    return m1, m2
