@@ -23,6 +23,15 @@ constexpr int TB = 256;
 
 __device__ __forceinline__ int slot_of(const int* sp, int r, int t) { return sp[r >> 5] + t * 32 + (r & 31); }
 
+// Row r and lane q of the row for K lanes per row (K = 1: one thread per row).
+template <int K>
+__device__ __forceinline__ void row_lane(int& r, int& q)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    r = g / K;
+    q = g % K;
+}
+
 // ---------------- exclusive scan ----------------
 __global__ void k_scan_block(int n, const int* __restrict__ in, int* __restrict__ out, int* __restrict__ bsum)
 {
@@ -125,36 +134,60 @@ __global__ void k_isolated(int n, const int* __restrict__ sp, const int* __restr
     join[i] = -1;
 }
 
-template <class T>
+// best candidate of K lanes: (strength, hash, column) is a strict total order over the distinct
+// columns of a row, so the reduction gives the one-lane scan's answer in any lane order
+template <int K>
+__device__ __forceinline__ void best_of_lanes(float& bs, unsigned& bh, int& bj)
+{
+#pragma unroll
+    for (int o = K >> 1; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, bs, o);
+        const unsigned h2 = __shfl_xor_sync(0xffffffffu, bh, o);
+        const int j2 = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (j2 >= 0 && (bj < 0 || stronger(s2, h2, j2, bs, bh, bj))) {
+            bs = s2;
+            bh = h2;
+            bj = j2;
+        }
+    }
+}
+
+// Strongest free neighbour of every free row (-1 if none).  K lanes per row (lane q scans the
+// entries q, q + K, ...): coarse levels have few, long rows, and one thread per row leaves the
+// SMs idle behind a chain of dependent gathers.
+template <class T, int K>
 __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
                        const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
                        int* __restrict__ best, int neg, float theta)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (state[i] != 0) {
-        best[i] = -1;
-        return;
-    }
-    const float ri = rs[i];
+    int i, q;
+    row_lane<K>(i, q);
+    const bool valid = i < n;
+    if (K == 1 && !valid) return;
+    const bool active = valid && state[i] == 0;
     float bs = 0.0f;
     unsigned bh = 0u;
     int bj = -1;
-    for (int t = 0; t < rowlen[i]; ++t) {
-        const int k = slot_of(sp, i, t);
-        const int j = col[k];
-        if (j == i || state[j] != 0) continue;
-        const float a = float(A[k]);
-        const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
-        if (!(s > 0.0f && s >= theta)) continue;
-        const unsigned h = edge_hash(i, j);
-        if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
-            bs = s;
-            bh = h;
-            bj = j;
+    if (active) {
+        const float ri = rs[i];
+        const int len = rowlen[i];
+        for (int t = q; t < len; t += K) {
+            const int k = slot_of(sp, i, t);
+            const int j = col[k];
+            if (j == i || state[j] != 0) continue;
+            const float a = float(A[k]);
+            const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
+            if (!(s > 0.0f && s >= theta)) continue;
+            const unsigned h = edge_hash(i, j);
+            if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
+                bs = s;
+                bh = h;
+                bj = j;
+            }
         }
     }
-    best[i] = bj;
+    if (K > 1) best_of_lanes<K>(bs, bh, bj);
+    if (valid && q == 0) best[i] = active ? bj : -1;
 }
 
 __global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ best, int* __restrict__ partner)
@@ -170,32 +203,39 @@ __global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ 
     }
 }
 
-// unmatched rows pick their strongest paired neighbour (|a_ij| scaled)
-template <class T>
+// unmatched rows pick their strongest paired neighbour (|a_ij| scaled); K lanes per row as k_pick
+template <class T, int K>
 __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
                        const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
                        int* __restrict__ join)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (state[i] != 0 && state[i] != 3)) return;
-    const float ri = rs[i];
+    int i, q;
+    row_lane<K>(i, q);
+    const bool valid = i < n;
+    if (K == 1 && !valid) return;
+    const bool active = valid && (state[i] == 0 || state[i] == 3);
     float bs = 0.0f;
     unsigned bh = 0u;
     int bj = -1;
-    for (int t = 0; t < rowlen[i]; ++t) {
-        const int k = slot_of(sp, i, t);
-        const int j = col[k];
-        if (j == i || state[j] != 1) continue;
-        const float s = fabsf(float(A[k])) * ri * rs[j];
-        if (!(s > 0.0f)) continue;
-        const unsigned h = edge_hash(i, j);
-        if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
-            bs = s;
-            bh = h;
-            bj = j;
+    if (active) {
+        const float ri = rs[i];
+        const int len = rowlen[i];
+        for (int t = q; t < len; t += K) {
+            const int k = slot_of(sp, i, t);
+            const int j = col[k];
+            if (j == i || state[j] != 1) continue;
+            const float s = fabsf(float(A[k])) * ri * rs[j];
+            if (!(s > 0.0f)) continue;
+            const unsigned h = edge_hash(i, j);
+            if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
+                bs = s;
+                bh = h;
+                bj = j;
+            }
         }
     }
-    join[i] = bj;
+    if (K > 1) best_of_lanes<K>(bs, bh, bj);
+    if (active && q == 0) join[i] = bj;
 }
 
 __global__ void k_rep_flag(int n, const int* __restrict__ state, const int* __restrict__ partner,
@@ -547,14 +587,6 @@ __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __rest
     d[i] = ri * inv_theta;
 }
 
-// Row r and lane q of the row for K lanes per row (K = 1: one thread per row).
-template <int K>
-__device__ __forceinline__ void row_lane(int& r, int& q)
-{
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    r = g / K;
-    q = g % K;
-}
 
 // sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, K lanes otherwise
 template <int K, class T, class V, class XF>
@@ -767,6 +799,17 @@ int lanes_for(int n, long long nent)
     return k;
 }
 
+// Lanes per row of the matching sweeps: rows longer than about 12 entries (the coarse
+// levels) are scanned by up to 16 lanes, at least 4 entries per lane.
+int pick_lanes(int n, long long nent)
+{
+    const double avg = n > 0 ? double(nent) / n : 0.0;
+    if (avg <= 12.0) return 1;
+    int k = 1;
+    while (k < 16 && 8 * k <= avg) k *= 2;
+    return k;
+}
+
 #define PORSOL_LANES(K, LAUNCH)                                                                                    \
     switch (K) {                                                                                                   \
     case 1: { constexpr int KL = 1; LAUNCH; } break;                                                              \
@@ -821,12 +864,17 @@ void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, b
     // Mutual-best matching: each sweep pairs at least the strongest remaining edge; the
     // stall fallback (join) runs more sweeps so chains and stars also pair up.
     const int sweeps = join ? 8 : 4;
+    const int lanes = pick_lanes(n, P.nent);
+    const int nbk = div_up((long long)n * lanes, TB);
     for (int sweep = 0; sweep < sweeps; ++sweep) {
-        PORSOL_LAUNCH(k_pick<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, best.p, neg ? 1 : 0,
-                                    float(theta)));
+        PORSOL_LANES(lanes, PORSOL_LAUNCH((k_pick<T, KL><<<nbk, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A,
+                                                                           d.p, state.p, best.p, neg ? 1 : 0,
+                                                                           float(theta)))));
         PORSOL_LAUNCH(k_match<<<nb, TB, 0, s>>>(n, state.p, best.p, partner.p));
     }
-    if (join) PORSOL_LAUNCH(k_join<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, jn.p));
+    if (join)
+        PORSOL_LANES(lanes, PORSOL_LAUNCH((k_join<T, KL><<<nbk, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p,
+                                                                           state.p, jn.p))));
     PORSOL_LAUNCH(k_rep_flag<<<nb, TB, 0, s>>>(n, state.p, partner.p, jn.p, flag.p));
     exclusive_scan(s, n, flag.p, cidx.p, cidx.p + n, scan_blocks_);
     out.n = n;
