@@ -34,6 +34,7 @@ struct AmgOpts {
     bool round2_negative = false;  // second round likewise; off: directly |a_ij| with joins (the
                                    // negative attempt stalls on these systems and is discarded)
     bool half_smoother = true;     // FP32 hierarchies: smoother/residual read D^-1 A stored in FP16
+    bool layout4 = true;           // ... from a SELL-32x4 copy on levels smoothed one thread per row
     bool autotune = false;         // time the lane schedules of each new level shape once (the
                                    // choice then depends on timing: off where runs must be
                                    // bitwise reproducible)
@@ -68,6 +69,11 @@ private:
         DBuf<__half> ah;
         DBuf<T> diagv;
         bool half = false;
+        // SELL-32x4 copy of ah (levels smoothed with one thread per row): slice offsets,
+        // columns, FP16 values
+        bool v4 = false;
+        DBuf<int> sp4, col4;
+        DBuf<__half> ah4;
         double lmax = 2.0;
         int lanes = 1;               // threads per row in the smoother/residual kernels
         Aggregates agg;              // to the next level

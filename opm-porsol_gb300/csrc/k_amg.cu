@@ -23,13 +23,15 @@ constexpr int TB = 256;
 
 __device__ __forceinline__ int slot_of(const int* sp, int r, int t) { return sp[r >> 5] + t * 32 + (r & 31); }
 
-// Row r and lane q of the row for K lanes per row (K = 1: one thread per row).
+// Row r and lane q of the row for K lanes per row (K = 1: one thread per row; K = 0: one thread
+// per row on the SELL-32x4 copy of the matrix).
 template <int K>
 __device__ __forceinline__ void row_lane(int& r, int& q)
 {
+    constexpr int KK = K < 1 ? 1 : K;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    r = g / K;
-    q = g % K;
+    r = g / KK;
+    q = g % KK;
 }
 
 // ---------------- exclusive scan ----------------
@@ -163,7 +165,7 @@ __global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict_
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
-    if (K == 1 && !valid) return;
+    if (K <= 1 && !valid) return;
     const bool active = valid && state[i] == 0;
     float bs = 0.0f;
     unsigned bh = 0u;
@@ -212,7 +214,7 @@ __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict_
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
-    if (K == 1 && !valid) return;
+    if (K <= 1 && !valid) return;
     const bool active = valid && (state[i] == 0 || state[i] == 3);
     float bs = 0.0f;
     unsigned bh = 0u;
@@ -588,12 +590,15 @@ __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __rest
 }
 
 
-// sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, K lanes otherwise
+// sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, the SELL-32x4 copy
+// (sp, col, A its slice offsets, columns and FP16 values) for K = 0, K lanes otherwise
 template <int K, class T, class V, class XF>
 __device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __restrict__ col, const V* __restrict__ A,
                                      const int* __restrict__ rowlen, int r, int q, bool valid, XF xf)
 {
-    if constexpr (K == 1) {
+    if constexpr (K == 0) {
+        return valid ? sell4_dot<T>(sp, col, A, r, xf) : T(0);
+    } else if constexpr (K == 1) {
         return valid ? sell_dot<T>(sp, col, A, r, xf) : T(0);
     } else {
         return sell_dot_lanes<K, T>(sp, col, A, rowlen, r, q, valid, xf);
@@ -615,7 +620,7 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __res
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
-    if (K == 1 && !valid) return;
+    if (K <= 1 && !valid) return;
     T acc;
     if (xc) {
         acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [t, xc, agg, wp](int j) {
@@ -646,7 +651,7 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
-    if (K == 1 && !valid) return;
+    if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
     if (!valid || q != 0) return;
     const T di = d_in[i];
@@ -668,7 +673,7 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
-    if (K == 1 && !valid) return;
+    if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
     if (!valid || q != 0) return;
     r[i] = SCALED ? b[i] - diagv[i] * acc : b[i] - acc;
@@ -690,6 +695,45 @@ __global__ void k_scale_half(int n, const int* __restrict__ sp, const int* __res
     for (int t = 0; t < w; ++t) {
         const int k = b + 32 * t + lane;
         ah[k] = __float2half_rn(row ? float(A[k] * di) : 0.0f);
+    }
+    if (row) diagv[r] = A[diag[r]];
+}
+
+// SELL-32x4 copy of a level for the one-thread-per-row smoother: per slice, groups of four
+// consecutive entries of each row, lane-interleaved (entry t of row r at
+// sp4[r/32] + 128 (t/4) + 4 (r%32) + t%4), so a row's four columns come in one 16-byte load and its
+// four FP16 values in one 8-byte load.  Rows are padded to a multiple of four entries (col = row,
+// value 0).  groups[s] = 128 * ceil(width / 4).
+__global__ void k_slice_groups(int nslices, const int* __restrict__ sp, int* __restrict__ groups)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nslices) groups[s] = ((((sp[s + 1] - sp[s]) >> 5) + 3) >> 2) * 128;
+}
+
+// the SELL-32x4 copy written straight from A (FP16 D^-1 A as k_scale_half), and the diagonal
+template <class T>
+__global__ void k_scale_half4(int n, int nslices, const int* __restrict__ sp, const int* __restrict__ col,
+                              const int* __restrict__ diag, const T* __restrict__ A, const T* __restrict__ dinv,
+                              const int* __restrict__ sp4, int* __restrict__ col4, __half* __restrict__ ah4,
+                              T* __restrict__ diagv)
+{
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (s >= nslices) return;
+    const int lane = threadIdx.x & 31, r = s * 32 + lane;
+    const bool row = r < n;
+    const T di = row ? dinv[r] : T(0);
+    const int b = sp[s], w = (sp[s + 1] - b) >> 5;
+    const int b4 = sp4[s], g4 = (sp4[s + 1] - b4) >> 7;
+    for (int t = 0; t < 4 * g4; ++t) {
+        const int dst = b4 + 128 * (t >> 2) + 4 * lane + (t & 3);
+        if (t < w) {
+            const int k = b + 32 * t + lane;
+            col4[dst] = col[k];
+            ah4[dst] = __float2half_rn(row ? float(A[k] * di) : 0.0f);
+        } else {
+            col4[dst] = row ? r : 0;
+            ah4[dst] = __float2half_rn(0.0f);
+        }
     }
     if (row) diagv[r] = A[diag[r]];
 }
@@ -995,7 +1039,24 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
                                                  s_gmax_.p + level, status_.p));
     PORSOL_CUDA(cudaGetLastError());
     L.half = o_.half_smoother && std::is_same<T, float>::value;
-    if (L.half) {
+    // one thread per row without timing (the rule's choice): the smoother reads the SELL-32x4
+    // copy only, written in place of the plain FP16 copy
+    L.v4 = L.half && o_.layout4 && !o_.autotune && lanes_for(n, L.P->nent) == 1;
+    const SellPattern& P = *L.P;
+    if (L.v4) {
+        L.sp4.alloc(size_t(P.nslices) + 1);
+        s_width_.alloc(std::max(P.nslices, 1));
+        PORSOL_LAUNCH(k_slice_groups<<<div_up(P.nslices, TB), TB, 0, s>>>(P.nslices, P.slice_ptr.p, s_width_.p));
+        exclusive_scan(s, P.nslices, s_width_.p, L.sp4.p, L.sp4.p + P.nslices, scan_blocks_);
+        // at most 3 padding entries per row: no host read of the exact size
+        const size_t cap = size_t(P.nent) + 96 * size_t(P.nslices);
+        L.col4.alloc(cap);
+        L.ah4.alloc(cap);
+        L.diagv.alloc(n);
+        PORSOL_LAUNCH(k_scale_half4<T><<<div_up(P.nslices, TB / 32), TB, 0, s>>>(
+            n, P.nslices, P.slice_ptr.p, P.col.p, P.diag.p, L.A, L.dinv.p, L.sp4.p, L.col4.p, L.ah4.p, L.diagv.p));
+        PORSOL_CUDA(cudaGetLastError());
+    } else if (L.half) {
         L.ah.alloc(size_t(L.P->nent));
         L.diagv.alloc(n);
         PORSOL_LAUNCH(k_scale_half<T><<<div_up(L.P->nslices, TB / 32), TB, 0, s>>>(
@@ -1006,7 +1067,7 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.r.alloc(n);
     L.d0.alloc(n);
     L.d1.alloc(n);
-    L.lanes = tune_lanes(s, L);
+    L.lanes = L.v4 ? 1 : tune_lanes(s, L);
 }
 
 // Lane schedule autotuner: for a level shape not seen before, time one smoother step with 1, 2,
@@ -1193,7 +1254,11 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
         const int nbk = div_up(n * L.lanes, TB);
-        if (L.half) {
+        if (L.v4) {
+            PORSOL_LAUNCH((k_cheb_start<T, 0, __half, true><<<nb, TB, 0, s>>>(
+                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d,
+                T(1.0 / theta), stop)));
+        } else if (L.half) {
             PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, __half, true><<<nbk, TB, 0, s>>>(
                                       n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg,
                                       T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop))));
@@ -1216,7 +1281,11 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
         const int nbk = div_up(n * L.lanes, TB);
-        if (L.half) {
+        if (L.v4) {
+            PORSOL_LAUNCH((k_cheb_step<T, 0, __half, true><<<nb, TB, 0, s>>>(
+                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
+                k == deg ? 1 : 0, stop)));
+        } else if (L.half) {
             PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, __half, true><<<nbk, TB, 0, s>>>(
                                       n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x,
                                       T(c1), T(c2), k == deg ? 1 : 0, stop))));
@@ -1249,7 +1318,10 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
     // restrict the residual
-    if (L.half) {
+    if (L.v4) {
+        PORSOL_LAUNCH((k_resid<T, 0, __half, true><<<nb, TB, 0, s>>>(n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.diagv.p,
+                                                                      b, L.t.p, L.r.p, stop)));
+    } else if (L.half) {
         PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL, __half, true><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
                                   n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop))));
     } else {
