@@ -71,9 +71,10 @@ __device__ __forceinline__ Acc sell_dot_lanes(const int* __restrict__ sp, const 
 // sp4[r/32] + 128 (t/4) + 4 (r%32) + t%4; the slice's group count is uniform in the warp): the
 // columns and values of GB groups (4 GB entries) are loaded as 16- and 8-byte vectors before their
 // gathers, then the products are added in entry order -- the same sequential sum as sell_dot on the
-// plain layout (the extra padding adds exact zeros).  GB = 2 measured fastest on the finest level
-// of the 1M-cell system (GB = 3 and 4 hold more registers and lose occupancy).
-template <class Acc, class XF, int GB = 2>
+// plain layout (the extra padding adds exact zeros).  GB = 1 keeps the smoother kernels at 32
+// registers (full occupancy); on the finest level of the 1M-cell system that beat 2-4 groups per
+// round (40-64 registers) by 7 % of the whole solve.
+template <class Acc, class XF, int GB = 1>
 __device__ __forceinline__ Acc sell4_dot(const int* __restrict__ sp4, const int* __restrict__ col4,
                                          const __half* __restrict__ a4, int r, XF xf)
 {
