@@ -640,6 +640,18 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __res
     d[i] = ri * inv_theta;
 }
 
+// y = t + w P xc (the coarse correction), for the levels whose smoother then gathers one vector
+template <class T>
+__global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
+                              T wp, T* __restrict__ y, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int ai = agg[i];
+    y[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
+}
+
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
 template <class T, int K, class V, bool SCALED>
 __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col,
@@ -1255,9 +1267,12 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         const T* t = xc ? L.t.p : x;
         const int nbk = div_up(n * L.lanes, TB);
         if (L.v4) {
+            // large levels: form y = t + w P xc first, so the start's row dot gathers one vector
+            // instead of t, agg and xc (the same y, the same sums)
+            if (xc) PORSOL_LAUNCH(k_prolong_add<T><<<nb, TB, 0, s>>>(n, t, xc, agg, T(o_.prolong), x, stop));
             PORSOL_LAUNCH((k_cheb_start<T, 0, __half, true><<<nb, TB, 0, s>>>(
-                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d,
-                T(1.0 / theta), stop)));
+                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p,
+                d, T(1.0 / theta), stop)));
         } else if (L.half) {
             PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, __half, true><<<nbk, TB, 0, s>>>(
                                       n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg,
