@@ -393,13 +393,16 @@ __global__ void k_gal_rowbound(int nc, const int* __restrict__ ptr, const int* _
     if ((threadIdx.x & 31) == 0) atomicMax(maxb, b);
 }
 
-// Warp-per-coarse-row Galerkin merge, one pass: the member rows' entries (column mapped
-// through agg) are loaded into shared memory, bitonic-sorted by column and duplicates summed
-// (FP64); the distinct (column, value) pairs go compactly to off[I] of a temporary buffer,
-// with the row length and the position of the diagonal.  The SELL layout is filled from there
-// once the slice widths are known (k_gal_scatter).
+// Galerkin merge, one pass, L lanes per coarse row (32 / L rows per warp): the member rows'
+// entries (column mapped through agg) are loaded into shared memory, bitonic-sorted by column and
+// duplicates summed (FP64); the distinct (column, value) pairs go compactly to off[I] of a
+// temporary buffer, with the row length and the position of the diagonal.  The SELL layout is
+// filled from there once the slice widths are known (k_gal_scatter).  The host picks L so that
+// each lane holds about four of the CAP candidates: short rows (the first levels: pairs of
+// 11-entry rows over millions of rows) share a warp, and each lane keeps several independent
+// compare-exchanges in flight per stage.
 constexpr int GW_WARPS = 4;
-template <class T, int CAP>
+template <class T, int CAP, int L>
 __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_merge(int nc, const int* __restrict__ sp,
                                                            const int* __restrict__ col, const int* __restrict__ rowlen,
                                                            const T* __restrict__ A, const int* __restrict__ agg,
@@ -408,36 +411,48 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_merge(int nc, const int* 
                                                            T* __restrict__ tval, int* __restrict__ rowlen_c,
                                                            int* __restrict__ dpos)
 {
-    __shared__ int sk[GW_WARPS][CAP];
-    __shared__ double sv[GW_WARPS][CAP];
+    constexpr int R = 32 / L;   // rows per warp
+    // row strides padded so that the R rows of a warp start L words (keys) and 8 words (values)
+    // apart modulo the 32 banks: same-position accesses of different rows do not collide
+    constexpr int KS = CAP + (L < 32 ? L : 0), VS = CAP + (L < 32 ? L / 2 : 0);
+    __shared__ int sk[GW_WARPS * R * KS];
+    __shared__ double sv[GW_WARPS * R * VS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int I = blockIdx.x * GW_WARPS + w;
-    if (I >= nc) return;   // warp-uniform
-    int* keys = sk[w];
-    double* vals = sv[w];
+    const int sub = lane / L, sl = lane % L;
+    const int I0 = (blockIdx.x * GW_WARPS + w) * R;
+    if (I0 >= nc) return;   // warp-uniform
+    const int I = I0 + sub;
+    const bool active = I < nc;
+    int* keys = sk + (w * R + sub) * KS;
+    double* vals = sv + (w * R + sub) * VS;
     int m = 0;
-    for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
-        const int r = idx[q];
-        const int len = rowlen[r];
-        const int base = sp[r >> 5] + (r & 31);
-        for (int t = lane; t < len; t += 32) {
-            const int k = base + t * 32;
-            const int c = agg[col[k]];
-            keys[m + t] = c < 0 ? INT_MAX : c;
-            vals[m + t] = double(A[k]);
+    if (active) {
+        for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
+            const int r = idx[q];
+            const int len = rowlen[r];
+            const int base = sp[r >> 5] + (r & 31);
+            for (int t = sl; t < len; t += L) {
+                const int k = base + t * 32;
+                const int c = agg[col[k]];
+                keys[m + t] = c < 0 ? INT_MAX : c;
+                vals[m + t] = double(A[k]);
+            }
+            m += len;
         }
-        m += len;
     }
+    // one network size for the warp: the largest power of two over its rows
     int m2 = 1;
     while (m2 < m) m2 <<= 1;
-    for (int p = m + lane; p < m2; p += 32) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m2 = max(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    for (int p = m + sl; p < m2; p += L) {
         keys[p] = INT_MAX;
         vals[p] = 0.0;
     }
     __syncwarp();
     for (int k = 2; k <= m2; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int p = lane; p < m2; p += 32) {
+            for (int p = sl; p < m2; p += L) {
                 const int q = p ^ j;
                 if (q > p) {
                     const bool up = (p & k) == 0;
@@ -445,33 +460,35 @@ __global__ void __launch_bounds__(GW_WARPS * 32) k_gal_merge(int nc, const int* 
                     if ((kp > kq) == up) {
                         keys[p] = kq;
                         keys[q] = kp;
-                        const double t = vals[p];
+                        const double tv = vals[p];
                         vals[p] = vals[q];
-                        vals[q] = t;
+                        vals[q] = tv;
                     }
                 }
             }
             __syncwarp();
         }
     }
-    const int o = off[I];
+    const int o = active ? off[I] : 0;
+    const unsigned rowmask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << (sub * L);
     int base = 0, dp = -1;
-    for (int c0 = 0; c0 < m2; c0 += 32) {
-        const int p = c0 + lane;
-        const bool head = p < m2 && keys[p] != INT_MAX && (p == 0 || keys[p] != keys[p - 1]);
-        const unsigned mask = __ballot_sync(0xffffffffu, head);
+    for (int c0 = 0; c0 < m2; c0 += L) {
+        const int p = c0 + sl;
+        const bool head = active && p < m2 && keys[p] != INT_MAX && (p == 0 || keys[p] != keys[p - 1]);
+        const unsigned mask = __ballot_sync(0xffffffffu, head) & rowmask;
         if (head) {
             double sum = vals[p];
             for (int q = p + 1; q < m2 && keys[q] == keys[p]; ++q) sum += vals[q];
-            const int t = base + __popc(mask & ((1u << lane) - 1u));
-            tcol[o + t] = keys[p];
-            tval[o + t] = T(sum);
-            if (keys[p] == I) dp = t;
+            const int tt = base + __popc(mask & ((1u << lane) - 1u));
+            tcol[o + tt] = keys[p];
+            tval[o + tt] = T(sum);
+            if (keys[p] == I) dp = tt;
         }
         base += __popc(mask);
     }
-    for (int q = 16; q > 0; q >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, q));
-    if (lane == 0) {
+#pragma unroll
+    for (int q = L / 2; q > 0; q >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, q));
+    if (active && sl == 0) {
         rowlen_c[I] = base;
         dpos[I] = dp;
     }
@@ -1001,11 +1018,14 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
         s_tcol_.alloc(std::max(total, 1));
         s_tval_.alloc(std::max(total, 1));
         s_dpos_.alloc(std::max(nc, 1));
-        const int nbw = div_up(nc, GW_WARPS);
 #define PORSOL_GALM(CAP)                                                                                            \
-    PORSOL_LAUNCH((k_gal_merge<T, CAP><<<nbw, GW_WARPS * 32, 0, s>>>(nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A,      \
-                                                                      a.agg.p, a.ptr.p, a.idx.p, s_goff_.p,         \
-                                                                      s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p)))
+    {                                                                                                               \
+        constexpr int LL = CAP / 4 < 8 ? 8 : (CAP / 4 > 32 ? 32 : CAP / 4);                                          \
+        const int nbw = div_up(nc, GW_WARPS * (32 / LL));                                                           \
+        PORSOL_LAUNCH((k_gal_merge<T, CAP, LL><<<nbw, GW_WARPS * 32, 0, s>>>(                                        \
+            nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p, s_goff_.p, s_tcol_.p, s_tval_.p,     \
+            Pc.rowlen.p, s_dpos_.p)));                                                                              \
+    }
         if (bound <= 32) { PORSOL_GALM(32); }
         else if (bound <= 64) { PORSOL_GALM(64); }
         else if (bound <= 128) { PORSOL_GALM(128); }
