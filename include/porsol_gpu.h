@@ -83,8 +83,9 @@ typedef struct porsol_solver porsol_solver;
 
 /* linsolver_type: 0 = ILU0-preconditioned CG, 1 = AMG-preconditioned CG (default),
  * 2 = KAMG (runs the type-1 AMG-CG), 3 = FastAMG (runs the type-1 AMG-CG).
- * precision: PORSOL_FP64 = the plain drop-in; PORSOL_MIXED = FP32 SpMV and
- * preconditioner inside FP64 iterative refinement. */
+ * precision: PORSOL_FP64 = the plain drop-in; PORSOL_MIXED = FP32 AMG hierarchy (FP16
+ * smoother matrices); single solves run FP32 CG recurrences with an FP64 solution and FP64
+ * residual replacements, batched upscaling runs FP64 CG around the FP32 hierarchy. */
 enum { PORSOL_FP64 = 0, PORSOL_MIXED = 1 };
 typedef struct porsol_solve_opts {
     double residual_tolerance;  /* 1e-8   (IncompFlowSolverHybrid.hpp:662) */
@@ -96,12 +97,12 @@ typedef struct porsol_solve_opts {
     int smooth_steps;           /* 1      (:668) pre/post smoothing sweeps */
     int precision;              /* PORSOL_FP64 */
     double inner_tolerance;     /* mixed only: residual drop that triggers an FP64 residual replacement (3e-3) */
-    int max_outer;              /* mixed batched upscaling only: refinement steps before giving up (30) */
+    int max_outer;              /* reserved (ignored; kept for layout compatibility) */
 } porsol_solve_opts;
 
 typedef struct porsol_solve_stats {
     int iterations;          /* CG iterations (sum of inner iterations in mixed mode) */
-    int outer_iterations;    /* refinement steps (mixed), 1 for FP64 */
+    int outer_iterations;    /* FP64 residual replacements (mixed single solves), 1 otherwise */
     double reduction;        /* final ||r||/||r0|| */
     int amg_levels;          /* levels of the AMG hierarchy (0 for ILU0) */
     double mass_balance;     /* max_c |sum_f v - q_c| / max(max_c |q_c|, max_f |v_f|), FP64 */

@@ -61,13 +61,25 @@ private:
                    const double* tol);
 };
 
-// Per-block helpers of the mixed-precision refinement around BatchedPcg.
+// FP64 Krylov with an FP32 block-diagonal preconditioner: z = isc_g * double(M32(float(sc_g r)))
+// per block g.  The preconditioner is linear and block diagonal, so the per-block scaling
+// (sc = 1 / ||r0_g||, isc = ||r0_g||) only keeps the FP32 vectors in range; the CG recurrences,
+// the solution and the stopping test stay FP64, so no restart is ever needed.
+class BatchCastPrecond : public Precond<double> {
+public:
+    void bind(Precond<float>* inner, const BatchRanges* B, const double* sc, const double* isc);
+    void apply(cudaStream_t s, const double* r, double* z, const int* stop) override;
+
+private:
+    Precond<float>* m_ = nullptr;
+    const BatchRanges* B_ = nullptr;
+    const double *sc_ = nullptr, *isc_ = nullptr;
+    long long inner_gen_ = -1;
+    DBuf<float> r32_, z32_;
+};
+
+// Per-block helper of the batched solve.
 // out[g] = ||a_g||_2 (deterministic order)
 template <class T>
 void batch_norms(cudaStream_t s, const BatchRanges& B, const T* a, double* out);
-// b = float(a * scale[blk])
-void batch_to_f32_scaled(cudaStream_t s, const BatchRanges& B, const double* a, float* b, const double* scale);
-// x += scale[blk] * double(y)
-void batch_add_f32_scaled(cudaStream_t s, const BatchRanges& B, const float* y, const double* scale, double* x);
-
 }  // namespace porsol

@@ -356,6 +356,9 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     ao.smooth_steps = std::max(1, o.smooth_steps);
     ao.prolong = o.prolongate_factor;
     ao.autotune = true;   // the sub-grid union's level shapes are unlike a single grid's
+    // FP32 smoother values: with the FP16 copy the full-tensor, rotated sub-grids needed 491 CG
+    // iterations for 512 sub-grids x 3 solves against 282 (and 239 in FP64)
+    ao.half_smoother = false;
     const bool mixed = o.precision == PORSOL_MIXED && o.linsolver_type != 0;
     if (!mixed) {
         Precond<double>* M = nullptr;
@@ -397,57 +400,30 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     PORSOL_CUDA(cudaStreamSynchronize(stream));
     st.ms_precond_setup = now_ms() - t_begin;
     st.amg_levels = amg32.levels();
+    // FP64 batched CG around the FP32 AMG hierarchy, per-block scaled into FP32 range
     ir_r.alloc(n);
-    ir_r32.alloc(n);
-    ir_d32.alloc(n);
     bnorm.alloc(nb);
-    std::vector<double> r0(nb), rn(nb), sc(nb);
-    auto norms = [&](std::vector<double>& out) {
-        residual<double, double>(stream, P, val.p, x.p, rhs.p, ir_r.p);
-        batch_norms<double>(stream, batch, ir_r.p, bnorm.p);
-        bnorm.download(out.data(), nb, stream);
-        PORSOL_CUDA(cudaStreamSynchronize(stream));
-    };
-    norms(r0);
-    rn = r0;
-    // restarted per-block refinement: each restart needs a 1e-3 drop to pay for itself
-    const double inner_tol = std::min(o.inner_tolerance > 0 ? o.inner_tolerance : 1e-3, 1e-3);
-    const int max_outer = o.max_outer > 0 ? o.max_outer : 30;
-    int total = 0, outer = 0;
-    auto worst = [&]() {
-        double w = 0.0;
-        for (int g = 0; g < nb; ++g)
-            if (r0[g] > 0) w = std::max(w, rn[g] / r0[g]);
-        return w;
-    };
-    for (;;) {
-        bool any = false;
-        for (int g = 0; g < nb; ++g) {
-            const bool act = rn[g] >= o.residual_tolerance * r0[g] && rn[g] >= 1e-30;
-            any = any || act;
-            sc[g] = act ? 1.0 / rn[g] : 0.0;
-            // the last refinement step of a block only needs its remaining reduction (x 0.3)
-            h[g] = act ? std::min(0.5, std::max(inner_tol, 0.3 * o.residual_tolerance * r0[g] / rn[g])) : 1.0;
-        }
-        if (!any) break;
-        if (outer >= max_outer || total >= maxit) fail(total, worst());
-        if (!std::isfinite(worst())) throw Error(PORSOL_ERR_NONFINITE, "iterative refinement diverged");
-        upload(bscale, sc);
-        upload(btol, h);
-        batch_to_f32_scaled(stream, batch, ir_r.p, ir_r32.p, bscale.p);
-        PORSOL_CUDA(cudaMemsetAsync(ir_d32.p, 0, n * sizeof(float), stream));
-        CgResult r = bcg32.solve(stream, P, val32.p, amg32, batch, ir_r32.p, ir_d32.p, btol.p, maxit - total);
-        total += r.iterations;
-        ++outer;
-        if (r.breakdown && r.iterations == 0) throw Error(PORSOL_ERR_NONFINITE, "inner CG breakdown");
-        for (int g = 0; g < nb; ++g) sc[g] = sc[g] > 0 ? rn[g] : 0.0;
-        upload(bscale, sc);
-        batch_add_f32_scaled(stream, batch, ir_d32.p, bscale.p, x.p);
-        norms(rn);
+    residual<double, double>(stream, P, val.p, x.p, rhs.p, ir_r.p);
+    batch_norms<double>(stream, batch, ir_r.p, bnorm.p);
+    std::vector<double> r0(nb), sc(nb);
+    bnorm.download(r0.data(), nb, stream);
+    PORSOL_CUDA(cudaStreamSynchronize(stream));
+    for (int g = 0; g < nb; ++g) {
+        const bool ok = r0[g] > 1e-300 && std::isfinite(r0[g]);
+        sc[g] = ok ? 1.0 / r0[g] : 0.0;
+        r0[g] = ok ? r0[g] : 0.0;
     }
-    st.iterations = total;
-    st.outer_iterations = outer;
-    st.reduction = worst();
+    upload(bscale, sc);
+    upload(bnorm, r0);
+    cast_pre.bind(&amg32, &batch, bscale.p, bnorm.p);
+    std::fill(h.begin(), h.end(), o.residual_tolerance);
+    upload(btol, h);
+    CgResult r = bcg64.solve(stream, P, val.p, cast_pre, batch, rhs.p, x.p, btol.p, maxit);
+    st.iterations = r.iterations;
+    st.outer_iterations = 1;
+    st.reduction = r.reduction;
+    if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+    if (!r.converged) fail(r.iterations, r.reduction);
 }
 
 void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const double* mobd, const int* bct,

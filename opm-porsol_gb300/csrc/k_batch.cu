@@ -213,21 +213,48 @@ __global__ void __launch_bounds__(BT) k_b_norms(const int* __restrict__ rg, cons
     if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s);
 }
 
-__global__ void k_b_to_f32(int n, const int* __restrict__ blk, const double* __restrict__ a, float* __restrict__ b,
-                           const double* __restrict__ scale)
+__global__ void k_b_cast_in(int n, const int* __restrict__ blk, const double* __restrict__ r,
+                            const double* __restrict__ sc, float* __restrict__ r32, const int* stop)
 {
+    if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = float(a[i] * scale[blk[i]]);
+    if (i < n) r32[i] = float(r[i] * sc[blk[i]]);
 }
 
-__global__ void k_b_add_f32(int n, const int* __restrict__ blk, const float* __restrict__ y,
-                            const double* __restrict__ scale, double* __restrict__ x)
+__global__ void k_b_cast_out(int n, const int* __restrict__ blk, const float* __restrict__ z32,
+                             const double* __restrict__ isc, double* __restrict__ z, const int* stop)
 {
+    if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += scale[blk[i]] * double(y[i]);
+    if (i < n) z[i] = double(z32[i]) * isc[blk[i]];
 }
 
 }  // namespace
+
+void BatchCastPrecond::bind(Precond<float>* inner, const BatchRanges* B, const double* sc, const double* isc)
+{
+    const float* r0 = r32_.p;
+    const float* z0 = z32_.p;
+    r32_.alloc(B->n);
+    z32_.alloc(B->n);
+    // captured graphs hold these pointers: a change of any of them is a new generation
+    if (inner != m_ || inner->generation() != inner_gen_ || B != B_ || sc != sc_ || isc != isc_ || r0 != r32_.p ||
+        z0 != z32_.p)
+        bump_generation();
+    m_ = inner;
+    B_ = B;
+    sc_ = sc;
+    isc_ = isc;
+    inner_gen_ = inner->generation();
+}
+
+void BatchCastPrecond::apply(cudaStream_t s, const double* r, double* z, const int* stop)
+{
+    const int n = B_->n;
+    PORSOL_LAUNCH(k_b_cast_in<<<div_up(n, BT), BT, 0, s>>>(n, B_->blk.p, r, sc_, r32_.p, stop));
+    m_->apply(s, r32_.p, z32_.p, stop);
+    PORSOL_LAUNCH(k_b_cast_out<<<div_up(n, BT), BT, 0, s>>>(n, B_->blk.p, z32_.p, isc_, z, stop));
+}
 
 void BatchRanges::build(const std::vector<int>& four, int n_unknowns, cudaStream_t s)
 {
@@ -391,7 +418,6 @@ CgResult BatchedPcg<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV
 }
 
 template class BatchedPcg<double, double>;
-template class BatchedPcg<float, float>;
 
 template <class T>
 void batch_norms(cudaStream_t s, const BatchRanges& B, const T* a, double* out)
@@ -401,17 +427,5 @@ void batch_norms(cudaStream_t s, const BatchRanges& B, const T* a, double* out)
 }
 template void batch_norms<double>(cudaStream_t, const BatchRanges&, const double*, double*);
 template void batch_norms<float>(cudaStream_t, const BatchRanges&, const float*, double*);
-
-void batch_to_f32_scaled(cudaStream_t s, const BatchRanges& B, const double* a, float* b, const double* scale)
-{
-    PORSOL_LAUNCH(k_b_to_f32<<<div_up(B.n, BT), BT, 0, s>>>(B.n, B.blk.p, a, b, scale));
-    PORSOL_CUDA(cudaGetLastError());
-}
-
-void batch_add_f32_scaled(cudaStream_t s, const BatchRanges& B, const float* y, const double* scale, double* x)
-{
-    PORSOL_LAUNCH(k_b_add_f32<<<div_up(B.n, BT), BT, 0, s>>>(B.n, B.blk.p, y, scale, x));
-    PORSOL_CUDA(cudaGetLastError());
-}
 
 }  // namespace porsol

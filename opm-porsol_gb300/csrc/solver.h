@@ -58,8 +58,7 @@ struct porsol_solver {
     porsol::Amg<float> amg32;
     bool amg_ready = false;
     int amg_precision = -1;
-    porsol::DBuf<double> ir_r;   // batched iterative refinement
-    porsol::DBuf<float> ir_r32, ir_d32;
+    porsol::DBuf<double> ir_r;   // batched residual
     porsol::RedScratch red;
 
     porsol::Profiler prof;
@@ -73,7 +72,7 @@ struct porsol_solver {
     // ... and solved with one CG per sub-grid (empty: one CG over the whole system)
     porsol::BatchRanges batch;
     porsol::BatchedPcg<double, double> bcg64;
-    porsol::BatchedPcg<float, float> bcg32;
+    porsol::BatchCastPrecond cast_pre;   // mixed: FP32 AMG inside the FP64 batched CG
     porsol::DBuf<double> btol, bscale, bnorm;
     void batched_solve(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit);
 
