@@ -124,29 +124,29 @@ bool porsol_solver::same_topology(const porsol_grid* grid, const int* flow_type,
     return true;
 }
 
+// Geometry goes to the device straight from the caller's arrays (the host keeps topology only).
+void porsol_solver::upload_geometry(const porsol_grid* grid)
+{
+    const size_t nc = size_t(grid->num_cells), nhf = size_t(grid->cell_facepos[nc]);
+    cudaStream_t s = stream;
+    area.upload(grid->hf_area, nhf, s);
+    fcent.upload(grid->hf_centroid, 3 * nhf, s);
+    fnormal.upload(grid->hf_normal, 3 * nhf, s);
+    cvol.upload(grid->cell_volume, nc, s);
+    ccent.upload(grid->cell_centroid, 3 * nc, s);
+    PORSOL_CUDA(cudaStreamSynchronize(s));   // pageable sources: the copies complete before return
+}
+
 void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
 {
     amg64.set_profiler(&prof);
     amg32.set_profiler(&prof);
     if (same_topology(grid, flow_type, partner_bid)) {
-        // geometry may differ: copy and upload it; everything derived from topology is kept
-        HostGrid& g = S.g;
-        const int nc = g.nc, nhf = g.nhf;
+        // geometry may differ: upload it; everything derived from topology is kept
         PORSOL_REQUIRE(grid->hf_area && grid->hf_centroid && grid->hf_normal && grid->cell_volume &&
                            grid->cell_centroid,
                        PORSOL_ERR_BAD_ARG, "grid: null array");
-        g.area.assign(grid->hf_area, grid->hf_area + nhf);
-        g.fcent.assign(grid->hf_centroid, grid->hf_centroid + 3 * size_t(nhf));
-        g.fnormal.assign(grid->hf_normal, grid->hf_normal + 3 * size_t(nhf));
-        g.cvol.assign(grid->cell_volume, grid->cell_volume + nc);
-        g.ccent.assign(grid->cell_centroid, grid->cell_centroid + 3 * size_t(nc));
-        cudaStream_t s = stream;
-        area.upload(g.area, s);
-        fcent.upload(g.fcent, s);
-        fnormal.upload(g.fnormal, s);
-        cvol.upload(g.cvol, s);
-        ccent.upload(g.ccent, s);
-        PORSOL_CUDA(cudaStreamSynchronize(s));
+        upload_geometry(grid);
         ip_valid = solved = false;
         amg_ready = false;
         return;
@@ -165,11 +165,7 @@ void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type
     facepos.upload(g.facepos, s);
     cf.upload(S.cf, s);
     pairs.upload(S.pairs, s);
-    area.upload(g.area, s);
-    fcent.upload(g.fcent, s);
-    fnormal.upload(g.fnormal, s);
-    cvol.upload(g.cvol, s);
-    ccent.upload(g.ccent, s);
+    upload_geometry(grid);
     S.pat.upload(s);
     status.alloc(1);
     status.zero(s);
@@ -640,7 +636,7 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     // per sub-grid: side areas A_i (high sides), extents L_d, first DOF
     std::vector<double> A(3 * size_t(ngrids), 0.0), L(3 * size_t(ngrids), 0.0);
     std::vector<int> dof0(ngrids);
-    const HostGrid& hg = S.g;
+    const HostGrid& hg = S.g;   // topology; the geometry is read from the caller's grid
     for (int g = 0; g < ngrids; ++g) {
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
         int d0 = S.N;
@@ -650,11 +646,11 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
                 const int sd = side[hf];
                 if (!hg.boundary(hf)) continue;
                 const int ax = (sd - 1) / 2;
-                const double x = hg.fcent[3 * size_t(hf) + ax];
+                const double x = grid->hf_centroid[3 * size_t(hf) + ax];
                 if (sd % 2 == 1) lo[ax] = std::min(lo[ax], x);
                 else {
                     hi[ax] = std::max(hi[ax], x);
-                    A[3 * size_t(g) + ax] += hg.area[hf];
+                    A[3 * size_t(g) + ax] += grid->hf_area[hf];
                 }
             }
         for (int ax = 0; ax < 3; ++ax) {

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <memory>
 #include <stdexcept>
+#include <type_traits>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -46,6 +47,35 @@ enum : int {
     ST_TIMEOUT = 16,      // bounded wait gave up
     ST_BAD_INDEX = 32,    // index check failed
 };
+
+// ------------------------------------------------------------------ host vectors
+// Allocator whose resize() leaves plain values uninitialised: the large host arrays of the
+// structure build are written in full by parallel loops, so the serial zero fill of a
+// std::vector (and its single-threaded first touch of every page) is skipped.
+template <class T>
+struct DefaultInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = DefaultInitAlloc<U>;
+    };
+    DefaultInitAlloc() = default;
+    template <class U>
+    DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept
+    {
+    }
+    template <class U>
+    void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value)
+    {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... Args>
+    void construct(U* p, Args&&... args)
+    {
+        ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+    }
+};
+template <class T>
+using HVec = std::vector<T, DefaultInitAlloc<T>>;
 
 // ------------------------------------------------------------------ device buffers
 template <class T>
@@ -91,7 +121,11 @@ struct DBuf {
         alloc(cnt);
         if (cnt) PORSOL_CUDA(cudaMemcpyAsync(p, h, cnt * sizeof(T), cudaMemcpyHostToDevice, s));
     }
-    void upload(const std::vector<T>& h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+    template <class A>
+    void upload(const std::vector<T, A>& h, cudaStream_t s)
+    {
+        upload(h.data(), h.size(), s);
+    }
     void download(T* h, size_t cnt, cudaStream_t s) const
     {
         if (cnt) PORSOL_CUDA(cudaMemcpyAsync(h, p, cnt * sizeof(T), cudaMemcpyDeviceToHost, s));
@@ -112,7 +146,7 @@ struct SellPattern {
     int n = 0;          // rows
     int nslices = 0;
     long long nent = 0; // stored entries incl. padding
-    std::vector<int> h_slice_ptr, h_col, h_rowlen;
+    HVec<int> h_slice_ptr, h_col, h_rowlen;
     DBuf<int> slice_ptr, col, rowlen, diag;   // diag: slot index of the diagonal
     void upload(cudaStream_t s);
 };
@@ -124,8 +158,7 @@ struct SellMatrix {
 };
 
 // Build a SELL pattern from CSR with sorted columns.  csr2sell[k] = slot of CSR entry k.
-void build_sell(int n, const std::vector<int>& rowptr, const std::vector<int>& col, SellPattern& P,
-                std::vector<long long>* csr2sell);
+void build_sell(int n, const HVec<int>& rowptr, const HVec<int>& col, SellPattern& P, HVec<int>* csr2sell);
 
 // ------------------------------------------------------------------ profiling
 enum ProfKernel { PK_SPMV64 = 0, PK_SPMV32 = 1, PK_ASSEMBLE = 2, PK_RECOVER = 3, PK_VCYCLE = 4, PK_CHEB = 5, PK_COUNT = 6 };

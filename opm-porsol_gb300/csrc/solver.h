@@ -83,6 +83,7 @@ struct porsol_solver {
     void require_structure() const;
     bool same_topology(const porsol_grid* grid, const int* flow_type, const int* partner_bid) const;
     void init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
+    void upload_geometry(const porsol_grid* grid);
     void compute_inner_products(const double* perm_h, const double* grav);
     void solve(const porsol_fluid* fluid, const double* sat, const double* mobdens, const int* bct,
                const double* bcv, const double* src, const porsol_solve_opts* opts, porsol_solve_stats* stats,

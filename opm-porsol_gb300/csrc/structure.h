@@ -20,7 +20,8 @@ struct HostGrid {
     int nc = 0, nhf = 0;
     std::vector<int> facepos, nb, bid;
     std::vector<double> area, fcent, fnormal, cvol, ccent;
-    void copy_from(const porsol_grid* g);
+    // geometry = false keeps only the topology (facepos, nb, bid); area .. ccent stay empty
+    void copy_from(const porsol_grid* g, bool geometry = true);
     int nf(int c) const { return facepos[c + 1] - facepos[c]; }
     bool boundary(int hf) const { return nb[hf] < 0; }
 };
@@ -35,8 +36,8 @@ struct Structure {
     std::vector<int> init_periodic;         // 1 where the face was periodic at init
     std::vector<int> ppartner;              // dof -> partner dof (-1); empty if no periodic face
     std::vector<int> partner_hf;            // half-face -> partner half-face for periodic faces (-1)
-    std::vector<int> rowptr, colind;        // CSR of S, sorted columns
-    std::vector<long long> csr2sell;
+    HVec<int> rowptr, colind;               // CSR of S, sorted columns
+    HVec<int> csr2sell;                     // SELL slot of each CSR entry (SELL offsets are 32-bit)
     SellPattern pat;
     std::vector<int> pairs;                 // post-process pairs (hf_first, hf_second) flattened
     std::vector<int> boundary_hf;           // all boundary half-faces in order
@@ -54,7 +55,7 @@ struct Recipe {
     bool valid = false;
     bool do_reg = true;
     std::vector<int> kind;               // HfKind per half-face
-    std::vector<int> h_slot_ptr, h_slot_ent, h_rhs_ptr, h_rhs_ent;
+    HVec<int> h_slot_ptr, h_slot_ent, h_rhs_ptr, h_rhs_ent;
     DBuf<int> kind_d, slot_ptr, slot_ent, rhs_ptr, rhs_ent;
     void build(const Structure& S, const int* flow_type, int max_nf_packed);
 };
