@@ -271,6 +271,10 @@ int porsol_transport_init(porsol_transport* t, const porsol_grid* grid, const do
                           const int* hf_sat_type, const double* hf_sat_value,
                           const int* hf_partner_bid, const porsol_transport_opts* opts);
 
+/* EulerUpstream::init(param) / setCourantNumber on an initialised solver
+ * (EulerUpstream_impl.hpp:95-108, 143-147): the parameters of later transportSolve calls. */
+int porsol_transport_set_options(porsol_transport* t, const porsol_transport_opts* opts);
+
 /* EulerUpstream::transportSolve (EulerUpstream_impl.hpp:153-218): sat [nc] in/out,
  * outflux [nhf] half-face fluxes of the pressure solution, injection [nc] (may be NULL). */
 int porsol_transport_solve(porsol_transport* t, double* sat, double time, const double* grav,

@@ -166,6 +166,7 @@ EXPORTS = [
                                    C.POINTER(TransportOpts)]),
     ("porsol_transport_solve", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
     ("porsol_transport_solve_device", _i, [_vp, _vp, _d, _vp, _vp, _vp, C.POINTER(TransportStats)]),
+    ("porsol_transport_set_options", _i, [_vp, C.POINTER(TransportOpts)]),
     ("porsol_transport_set_rock_tables", _i, [_vp, C.POINTER(RockTablesStruct)]),
     ("porsol_capillary_opts_default", None, [C.POINTER(CapillaryOpts)]),
     ("porsol_capillary_solve", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(CapillaryOpts),

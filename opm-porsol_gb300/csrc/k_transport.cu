@@ -779,6 +779,14 @@ int porsol_transport_solve_device(porsol_transport* t, double* sat, double time,
     return tguard(t, [&] { t->solve(sat, time, grav, outflux, injection, stats, true); });
 }
 
+int porsol_transport_set_options(porsol_transport* t, const porsol_transport_opts* opts)
+{
+    return tguard(t, [&] {
+        PORSOL_REQUIRE(opts, PORSOL_ERR_BAD_ARG, "transport options: null argument");
+        t->o = *opts;
+    });
+}
+
 int porsol_transport_set_rock_tables(porsol_transport* t, const porsol_rock_tables* rocks)
 {
     return tguard(t, [&] { t->set_rock_tables(rocks); });

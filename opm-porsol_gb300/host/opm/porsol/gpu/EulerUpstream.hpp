@@ -13,6 +13,7 @@
 #ifndef OPM_PORSOL_GPU_EULERUPSTREAM_HPP
 #define OPM_PORSOL_GPU_EULERUPSTREAM_HPP
 
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -81,6 +82,7 @@ public:
         o_.maximum_small_steps = param.getDefault("maximum_small_steps", o_.maximum_small_steps);
         o_.check_sat = param.getDefault("check_sat", bool(o_.check_sat));
         o_.clamp_sat = param.getDefault("clamp_sat", bool(o_.clamp_sat));
+        if (ready_) check(porsol_transport_set_options(t_, &o_));
     }
     template <class ParamGroup>
     void init(const ParamGroup& param, const GridInterface& g, const ReservoirProperties& r,
@@ -124,9 +126,24 @@ public:
                         r.densityFirstPhase(), r.densitySecondPhase()};
         const porsol_grid v = grid_.view();
         check(porsol_transport_init(t_, &v, K.data(), poro.data(), &fl, st.data(), sv.data(), partner.data(), &o_));
+        ready_ = true;
     }
 
-    void setCourantNumber(double cn) { o_.courant_number = cn; }
+    // EulerUpstream_impl.hpp:132-139
+    void display()
+    {
+        std::cout << std::endl;
+        std::cout << "Displaying some members of EulerUpstream" << std::endl;
+        std::cout << std::endl;
+        std::cout << "courant_number = " << o_.courant_number << std::endl;
+    }
+
+    // EulerUpstream_impl.hpp:143-147 (takes effect for the next transportSolve)
+    void setCourantNumber(double cn)
+    {
+        o_.courant_number = cn;
+        if (ready_) check(porsol_transport_set_options(t_, &o_));
+    }
 
     // ReservoirPropertyCapillary with rock tables: table mobilities and capillary pressure,
     // per-rock CFL factors (call after initObj; an empty table list returns to Corey-2)
@@ -155,12 +172,18 @@ public:
         const double g[3] = {gravity[0], gravity[1], gravity[2]};
         porsol_transport_stats st{};
         check(porsol_transport_solve(t_, s.data(), time, g, flux.data(), inj.data(), &st));
+        last_ = st;
         grid_.fromPositions(s, saturation);
     }
+
+    // sub-steps, retries and CFL step of the last transportSolve (GPU extension)
+    const porsol_transport_stats& lastStats() const { return last_; }
 
 private:
     porsol_transport* t_ = nullptr;
     porsol_transport_opts o_{};
+    bool ready_ = false;
+    mutable porsol_transport_stats last_{};
     FlatGrid grid_;
 
     void create()

@@ -17,9 +17,11 @@
 #define OPM_PORSOL_GPU_INCOMPFLOWSOLVERHYBRID_HPP
 
 #include <array>
+#include <fstream>
 #include <iterator>
 #include <ostream>
 #include <stdexcept>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -223,8 +225,33 @@ public:
            << "\tNon-zeros of S               = " << nnz << '\n';
     }
 
+    // IncompFlowSolverHybrid.hpp:895-905: the assembled system of the last solve (before the
+    // pure-Neumann regularisation) as prefix + "-mat.dat" (one "row col value" line per stored
+    // entry, 1-based, the coordinate format of dune-istl's writeMatrixToMatlab) and
+    // prefix + "-rhs.dat" (one value per line, 15 digits, scientific with sign, as the reference).
+    void printSystem(const std::string& prefix)
+    {
+        int n = 0, nnz = 0, mx = 0, ni = 0;
+        check(porsol_num_dofs(h_, &n, &nnz, &mx, &ni));
+        std::vector<int> cf(grid_.numHalfFaces()), rp(n + 1), ci(nnz), pp(n);
+        std::vector<double> val(nnz), rhs(n);
+        check(porsol_get_structure(h_, cf.data(), rp.data(), ci.data(), pp.data()));
+        check(porsol_get_system(h_, val.data(), rhs.data()));
+        std::ofstream mat((prefix + "-mat.dat").c_str());
+        mat.precision(15);
+        mat.setf(std::ios::scientific);
+        for (int i = 0; i < n; ++i)
+            for (int k = rp[i]; k < rp[i + 1]; ++k) mat << i + 1 << ' ' << ci[k] + 1 << ' ' << val[k] << '\n';
+        std::ofstream r((prefix + "-rhs.dat").c_str());
+        r.precision(15);
+        r.setf(std::ios::scientific | std::ios::showpos);
+        std::copy(rhs.begin(), rhs.end(), std::ostream_iterator<double>(r, "\n"));
+        if (!mat || !r) throw std::runtime_error("printSystem: could not write " + prefix + "-mat.dat / -rhs.dat");
+    }
+
     // ---- GPU extensions (no counterpart in the reference) ----
-    // PORSOL_FP64 (default, the plain drop-in) or PORSOL_MIXED (FP32 in FP64 refinement).
+    // PORSOL_FP64 (default, the plain drop-in) or PORSOL_MIXED (FP32 AMG hierarchy under FP32 CG
+    // recurrences with an FP64 solution and FP64 residual replacements).
     void setPrecision(int mode) { extra_.precision = mode; }
     const porsol_solve_stats& lastStats() const { return stats_; }
     porsol_solver* handle() const { return h_; }

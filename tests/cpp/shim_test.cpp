@@ -10,6 +10,7 @@
 // saturation volume.  Prints "OK" on success.
 #include <cmath>
 #include <cstdio>
+#include <fstream>
 #include <iostream>
 #include <stdexcept>
 #include <vector>
@@ -262,6 +263,24 @@ int main()
                 }
             }
         s.printStats(std::cout);
+        // printSystem: one line per stored entry and one per unknown, the diagonal positive
+        s.printSystem("/tmp/porsol_shim_system");
+        std::ifstream mat("/tmp/porsol_shim_system-mat.dat"), rhs("/tmp/porsol_shim_system-rhs.dat");
+        long long lines = 0, diag_ok = 0, rlines = 0;
+        int i, j;
+        double v;
+        while (mat >> i >> j >> v) {
+            ++lines;
+            if (i == j && v > 0) ++diag_ok;
+        }
+        while (rhs >> v) ++rlines;
+        int n = 0, nnz = 0, mx = 0, ni = 0;
+        porsol_num_dofs(s.handle(), &n, &nnz, &mx, &ni);
+        if (lines != nnz || diag_ok != n || rlines != n) {
+            std::printf("printSystem: %lld entries (%d), %lld positive diagonals, %lld rhs lines (%d)\n", lines, nnz,
+                        diag_ok, rlines, n);
+            return 1;
+        }
     }
     // tensor mobilities (the anisotropic-relperm inner product): still exact for a linear field
     {
@@ -300,6 +319,21 @@ int main()
             if (f->boundary() && s.getSolution().outflux(f) < 0) qin -= s.getSolution().outflux(f);
     }
     const double T = 0.01 * pv / qin;
+    // setCourantNumber after init applies to the next transportSolve: half the Courant number,
+    // twice the sub-steps (up to the rounding of the step count)
+    {
+        std::vector<double> s1 = s0, s2 = s0;
+        tr.transportSolve(s1, 4 * T, grav, s.getSolution(), inj);
+        const int n1 = tr.lastStats().small_steps;
+        tr.setCourantNumber(0.25);
+        tr.transportSolve(s2, 4 * T, grav, s.getSolution(), inj);
+        const int n2 = tr.lastStats().small_steps;
+        tr.setCourantNumber(0.5);
+        if (n2 < 2 * n1 - 1 || n2 > 2 * n1 + 1) {
+            std::printf("setCourantNumber: %d sub-steps at 0.5, %d at 0.25\n", n1, n2);
+            return 1;
+        }
+    }
     tr.transportSolve(sw, T, grav, s.getSolution(), inj);
     double water = 0.0, smin = 1, smax = 0;
     for (int c = 0; c < nc; ++c) {
