@@ -7,8 +7,8 @@ layer means ~ N(ln 100 mD, 1) and ln k ~ N(mean, 2^2) i.i.d. within a layer, Cor
 mobilities (viscosity ratio 10) at the initial state s = 0 of the IMPES run, Dirichlet
 p = 1 / p = 0 on x- / x+, AMG-preconditioned CG.  Synthetic inputs from a fixed seed.
 
-  value  = mixed-precision solves/s (FP32 SpMV + FP32 AMG inside FP64 iterative
-           refinement) with inputs resident in HBM, all ranks together;
+  value  = mixed-precision solves/s (FP32 CG recurrences and FP32 AMG with an FP64 solution
+           and FP64 residual replacements) with inputs resident in HBM, all ranks together;
   fp64   = the plain FP64 drop-in on the same inputs;
   e2e    = the same metric through the host-pointer C ABI (inputs copied H2D and the
            solution D2H inside the timed region);
@@ -369,7 +369,7 @@ def run_gpu(args):
                                "(1M cells, 3.05M face unknowns), Corey-2 mobilities at s=0, AMG-CG",
                    "dims": list(dims), "cells": nc, "face_unknowns": s.n, "nnz": s.nnz,
                    "residual_tolerance": args.tol, "residual_tolerance_fp64": args.tol64,
-                   "precision": "FP32 SpMV/AMG in FP64 iterative refinement",
+                   "precision": "FP32 CG recurrences and FP32 AMG (FP16 smoother copy), FP64 solution with FP64 residual replacements",
                    "l2": "inputs larger than L2 (FP64 matrix 400 MB, FP32 copy 270 MB)",
                    "parallelism": "replicas" if world > 1 else "single GPU", "init_s": round(init_s, 3)},
         "flux_rel_err_vs_fp64": mixed["err_v"], "pressure_rel_err_vs_fp64": mixed["err_p"],

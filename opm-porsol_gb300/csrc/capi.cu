@@ -4,7 +4,7 @@
 //   1. assembleDynamic: k_assemble_cells (per-cell Schur complements and rhs pieces), then
 //      the recipe gathers write the global matrix (SELL) and right-hand side;
 //   2. pure-Neumann regularisation S[0][0] *= 2 (:1398-1400, :1493-1495);
-//   3. linear solve: ILU0-CG (type 0) or AMG-CG (types 1-3), FP64 or FP32-in-FP64-refinement;
+//   3. linear solve: ILU0-CG (type 0) or AMG-CG (types 1-3), FP64, or mixed (FP32 AMG and CG recurrences, FP64 solution and residual replacements);
 //   4. computePressureAndFluxes: k_recover.
 #include <algorithm>
 #include <chrono>

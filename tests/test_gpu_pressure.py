@@ -184,7 +184,8 @@ def test_post_process_antisymmetric(pkg, gpulib, workloads, cart):
 
 
 def test_mixed_precision_flux_error(pkg, gpulib, orc, workloads):
-    """FP32 SpMV/AMG inside FP64 refinement reaches 1e-8 relative flux error (sigma=2 field)."""
+    """Mixed precision (FP32 CG recurrences and AMG, FP64 solution with residual replacements) reaches
+    1e-8 relative flux error (sigma=2 field)."""
     prob = workloads.anisotropic_corey(dims=(24, 20, 10))
     o = oracle_solve(orc, prob, tol=1e-13, dirichlet_guess=True)
     g = gpu_solve(pkg, prob, ltype=1, tol=1e-11, precision=pkg.MIXED)
