@@ -19,6 +19,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <exception>
+#include <mutex>
 #include <numeric>
 #include <thread>
 
@@ -36,7 +38,8 @@ int host_threads()
 }
 
 // fn(begin, end, chunk) over [0, n) in contiguous chunks (chunk order = index order); serial
-// below `grain` items per extra thread.
+// below `grain` items per extra thread.  An exception in any chunk is rethrown on the calling
+// thread after all chunks have finished (the first one caught).
 template <class F>
 int parallel_chunks(long long n, F&& fn, long long grain = 1 << 16)
 {
@@ -47,6 +50,16 @@ int parallel_chunks(long long n, F&& fn, long long grain = 1 << 16)
     }
     std::vector<std::thread> th;
     th.reserve(T - 1);
+    std::exception_ptr err;
+    std::mutex err_mutex;
+    auto run = [&](long long b, long long e, int t) {
+        try {
+            fn(b, e, t);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(err_mutex);
+            if (!err) err = std::current_exception();
+        }
+    };
     auto range = [&](int t, long long& b, long long& e) {
         b = n * t / T;
         e = n * (t + 1) / T;
@@ -54,12 +67,13 @@ int parallel_chunks(long long n, F&& fn, long long grain = 1 << 16)
     for (int t = 1; t < T; ++t) {
         long long b, e;
         range(t, b, e);
-        th.emplace_back([&fn, b, e, t] { fn(b, e, t); });
+        th.emplace_back([&run, b, e, t] { run(b, e, t); });
     }
     long long b, e;
     range(0, b, e);
-    fn(b, e, 0);
+    run(b, e, 0);
     for (auto& x : th) x.join();
+    if (err) std::rethrow_exception(err);
     return T;
 }
 
