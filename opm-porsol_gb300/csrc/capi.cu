@@ -139,6 +139,9 @@ void porsol_solver::upload_geometry(const porsol_grid* grid)
 
 void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
 {
+    // the reference's init skips an empty grid (IncompFlowSolverHybrid.hpp:483-486); a solver
+    // without cells has nothing to do, so the C ABI reports it instead of building empty arrays
+    PORSOL_REQUIRE(grid && grid->num_cells > 0, PORSOL_ERR_BAD_ARG, "grid: no cells");
     amg64.set_profiler(&prof);
     amg32.set_profiler(&prof);
     if (same_topology(grid, flow_type, partner_bid)) {

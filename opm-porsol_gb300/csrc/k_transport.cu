@@ -429,6 +429,7 @@ void porsol_transport::init(const porsol_grid* grid, const double* K, const doub
 {
     ready = false;
     PORSOL_REQUIRE(K && phi && fl && stype && sval, PORSOL_ERR_BAD_ARG, "transport init: null argument");
+    PORSOL_REQUIRE(grid && grid->num_cells > 0, PORSOL_ERR_BAD_ARG, "grid: no cells");
     PORSOL_REQUIRE(fl->model == PORSOL_FLUID_COREY2, PORSOL_ERR_BAD_ARG,
                    "transport needs the two-phase Corey-2 fluid model");
     g.copy_from(grid);

@@ -226,3 +226,16 @@ def test_errors_are_reported(pkg, gpulib, workloads, cart):
     assert e.value.code == 3
     # the handle stays usable after errors
     s.solve(fl, prob.sat, prob.bc_type, prob.bc_value, prob.src)
+    # an empty grid is rejected up front (the reference's init skips it)
+    empty = cart.CartesianGrid(1, 1, 1)
+    empty.num_cells = 0
+    empty.facepos = np.zeros(1, np.int32)
+    for k in ("neighbour", "bid", "area"):
+        setattr(empty, k, getattr(empty, k)[:0])
+    for k in ("fcentroid", "fnormal", "ccentroid"):
+        setattr(empty, k, getattr(empty, k)[:0])
+    empty.volume = empty.volume[:0]
+    e2 = pkg.PressureSolver()
+    with pytest.raises(pkg.PorsolError) as e:
+        e2.init(empty, np.zeros(0), (0, 0, 0), np.zeros(0, np.int32))
+    assert e.value.code == 2 and "no cells" in str(e.value)
