@@ -65,6 +65,26 @@ def test_static_inner_products(pkg, gpulib, orc, workloads, cart):
     assert relmax(gg, go) < 1e-13
 
 
+@pytest.mark.parametrize("n", [1, 2, 4])
+def test_ipeval_fixture_on_gpu(pkg, gpulib, cart, n):
+    """The static inverse inner products of the attic/mimetic/mimetic_ipeval_test.cpp fixture
+    (K = diag(10, 1, 0.1), unit cube in 1, 8, 64 cells) equal the recorded copy
+    (tests/golden/ipeval_binv.json)."""
+    import json
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ipeval_binv.json")))["grids"][str(n)]
+    g = cart.CartesianGrid(n, n, n, 1.0 / n, 1.0 / n, 1.0 / n)
+    K = np.zeros((g.num_cells, 9))
+    K[:, 0], K[:, 4], K[:, 8] = 10.0, 1.0, 0.1
+    s = pkg.PressureSolver()
+    s.init(g, K.ravel(), (0.0, 0.0, 0.0), np.full(g.num_half_faces, pkg.BC_NEUMANN, np.int32))
+    B, _ = s.inner_products()
+    B = B.reshape(g.num_cells, 36)
+    np.testing.assert_allclose(B[0], gold["first_cell"], rtol=1e-13, atol=1e-12)
+    np.testing.assert_allclose(B[-1], gold["last_cell"], rtol=1e-13, atol=1e-12)
+    np.testing.assert_allclose(np.linalg.norm(B, axis=1), gold["cell_norms"], rtol=1e-13)
+
+
 @pytest.mark.parametrize("fluid", ["corey", "cellwise_gravity"])
 def test_assembled_system(pkg, gpulib, orc, workloads, cart, fluid):
     """assembleDynamic: the global matrix and right-hand side entry by entry."""
