@@ -139,6 +139,7 @@ void porsol_solver::upload_geometry(const porsol_grid* grid)
 
 void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type, const int* partner_bid)
 {
+    NvtxRange range("porsol initSystemStructure");
     // the reference's init skips an empty grid (IncompFlowSolverHybrid.hpp:483-486); a solver
     // without cells has nothing to do, so the C ABI reports it instead of building empty arrays
     PORSOL_REQUIRE(grid && grid->num_cells > 0, PORSOL_ERR_BAD_ARG, "grid: no cells");
@@ -199,6 +200,7 @@ void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type
 
 void porsol_solver::compute_inner_products(const double* perm_h, const double* grav)
 {
+    NvtxRange range("porsol computeInnerProducts");
     require_structure();
     PORSOL_REQUIRE(perm_h, PORSOL_ERR_BAD_ARG, "permeability array is null");
     const double g0[3] = {grav ? grav[0] : 0.0, grav ? grav[1] : 0.0, grav ? grav[2] : 0.0};
@@ -259,6 +261,7 @@ double now_ms()
 
 void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st)
 {
+    NvtxRange range("porsol linear solve (setup + CG)");
     const double t_begin = now_ms();
     const int n = S.N;
     const int maxit = o.linsolver_maxit > 0 ? o.linsolver_maxit : n;
@@ -429,6 +432,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
                           const double* bcv, const double* src, const porsol_solve_opts* opts_in,
                           porsol_solve_stats* stats, bool dev)
 {
+    NvtxRange range("porsol solve");
     require_structure();
     PORSOL_REQUIRE(ip_valid, PORSOL_ERR_STATE, "computeInnerProducts must be called before solve");
     PORSOL_REQUIRE(fluid && sat && bct && bcv && src, PORSOL_ERR_BAD_ARG, "solve: null argument");
@@ -603,6 +607,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
 
 double porsol_solver::post_process()
 {
+    NvtxRange range("porsol postProcessFluxes");
     PORSOL_REQUIRE(solved, PORSOL_ERR_STATE, "postProcessFluxes before solve");
     PORSOL_CUDA(cudaMemsetAsync(redbits.p + 3, 0, sizeof(unsigned long long), stream));
     launch_post_process(stream, int(S.pairs.size() / 2), pairs.p, outflux.p, redbits.p + 3);
@@ -620,6 +625,7 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
                             const int* side, const double* perm_h, const porsol_solve_opts* opts_in, double* keff,
                             porsol_solve_stats* stats)
 {
+    NvtxRange range("porsol upscale periodic");
     PORSOL_REQUIRE(grid && cellpos && partner && side && perm_h && keff && ngrids > 0, PORSOL_ERR_BAD_ARG,
                    "upscale: null argument");
     const int nc = grid->num_cells;
@@ -792,6 +798,7 @@ double porsol_solver::objective(const porsol_objective* obj)
 void porsol_solver::adjoint_gradient(const porsol_objective* obj, int mode, const porsol_solve_opts* opts_in,
                                      double* value, double* grad, porsol_solve_stats* stats)
 {
+    NvtxRange range("porsol adjoint gradient");
     PORSOL_REQUIRE(mode == PORSOL_GRAD_LOGK || mode == PORSOL_GRAD_LOGK_AXES, PORSOL_ERR_BAD_ARG,
                    "adjoint: unknown gradient mode");
     PORSOL_REQUIRE(grad, PORSOL_ERR_BAD_ARG, "adjoint: null gradient array");

@@ -149,6 +149,7 @@ void porsol_transport::capillary_solve(porsol_solver* P, double* sat, const doub
                                        const double* inj, const int* bct, const double* bcv,
                                        const porsol_capillary_opts* opts_in, porsol_capillary_stats* stats, bool dev)
 {
+    NvtxRange range("porsol ImplicitCapillarity step");
     PORSOL_REQUIRE(ready, PORSOL_ERR_STATE, "transport solver not initialised");
     PORSOL_REQUIRE(P && sat && flux && bct && bcv, PORSOL_ERR_BAD_ARG, "capillary solve: null argument");
     P->require_structure();

@@ -585,6 +585,7 @@ void porsol_transport::build_entries(const double* grav)
 void porsol_transport::solve(double* sat, double time, const double* grav, const double* flux, const double* inj,
                              porsol_transport_stats* stats, bool dev)
 {
+    NvtxRange range("porsol transportSolve");
     PORSOL_REQUIRE(ready, PORSOL_ERR_STATE, "transport solver not initialised");
     PORSOL_REQUIRE(sat && flux, PORSOL_ERR_BAD_ARG, "transportSolve: null argument");
     build_entries(grav);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 
@@ -193,6 +194,16 @@ struct ProfScope {
     {
         if (P.on && a) P.end(s, k, bytes, a);
     }
+};
+
+// ------------------------------------------------------------------ tracing
+// NVTX range for the duration of a scope (header-only NVTX 3: a no-op unless a profiler such as
+// Nsight Systems or Nsight Compute is attached), so timelines show the phases of a call.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // ------------------------------------------------------------------ launch helpers

@@ -17,6 +17,8 @@
 #define OPM_PORSOL_GPU_INCOMPFLOWSOLVERHYBRID_HPP
 
 #include <array>
+#include <iostream>
+#include <cmath>
 #include <fstream>
 #include <iterator>
 #include <ostream>
@@ -196,6 +198,7 @@ private:
         o.smooth_steps = smooth_steps;
         check(porsol_solve(h_, &f, totmob.data(), mobdens.data(), bct_.data(), bcv_.data(), srcp.data(), &o,
                            &stats_));
+        report(linsolver_verbosity);
         fetchSolution();
     }
 
@@ -258,6 +261,18 @@ public:
     const FlatGrid& flatGrid() const { return grid_; }
 
 private:
+    // linsolver_verbosity > 0: the summary line the reference's CG solver prints
+    // (dune-istl CGSolver with verbose >= 1: convergence rate, time, time per iteration, iterations)
+    void report(int verbosity) const
+    {
+        if (verbosity <= 0) return;
+        const int it = stats_.iterations;
+        const double T = 1e-3 * stats_.ms_krylov;
+        const double rate = it > 0 && stats_.reduction > 0 ? std::pow(stats_.reduction, 1.0 / it) : 0.0;
+        std::cout << "=== rate=" << rate << ", T=" << T << ", TIT=" << (it > 0 ? T / it : 0.0) << ", IT=" << it
+                  << std::endl;
+    }
+
     porsol_solver* h_ = nullptr;
     const GridInterface* pgrid_ = nullptr;
     FlatGrid grid_;
@@ -307,6 +322,7 @@ private:
         o.prolongate_factor = prolongate_factor;
         o.smooth_steps = smooth_steps;
         check(porsol_solve(h_, &f, lam.data(), rlam.data(), bct_.data(), bcv_.data(), srcp.data(), &o, &stats_));
+        report(linsolver_verbosity);
         fetchSolution();
     }
     void fetchSolution()

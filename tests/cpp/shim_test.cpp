@@ -304,7 +304,7 @@ int main()
     Solver s;
     s.init(g, r, grav, bcx);
     std::vector<double> s0(nc, 0.0);
-    s.solve(fl, s0, bcx, src, 1e-12, 0, 1);
+    s.solve(fl, s0, bcx, src, 1e-12, 1, 1);   // verbosity 1: the CG summary line
     s.postProcessFluxes();
     Opm::gpu::Params prm;
     prm.o.method_capillary = 0;

@@ -32,3 +32,4 @@ def test_shim_runs_on_gpu(pkg, gpulib, tmp_path):
     exe = _compile(pkg, str(tmp_path / "shim_test"))
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+    assert "=== rate=" in r.stdout and ", IT=" in r.stdout   # linsolver_verbosity 1 reports the CG
