@@ -337,7 +337,7 @@ def run_gpu(args):
     roof = None
     if n_cheb:
         achieved = (bytes_cheb / n_cheb) / (ms_cheb / n_cheb * 1e-3) / 1e9
-        roof = {"bound": "hbm", "kernel": "k_cheb_step<float, 0, __half, true> (finest AMG level, FP16 D^-1 A, SELL-32x4 copy)", "achieved": round(achieved, 1),
+        roof = {"bound": "hbm", "kernel": "k_cheb_step_bulk<float> (finest AMG level, FP16 D^-1 A, SELL-32x4 slices bulk-copied to shared memory)", "achieved": round(achieved, 1),
                 "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                 "traffic": None, "launches": n_cheb, "avg_us": round(ms_cheb / n_cheb * 1e3, 2),
                 "algorithmic_bytes_per_launch": bytes_cheb / n_cheb,

@@ -35,6 +35,7 @@ struct AmgOpts {
                                    // negative attempt stalls on these systems and is discarded)
     bool half_smoother = true;     // FP32 hierarchies: smoother/residual read D^-1 A stored in FP16
     bool layout4 = true;           // ... from a SELL-32x4 copy on levels smoothed one thread per row
+    bool bulk_stage = true;        // finest level: Chebyshev step with the slices bulk-copied to shared memory
     bool autotune = false;         // time the lane schedules of each new level shape once (the
                                    // choice then depends on timing: off where runs must be
                                    // bitwise reproducible)
@@ -55,6 +56,9 @@ public:
     void set_profiler(Profiler* p) { prof_ = p; }
     const std::vector<int>& level_sizes() const { return sizes_; }
     const std::vector<long long>& level_nnz() const { return nnzs_; }
+    // error bits set by the apply kernels (ST_TIMEOUT: a bounded wait for a bulk copy gave up);
+    // synchronises the stream
+    int solve_status(cudaStream_t s) const;
 
 private:
     struct Level {
@@ -72,6 +76,7 @@ private:
         // SELL-32x4 copy of ah (levels smoothed with one thread per row): slice offsets,
         // columns, FP16 values
         bool v4 = false;
+        int bulk_groups = 0;         // > 0: the Chebyshev step stages the x4 slices by bulk copy
         DBuf<int> sp4, col4;
         DBuf<__half> ah4;
         double lmax = 2.0;

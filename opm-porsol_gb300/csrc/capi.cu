@@ -329,6 +329,11 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     st.amg_levels = amg32.levels();
     const double inner_tol = o.inner_tolerance > 0 ? o.inner_tolerance : 3e-3;
     CgResult r = rcg.solve(stream, P, val.p, val32.p, amg32, rhs.p, x.p, o.residual_tolerance, maxit, inner_tol, &prof);
+    if (const int ast = amg32.solve_status(stream)) {
+        amg_ready = false;   // the next solve sets the hierarchy (and its status) up again
+        throw Error((ast & ST_TIMEOUT) ? PORSOL_ERR_TIMEOUT : PORSOL_ERR_BAD_ARG,
+                    "AMG smoother: bulk copy of the matrix slices failed (wait gave up or staging area too small)");
+    }
     st.iterations = r.iterations;
     st.outer_iterations = rcg.replacements();
     st.reduction = r.reduction;

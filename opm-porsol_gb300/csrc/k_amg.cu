@@ -693,6 +693,102 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
     x_out[i] = xi;
 }
 
+// ---- finest-level smoother step with bulk-copied matrix slices ----
+// The finest level's SELL-32x4 copy streams 6 bytes per entry.  Here lane 0 of each warp (one
+// slice) has the TMA engine copy the slice's columns and FP16 values into the warp's part of
+// shared memory with two cp.async.bulk transfers completing on the warp's own mbarrier, so the
+// warp waits for one transfer instead of a column load per group before its gathers.  The sums are
+// those of k_cheb_step<T, 0, __half, true> in the same order.  Every wait is bounded: on a timeout
+// the warp sets ST_TIMEOUT, waits once more (bounded) for its copies and returns without writing.
+constexpr int BULK_SLICES = 8;
+constexpr long long BULK_SPIN = 1LL << 20;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, long long limit)
+{
+    for (long long it = 0; it < limit; ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Dynamic shared memory: 128 bytes for the warps' barriers, then BULK_SLICES column areas of cap
+// entries (4 B each), then BULK_SLICES value areas (2 B each).  cap and the slice offsets are
+// multiples of 128 entries, so every copy starts and ends on a 16-byte boundary.
+template <class T>
+__global__ void __launch_bounds__(BULK_SLICES * 32)
+    k_cheb_step_bulk(int n, int nslices, const int* __restrict__ sp4, const int* __restrict__ col4,
+                     const __half* __restrict__ a4, const T* x_in, const T* __restrict__ d_in, T* __restrict__ r,
+                     T* __restrict__ d_out, T* x_out, T c1, T c2, int final_step, const int* stop, int cap,
+                     int* status)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    if (*stop) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int s = blockIdx.x * BULK_SLICES + w;
+    if (s >= nslices) return;  // whole warps
+    const int e0 = sp4[s], ne = sp4[s + 1] - e0;
+    if (ne <= 0 || ne > cap || (e0 & 127)) {  // a slice wider than its staging area: no copy
+        if (lane == 0) atomicOr(status, ST_BAD_INDEX);
+        return;
+    }
+    const unsigned bar = smem_u32(smem + 8 * w);
+    int* scol = reinterpret_cast<int*>(smem + 128) + size_t(w) * cap;
+    __half* sval = reinterpret_cast<__half*>(smem + 128 + size_t(BULK_SLICES) * cap * 4) + size_t(w) * cap;
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(unsigned(ne) * 6u)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(scol)),
+                     "l"(col4 + e0), "r"(unsigned(ne) * 4u), "r"(bar)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(sval)),
+                     "l"(a4 + e0), "r"(unsigned(ne) * 2u), "r"(bar)
+                     : "memory");
+    }
+    __syncwarp();
+    if (!mbar_wait_bounded(bar, BULK_SPIN)) {
+        if (lane == 0) atomicOr(status, ST_TIMEOUT);
+        mbar_wait_bounded(bar, BULK_SPIN);
+        return;
+    }
+    const int i = s * 32 + lane;
+    if (i >= n) return;  // padding rows of the last slice
+    const int G = ne >> 7;
+    const int4* cp = reinterpret_cast<const int4*>(scol) + lane;
+    const uint2* vp = reinterpret_cast<const uint2*>(sval) + lane;
+    T acc = T(0);
+    for (int g = 0; g < G; ++g) {
+        const int4 c = cp[32 * g];
+        const uint2 h = vp[32 * g];
+        const T x0 = d_in[c.x], x1 = d_in[c.y], x2 = d_in[c.z], x3 = d_in[c.w];
+        const float2 v01 = __half22float2(*reinterpret_cast<const __half2*>(&h.x));
+        const float2 v23 = __half22float2(*reinterpret_cast<const __half2*>(&h.y));
+        acc += T(v01.x) * x0;
+        acc += T(v01.y) * x1;
+        acc += T(v23.x) * x2;
+        acc += T(v23.y) * x3;
+    }
+    const T di = d_in[i];
+    T xi = (x_in ? x_in[i] : T(0)) + di;
+    const T ri = r[i] - acc;
+    const T dn = c1 * di + c2 * ri;
+    if (final_step) xi += dn;
+    r[i] = ri;
+    d_out[i] = dn;
+    x_out[i] = xi;
+}
+
 template <class T, int K, class V, bool SCALED>
 __global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
@@ -1100,6 +1196,15 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.d0.alloc(n);
     L.d1.alloc(n);
     L.lanes = L.v4 ? 1 : tune_lanes(s, L);
+    // bulk-staged step: FP32 hierarchies on the level whose slice widths the host knows (the system
+    // matrix), when every slice has at most four groups (18 KB of shared memory per 8 slices at 3)
+    L.bulk_groups = 0;
+    if (L.v4 && o_.bulk_stage && std::is_same<T, float>::value && P.h_slice_ptr.size() == size_t(P.nslices) + 1) {
+        int gmax = 0;
+        for (int sl = 0; sl < P.nslices; ++sl)
+            gmax = std::max(gmax, (((P.h_slice_ptr[sl + 1] - P.h_slice_ptr[sl]) / 32) + 3) / 4);
+        if (gmax >= 1 && gmax <= 4) L.bulk_groups = gmax;
+    }
 }
 
 // Lane schedule autotuner: for a level shape not seen before, time one smoother step with 1, 2,
@@ -1265,6 +1370,12 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
     PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "AMG setup: non-positive diagonal or missing diagonal entry");
 }
 
+template <class T>
+int Amg<T>::solve_status(cudaStream_t s) const
+{
+    return status_.p ? read_int(s, status_.p) : 0;
+}
+
 // One Chebyshev application (degree o_.cheb_degree) on [lmax/30, lmax]:
 //   from_zero: x = p(D^-1 A) D^-1 b;  otherwise from y = x0 (+ w P xc when xc is given).
 template <class T>
@@ -1316,7 +1427,13 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
         const int nbk = div_up(n * L.lanes, TB);
-        if (L.v4) {
+        if (L.bulk_groups > 0) {
+            const int cap = 128 * L.bulk_groups;   // entries per slice
+            const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
+            PORSOL_LAUNCH((k_cheb_step_bulk<T><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
+                n, P.nslices, L.sp4.p, L.col4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
+                cap, status_.p)));
+        } else if (L.v4) {
             PORSOL_LAUNCH((k_cheb_step<T, 0, __half, true><<<nb, TB, 0, s>>>(
                 n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
                 k == deg ? 1 : 0, stop)));
