@@ -387,6 +387,16 @@ void* porsol_stream(porsol_solver* h);
 /* Number of kernel launches this library has issued in the process so far. */
 long long porsol_launch_count(void);
 
+/* ------------------------------------------------------ self-test (no counterpart in the reference) */
+/* Runs the finest-level smoother step that stages its matrix slices by bulk copy once, on a fixed
+ * 64-row system on the current device, and writes its 64 outputs r, d, x (arrays of 64 floats).
+ * Row i holds the values 1/4, 1/2, 3/4, 1 at columns i, i+1, i+5, i+17 (mod 64); d_j = 1 + j/64,
+ * r = 2, x = 0, c1 = 1/2, c2 = 1/4, so r' = 2 - row_i . d, d' = d/2 + r'/4, x' = d + d' exactly.
+ * expire != 0 makes every wait for the copies run out (about 40 ms): the step then writes nothing
+ * and the call returns PORSOL_ERR_TIMEOUT with the context still usable.  Returns PORSOL_OK after a
+ * normal step. */
+int porsol_selftest_bulk_wait(int expire, float* r, float* d, float* x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -178,6 +178,7 @@ EXPORTS = [
     ("porsol_profile_reset", _i, [_vp]),
     ("porsol_stream", _vp, [_vp]),
     ("porsol_launch_count", C.c_longlong, []),
+    ("porsol_selftest_bulk_wait", C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("porsol_transport_cfl_noalloc", _i, [_i, _vp, _vp, _vp, _vp, _d, C.POINTER(_d), _vp]),
 ]
 
@@ -197,6 +198,17 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def selftest_bulk_wait(expire: bool = False):
+    """One run of the finest-level smoother step that stages its slices by bulk copy, on the fixed
+    64-row system of porsol_selftest_bulk_wait; expire makes every wait for the copies run out.
+    Returns (status code, r, d, x)."""
+    r = np.zeros(64, np.float32)
+    d = np.zeros(64, np.float32)
+    x = np.zeros(64, np.float32)
+    rc = lib().porsol_selftest_bulk_wait(1 if expire else 0, _p(r), _p(d), _p(x))
+    return rc, r, d, x
 
 
 class PorsolError(RuntimeError):

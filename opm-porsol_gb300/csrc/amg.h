@@ -41,6 +41,10 @@ struct AmgOpts {
                                    // bitwise reproducible)
 };
 
+// One finest-level bulk-staged Chebyshev step on a fixed 64-row system (expire: every wait for the
+// bulk copies runs out); returns the kernel's status bits and the 64 values of r, d and x.
+int bulk_step_selftest(bool expire, float* r, float* d, float* x);
+
 // Device aggregation result: agg (row -> aggregate or -1), members CSR (aggregate -> rows).
 struct Aggregates {
     int n = 0, nc = 0;

@@ -1216,4 +1216,18 @@ void* porsol_stream(porsol_solver* h) { return h ? (void*)h->stream : nullptr; }
 
 long long porsol_launch_count(void) { return porsol::g_launches.load(); }
 
+int porsol_selftest_bulk_wait(int expire, float* r, float* d, float* x)
+{
+    if (!r || !d || !x) return PORSOL_ERR_BAD_ARG;
+    try {
+        const int st = porsol::bulk_step_selftest(expire != 0, r, d, x);
+        if (st & porsol::ST_TIMEOUT) return PORSOL_ERR_TIMEOUT;
+        return st ? PORSOL_ERR_BAD_ARG : PORSOL_OK;
+    } catch (const porsol::Error& e) {
+        return e.code;
+    } catch (...) {
+        return PORSOL_ERR_CUDA;
+    }
+}
+
 }  // extern "C"

@@ -701,13 +701,23 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __rest
 // those of k_cheb_step<T, 0, __half, true> in the same order.  Every wait is bounded: on a timeout
 // the warp sets ST_TIMEOUT, waits once more (bounded) for its copies and returns without writing.
 constexpr int BULK_SLICES = 8;
-constexpr long long BULK_SPIN = 1LL << 20;
+constexpr unsigned long long BULK_WAIT_NS = 20000000ull;  // 20 ms: a copy of a few KB takes microseconds
+constexpr long long BULK_WAIT_TRIES = 1LL << 26;          // backstop should the timer not advance
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, long long limit)
+__device__ __forceinline__ unsigned long long global_ns()
 {
-    for (long long it = 0; it < limit; ++it) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for phase 0 of the barrier; false when it has not completed within limit_ns
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned long long limit_ns)
+{
+    const unsigned long long t0 = global_ns();
+    for (long long it = 0; it < BULK_WAIT_TRIES; ++it) {
         unsigned ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
@@ -715,19 +725,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, long long limit)
             : "r"(bar)
             : "memory");
         if (ok) return true;
+        if (global_ns() - t0 > limit_ns) return false;
     }
     return false;
 }
 
 // Dynamic shared memory: 128 bytes for the warps' barriers, then BULK_SLICES column areas of cap
 // entries (4 B each), then BULK_SLICES value areas (2 B each).  cap and the slice offsets are
-// multiples of 128 entries, so every copy starts and ends on a 16-byte boundary.
+// multiples of 128 entries, so every copy starts and ends on a 16-byte boundary.  extra_tx (0 in
+// solves) adds bytes the barrier waits for that no copy delivers: the self-test of the timeout path.
 template <class T>
 __global__ void __launch_bounds__(BULK_SLICES * 32)
     k_cheb_step_bulk(int n, int nslices, const int* __restrict__ sp4, const int* __restrict__ col4,
                      const __half* __restrict__ a4, const T* x_in, const T* __restrict__ d_in, T* __restrict__ r,
                      T* __restrict__ d_out, T* x_out, T c1, T c2, int final_step, const int* stop, int cap,
-                     int* status)
+                     int* status, unsigned extra_tx)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     if (*stop) return;
@@ -745,7 +757,8 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
     if (lane == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(unsigned(ne) * 6u)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(unsigned(ne) * 6u + extra_tx)
                      : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                          smem_u32(scol)),
@@ -757,9 +770,9 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
                      : "memory");
     }
     __syncwarp();
-    if (!mbar_wait_bounded(bar, BULK_SPIN)) {
+    if (!mbar_wait_bounded(bar, BULK_WAIT_NS)) {
         if (lane == 0) atomicOr(status, ST_TIMEOUT);
-        mbar_wait_bounded(bar, BULK_SPIN);
+        mbar_wait_bounded(bar, BULK_WAIT_NS);  // the copies themselves may still be in flight
         return;
     }
     const int i = s * 32 + lane;
@@ -1432,7 +1445,7 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
             const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
             PORSOL_LAUNCH((k_cheb_step_bulk<T><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
                 n, P.nslices, L.sp4.p, L.col4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
-                cap, status_.p)));
+                cap, status_.p, 0u)));
         } else if (L.v4) {
             PORSOL_LAUNCH((k_cheb_step<T, 0, __half, true><<<nb, TB, 0, s>>>(
                 n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
@@ -1500,5 +1513,53 @@ void Amg<T>::apply(cudaStream_t s, const T* r, T* z, const int* stop)
 
 template class Amg<double>;
 template class Amg<float>;
+
+// Self-test of k_cheb_step_bulk and of its bounded wait: one step (c1 = 1/2, c2 = 1/4, from x = 0,
+// final) on a 64-row system of two slices with one group each; row i holds the FP16 values
+// 1/4, 1/2, 3/4, 1 at columns i, (i+1)%64, (i+5)%64, (i+17)%64 and d_j = 1 + j/64, r = 2 (every
+// product and sum exact in FP32).  expire adds 16 bytes to what each warp's barrier waits for, so
+// every wait runs out.  Returns the kernel's status bits; r, d, x receive the 64 outputs.
+int bulk_step_selftest(bool expire, float* r_host, float* d_host, float* x_host)
+{
+    const int n = 64, ns = 2, cap = 128;
+    std::vector<int> sp4 = {0, 128, 256}, col4(256);
+    std::vector<__half> a4(256);
+    std::vector<float> din(n), r0(n, 2.0f);
+    const int off[4] = {0, 1, 5, 17};
+    for (int i = 0; i < n; ++i) {
+        din[i] = 1.0f + float(i) / 64.0f;
+        for (int t = 0; t < 4; ++t) {
+            const int dst = sp4[i / 32] + 4 * (i % 32) + t;
+            col4[dst] = (i + off[t]) % n;
+            a4[dst] = __float2half_rn(0.25f * float(t + 1));
+        }
+    }
+    cudaStream_t s = nullptr;
+    DBuf<int> dsp, dcol, dstop, dstat;
+    DBuf<__half> da;
+    DBuf<float> dd, dr, ddn, dx;
+    dsp.upload(sp4, s);
+    dcol.upload(col4, s);
+    da.upload(a4, s);
+    dd.upload(din, s);
+    dr.upload(r0, s);
+    ddn.alloc(n);
+    dx.alloc(n);
+    dstop.alloc(1);
+    dstop.zero(s);
+    dstat.alloc(1);
+    dstat.zero(s);
+    const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
+    PORSOL_LAUNCH((k_cheb_step_bulk<float><<<1, BULK_SLICES * 32, shm, s>>>(
+        n, ns, dsp.p, dcol.p, da.p, nullptr, dd.p, dr.p, ddn.p, dx.p, 0.5f, 0.25f, 1, dstop.p, cap, dstat.p,
+        expire ? 16u : 0u)));
+    PORSOL_CUDA(cudaGetLastError());
+    const int st = read_int(s, dstat.p);
+    dr.download(r_host, n, s);
+    ddn.download(d_host, n, s);
+    dx.download(x_host, n, s);
+    PORSOL_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
 
 }  // namespace porsol
