@@ -113,3 +113,32 @@ def test_transport_periodic_and_wells(pkg, gpulib, orc, workloads, cart):
     rc, s_orc, ns, rep = O.solve(sat, t, flux, injection=src)
     assert rc == 0 and st.small_steps == ns and st.repeats == rep
     assert relmax(s_gpu, s_orc) < 1e-11
+
+
+def test_transport_slug_constant_velocity(pkg, gpulib, orc, cart):
+    """The fixture of attic/euler/EulerSolverTester.hpp:69-100,155-180 on the GPU: a constant velocity
+    v = (1, 0, 0) (flux = (v . n) A), a slug of water in the middle third, water entering through x-.
+    GPU = oracle, and the water volume grows by exactly the injected amount while the front has not
+    reached x+."""
+    g = cart.CartesianGrid(12, 3, 2)
+    nc = g.num_cells
+    q = (g.fnormal[:, 0] * 1.0) * g.area
+    K = np.zeros((nc, 9))
+    K[:, 0] = K[:, 4] = K[:, 8] = 1.0
+    poro = np.full(nc, 0.25)
+    st = np.full(g.num_half_faces, pkg.BC_DIRICHLET, np.int32)
+    sv = np.ones(g.num_half_faces)
+    T = pkg.TransportSolver()
+    T.init(g, K.ravel(), poro, pkg.Fluid(pkg.FLUID_COREY2, 1.0, 2.0, 1000.0, 800.0), st, sv,
+           opts=pkg.default_transport_opts(method_capillary=0))
+    O = orc.OracleTransport(g, K.ravel(), poro, orc.Fluid(1.0, 2.0, 1000.0, 800.0), st, sv,
+                            opts=orc.TransportOpts.defaults(method_capillary=0))
+    s0 = np.zeros(nc)
+    s0[(g.ccentroid[:, 0] > 1 / 3) & (g.ccentroid[:, 0] < 2 / 3)] = 1.0
+    s_gpu, stats = T.solve(s0, 0.005, q)
+    rc, s_orc, ns, rep = O.solve(s0, 0.005, q)
+    assert rc == 0 and stats.small_steps == ns and stats.repeats == rep
+    assert relmax(s_gpu, s_orc) < 1e-12
+    inflow = -q[g.side == 1].sum()
+    assert s_gpu[g.ccentroid[:, 0] > 0.9].max() == 0.0
+    assert abs(((s_gpu - s0) * poro * g.volume).sum() - inflow * 0.005) < 1e-12
