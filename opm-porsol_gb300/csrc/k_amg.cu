@@ -1182,7 +1182,9 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.half = o_.half_smoother && std::is_same<T, float>::value;
     // one thread per row without timing (the rule's choice): the smoother reads the SELL-32x4
     // copy only, written in place of the plain FP16 copy
-    L.v4 = L.half && o_.layout4 && !o_.autotune && lanes_for(n, L.P->nent) == 1;
+    // (the x4 copy pads each row to a multiple of four entries; its offsets are 32-bit too)
+    L.v4 = L.half && o_.layout4 && !o_.autotune && lanes_for(n, L.P->nent) == 1 &&
+           (long long)L.P->nent + 96LL * L.P->nslices < (1LL << 31) - 1;
     const SellPattern& P = *L.P;
     if (L.v4) {
         L.sp4.alloc(size_t(P.nslices) + 1);
