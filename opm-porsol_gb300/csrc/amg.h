@@ -28,6 +28,8 @@ struct AmgOpts {
     double prolong = 1.6;       // coarse-correction damping (dune-istl prolongation damping factor)
     int coarse_target = 128;
     int max_levels = 24;
+    int round3_below = 0;       // coarse levels with fewer rows pair a third time (aggregates of about
+                                // eight rows): fewer of the small, launch-latency-bound levels
     double strength = 0.25;
     int cheb_degree = 2;
     bool round1_negative = true;   // first pairing round of a level on strong negative couplings
@@ -95,6 +97,7 @@ private:
     void galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Aggregates& a, SellPattern& Pc,
                   DBuf<T>& Ac);
     void smoother_setup(cudaStream_t s, Level& L, int level);
+    void adopt_tmp(Level& next);
     int tune_lanes(cudaStream_t s, Level& L);
     DBuf<int> tune_stop_;
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);

@@ -320,7 +320,12 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     // solution in FP64 and reliable updates (the iterated residual replaced by the FP64 residual
     // b - A x whenever it has dropped by inner_tolerance); see ReliableCg.
     if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED)) {
-        amg32.setup(stream, P, val32.p, ao);
+        // the throughput path coarsens its small coarse levels by three pairing rounds instead of
+        // two (on the 1M-cell system: 9 levels instead of 10, same CG iteration count, 2 % faster);
+        // the FP64 drop-in keeps the two-round hierarchy
+        AmgOpts ao32 = ao;
+        ao32.round3_below = 30000;
+        amg32.setup(stream, P, val32.p, ao32);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
     }

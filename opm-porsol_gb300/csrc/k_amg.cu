@@ -1304,6 +1304,20 @@ void Amg<T>::build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* 
     PORSOL_REQUIRE(st == 0, PORSOL_ERR_NONFINITE, "AMG: coarsest matrix is not positive definite");
 }
 
+// the next level takes the Galerkin product held in tmp_pat_ / tmp_val_
+template <class T>
+void Amg<T>::adopt_tmp(Level& next)
+{
+    std::swap(next.own.slice_ptr, tmp_pat_.slice_ptr);
+    std::swap(next.own.col, tmp_pat_.col);
+    std::swap(next.own.rowlen, tmp_pat_.rowlen);
+    std::swap(next.own.diag, tmp_pat_.diag);
+    next.own.n = tmp_pat_.n;
+    next.own.nslices = tmp_pat_.nslices;
+    next.own.nent = tmp_pat_.nent;
+    std::swap(next.own_val, tmp_val_);
+}
+
 template <class T>
 void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const AmgOpts& o)
 {
@@ -1344,16 +1358,18 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
             galerkin(s, tmp_pat_, tmp_val_.p, agg2_, next.own, next.own_val);
             PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, L.agg.agg.p, agg2_.agg.p));
             L.agg.nc = agg2_.nc;
+            if (nlev_ > 1 && n < o.round3_below && agg2_.nc > o.coarse_target) {
+                // round 3 on the level just formed (coarse levels only)
+                aggregate_round(s, next.own, next.own_val.p, agg2_.nc, o_.round2_negative, agg2_);
+                members(s, agg2_);
+                galerkin(s, next.own, next.own_val.p, agg2_, tmp_pat_, tmp_val_);
+                adopt_tmp(next);
+                PORSOL_LAUNCH(k_compose<<<div_up(n, TB), TB, 0, s>>>(n, L.agg.agg.p, agg2_.agg.p));
+                L.agg.nc = agg2_.nc;
+            }
             members(s, L.agg);
         } else {
-            std::swap(next.own.slice_ptr, tmp_pat_.slice_ptr);
-            std::swap(next.own.col, tmp_pat_.col);
-            std::swap(next.own.rowlen, tmp_pat_.rowlen);
-            std::swap(next.own.diag, tmp_pat_.diag);
-            next.own.n = tmp_pat_.n;
-            next.own.nslices = tmp_pat_.nslices;
-            next.own.nent = tmp_pat_.nent;
-            std::swap(next.own_val, tmp_val_);
+            adopt_tmp(next);
         }
         PORSOL_CUDA(cudaGetLastError());
         next.n = L.agg.nc;
