@@ -362,13 +362,15 @@ int porsol_capillary_solve_device(porsol_transport* t, porsol_solver* p, double*
 /* No counterpart in the reference.  The viscous CFL time step of the transport solver
  * (the quantity findCFLtimeVelocity bounds, before the Courant factor), for callers that may
  * not allocate device memory when they need it -- e.g. a simulator whose device memory is
- * owned by its own pool, or code running while a stream is captured into a CUDA graph.
+ * owned by its own pool allocator, where a cudaMalloc behind the pool's back would break the
+ * budget the pool manages.
  * All arrays are device pointers of the current device (layout of porsol_grid; outflux per
- * half-face, porosity per cell); *dt is a host double.  No device memory is allocated: the
- * scratch is a fixed array inside the library (256 KiB, held by every GPU that loads
- * the library until exit), so num_cells must be <= 4,194,304 (PORSOL_ERR_BAD_ARG beyond).
- * The first call on a device looks that array up, so make it before any stream capture.
- * Calls that overlap on the GPU share the array and race.  stream may be NULL.
+ * half-face, porosity per cell); *dt is a host double, so the call waits for the stream.
+ * No device memory is allocated: the scratch is a fixed array inside the library (256 KiB,
+ * held by every GPU that loads the library until exit), so num_cells must be <= 4,194,304
+ * (PORSOL_ERR_BAD_ARG beyond).  The first call on a device (and the first after that
+ * device's context was reset) looks that array's address up, so make it before any stream
+ * capture.  Calls that overlap on the GPU share the array and race.  stream may be NULL.
  * Returns PORSOL_ERR_CFL (with *dt = 0) when a cell's step is zero. */
 int porsol_transport_cfl_noalloc(int num_cells, const int* cell_facepos, const double* outflux,
                                  const double* cell_volume, const double* porosity, double cfl_factor,

@@ -2,10 +2,11 @@
 // solver, computed without allocating any device memory.
 //
 // Who needs it: callers that may not allocate device memory at the moment they need the
-// step bound, for example a simulator whose device memory is owned by its own pool, or code
-// that runs while a stream is being captured into a CUDA graph.  The transport handle
-// (porsol_transport_*) allocates its buffers at init; this entry point takes the caller's
-// device arrays and uses a fixed scratch array compiled into the library instead.
+// step bound, for example a simulator whose device memory is owned by its own pool allocator
+// (a cudaMalloc behind the pool's back would fragment or exceed the budget the pool manages).
+// The transport handle (porsol_transport_*) allocates its buffers at init; this entry point
+// takes the caller's device arrays and uses a fixed scratch array compiled into the library
+// instead.
 //
 // Scratch: s_cfl_scratch, a file-scope __device__ array of CFL_MAX_BLOCKS per-block minima
 // and flags plus the final result.  Every GPU that loads the library holds it
@@ -29,10 +30,37 @@ constexpr int CFL_MAX_CELLS = CFL_MAX_BLOCKS * CFL_THREADS;
 constexpr int CFL_SCRATCH = 2 * CFL_MAX_BLOCKS + 2;
 static __device__ __align__(256) double s_cfl_scratch[CFL_SCRATCH];
 
-// Per-device address of s_cfl_scratch, looked up once per device.
+// Per-device address of s_cfl_scratch, looked up once per device context.  The address belongs
+// to the module loaded into that context: after cudaDeviceReset (or a primary-context release)
+// the module is loaded again, possibly elsewhere, so each cached address is kept together with
+// the context it was looked up in and is looked up again when the current context differs.
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mutex;
 double* g_scratch[MAX_DEVICES] = {nullptr};
+void* g_context[MAX_DEVICES] = {nullptr};
+
+// cuCtxGetCurrent from the driver through the runtime (no link-time dependency on libcuda).
+using CtxGetCurrent = int (*)(void**);
+CtxGetCurrent ctx_get_current()
+{
+    static const CtxGetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(p);
+    }();
+    return fn;
+}
+
+void* current_context()
+{
+    void* c = nullptr;
+    const CtxGetCurrent fn = ctx_get_current();
+    if (!fn || fn(&c) != 0) return nullptr;
+    return c;
+}
 
 // Stage 1 -- the per-cell bound of findCFLtimeVelocity (CflCalculator.hpp:55-88):
 // cfl_factor |c| phi_c / max(sum of outfluxes, sum of influxes); one minimum per block.
@@ -109,7 +137,9 @@ __global__ void __launch_bounds__(CFL_THREADS) k_cfl_final(int nblocks, double* 
     }
 }
 
-// Address of the scratch array on the current device (first call per device looks it up).
+// Address of the scratch array on the current device.  The first call on a device (and the
+// first call after its context was replaced) looks it up with cudaGetSymbolAddress; the host
+// symbol s_cfl_scratch itself is only a host-side stand-in and is never passed to a kernel.
 cudaError_t scratch_on_current_device(double** out)
 {
     int dev = 0;
@@ -117,11 +147,13 @@ cudaError_t scratch_on_current_device(double** out)
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch[dev]) {
+    void* ctx = current_context();
+    if (!g_scratch[dev] || !ctx || ctx != g_context[dev]) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, s_cfl_scratch);
+        e = cudaGetSymbolAddress(&p, s_cfl_scratch);   // also makes the device's context current
         if (e != cudaSuccess) return e;
         g_scratch[dev] = static_cast<double*>(p);
+        g_context[dev] = current_context();
     }
     *out = g_scratch[dev];
     return cudaSuccess;

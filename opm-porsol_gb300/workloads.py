@@ -135,11 +135,14 @@ def random_rotations(rng, n):
     return Q
 
 
-def periodic_subgrids(num=512, nmin=8, nmax=32, seed=None, sigma=1.5):
+def periodic_subgrids(num=512, nmin=8, nmax=32, seed=None, sigma=1.5, sides=None):
     """Batched periodic upscaling: `num` unit-cube sub-grids of n^3 cells, n ~ U{nmin..nmax},
-    full SPD tensors K = R diag(exp(g)) R^T per cell, g ~ N(ln 100 mD, sigma^2), R uniform."""
+    full SPD tensors K = R diag(exp(g)) R^T per cell, g ~ N(ln 100 mD, sigma^2), R uniform.
+    `sides` (a list of n) replaces the drawn sides (num is then its length)."""
     rng = np.random.default_rng(SEED0 + 3 if seed is None else seed)
     sizes = rng.integers(nmin, nmax + 1, size=num)
+    if sides is not None:
+        sizes = np.asarray(sides, dtype=sizes.dtype)
     grids = [CartesianGrid(int(n), int(n), int(n), unique_bids=True) for n in sizes]
     union = UnionGrid(grids)
     nc = union.num_cells

@@ -1,8 +1,9 @@
 """porsol_transport_cfl_noalloc: the viscous CFL step for callers that cannot allocate device
-memory (their device memory belongs to their own pool, or they run during a CUDA graph
-capture).  It must agree with the CFL step that the allocating transport entry point
-(porsol_transport_solve) computes with the same kernel arithmetic, on two calls in a row
-(the fixed scratch array keeps the previous call's contents).  Collected last on purpose."""
+memory (their device memory belongs to their own pool allocator).  It must agree with the CFL
+step that the allocating transport entry point (porsol_transport_solve) computes with the same
+kernel arithmetic, on two calls in a row (the fixed scratch array keeps the previous call's
+contents), and report a zero step as findCFLtimeVelocity's zero-step error
+(CflCalculator.hpp:75-77).  Collected last on purpose."""
 import ctypes as C
 
 import numpy as np
@@ -41,3 +42,22 @@ def test_noalloc_cfl_matches_transport_entry_point(pkg, gpulib, orc, workloads):
     rc = pkg.lib().porsol_transport_cfl_noalloc(4194305, d["fp"].data_ptr(), d["q"].data_ptr(),
                                                 d["vol"].data_ptr(), d["phi"].data_ptr(), fac, C.byref(dt), None)
     assert rc == 2   # PORSOL_ERR_BAD_ARG
+
+    # a cell with zero porosity and non-zero flux has a zero step: PORSOL_ERR_CFL with *dt = 0,
+    # after a call that left a non-zero result in the shared scratch array
+    phi0 = prob.poro.copy()
+    fp = g.facepos
+    busy = int(np.argmax([np.abs(flux[fp[c]:fp[c + 1]]).sum() for c in range(g.num_cells)]))
+    phi0[busy] = 0.0
+    d_phi0 = torch.from_numpy(phi0).to(dev)
+    torch.cuda.synchronize()
+    dt = C.c_double(-1.0)
+    rc = pkg.lib().porsol_transport_cfl_noalloc(g.num_cells, d["fp"].data_ptr(), d["q"].data_ptr(),
+                                                d["vol"].data_ptr(), d_phi0.data_ptr(), fac, C.byref(dt), None)
+    assert rc == 9, f"status {rc}"   # PORSOL_ERR_CFL
+    assert dt.value == 0.0
+    # and the next ordinary call is exact again
+    dt = C.c_double(-1.0)
+    rc = pkg.lib().porsol_transport_cfl_noalloc(g.num_cells, d["fp"].data_ptr(), d["q"].data_ptr(),
+                                                d["vol"].data_ptr(), d["phi"].data_ptr(), fac, C.byref(dt), None)
+    assert rc == 0 and abs(dt.value - ref) <= 1e-12 * ref
