@@ -168,6 +168,13 @@ int porsol_get_solution_device(porsol_solver* h, const double** pressure, const 
                                const double** face_pressure);
 
 /* Introspection (printStats, IncompFlowSolverHybrid.hpp:849-871; printSystem :895-905). */
+/* No counterpart in the reference (measurement).  Algorithmic bytes of the last solve:
+ * out4[0] assembly, [1] linear solve (every CG iteration with its preconditioner application,
+ * residual replacements and the start), [2] recovery, [3] the postProcessFluxes that followed
+ * it (0 if none); and, for AMG solves, the bytes of one V-cycle per level (up to max_levels
+ * values; vcycle_level_bytes may be NULL).  Each kernel is counted as its stored matrix entries
+ * (values and column indices) read once plus every vector it gathers, reads or writes once. */
+int porsol_solve_bytes(porsol_solver* h, double* out4, int max_levels, double* vcycle_level_bytes);
 /* AMG hierarchy of the last type-1..3 solve: rows and stored entries per level (finest
  * first, at most max_levels written); returns the level count in *levels. */
 int porsol_amg_info(porsol_solver* h, int max_levels, int* levels, int* rows, long long* entries);

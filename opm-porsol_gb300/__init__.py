@@ -151,6 +151,7 @@ EXPORTS = [
     ("porsol_get_inner_products", _i, [_vp, _vp, _vp]),
     ("porsol_get_system", _i, [_vp, _vp, _vp]),
     ("porsol_amg_info", _i, [_vp, _i, C.POINTER(_i), _vp, _vp]),
+    ("porsol_solve_bytes", _i, [_vp, _vp, _i, _vp]),
     ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
                                      C.POINTER(SolveStats)]),
     ("porsol_cell_fields", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -423,6 +424,14 @@ class PressureSolver:
         ent = np.zeros(64, np.int64)
         self._check(lib().porsol_amg_info(self.h, 64, C.byref(nl), _p(rows), _p(ent)))
         return rows[:nl.value].tolist(), ent[:nl.value].tolist()
+
+    def solve_bytes(self, max_levels=64):
+        """Algorithmic bytes of the last solve: dict(assembly, krylov, recovery, post, vcycle_levels)."""
+        out = np.zeros(4)
+        lv = np.zeros(max_levels)
+        self._check(lib().porsol_solve_bytes(self.h, _p(out), max_levels, _p(lv)))
+        return dict(assembly=out[0], krylov=out[1], recovery=out[2], post=out[3],
+                    vcycle_levels=lv[:int(np.count_nonzero(lv))].tolist())
 
     def system(self):
         S = np.empty(self.nnz)

@@ -61,6 +61,10 @@ public:
     int levels() const { return nlev_; }
     void set_profiler(Profiler* p) { prof_ = p; }
     const std::vector<int>& level_sizes() const { return sizes_; }
+    // Algorithmic bytes of one apply() (one V-cycle) of the current hierarchy, in total and per
+    // level: every kernel's stored matrix entries (values + columns or 16-bit offsets) read once,
+    // each vector it gathers read once, the vectors it streams read or written once.
+    double apply_bytes(std::vector<double>* per_level = nullptr) const;
     const std::vector<long long>& level_nnz() const { return nnzs_; }
     // error bits set by the apply kernels (ST_TIMEOUT: a bounded wait for a bulk copy gave up);
     // synchronises the stream
@@ -85,6 +89,10 @@ private:
         int bulk_groups = 0;         // > 0: the Chebyshev step stages the x4 slices by bulk copy
         DBuf<int> sp4, col4;
         DBuf<__half> ah4;
+        // the x4 copy's columns as 16-bit offsets from the row (off4) when every coupling of the
+        // level lies within 32767 rows of the diagonal (c16); col4 otherwise
+        bool c16 = false;
+        DBuf<short> off4;
         double lmax = 2.0;
         int lanes = 1;               // threads per row in the smoother/residual kernels
         Aggregates agg;              // to the next level
@@ -100,6 +108,7 @@ private:
     void adopt_tmp(Level& next);
     int tune_lanes(cudaStream_t s, Level& L);
     DBuf<int> tune_stop_;
+    DBuf<int> s_maxoff_;   // per level: largest |col - row| of the x4 copy (16-bit offset check)
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);
     void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
                    const int* stop);
@@ -114,7 +123,7 @@ private:
     DBuf<float> s_rs_;
     DBuf<int> s_state_, s_partner_, s_join_, s_best_, s_flag_, s_cidx_, s_cnt_, s_pos_, s_width_;
     DBuf<unsigned long long> s_gmax_;
-    DBuf<int> s_bnd_, s_goff_, s_tcol_, s_dpos_;   // single-pass Galerkin temporaries
+    DBuf<int> s_bnd_, s_goff_, s_tcol_, s_dpos_, s_woff_;   // Galerkin temporaries
     DBuf<T> s_tval_;
     Aggregates agg2_;
     std::vector<int> sizes_;

@@ -167,8 +167,9 @@ void porsol_solver::init_structure(const porsol_grid* grid, const int* flow_type
     const HostGrid& g = S.g;
     cudaStream_t s = stream;
     facepos.upload(g.facepos, s);
-    cf.upload(S.cf, s);
+    cf.upload(S.renumbered() ? S.cf_int : S.cf, s);   // the device system's (internal) numbering
     pairs.upload(S.pairs, s);
+    if (S.renumbered()) dof_perm_d.upload(S.dof_perm, s);
     upload_geometry(grid);
     S.pat.upload(s);
     status.alloc(1);
@@ -259,6 +260,36 @@ double now_ms()
 }
 }  // namespace
 
+// Algorithmic bytes of the linear solve just finished (values + columns of each stored entry read
+// once per matrix pass, each vector read or written once per kernel; s_v / s_x the value and
+// vector widths):
+//   FP64 AMG-CG:  per iteration SpMV + p.q  Z(8+4) + 16N, update x, r  48N, z.r  16N,
+//                 direction 24N, V-cycle; start: residual Z 12 + 24N, V-cycle, z.r, direction
+//   mixed:        per iteration FP32 SpMV + p.q  Z(4+4) + 8N, update (x FP64)  32N, z.r  8N,
+//                 direction 12N, FP32 V-cycle; per FP64 residual replacement Z 12 + 24N and the
+//                 rescale 20N; start: FP64 residual, rescale, V-cycle, z.r, direction
+//   ILU0-CG:      per iteration 2 Z (8+4) + 8 (N+1) + 19 N 8 (SpMV, both triangular sweeps, two
+//                 dots, three vector updates)
+void porsol_solver::count_krylov_bytes(const porsol_solve_opts& o, int iterations, int replacements)
+{
+    const double Z = double(S.pat.nent), N = double(S.N), it = iterations;
+    vcycle_level_bytes.clear();
+    if (o.linsolver_type == 0) {
+        bytes_krylov = (it + 1) * (2.0 * Z * 12.0 + 8.0 * (N + 1) + 19.0 * N * 8.0);
+        return;
+    }
+    if (o.precision == PORSOL_FP64) {
+        const double vc = amg64.apply_bytes(&vcycle_level_bytes);
+        bytes_krylov = it * (Z * 12.0 + 16.0 * N + 48.0 * N + 16.0 * N + 24.0 * N + vc) +
+                       (Z * 12.0 + 24.0 * N + vc + 16.0 * N + 16.0 * N);
+    } else {
+        const double vc = amg32.apply_bytes(&vcycle_level_bytes);
+        bytes_krylov = it * (Z * 8.0 + 8.0 * N + 32.0 * N + 8.0 * N + 12.0 * N + vc) +
+                       replacements * (Z * 12.0 + 24.0 * N + 20.0 * N) +
+                       (Z * 12.0 + 24.0 * N + 12.0 * N + vc + 8.0 * N + 8.0 * N);
+    }
+}
+
 void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st)
 {
     NvtxRange range("porsol linear solve (setup + CG)");
@@ -278,6 +309,10 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         batched_solve(o, st, maxit);
         return;
     }
+    if (o.linsolver_type == 0 && S.renumbered()) {
+        ilu_solve_reference_order(o, st, maxit);
+        return;
+    }
     if (o.linsolver_type == 0) {
         // solveLinearSystem (:1387-1420): ILU0(S, 1.0), CG, zero initial guess
         if (!ilu_levels) {
@@ -290,6 +325,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         CgResult r = cg64.solve(stream, P, val.p, ilu, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
         st.iterations = r.iterations;
         st.reduction = r.reduction;
+        count_krylov_bytes(o, r.iterations, 0);
         if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
         if (!r.converged) fail(r.iterations, r.reduction);
         return;
@@ -312,6 +348,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         CgResult r = cg64.solve(stream, P, val.p, amg64, rhs.p, x.p, o.residual_tolerance, maxit, &prof, PK_SPMV64);
         st.iterations = r.iterations;
         st.reduction = r.reduction;
+        count_krylov_bytes(o, r.iterations, 0);
         if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
         if (!r.converged) fail(r.iterations, r.reduction);
         return;
@@ -342,8 +379,51 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     st.iterations = r.iterations;
     st.outer_iterations = rcg.replacements();
     st.reduction = r.reduction;
+    count_krylov_bytes(o, r.iterations, rcg.replacements());
     if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature or non-finite residual)");
     if (!r.converged) fail(r.iterations, r.reduction);
+}
+
+// ILU0-CG (solveLinearSystem, :1387-1420) of a structure whose device numbering differs from the
+// reference's: ILU(0) depends on the order of the unknowns, so the factorisation and the CG run on
+// the system gathered into the reference numbering (same factors, iterates and iteration counts as
+// the reference), and the solution is scattered back.
+void porsol_solver::ilu_solve_reference_order(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit)
+{
+    const double t_begin = now_ms();
+    const int n = S.N;
+    if (!S.ref_pattern_built) {
+        S.build_ref_pattern();
+        S.pat_ref.upload(stream);
+        ref_slot_src_d.upload(S.ref_slot_src, stream);
+        ilu_levels = false;
+    }
+    const SellPattern& P = S.pat_ref;
+    val_ref.alloc(size_t(P.nent));
+    rhs_ref.alloc(n);
+    x_ref.alloc(n);
+    launch_gather_values(stream, P.nent, ref_slot_src_d.p, val.p, val_ref.p);
+    launch_permute(stream, n, dof_perm_d.p, rhs.p, rhs_ref.p, true);
+    if (!ilu_levels) {
+        ilu.build_levels(P, stream);
+        ilu_levels = true;
+    }
+    ilu.factor(stream, P, val_ref.p);
+    st.ms_precond_setup = now_ms() - t_begin;
+    x_ref.zero(stream);
+    CgResult r = cg64.solve(stream, P, val_ref.p, ilu, rhs_ref.p, x_ref.p, o.residual_tolerance, maxit, &prof,
+                            PK_SPMV64);
+    launch_permute(stream, n, dof_perm_d.p, x_ref.p, x.p, false);
+    st.iterations = r.iterations;
+    st.reduction = r.reduction;
+    count_krylov_bytes(o, r.iterations, 0);
+    if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+    if (!r.converged) {
+        std::ostringstream os;
+        os << "Linear solver failed to converge in " << r.iterations << " iterations.\n"
+           << "Residual reduction achieved is " << r.reduction << '\n';
+        throw Error(PORSOL_ERR_NOT_CONVERGED, os.str());
+    }
 }
 
 // Block-diagonal systems (batched upscaling): one CG per block (BatchedPcg), each block with
@@ -535,6 +615,12 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     W_last = W_use;
     tensor_last = tensor;
     {
+        // per cell: packed W read, local Schur entries written, mobilities/sources/F/L/g/rhs pieces
+        // ~64 B; per SELL slot: recipe pointer + entry + gathered local entry + value written (+ the
+        // FP32 copy); per row: right-hand-side recipe and pieces
+        bytes_asm = double(nc) * (npk * 16.0 + 64.0) + double(S.pat.nent) * (4.0 + 4.0 + 8.0 + 8.0 + (mixed ? 4.0 : 0.0)) +
+                    double(S.N) * (4.0 + 2.0 * (4.0 + 8.0) + 8.0);
+        bytes_krylov = bytes_rec = bytes_post = 0.0;
         ProfScope ps(prof, s, PK_ASSEMBLE, double(nc) * (npk * 16.0 + 64) + double(S.pat.nent) * 16.0);
         AssembleArgs a;
         a.nc = nc;
@@ -573,7 +659,7 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
         launch_pin_rows(s, int(reg_rows.size()), reg_rows_d.p, S.pat.slice_ptr.p, S.pat.col.p, S.pat.rowlen.p, val.p,
                         mixed ? val32.p : nullptr, rhs.p);
     } else if (R.do_reg && (o.linsolver_type == 0 || !o.same_matrix)) {
-        launch_scale_entry(s, val.p, S.pat.diag.p, 0, 2.0, mixed ? val32.p : nullptr);
+        launch_scale_entry(s, val.p, S.pat.diag.p, S.dof(0), 2.0, mixed ? val32.p : nullptr);
         reg_applied = true;
     }
     porsol_solve_stats st{};
@@ -583,6 +669,9 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     st.ms_krylov = now_ms() - t_lin - st.ms_precond_setup;
     const double t_rec = now_ms();
     {
+        // per cell: W, the face pressures gathered through cf, F, L, g, mobility in; pressure and
+        // half-face fluxes out (the profiler's figure for this kernel)
+        bytes_rec = double(nc) * (npk * 8.0 + 6 * 8 * 4 + 32) + double(S.N) * 8.0;
         ProfScope ps(prof, s, PK_RECOVER, double(nc) * (npk * 8.0 + 6 * 8 * 4 + 32) + double(S.N) * 8.0);
         RecoverArgs ra;
         ra.nc = nc;
@@ -621,6 +710,7 @@ double porsol_solver::post_process()
     PORSOL_REQUIRE(solved, PORSOL_ERR_STATE, "postProcessFluxes before solve");
     PORSOL_CUDA(cudaMemsetAsync(redbits.p + 3, 0, sizeof(unsigned long long), stream));
     launch_post_process(stream, int(S.pairs.size() / 2), pairs.p, outflux.p, redbits.p + 3);
+    bytes_post = double(S.pairs.size() / 2) * (2 * 4.0 + 2 * 8.0 + 2 * 8.0);   // pair indices, fluxes in and out
     unsigned long long b = 0;
     PORSOL_CUDA(cudaMemcpyAsync(&b, redbits.p + 3, sizeof(b), cudaMemcpyDeviceToHost, stream));
     PORSOL_CUDA(cudaStreamSynchronize(stream));
@@ -650,6 +740,9 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             bct[hf] = PORSOL_BC_PERIODIC;
         }
     init_structure(grid, bct.data(), partner);
+    // every boundary face is periodic, so the face numbering is the reference's (the sub-grids'
+    // unknown ranges below rely on it)
+    PORSOL_REQUIRE(!S.renumbered(), PORSOL_ERR_STATE, "upscale: unexpected internal face numbering");
     const double zero3[3] = {0.0, 0.0, 0.0};
     compute_inner_products(perm_h, zero3);
     // per sub-grid: side areas A_i (high sides), extents L_d, first DOF
@@ -1097,7 +1190,15 @@ int porsol_get_solution(porsol_solver* h, double* p, double* v, double* pi)
         PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "getSolution before solve");
         if (p) h->pressure.download(p, h->S.g.nc, h->stream);
         if (v) h->outflux.download(v, h->S.g.nhf, h->stream);
-        if (pi) h->x.download(pi, h->S.N, h->stream);
+        if (pi) {
+            if (h->S.renumbered()) {
+                h->pi_ref.alloc(h->S.N);
+                launch_permute(h->stream, h->S.N, h->dof_perm_d.p, h->x.p, h->pi_ref.p, true);
+                h->pi_ref.download(pi, h->S.N, h->stream);
+            } else {
+                h->x.download(pi, h->S.N, h->stream);
+            }
+        }
         PORSOL_CUDA(cudaStreamSynchronize(h->stream));
     });
 }
@@ -1109,7 +1210,16 @@ int porsol_get_solution_device(porsol_solver* h, const double** p, const double*
         PORSOL_CUDA(cudaStreamSynchronize(h->stream));
         if (p) *p = h->pressure.p;
         if (v) *v = h->outflux.p;
-        if (pi) *pi = h->x.p;
+        if (pi) {
+            if (h->S.renumbered()) {   // face pressures in the reference numbering
+                h->pi_ref.alloc(h->S.N);
+                launch_permute(h->stream, h->S.N, h->dof_perm_d.p, h->x.p, h->pi_ref.p, true);
+                PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+                *pi = h->pi_ref.p;
+            } else {
+                *pi = h->x.p;
+            }
+        }
     });
 }
 
@@ -1177,8 +1287,32 @@ int porsol_get_system(porsol_solver* h, double* values, double* rhs)
                     if (S.csr2sell[k] == k0) values[k] = v[k0] / 2.0;
             }
         }
-        if (rhs) h->rhs.download(rhs, S.N, h->stream);
+        if (rhs) {
+            if (S.renumbered()) {
+                std::vector<double> r(S.N);
+                h->rhs.download(r.data(), S.N, h->stream);
+                PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+                for (int i = 0; i < S.N; ++i) rhs[i] = r[S.dof_perm[i]];
+            } else {
+                h->rhs.download(rhs, S.N, h->stream);
+            }
+        }
         PORSOL_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int porsol_solve_bytes(porsol_solver* h, double* out4, int max_levels, double* vcycle_level_bytes)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(h->solved, PORSOL_ERR_STATE, "solve_bytes before solve");
+        if (out4) {
+            out4[0] = h->bytes_asm;
+            out4[1] = h->bytes_krylov;
+            out4[2] = h->bytes_rec;
+            out4[3] = h->bytes_post;
+        }
+        for (int l = 0; vcycle_level_bytes && l < max_levels && l < int(h->vcycle_level_bytes.size()); ++l)
+            vcycle_level_bytes[l] = h->vcycle_level_bytes[size_t(l)];
     });
 }
 

@@ -393,103 +393,110 @@ __global__ void k_gal_rowbound(int nc, const int* __restrict__ ptr, const int* _
     if ((threadIdx.x & 31) == 0) atomicMax(maxb, b);
 }
 
-// Galerkin merge, one pass, L lanes per coarse row (32 / L rows per warp): the member rows'
-// entries (column mapped through agg) are loaded into shared memory, bitonic-sorted by column and
-// duplicates summed (FP64); the distinct (column, value) pairs go compactly to off[I] of a
-// temporary buffer, with the row length and the position of the diagonal.  The SELL layout is
-// filled from there once the slice widths are known (k_gal_scatter).  The host picks L so that
-// each lane holds about four of the CAP candidates: short rows (the first levels: pairs of
-// 11-entry rows over millions of rows) share a warp, and each lane keeps several independent
-// compare-exchanges in flight per stage.
-constexpr int GW_WARPS = 4;
-template <class T, int CAP, int L>
-__global__ void __launch_bounds__(GW_WARPS * 32) k_gal_merge(int nc, const int* __restrict__ sp,
-                                                           const int* __restrict__ col, const int* __restrict__ rowlen,
-                                                           const T* __restrict__ A, const int* __restrict__ agg,
-                                                           const int* __restrict__ ptr, const int* __restrict__ idx,
-                                                           const int* __restrict__ off, int* __restrict__ tcol,
-                                                           T* __restrict__ tval, int* __restrict__ rowlen_c,
-                                                           int* __restrict__ dpos)
+// ---- Galerkin product in two passes: candidates, then a sort-free merge ----
+// Pass 0: where each member row's candidates go: aggregate I's segment starts at goff[I]; its
+// members (sorted) follow one another.
+__global__ void k_gal_woff(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
+                           const int* __restrict__ rowlen, const int* __restrict__ goff, int* __restrict__ woff)
 {
-    constexpr int R = 32 / L;   // rows per warp
-    // row strides padded so that the R rows of a warp start L words (keys) and 8 words (values)
-    // apart modulo the 32 banks: same-position accesses of different rows do not collide
-    constexpr int KS = CAP + (L < 32 ? L : 0), VS = CAP + (L < 32 ? L / 2 : 0);
-    __shared__ int sk[GW_WARPS * R * KS];
-    __shared__ double sv[GW_WARPS * R * VS];
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    int w = goff[I];
+    for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
+        const int r = idx[q];
+        woff[r] = w;
+        w += rowlen[r];
+    }
+}
+
+// Pass 1, one thread per fine row (consecutive rows read consecutive SELL entries): the row's
+// entries with their columns mapped through agg (-1: an isolated column, no coupling) written to
+// its aggregate's candidate segment.  Rows outside every aggregate (isolated) are skipped.
+template <class T>
+__global__ void k_gal_cand(int n, const int* __restrict__ sp, const int* __restrict__ col,
+                           const int* __restrict__ rowlen, const T* __restrict__ A, const int* __restrict__ agg,
+                           const int* __restrict__ woff, int* __restrict__ ckey, T* __restrict__ cval)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || agg[i] < 0) return;
+    const int w = woff[i], len = rowlen[i];
+    const int b = sp[i >> 5] + (i & 31);
+    for (int t = 0; t < len; ++t) {
+        const int k = b + 32 * t;
+        ckey[w + t] = agg[col[k]];
+        cval[w + t] = A[k];
+    }
+}
+
+// Pass 2, one warp per coarse row: the candidates [goff[I], goff[I+1]) in chunks of 32 (one per
+// lane).  Equal columns of a chunk are found with __match_any_sync; the lowest lane of each group
+// sums the group's values in lane order (FP64) and adds the sum to the column's entry of the row's
+// list (found by a scan of the list, or appended in lane order when new).  The list (first-occurrence
+// order) is written over the row's own segment, with its length and the diagonal's position.
+// Every sum has a fixed order, so the product is run-to-run reproducible.  Shared memory per warp:
+// cap column and cap FP64 entries of the list, 32 FP64 staging values.
+constexpr int GD_WARPS = 4;
+template <class T>
+__global__ void __launch_bounds__(GD_WARPS * 32) k_gal_dedup(int nc, int cap, const int* __restrict__ goff,
+                                                            int* __restrict__ tcol, T* __restrict__ tval,
+                                                            int* __restrict__ rowlen_c, int* __restrict__ dpos,
+                                                            int* __restrict__ status)
+{
+    extern __shared__ __align__(16) unsigned char gd_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / L, sl = lane % L;
-    const int I0 = (blockIdx.x * GW_WARPS + w) * R;
-    if (I0 >= nc) return;   // warp-uniform
-    const int I = I0 + sub;
-    const bool active = I < nc;
-    int* keys = sk + (w * R + sub) * KS;
-    double* vals = sv + (w * R + sub) * VS;
-    int m = 0;
-    if (active) {
-        for (int q = ptr[I]; q < ptr[I + 1]; ++q) {
-            const int r = idx[q];
-            const int len = rowlen[r];
-            const int base = sp[r >> 5] + (r & 31);
-            for (int t = sl; t < len; t += L) {
-                const int k = base + t * 32;
-                const int c = agg[col[k]];
-                keys[m + t] = c < 0 ? INT_MAX : c;
-                vals[m + t] = double(A[k]);
-            }
-            m += len;
-        }
-    }
-    // one network size for the warp: the largest power of two over its rows
-    int m2 = 1;
-    while (m2 < m) m2 <<= 1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m2 = max(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-    for (int p = m + sl; p < m2; p += L) {
-        keys[p] = INT_MAX;
-        vals[p] = 0.0;
-    }
-    __syncwarp();
-    for (int k = 2; k <= m2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int p = sl; p < m2; p += L) {
-                const int q = p ^ j;
-                if (q > p) {
-                    const bool up = (p & k) == 0;
-                    const int kp = keys[p], kq = keys[q];
-                    if ((kp > kq) == up) {
-                        keys[p] = kq;
-                        keys[q] = kp;
-                        const double tv = vals[p];
-                        vals[p] = vals[q];
-                        vals[q] = tv;
-                    }
+    const int I = blockIdx.x * GD_WARPS + w;
+    if (I >= nc) return;   // warp-uniform
+    double* stage = reinterpret_cast<double*>(gd_smem) + w * (32 + cap);
+    double* lsum = stage + 32;
+    int* lkey = reinterpret_cast<int*>(reinterpret_cast<double*>(gd_smem) + GD_WARPS * (32 + cap)) + w * cap;
+    const int b = goff[I], e = goff[I + 1];
+    int d = 0;
+    for (int c0 = b; c0 < e; c0 += 32) {
+        const int p = c0 + lane;
+        const bool valid = p < e;
+        const int key = valid ? tcol[p] : -1;
+        const bool active = key >= 0;
+        stage[lane] = valid ? double(tval[p]) : 0.0;
+        const unsigned peers = __match_any_sync(0xffffffffu, active ? key : -2 - lane);
+        const bool leader = active && (__ffs(peers) - 1) == lane;
+        __syncwarp();
+        double csum = 0.0;
+        int at = -1;
+        if (leader) {
+            for (unsigned m = peers; m; m &= m - 1) csum += stage[__ffs(m) - 1];
+            for (int q = 0; q < d; ++q)
+                if (lkey[q] == key) {
+                    at = q;
+                    break;
                 }
+        }
+        const unsigned fresh = __ballot_sync(0xffffffffu, leader && at < 0);
+        if (leader) {
+            if (at < 0) {
+                at = d + __popc(fresh & ((1u << lane) - 1u));
+                if (at < cap) {
+                    lkey[at] = key;
+                    lsum[at] = csum;
+                } else {
+                    atomicOr(status, ST_BAD_INDEX);
+                }
+            } else {
+                lsum[at] += csum;
             }
-            __syncwarp();
         }
+        d = min(d + __popc(fresh), cap);
+        __syncwarp();
     }
-    const int o = active ? off[I] : 0;
-    const unsigned rowmask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << (sub * L);
-    int base = 0, dp = -1;
-    for (int c0 = 0; c0 < m2; c0 += L) {
-        const int p = c0 + sl;
-        const bool head = active && p < m2 && keys[p] != INT_MAX && (p == 0 || keys[p] != keys[p - 1]);
-        const unsigned mask = __ballot_sync(0xffffffffu, head) & rowmask;
-        if (head) {
-            double sum = vals[p];
-            for (int q = p + 1; q < m2 && keys[q] == keys[p]; ++q) sum += vals[q];
-            const int tt = base + __popc(mask & ((1u << lane) - 1u));
-            tcol[o + tt] = keys[p];
-            tval[o + tt] = T(sum);
-            if (keys[p] == I) dp = tt;
-        }
-        base += __popc(mask);
+    int dp = -1;
+    for (int q = lane; q < d; q += 32) {
+        tcol[b + q] = lkey[q];
+        tval[b + q] = T(lsum[q]);
+        if (lkey[q] == I) dp = q;
     }
 #pragma unroll
-    for (int q = L / 2; q > 0; q >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, q));
-    if (active && sl == 0) {
-        rowlen_c[I] = base;
+    for (int o = 16; o > 0; o >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, o));
+    if (lane == 0) {
+        rowlen_c[I] = d;
         dpos[I] = dp;
     }
 }
@@ -608,12 +615,15 @@ __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __rest
 
 
 // sum_j a_rj x(j) for row r: the coalesced one-thread-per-row form for K = 1, the SELL-32x4 copy
-// (sp, col, A its slice offsets, columns and FP16 values) for K = 0, K lanes otherwise
-template <int K, class T, class V, class XF>
-__device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __restrict__ col, const V* __restrict__ A,
+// (sp, col, A its slice offsets, columns and FP16 values) for K = 0, the SELL-32x4 copy with 16-bit
+// column offsets (col: CI = short) for K = -1, K lanes otherwise
+template <int K, class T, class V, class XF, class CI>
+__device__ __forceinline__ T row_dot(const int* __restrict__ sp, const CI* __restrict__ col, const V* __restrict__ A,
                                      const int* __restrict__ rowlen, int r, int q, bool valid, XF xf)
 {
-    if constexpr (K == 0) {
+    if constexpr (K == -1) {
+        return valid ? sell4_dot16<T>(sp, col, A, r, xf) : T(0);
+    } else if constexpr (K == 0) {
         return valid ? sell4_dot<T>(sp, col, A, r, xf) : T(0);
     } else if constexpr (K == 1) {
         return valid ? sell_dot<T>(sp, col, A, r, xf) : T(0);
@@ -626,8 +636,8 @@ __device__ __forceinline__ T row_dot(const int* __restrict__ sp, const int* __re
 // row dot already carries the 1/a_ii factor; the unscaled residual multiplies it back by a_ii.
 
 // start from y = t + w P xc (xc may be null: y = t): x = y, r = D^-1 (b - A y), d = r / theta
-template <class T, int K, class V, bool SCALED>
-__global__ void k_cheb_start(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class T, int K, class V, bool SCALED, class CI = int>
+__global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                              const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                              const T* __restrict__ b, const T* __restrict__ t, const T* __restrict__ xc,
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
@@ -670,8 +680,8 @@ __global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restric
 }
 
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
-template <class T, int K, class V, bool SCALED>
-__global__ void k_cheb_step(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class T, int K, class V, bool SCALED, class CI = int>
+__global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                             const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
                             T* x_out, T c1, T c2, int final_step, const int* stop)
@@ -731,16 +741,32 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned long lo
 }
 
 // Dynamic shared memory: 128 bytes for the warps' barriers, then BULK_SLICES column areas of cap
-// entries (4 B each), then BULK_SLICES value areas (2 B each).  cap and the slice offsets are
-// multiples of 128 entries, so every copy starts and ends on a 16-byte boundary.  extra_tx (0 in
-// solves) adds bytes the barrier waits for that no copy delivers: the self-test of the timeout path.
-template <class T>
+// entries (sizeof(CI) B each: 4 for columns, 2 for 16-bit column offsets), then BULK_SLICES value
+// areas (2 B each).  cap and the slice offsets are multiples of 128 entries, so every copy starts
+// and ends on a 16-byte boundary.  extra_tx (0 in solves) adds bytes the barrier waits for that no
+// copy delivers: the self-test of the timeout path.
+template <class CI>
+__device__ __forceinline__ int4 x4_columns(const CI* p, int row);
+template <>
+__device__ __forceinline__ int4 x4_columns<int>(const int* p, int)
+{
+    return *reinterpret_cast<const int4*>(p);
+}
+template <>
+__device__ __forceinline__ int4 x4_columns<short>(const short* p, int row)
+{
+    const short4 c = *reinterpret_cast<const short4*>(p);
+    return make_int4(row + c.x, row + c.y, row + c.z, row + c.w);
+}
+
+template <class T, class CI>
 __global__ void __launch_bounds__(BULK_SLICES * 32)
-    k_cheb_step_bulk(int n, int nslices, const int* __restrict__ sp4, const int* __restrict__ col4,
+    k_cheb_step_bulk(int n, int nslices, const int* __restrict__ sp4, const CI* __restrict__ col4,
                      const __half* __restrict__ a4, const T* x_in, const T* __restrict__ d_in, T* __restrict__ r,
                      T* __restrict__ d_out, T* x_out, T c1, T c2, int final_step, const int* stop, int cap,
                      int* status, unsigned extra_tx)
 {
+    constexpr unsigned CB = sizeof(CI);
     extern __shared__ __align__(128) unsigned char smem[];
     if (*stop) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -752,17 +778,17 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
         return;
     }
     const unsigned bar = smem_u32(smem + 8 * w);
-    int* scol = reinterpret_cast<int*>(smem + 128) + size_t(w) * cap;
-    __half* sval = reinterpret_cast<__half*>(smem + 128 + size_t(BULK_SLICES) * cap * 4) + size_t(w) * cap;
+    CI* scol = reinterpret_cast<CI*>(smem + 128) + size_t(w) * cap;
+    __half* sval = reinterpret_cast<__half*>(smem + 128 + size_t(BULK_SLICES) * cap * CB) + size_t(w) * cap;
     if (lane == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"(unsigned(ne) * 6u + extra_tx)
+                     "r"(unsigned(ne) * (CB + 2u) + extra_tx)
                      : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                          smem_u32(scol)),
-                     "l"(col4 + e0), "r"(unsigned(ne) * 4u), "r"(bar)
+                     "l"(col4 + e0), "r"(unsigned(ne) * CB), "r"(bar)
                      : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                          smem_u32(sval)),
@@ -778,11 +804,11 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
     const int i = s * 32 + lane;
     if (i >= n) return;  // padding rows of the last slice
     const int G = ne >> 7;
-    const int4* cp = reinterpret_cast<const int4*>(scol) + lane;
+    const CI* cp = scol + 4 * lane;
     const uint2* vp = reinterpret_cast<const uint2*>(sval) + lane;
     T acc = T(0);
     for (int g = 0; g < G; ++g) {
-        const int4 c = cp[32 * g];
+        const int4 c = x4_columns<CI>(cp + 128 * g, i);
         const uint2 h = vp[32 * g];
         const T x0 = d_in[c.x], x1 = d_in[c.y], x2 = d_in[c.z], x3 = d_in[c.w];
         const float2 v01 = __half22float2(*reinterpret_cast<const __half2*>(&h.x));
@@ -802,8 +828,8 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
     x_out[i] = xi;
 }
 
-template <class T, int K, class V, bool SCALED>
-__global__ void k_resid(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
+template <class T, int K, class V, bool SCALED, class CI = int>
+__global__ void k_resid(int n, const int* __restrict__ sp, const CI* __restrict__ col, const int* __restrict__ rowlen,
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
                         const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
@@ -848,12 +874,15 @@ __global__ void k_slice_groups(int nslices, const int* __restrict__ sp, int* __r
     if (s < nslices) groups[s] = ((((sp[s + 1] - sp[s]) >> 5) + 3) >> 2) * 128;
 }
 
-// the SELL-32x4 copy written straight from A (FP16 D^-1 A as k_scale_half), and the diagonal
-template <class T>
+// the SELL-32x4 copy written straight from A (FP16 D^-1 A as k_scale_half), and the diagonal.
+// CI = int stores the columns; CI = short stores col - row (padding 0), and the largest |col - row|
+// of the level goes to *maxoff: above 32767 the offsets do not fit and the int copy is written
+// instead (the padding rows of the last slice point at row 0 in the int copy, at themselves here).
+template <class T, class CI>
 __global__ void k_scale_half4(int n, int nslices, const int* __restrict__ sp, const int* __restrict__ col,
                               const int* __restrict__ diag, const T* __restrict__ A, const T* __restrict__ dinv,
-                              const int* __restrict__ sp4, int* __restrict__ col4, __half* __restrict__ ah4,
-                              T* __restrict__ diagv)
+                              const int* __restrict__ sp4, CI* __restrict__ col4, __half* __restrict__ ah4,
+                              T* __restrict__ diagv, int* __restrict__ maxoff)
 {
     const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= nslices) return;
@@ -862,18 +891,32 @@ __global__ void k_scale_half4(int n, int nslices, const int* __restrict__ sp, co
     const T di = row ? dinv[r] : T(0);
     const int b = sp[s], w = (sp[s + 1] - b) >> 5;
     const int b4 = sp4[s], g4 = (sp4[s + 1] - b4) >> 7;
+    int mo = 0;
     for (int t = 0; t < 4 * g4; ++t) {
         const int dst = b4 + 128 * (t >> 2) + 4 * lane + (t & 3);
         if (t < w) {
             const int k = b + 32 * t + lane;
-            col4[dst] = col[k];
+            const int c = col[k];
+            if constexpr (std::is_same<CI, short>::value) {
+                const int o = row ? c - r : 0;
+                mo = max(mo, abs(o));
+                col4[dst] = short(max(-32768, min(32767, o)));
+            } else {
+                col4[dst] = c;
+            }
             ah4[dst] = __float2half_rn(row ? float(A[k] * di) : 0.0f);
         } else {
-            col4[dst] = row ? r : 0;
+            if constexpr (std::is_same<CI, short>::value) col4[dst] = 0;
+            else col4[dst] = row ? r : 0;
             ah4[dst] = __float2half_rn(0.0f);
         }
     }
     if (row) diagv[r] = A[diag[r]];
+    if (maxoff) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mo = max(mo, __shfl_xor_sync(0xffffffffu, mo, o));
+        if (lane == 0 && mo > 0) atomicMax(maxoff, mo);
+    }
 }
 
 template <class T>
@@ -940,6 +983,39 @@ __global__ void k_dense_cholesky_inverse(int n, double* __restrict__ D, double* 
     }
 }
 
+// Inverse of the dense SPD matrix D (n <= DENSE_SMEM_N) by Gauss-Jordan elimination in shared
+// memory, one block: for SPD matrices the pivots are the diagonal (no pivoting, as LDL^T).  Three
+// barriers per pivot, all in shared memory; non-positive or non-finite pivots set ST_NONFINITE.
+constexpr int DENSE_SMEM_N = 160;   // 200 KB of doubles
+__global__ void __launch_bounds__(1024) k_dense_gauss_jordan(int n, const double* __restrict__ D,
+                                                             double* __restrict__ Dinv, int* status)
+{
+    extern __shared__ double A[];
+    const int nn = n * n;
+    for (int q = threadIdx.x; q < nn; q += blockDim.x) A[q] = D[q];
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        const double akk = A[k * n + k];
+        if (!(akk > 0.0) || !isfinite(akk)) {
+            if (threadIdx.x == 0) atomicOr(status, ST_NONFINITE);
+            return;   // uniform: every thread read the same pivot
+        }
+        const double piv = 1.0 / akk;
+        for (int j = threadIdx.x; j < n; j += blockDim.x)
+            if (j != k) A[k * n + j] *= piv;
+        __syncthreads();
+        for (int q = threadIdx.x; q < nn; q += blockDim.x) {
+            const int i = q / n, j = q - i * n;
+            if (i != k && j != k) A[q] -= A[i * n + k] * A[k * n + j];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            A[i * n + k] = (i == k) ? piv : -A[i * n + k] * piv;
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < nn; q += blockDim.x) Dinv[q] = A[q];
+}
+
 template <class T>
 __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
                               const int* stop)
@@ -971,11 +1047,23 @@ int read_int(cudaStream_t s, const int* d)
 // Lanes per row of a level.  Levels with many rows are bandwidth-bound and keep one thread per
 // row (consecutive threads on consecutive rows give fully coalesced SELL loads; more lanes only
 // add instructions).  Small levels (under 20k rows, 30-60 entries per row) are latency-bound:
-// one thread would walk its long row serially, so 3-6 entries per lane are used there.
+// one thread would walk its long row serially, so 3-6 entries per lane are used there.  Between
+// the two, levels of long rows under 64k rows, whose one-thread-per-row launch fills about one
+// 256-thread block per SM (on the 1M-cell system: 44k rows of 52 entries, 14.5 us per smoothing
+// step against 12.5 us with 8 lanes), double the lanes until the launch has about 2^18 threads,
+// keeping at least five entries per lane.  At 121k rows of 42 entries the one-thread-per-row
+// SELL-32x4 step was faster than 4 lanes (13.8 against 15.0 us).
+constexpr long long LANES_FILL_THREADS = 1LL << 18;
 int lanes_for(int n, long long nent)
 {
     const double avg = n > 0 ? double(nent) / n : 0.0;
-    if (n >= 20000 || avg <= 8.0) return 1;
+    if (avg <= 8.0) return 1;
+    if (n >= 65536) return 1;
+    if (n >= 20000) {
+        int k = 1;
+        while (k < 8 && (long long)n * k < LANES_FILL_THREADS && avg / (2 * k) >= 5.0) k *= 2;
+        return k;
+    }
     int k = 2;
     while (k < 16 && k * 6 < avg) k *= 2;
     return k;
@@ -1123,25 +1211,21 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
     PORSOL_REQUIRE(bound <= 2048, PORSOL_ERR_BAD_ARG, "AMG: aggregate rows too long for the Galerkin merge");
     const bool warp = bound <= 1024;
     if (warp) {
-        // one merge pass into a compact temporary, then the SELL layout
+        // candidates of every aggregate row into a compact temporary, merged there, then the SELL layout
         s_tcol_.alloc(std::max(total, 1));
         s_tval_.alloc(std::max(total, 1));
         s_dpos_.alloc(std::max(nc, 1));
-#define PORSOL_GALM(CAP)                                                                                            \
-    {                                                                                                               \
-        constexpr int LL = CAP / 4 < 8 ? 8 : (CAP / 4 > 32 ? 32 : CAP / 4);                                          \
-        const int nbw = div_up(nc, GW_WARPS * (32 / LL));                                                           \
-        PORSOL_LAUNCH((k_gal_merge<T, CAP, LL><<<nbw, GW_WARPS * 32, 0, s>>>(                                        \
-            nc, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, a.ptr.p, a.idx.p, s_goff_.p, s_tcol_.p, s_tval_.p,     \
-            Pc.rowlen.p, s_dpos_.p)));                                                                              \
-    }
-        if (bound <= 32) { PORSOL_GALM(32); }
-        else if (bound <= 64) { PORSOL_GALM(64); }
-        else if (bound <= 128) { PORSOL_GALM(128); }
-        else if (bound <= 256) { PORSOL_GALM(256); }
-        else if (bound <= 512) { PORSOL_GALM(512); }
-        else { PORSOL_GALM(1024); }
-#undef PORSOL_GALM
+        s_woff_.alloc(std::max(P.n, 1));
+        PORSOL_LAUNCH(k_gal_woff<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p, P.rowlen.p, s_goff_.p,
+                                                               s_woff_.p));
+        PORSOL_LAUNCH(k_gal_cand<T><<<div_up(P.n, TB), TB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, A,
+                                                                   a.agg.p, s_woff_.p, s_tcol_.p, s_tval_.p));
+        const int cap = std::max(32, (bound + 31) / 32 * 32);
+        const size_t shm = size_t(GD_WARPS) * ((32 + cap) * sizeof(double) + cap * sizeof(int));
+        if (shm > 48 * 1024)
+            PORSOL_CUDA(cudaFuncSetAttribute(k_gal_dedup<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+        PORSOL_LAUNCH(k_gal_dedup<T><<<div_up(nc, GD_WARPS), GD_WARPS * 32, shm, s>>>(
+            nc, cap, s_goff_.p, s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p, status_.p));
     } else {
         const int nb = div_up(nc, 64);
         PORSOL_COUNT_LAUNCH();
@@ -1186,6 +1270,7 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.v4 = L.half && o_.layout4 && !o_.autotune && lanes_for(n, L.P->nent) == 1 &&
            (long long)L.P->nent + 96LL * L.P->nslices < (1LL << 31) - 1;
     const SellPattern& P = *L.P;
+    L.c16 = false;
     if (L.v4) {
         L.sp4.alloc(size_t(P.nslices) + 1);
         s_width_.alloc(std::max(P.nslices, 1));
@@ -1193,11 +1278,15 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
         exclusive_scan(s, P.nslices, s_width_.p, L.sp4.p, L.sp4.p + P.nslices, scan_blocks_);
         // at most 3 padding entries per row: no host read of the exact size
         const size_t cap = size_t(P.nent) + 96 * size_t(P.nslices);
-        L.col4.alloc(cap);
         L.ah4.alloc(cap);
         L.diagv.alloc(n);
-        PORSOL_LAUNCH(k_scale_half4<T><<<div_up(P.nslices, TB / 32), TB, 0, s>>>(
-            n, P.nslices, P.slice_ptr.p, P.col.p, P.diag.p, L.A, L.dinv.p, L.sp4.p, L.col4.p, L.ah4.p, L.diagv.p));
+        // 16-bit column offsets first; setup() checks the level's largest offset with the other
+        // levels' bounds in one copy and rewrites the copy with 32-bit columns where it does not fit
+        L.off4.alloc(cap);
+        L.c16 = true;
+        PORSOL_LAUNCH(k_scale_half4<T, short><<<div_up(P.nslices, TB / 32), TB, 0, s>>>(
+            n, P.nslices, P.slice_ptr.p, P.col.p, P.diag.p, L.A, L.dinv.p, L.sp4.p, L.off4.p, L.ah4.p, L.diagv.p,
+            s_maxoff_.p + level));
         PORSOL_CUDA(cudaGetLastError());
     } else if (L.half) {
         L.ah.alloc(size_t(L.P->nent));
@@ -1297,7 +1386,14 @@ void Amg<T>::build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* 
     cinv_.alloc(std::max<size_t>((size_t)n * n, 1));
     if (n > 0) {
         PORSOL_LAUNCH(k_dense_from_sell<T><<<div_up(n, 128), 128, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, D.p));
-        PORSOL_LAUNCH(k_dense_cholesky_inverse<<<1, 1024, 0, s>>>(n, D.p, Linv.p, cinv_.p, status_.p));
+        if (n <= DENSE_SMEM_N) {
+            const int shm = n * n * int(sizeof(double));
+            PORSOL_CUDA(cudaFuncSetAttribute(k_dense_gauss_jordan, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             DENSE_SMEM_N * DENSE_SMEM_N * int(sizeof(double))));
+            PORSOL_LAUNCH(k_dense_gauss_jordan<<<1, 1024, shm, s>>>(n, D.p, cinv_.p, status_.p));
+        } else {
+            PORSOL_LAUNCH(k_dense_cholesky_inverse<<<1, 1024, 0, s>>>(n, D.p, Linv.p, cinv_.p, status_.p));
+        }
     }
     PORSOL_CUDA(cudaGetLastError());
     const int st = read_int(s, status_.p);
@@ -1329,6 +1425,8 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
     status_.zero(s);
     s_gmax_.alloc(size_t(std::max(o.max_levels, 1)));
     s_gmax_.zero(s);
+    s_maxoff_.alloc(size_t(std::max(o.max_levels, 1)));
+    s_maxoff_.zero(s);
     if (lv_.empty()) lv_.push_back(std::make_unique<Level>());
     nlev_ = 1;
     {
@@ -1382,16 +1480,30 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         ++nlev_;
         if (next.n > 0.9 * n) break;   // coarsening stalled
     }
-    // Chebyshev intervals of the smoothed levels (one copy for all levels)
+    // Chebyshev intervals of the smoothed levels and the x4 copies' largest column offsets (one
+    // copy each for all levels)
     {
         std::vector<unsigned long long> gb(size_t(nlev_), 0ULL);
+        std::vector<int> mo(size_t(nlev_), 0);
         PORSOL_CUDA(cudaMemcpyAsync(gb.data(), s_gmax_.p, sizeof(unsigned long long) * gb.size(),
                                     cudaMemcpyDeviceToHost, s));
+        PORSOL_CUDA(cudaMemcpyAsync(mo.data(), s_maxoff_.p, sizeof(int) * mo.size(), cudaMemcpyDeviceToHost, s));
         PORSOL_CUDA(cudaStreamSynchronize(s));
         for (int l = 0; l + 1 < nlev_; ++l) {
             double gm;
             std::memcpy(&gm, &gb[size_t(l)], sizeof(gm));
             lv_[l]->lmax = gm > 0 ? gm : 1.0;
+            Level& L = *lv_[l];
+            if (L.v4 && L.c16 && mo[size_t(l)] > 32767) {
+                // couplings too far from the diagonal for 16-bit offsets: 32-bit columns
+                const SellPattern& P = *L.P;
+                L.col4.alloc(size_t(P.nent) + 96 * size_t(P.nslices));
+                PORSOL_LAUNCH(k_scale_half4<T, int><<<div_up(P.nslices, TB / 32), TB, 0, s>>>(
+                    L.n, P.nslices, P.slice_ptr.p, P.col.p, P.diag.p, L.A, L.dinv.p, L.sp4.p, L.col4.p, L.ah4.p,
+                    L.diagv.p, nullptr));
+                PORSOL_CUDA(cudaGetLastError());
+                L.c16 = false;
+            }
         }
     }
     Level& C = *lv_[nlev_ - 1];
@@ -1428,10 +1540,18 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
         const int nbk = div_up(n * L.lanes, TB);
-        if (L.v4) {
-            // large levels: form y = t + w P xc first, so the start's row dot gathers one vector
-            // instead of t, agg and xc (the same y, the same sums)
-            if (xc) PORSOL_LAUNCH(k_prolong_add<T><<<nb, TB, 0, s>>>(n, t, xc, agg, T(o_.prolong), x, stop));
+        // levels smoothed one thread per row (the large ones): form y = t + w P xc first, so the
+        // start's row dot gathers one vector instead of t, agg and xc (the same y, the same sums)
+        if (xc && L.lanes == 1) {
+            PORSOL_LAUNCH(k_prolong_add<T><<<nb, TB, 0, s>>>(n, t, xc, agg, T(o_.prolong), x, stop));
+            t = x;
+            xc = nullptr;
+        }
+        if (L.v4 && L.c16) {
+            PORSOL_LAUNCH((k_cheb_start<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
+                n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p,
+                d, T(1.0 / theta), stop)));
+        } else if (L.v4) {
             PORSOL_LAUNCH((k_cheb_start<T, 0, __half, true><<<nb, TB, 0, s>>>(
                 n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p,
                 d, T(1.0 / theta), stop)));
@@ -1450,20 +1570,30 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         const double rho1 = 1.0 / (2.0 * sigma - rho);
         const double c1 = rho1 * rho, c2 = 2.0 * rho1 / delta;
         const T* xin = (from_zero && k == 1) ? nullptr : x;
-        // algorithmic bytes: matrix values + columns, d gathered once, dinv (unscaled form only),
-        // r and x in, r/d/x out
-        const double bytes = double(P.nent) * ((L.half ? 2 : sizeof(T)) + 4) +
+        // algorithmic bytes: matrix values + columns (16-bit offsets on c16 levels), d gathered
+        // once, dinv (unscaled form only), r and x in, r/d/x out
+        const double bytes = double(P.nent) * ((L.half ? 2 : sizeof(T)) + (L.v4 && L.c16 ? 2 : 4)) +
                              double(n) * sizeof(T) * ((xin ? 7 : 6) - (L.half ? 1 : 0));
         const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();  // finest level only
         cudaEvent_t ev = nullptr;
         if (prof_here) prof_->begin(s, PK_CHEB, bytes, &ev);
         const int nbk = div_up(n * L.lanes, TB);
-        if (L.bulk_groups > 0) {
+        if (L.bulk_groups > 0 && L.c16) {
+            const int cap = 128 * L.bulk_groups;   // entries per slice
+            const size_t shm = 128 + size_t(BULK_SLICES) * cap * 4;
+            PORSOL_LAUNCH((k_cheb_step_bulk<T, short><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
+                n, P.nslices, L.sp4.p, L.off4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
+                cap, status_.p, 0u)));
+        } else if (L.bulk_groups > 0) {
             const int cap = 128 * L.bulk_groups;   // entries per slice
             const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
-            PORSOL_LAUNCH((k_cheb_step_bulk<T><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
+            PORSOL_LAUNCH((k_cheb_step_bulk<T, int><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
                 n, P.nslices, L.sp4.p, L.col4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
                 cap, status_.p, 0u)));
+        } else if (L.v4 && L.c16) {
+            PORSOL_LAUNCH((k_cheb_step<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
+                n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
+                k == deg ? 1 : 0, stop)));
         } else if (L.v4) {
             PORSOL_LAUNCH((k_cheb_step<T, 0, __half, true><<<nb, TB, 0, s>>>(
                 n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
@@ -1501,7 +1631,10 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
     // restrict the residual
-    if (L.v4) {
+    if (L.v4 && L.c16) {
+        PORSOL_LAUNCH((k_resid<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
+            n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.diagv.p, b, L.t.p, L.r.p, stop)));
+    } else if (L.v4) {
         PORSOL_LAUNCH((k_resid<T, 0, __half, true><<<nb, TB, 0, s>>>(n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.diagv.p,
                                                                       b, L.t.p, L.r.p, stop)));
     } else if (L.half) {
@@ -1517,6 +1650,51 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     chebyshev(s, L, b, x, false, Nx.x.p, L.agg.agg.p, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, x, false, nullptr, nullptr, stop);
     PORSOL_CUDA(cudaGetLastError());
+}
+
+// Mirrors the launches of vcycle() and chebyshev(): the algorithmic bytes of each kernel (see the
+// declaration).
+template <class T>
+double Amg<T>::apply_bytes(std::vector<double>* per_level) const
+{
+    const double sx = sizeof(T);
+    if (per_level) per_level->assign(size_t(nlev_), 0.0);
+    double total = 0.0;
+    for (int l = 0; l < nlev_; ++l) {
+        double b = 0.0;
+        if (l == nlev_ - 1) {
+            b = double(nc_) * nc_ * 8.0 + 2.0 * nc_ * sx;   // dense inverse, b in, x out
+        } else {
+            const Level& L = *lv_[l];
+            const double n = L.n, nc = lv_[l + 1]->n;
+            const double vb = L.half ? 2.0 : sx, cb = (L.v4 && L.c16) ? 2.0 : 4.0;
+            const double mat = double(L.P->nent) * (vb + cb);
+            const int deg = std::max(1, o_.cheb_degree);
+            // Chebyshev steps of one application: the first from x = 0 after start0 has no x_in
+            auto steps = [&](bool from_zero) {
+                double t = 0.0;
+                for (int k = 1; k <= deg; ++k) {
+                    const bool xin = !(from_zero && k == 1);
+                    t += mat + n * sx * (5.0 + (xin ? 1.0 : 0.0) + (L.half ? 0.0 : 1.0));
+                }
+                return t;
+            };
+            const double start = mat + 5.0 * n * sx;           // t gathered, dinv, b in; r, d out
+            b += 4.0 * n * sx + steps(true);                    // pre-smoothing from zero
+            b += (o_.smooth_steps - 1) * (start + steps(false));
+            b += mat + n * sx * (L.half ? 4.0 : 3.0);            // residual
+            b += n * (sx + 4.0) + nc * (4.0 + sx);               // restriction
+            if (L.lanes == 1)                                    // post-smoothing from t + w P xc
+                b += n * (2.0 * sx + 4.0) + nc * sx + start;
+            else
+                b += start + n * (sx + 4.0) + nc * sx;
+            b += steps(false);
+            b += (o_.smooth_steps - 1) * (start + steps(false));
+        }
+        if (per_level) (*per_level)[size_t(l)] = b;
+        total += b;
+    }
+    return total;
 }
 
 template <class T>
@@ -1568,7 +1746,7 @@ int bulk_step_selftest(bool expire, float* r_host, float* d_host, float* x_host)
     dstat.alloc(1);
     dstat.zero(s);
     const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
-    PORSOL_LAUNCH((k_cheb_step_bulk<float><<<1, BULK_SLICES * 32, shm, s>>>(
+    PORSOL_LAUNCH((k_cheb_step_bulk<float, int><<<1, BULK_SLICES * 32, shm, s>>>(
         n, ns, dsp.p, dcol.p, da.p, nullptr, dd.p, dr.p, ddn.p, dx.p, 0.5f, 0.25f, 1, dstop.p, cap, dstat.p,
         expire ? 16u : 0u)));
     PORSOL_CUDA(cudaGetLastError());

@@ -529,6 +529,38 @@ void launch_gather_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs
     PORSOL_CUDA(cudaGetLastError());
 }
 
+__global__ void k_permute(int n, const int* __restrict__ perm, const double* __restrict__ x, double* __restrict__ y,
+                          int gather)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    if (gather) y[r] = x[perm[r]];
+    else y[perm[r]] = x[r];
+}
+
+__global__ void k_gather_values(long long nent, const int* __restrict__ src, const double* __restrict__ val,
+                                double* __restrict__ out)
+{
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= nent) return;
+    const int j = src[k];
+    out[k] = j >= 0 ? val[j] : 0.0;
+}
+
+void launch_permute(cudaStream_t s, int n, const int* perm, const double* x, double* y, bool gather)
+{
+    if (n <= 0) return;
+    PORSOL_LAUNCH(k_permute<<<div_up(n, 256), 256, 0, s>>>(n, perm, x, y, gather ? 1 : 0));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_gather_values(cudaStream_t s, long long nent, const int* src, const double* val, double* val_ref)
+{
+    if (nent <= 0) return;
+    PORSOL_LAUNCH(k_gather_values<<<div_up(nent, 256), 256, 0, s>>>(nent, src, val, val_ref));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
 void launch_scale_entry(cudaStream_t s, double* val, const int* diag, int row, double factor, float* val32)
 {
     PORSOL_LAUNCH(k_scale_entry<<<1, 1, 0, s>>>(val, diag, row, factor, val32));

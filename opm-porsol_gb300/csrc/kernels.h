@@ -61,6 +61,11 @@ void launch_gather_slots(cudaStream_t s, long long nent, const int* slot_ptr, co
 void launch_gather_rhs(cudaStream_t s, int n, const int* rhs_ptr, const int* rhs_ent, const double* rrow,
                        const double* pb, double* rhs);
 void launch_scale_entry(cudaStream_t s, double* val, const int* diag, int row, double factor, float* val32);
+// Between the internal and the reference numbering of the face unknowns (perm[reference] =
+// internal): y[r] = x[perm[r]] (gather = true) or y[perm[r]] = x[r] (gather = false), r < n.
+void launch_permute(cudaStream_t s, int n, const int* perm, const double* x, double* y, bool gather);
+// val_ref[k] = src[k] >= 0 ? val[src[k]] : 0 for k < nent (the system in the reference numbering)
+void launch_gather_values(cudaStream_t s, long long nent, const int* src, const double* val, double* val_ref);
 
 struct RecoverArgs {
     int nc;

@@ -115,4 +115,31 @@ __device__ __forceinline__ Acc sell4_dot(const int* __restrict__ sp4, const int*
     return acc;
 }
 
+// The same row dot product on the SELL-32x4 layout with 16-bit column offsets: entry t of row r
+// stores col - r as a signed 16-bit value (levels whose couplings all lie within 32767 rows of the
+// diagonal, which the internal face numbering gives the finest levels), so a group's four columns
+// come in one 8-byte load.  Same sum, in the same order, as sell4_dot.
+template <class Acc, class XF>
+__device__ __forceinline__ Acc sell4_dot16(const int* __restrict__ sp4, const short* __restrict__ off4,
+                                           const __half* __restrict__ a4, int r, XF xf)
+{
+    const int s = r >> 5, lane = r & 31;
+    const int b = sp4[s], G = (sp4[s + 1] - b) >> 7;
+    const short4* cp = reinterpret_cast<const short4*>(off4 + b) + lane;
+    const uint2* vp = reinterpret_cast<const uint2*>(a4 + b) + lane;
+    Acc acc = Acc(0);
+    for (int g = 0; g < G; ++g) {
+        const short4 c = __ldg(cp + 32 * g);
+        const uint2 h = __ldg(vp + 32 * g);
+        const Acc x0 = Acc(xf(r + c.x)), x1 = Acc(xf(r + c.y)), x2 = Acc(xf(r + c.z)), x3 = Acc(xf(r + c.w));
+        const float2 v01 = __half22float2(*reinterpret_cast<const __half2*>(&h.x));
+        const float2 v23 = __half22float2(*reinterpret_cast<const __half2*>(&h.y));
+        acc += Acc(v01.x) * x0;
+        acc += Acc(v01.y) * x1;
+        acc += Acc(v23.x) * x2;
+        acc += Acc(v23.y) * x3;
+    }
+    return acc;
+}
+
 }  // namespace porsol

@@ -59,6 +59,11 @@ struct porsol_solver {
     bool amg_ready = false;
     int amg_precision = -1;
     porsol::DBuf<double> ir_r;   // batched residual
+    // the reference numbering's system for the ILU0 path of a renumbered structure:
+    // dof permutation, slot sources, values, right-hand side and solution
+    porsol::DBuf<int> dof_perm_d, ref_slot_src_d;
+    porsol::DBuf<double> val_ref, rhs_ref, x_ref, pi_ref;
+    void ilu_solve_reference_order(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit);
     porsol::RedScratch red;
 
     porsol::Profiler prof;
@@ -78,6 +83,12 @@ struct porsol_solver {
 
     // adjoint (permeability sensitivity) of the last solve
     porsol_solve_opts last_opts{};
+    // algorithmic bytes of the last solve: assembly, linear solve (every CG iteration with its
+    // preconditioner application, residual replacements, start), recovery, postProcessFluxes;
+    // one V-cycle per level (AMG solves)
+    double bytes_asm = 0, bytes_krylov = 0, bytes_rec = 0, bytes_post = 0;
+    std::vector<double> vcycle_level_bytes;
+    void count_krylov_bytes(const porsol_solve_opts& o, int iterations, int replacements);
     porsol::DBuf<double> adj_wp, adj_pstar, adj_wv, adj_y, adj_jc, adj_rhs, adj_x, adj_grad, adj_sum;
 
     void require_structure() const;

@@ -19,6 +19,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <cstdlib>
 #include <exception>
 #include <mutex>
 #include <numeric>
@@ -115,6 +117,143 @@ void parallel_exclusive_scan(long long n, F&& cnt, Out* out)
         }
     });
     out[n] = part[T];
+}
+
+// Lattice indices of the cell centroids along one axis: the sorted distinct coordinates (values
+// within 1e-9 of the axis extent merge) and each cell's position among them.
+int lattice_axis(const double* cent, int nc, int a, std::vector<int>& idx)
+{
+    std::vector<double> v(nc);
+    double lo = 1e300, hi = -1e300;
+    for (int c = 0; c < nc; ++c) {
+        v[c] = cent[3 * size_t(c) + a];
+        lo = std::min(lo, v[c]);
+        hi = std::max(hi, v[c]);
+    }
+    if (!(hi >= lo)) return -1;   // non-finite coordinates
+    const double tol = 1e-9 * std::max(hi - lo, 1e-300);
+    std::vector<double> u(v);
+    std::sort(u.begin(), u.end());
+    std::vector<double> w;
+    for (double x : u)
+        if (w.empty() || x - w.back() > tol) w.push_back(x);
+    idx.resize(nc);
+    for (int c = 0; c < nc; ++c) {
+        auto it = std::lower_bound(w.begin(), w.end(), v[c] - tol);
+        if (it == w.end() || std::fabs(*it - v[c]) > tol) return -1;
+        idx[c] = int(it - w.begin());
+    }
+    return int(w.size());
+}
+
+// Reverse Cuthill-McKee order of the cell graph (cells adjacent through internal faces): per
+// connected component a breadth-first search from a pseudo-peripheral cell, neighbours taken in
+// order of increasing degree, the whole sequence reversed.
+std::vector<int> rcm_order(const HostGrid& g)
+{
+    const int nc = g.nc;
+    std::vector<int> deg(nc, 0);
+    for (int c = 0; c < nc; ++c)
+        for (int hf = g.facepos[c]; hf < g.facepos[c + 1]; ++hf) deg[c] += g.nb[hf] >= 0 ? 1 : 0;
+    std::vector<int> stamp(nc, -1), level(nc, 0), queue;
+    queue.reserve(nc);
+    int run = 0;
+    // breadth-first levels from r (stamp marks this run); returns the last level's cells
+    auto bfs = [&](int r, std::vector<int>& last) {
+        ++run;
+        queue.clear();
+        queue.push_back(r);
+        stamp[r] = run;
+        level[r] = 0;
+        int maxl = 0;
+        for (size_t h = 0; h < queue.size(); ++h) {
+            const int u = queue[h];
+            maxl = std::max(maxl, level[u]);
+            for (int hf = g.facepos[u]; hf < g.facepos[u + 1]; ++hf) {
+                const int v = g.nb[hf];
+                if (v >= 0 && stamp[v] != run) {
+                    stamp[v] = run;
+                    level[v] = level[u] + 1;
+                    queue.push_back(v);
+                }
+            }
+        }
+        last.clear();
+        for (int u : queue)
+            if (level[u] == maxl) last.push_back(u);
+        return maxl;
+    };
+    std::vector<char> placed(nc, 0);
+    std::vector<int> order;
+    order.reserve(nc);
+    std::vector<int> last, nbrs;
+    for (int seed = 0; seed < nc; ++seed) {
+        if (placed[seed]) continue;
+        // pseudo-peripheral start: repeat "farthest cell of least degree" while the eccentricity grows
+        int r = seed;
+        int ecc = bfs(r, last);
+        for (int it = 0; it < 8; ++it) {
+            int best = last[0];
+            for (int u : last)
+                if (deg[u] < deg[best] || (deg[u] == deg[best] && u < best)) best = u;
+            std::vector<int> last2;
+            const int e2 = bfs(best, last2);
+            if (e2 <= ecc) break;
+            r = best;
+            ecc = e2;
+            last.swap(last2);
+        }
+        const size_t first = order.size();
+        order.push_back(r);
+        placed[r] = 1;
+        for (size_t h = first; h < order.size(); ++h) {
+            const int u = order[h];
+            nbrs.clear();
+            for (int hf = g.facepos[u]; hf < g.facepos[u + 1]; ++hf) {
+                const int v = g.nb[hf];
+                if (v >= 0 && !placed[v]) {
+                    placed[v] = 1;
+                    nbrs.push_back(v);
+                }
+            }
+            std::sort(nbrs.begin(), nbrs.end(),
+                      [&](int a, int b) { return deg[a] != deg[b] ? deg[a] < deg[b] : a < b; });
+            order.insert(order.end(), nbrs.begin(), nbrs.end());
+        }
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+// Visiting order of the cells for the internal face numbering.  Cells whose centroids form a
+// Cartesian lattice (nx x ny x nz distinct coordinates, one cell per node) are taken in lattice
+// order with the axis of fewest cells fastest and the axis of most cells slowest, which gives the
+// smallest bandwidth of the orders along the axes (n_fast * n_mid cells); other grids in reverse
+// Cuthill-McKee order.
+std::vector<int> cell_order(const porsol_grid* grid, const HostGrid& g)
+{
+    const int nc = g.nc;
+    std::vector<int> idx[3];
+    int n[3] = {-1, -1, -1};
+    bool lattice = grid->cell_centroid != nullptr;
+    for (int a = 0; a < 3 && lattice; ++a) {
+        n[a] = lattice_axis(grid->cell_centroid, nc, a, idx[a]);
+        lattice = n[a] > 0;
+    }
+    if (lattice && (long long)n[0] * n[1] * n[2] == nc) {
+        int ax[3] = {0, 1, 2};   // slowest .. fastest
+        std::stable_sort(ax, ax + 3, [&](int a, int b) { return n[a] > n[b]; });
+        std::vector<int> order(nc, -1);
+        bool ok = true;
+        for (int c = 0; c < nc && ok; ++c) {
+            const long long key =
+                (long long)idx[ax[2]][c] + (long long)n[ax[2]] * (idx[ax[1]][c] + (long long)n[ax[1]] * idx[ax[0]][c]);
+            if (order[key] >= 0) ok = false;
+            else order[key] = c;
+        }
+        if (ok) return order;
+    }
+    return rcm_order(g);
 }
 
 }  // namespace
@@ -343,7 +482,77 @@ void Structure::build(const porsol_grid* grid, const int* flow_type, const int* 
         std::copy(b, b + ulen[i], colind.begin() + rowptr[i]);
     });
     HVec<int>().swap(cand);
-    build_sell(N, rowptr, colind, pat, &csr2sell);
+
+    // ---- internal numbering (not with periodic faces: their couplings span the grid in any order)
+    dof_perm.clear();
+    dof_iperm.clear();
+    cf_int.clear();
+    ref_pattern_built = false;
+    auto csr_bandwidth = [&](const int* perm) {
+        std::vector<int> part(host_threads(), 0);
+        parallel_chunks(N, [&](long long b, long long e, int t) {
+            int m = 0;
+            for (long long i = b; i < e; ++i) {
+                const int pi = perm ? perm[i] : int(i);
+                for (long long k = rowptr[i]; k < rowptr[i + 1]; ++k)
+                    m = std::max(m, std::abs((perm ? perm[colind[k]] : colind[k]) - pi));
+            }
+            part[t] = std::max(part[t], m);
+        });
+        return *std::max_element(part.begin(), part.end());
+    };
+    bandwidth_ref = csr_bandwidth(nullptr);
+    bandwidth = bandwidth_ref;
+    if (per_hf.empty() && nc > 1) {
+        const std::vector<int> order = cell_order(grid, g);
+        std::vector<int> perm(N, -1);
+        int next = 0;
+        for (int c : order)
+            for (int hf = g.facepos[c]; hf < g.facepos[c + 1]; ++hf)
+                if (perm[cf[hf]] < 0) perm[cf[hf]] = next++;
+        if (next == N) {
+            const int bw = csr_bandwidth(perm.data());
+            if (bw < bandwidth_ref) {
+                bandwidth = bw;
+                dof_perm.swap(perm);
+            }
+        }
+    }
+    if (dof_perm.empty()) {
+        build_sell(N, rowptr, colind, pat, &csr2sell);
+    } else {
+        dof_iperm.assign(N, 0);
+        for (int i = 0; i < N; ++i) dof_iperm[dof_perm[i]] = i;
+        cf_int.resize(nhf);
+        parallel_for(nhf, [&](long long hf) { cf_int[hf] = dof_perm[cf[hf]]; });
+        // the system's rows in the internal order, columns renumbered and sorted; src = CSR entry
+        HVec<int> rp(size_t(N) + 1), ci(colind.size()), src(colind.size());
+        parallel_exclusive_scan(N, [&](long long r) { return rowptr[dof_iperm[r] + 1] - rowptr[dof_iperm[r]]; },
+                                rp.data());
+        parallel_for(N, [&](long long r) {
+            const int i = dof_iperm[r];
+            const long long b = rowptr[i], len = rowptr[i + 1] - b, o = rp[r];
+            for (long long q = 0; q < len; ++q) {
+                ci[o + q] = dof_perm[colind[b + q]];
+                src[o + q] = int(b + q);
+            }
+            for (long long q = 1; q < len; ++q) {   // insertion sort by column (rows are short)
+                const int kc = ci[o + q], ks = src[o + q];
+                long long p = q - 1;
+                while (p >= 0 && ci[o + p] > kc) {
+                    ci[o + p + 1] = ci[o + p];
+                    src[o + p + 1] = src[o + p];
+                    --p;
+                }
+                ci[o + p + 1] = kc;
+                src[o + p + 1] = ks;
+            }
+        });
+        HVec<int> c2s;
+        build_sell(N, rp, ci, pat, &c2s);
+        csr2sell.resize(colind.size());
+        parallel_for((long long)colind.size(), [&](long long k) { csr2sell[src[k]] = c2s[k]; });
+    }
 
     // ---- postProcessFluxes pairs (:754-807): twin half-faces of every internal face and
     // the half-faces of periodic partners, ordered by visit order (half-face index)
@@ -387,6 +596,17 @@ void Structure::build(const porsol_grid* grid, const int* flow_type, const int* 
             }
         }
     }
+}
+
+void Structure::build_ref_pattern()
+{
+    if (ref_pattern_built || !renumbered()) return;
+    HVec<int> c2s;
+    build_sell(N, rowptr, colind, pat_ref, &c2s);
+    ref_slot_src.resize(size_t(pat_ref.nent));
+    parallel_for(pat_ref.nent, [&](long long k) { ref_slot_src[k] = -1; });
+    parallel_for((long long)c2s.size(), [&](long long k) { ref_slot_src[c2s[k]] = int(csr2sell[k]); });
+    ref_pattern_built = true;
 }
 
 void build_sell(int n, const HVec<int>& rowptr, const HVec<int>& col, SellPattern& P, HVec<int>* csr2sell)
@@ -528,9 +748,10 @@ void Recipe::build(const Structure& S, const int* flow_type, int npk)
     HVec<int> scount, rcount;
     parallel_fill(scount, size_t(nent), 0);
     parallel_fill(rcount, size_t(N), 0);
+    // right-hand-side rows in the internal numbering (matrix slots already are: S.slot)
     parallel_for(nc, [&](long long c) {
         visit_cell(int(c), [&](long long k, int, int) { atomic_inc(&scount[k]); },
-                   [&](int i, int, int) { atomic_inc(&rcount[i]); });
+                   [&](int i, int, int) { atomic_inc(&rcount[S.dof(i)]); });
     }, 1 << 12);
     h_slot_ptr.resize(size_t(nent) + 1);
     parallel_exclusive_scan(nent, [&](long long k) { return scount[k]; }, h_slot_ptr.data());
@@ -546,7 +767,10 @@ void Recipe::build(const Structure& S, const int* flow_type, int npk)
     parallel_for(nc, [&](long long c) {
         visit_cell(
             int(c), [&](long long k, int e, int) { h_slot_ent[h_slot_ptr[k] + atomic_inc(&scount[k])] = e; },
-            [&](int i, int e, int) { h_rhs_ent[h_rhs_ptr[i] + atomic_inc(&rcount[i])] = e; });
+            [&](int i, int e, int) {
+                const int r = S.dof(i);
+                h_rhs_ent[h_rhs_ptr[r] + atomic_inc(&rcount[r])] = e;
+            });
     }, 1 << 12);
     // stable insertion sort by cell (lists hold a few entries)
     auto order = [](HVec<int>& ent, long long b, long long e, auto&& cell) {

@@ -42,10 +42,31 @@ struct Structure {
     std::vector<int> pairs;                 // post-process pairs (hf_first, hf_second) flattened
     std::vector<int> boundary_hf;           // all boundary half-faces in order
 
+    // Internal numbering of the face unknowns.  Everything above (cf, rowptr/colind, ppartner,
+    // the recipe's semantics) is in the reference's numbering; the device system (pat, the
+    // assembly targets, every N-vector) uses the internal one, dof_perm[reference dof] = internal
+    // dof (empty: the two coincide).  The internal numbering visits the cells in an order of small
+    // bandwidth and numbers each cell's faces when the cell is first reached, so the couplings of a
+    // row lie close to it (|i - j| <= bandwidth) and rows next to each other gather neighbouring
+    // entries.
+    std::vector<int> dof_perm, dof_iperm;   // reference -> internal, internal -> reference
+    std::vector<int> cf_int;                // half-face -> internal dof
+    int bandwidth = 0;                      // max |i - j| over the couplings, internal numbering
+    int bandwidth_ref = 0;                  // the same in the reference numbering
+    // The system in the reference numbering, for the ILU0 path (its factorisation depends on the
+    // ordering): SELL pattern and, per slot of it, the internal slot (-1 for padding); built on
+    // first use.
+    SellPattern pat_ref;
+    HVec<int> ref_slot_src;
+    bool ref_pattern_built = false;
+
     void build(const porsol_grid* grid, const int* flow_type, const int* partner_bid);
     int partner_dof(int hf) const;
     int partner_cell(int hf) const;
-    long long slot(int i, int j) const;     // SELL slot of (i, j); throws if absent
+    long long slot(int i, int j) const;     // SELL slot of (i, j) (reference dofs); throws if absent
+    int dof(int i) const { return dof_perm.empty() ? i : dof_perm[i]; }   // reference -> internal
+    bool renumbered() const { return !dof_perm.empty(); }
+    void build_ref_pattern();               // pat_ref and ref_slot_src (renumbered systems only)
 };
 
 // The assembly recipe: which local Schur entries are summed into which SELL slot and

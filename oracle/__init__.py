@@ -134,6 +134,8 @@ def lib():
         L.orc_solve.argtypes = [vp, dp, dp, ip, dp, dp, d, i, i, ip, dp]
         L.orc_solve_timed.restype = i
         L.orc_solve_timed.argtypes = [vp, dp, dp, ip, dp, dp, d, i, i, ip, dp, dp]
+        L.orc_solve_milestone.restype = i
+        L.orc_solve_milestone.argtypes = [vp, dp, dp, ip, dp, dp, d, i, i, ip, dp, dp, d, ip, dp]
         L.orc_get_solution.argtypes = [vp, dp, dp, dp]
         L.orc_post_process_fluxes.restype = d
         L.orc_post_process_fluxes.argtypes = [vp]
@@ -268,6 +270,22 @@ class OraclePressure:
         self.iterations = int(it[0])
         self.reduction = float(red[0])
         return rc, float(sec[0]), float(sec[1]), float(sec[2])
+
+    def solve_milestone(self, totmob, mobdens, bc_type, bc_value, src, tol, milestone_tol, maxit=0,
+                        dirichlet_guess=False):
+        """As solve_timed(); also (iteration, CG seconds) at which the residual reduction first fell
+        below milestone_tol.  Returns (rc, t_fixed, t_factor, t_cg, milestone_iteration, milestone_seconds)."""
+        args = [_f64(totmob), _f64(mobdens), _i32(bc_type), _f64(bc_value), _f64(src)]
+        it = np.zeros(1, np.int32)
+        red = np.zeros(1)
+        sec = np.zeros(3)
+        mit = np.zeros(1, np.int32)
+        msec = np.zeros(1)
+        rc = lib().orc_solve_milestone(self.h, *[_p(a) for a in args], float(tol), int(maxit), int(dirichlet_guess),
+                                       _p(it), _p(red), _p(sec), float(milestone_tol), _p(mit), _p(msec))
+        self.iterations = int(it[0])
+        self.reduction = float(red[0])
+        return rc, float(sec[0]), float(sec[1]), float(sec[2]), int(mit[0]), float(msec[0])
 
     def solution(self):
         p = np.empty(self.g.num_cells)

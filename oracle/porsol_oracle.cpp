@@ -187,12 +187,22 @@ double dot(int n, const double* a, const double* b)
     return s;
 }
 
+// Optional record of when a CG run first reaches a looser residual reduction than its stopping
+// tolerance (iteration and seconds since the CG started), so one solve to a tight tolerance also
+// times the solve to the looser one.
+struct Milestone {
+    double tol = 0.0;
+    int iteration = -1;
+    double seconds = 0.0;
+};
+
 // Preconditioned CG as dune-istl's CGSolver::apply: x is the initial guess, b is
 // overwritten by the defect; stop when ||b - A x||_2 < tol * ||b - A x0||_2 or < 1e-30.
 // Returns true when converged.
 bool pcg(const Csr& A, const Ilu0& M, std::vector<double>& x, std::vector<double> b,
-         double tol, int maxit, int* iters, double* reduction)
+         double tol, int maxit, int* iters, double* reduction, Milestone* ms = nullptr)
 {
+    const auto t_start = std::chrono::steady_clock::now();
     const int n = A.n;
     std::vector<double> p(n), q(n);
     spmv(A, x.data(), q.data());
@@ -215,6 +225,10 @@ bool pcg(const Csr& A, const Ilu0& M, std::vector<double>& x, std::vector<double
         for (int k = 0; k < n; ++k) x[k] += lambda * p[k];
         for (int k = 0; k < n; ++k) b[k] -= lambda * q[k];
         def = std::sqrt(dot(n, b.data(), b.data()));
+        if (ms && ms->iteration < 0 && def < def0 * ms->tol) {
+            ms->iteration = i;
+            ms->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        }
         if (def < def0 * tol || def < 1e-30) {
             converged = true;
             break;
@@ -612,7 +626,7 @@ struct Pressure {
 
     // solveLinearSystem / solveLinearSystemAMG (the Krylov part), :1387-1420, :1481-1541
     double t_factor = 0.0;
-    int solve(double tol, int maxit, int dirichlet_guess, int* iters, double* red)
+    int solve(double tol, int maxit, int dirichlet_guess, int* iters, double* red, Milestone* ms = nullptr)
     {
         if (do_reg) S.at(0, 0) *= 2;
         const auto tf0 = std::chrono::steady_clock::now();
@@ -627,7 +641,7 @@ struct Pressure {
                 if (isD) soln[i] = rhs[i] / S.get(i, i);
             }
         }
-        const bool ok = pcg(S, M, soln, rhs, tol, maxit > 0 ? maxit : S.n, iters, red);
+        const bool ok = pcg(S, M, soln, rhs, tol, maxit > 0 ? maxit : S.n, iters, red, ms);
         return ok ? 0 : 1;
     }
 
@@ -1379,7 +1393,18 @@ int orc_solve_timed(void* h, const double* totmob, const double* mobdens, const 
                     const double* src, double tol, int maxit, int dirichlet_guess, int* iterations,
                     double* reduction, double* seconds3)
 {
+    return orc_solve_milestone(h, totmob, mobdens, bct, bcv, src, tol, maxit, dirichlet_guess, iterations, reduction,
+                               seconds3, 0.0, nullptr, nullptr);
+}
+
+int orc_solve_milestone(void* h, const double* totmob, const double* mobdens, const int* bct, const double* bcv,
+                        const double* src, double tol, int maxit, int dirichlet_guess, int* iterations,
+                        double* reduction, double* seconds3, double milestone_tol, int* milestone_iteration,
+                        double* milestone_seconds)
+{
     using clk = std::chrono::steady_clock;
+    Milestone ms;
+    ms.tol = milestone_tol;
     Pressure* P = static_cast<Pressure*>(h);
     const auto t0 = clk::now();
     P->useStatic();
@@ -1387,8 +1412,10 @@ int orc_solve_timed(void* h, const double* totmob, const double* mobdens, const 
     const auto t1 = clk::now();
     int it = 0;
     double red = 0.0;
-    const int rc = P->solve(tol, maxit, dirichlet_guess, &it, &red);
+    const int rc = P->solve(tol, maxit, dirichlet_guess, &it, &red, milestone_tol > 0.0 ? &ms : nullptr);
     const auto t2 = clk::now();
+    if (milestone_iteration) *milestone_iteration = ms.iteration;
+    if (milestone_seconds) *milestone_seconds = ms.seconds;
     if (iterations) *iterations = it;
     if (reduction) *reduction = red;
     P->recover();

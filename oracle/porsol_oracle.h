@@ -69,6 +69,12 @@ int   orc_solve_timed(void* h, const double* totmob, const double* mobdens,
                       const int* hf_flow_type, const double* hf_flow_value, const double* src,
                       double tol, int maxit, int dirichlet_guess, int* iterations, double* reduction,
                       double* seconds3);
+/* As orc_solve_timed; also the CG iteration and the seconds since the CG started at which the
+ * residual reduction first fell below milestone_tol (-1 and 0 if it never did). */
+int   orc_solve_milestone(void* h, const double* totmob, const double* mobdens,
+                          const int* bct, const double* bcv, const double* src, double tol, int maxit,
+                          int dirichlet_guess, int* iterations, double* reduction, double* seconds3,
+                          double milestone_tol, int* milestone_iteration, double* milestone_seconds);
 void  orc_get_solution(void* h, double* pressure, double* outflux, double* facepressure);
 double orc_post_process_fluxes(void* h);
 /* Solve with the tensor-mobility inner product of MimeticIPAnisoRelpermEvaluator: lam = total
