@@ -546,6 +546,7 @@ def run_impes(args):
     out = {"metric": "IMPES steps/s @1M cells (pressure + explicit upstream transport)", "unit": "IMPES steps/s",
            "config": {"workload": "200x200x25 layered log-normal, Corey-2 viscosity ratio 10, water through x-",
                       "dims": list(dims), "steps": args.impes, "pv_injected": 0.1}}
+    sats = {}
     for name, prec, tol in (("mixed", pkg.MIXED, args.tol), ("fp64", pkg.FP64, args.tol64)):
         s = pkg.PressureSolver()
         s.init(g, prob.perm.ravel(), (0.0, 0.0, 0.0), prob.bc_type)
@@ -576,6 +577,7 @@ def run_impes(args):
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         sat = d_sat.cpu().numpy()
+        sats[name] = sat
         out[name] = {"value": round(args.impes / el, 3), "seconds": round(el, 3), "cg_iterations": iters,
                      "transport_substeps": substeps, "water_pv": round(float((sat * prob.poro * g.volume).sum()) / pv, 6),
                      "sat_min": float(sat.min()), "sat_max": float(sat.max())}
@@ -583,6 +585,10 @@ def run_impes(args):
         T.close()
     out["value"] = out["mixed"]["value"]
     out["speedup_mixed_vs_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    dsat = sats["mixed"] - sats["fp64"]
+    out["sat_diff_mixed_vs_fp64"] = {"max_abs": float(np.abs(dsat).max()),
+                                     "l2_rel": float(np.linalg.norm(dsat) / np.linalg.norm(sats["fp64"])),
+                                     "after_steps": args.impes}
     print(json.dumps(out), flush=True)
 
 

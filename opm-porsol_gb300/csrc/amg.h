@@ -122,6 +122,7 @@ private:
     DBuf<double> s_D_, s_Linv_;
     DBuf<float> s_rs_;
     DBuf<int> s_state_, s_partner_, s_join_, s_best_, s_flag_, s_cidx_, s_cnt_, s_pos_, s_width_;
+    DBuf<int> s_wl_[2], s_wlcnt_;   // matching worklists (the free rows of a sweep) and their lengths
     DBuf<unsigned long long> s_gmax_;
     DBuf<int> s_bnd_, s_goff_, s_tcol_, s_dpos_, s_woff_;   // Galerkin temporaries
     DBuf<T> s_tval_;

@@ -263,16 +263,18 @@ double now_ms()
 // Algorithmic bytes of the linear solve just finished (values + columns of each stored entry read
 // once per matrix pass, each vector read or written once per kernel; s_v / s_x the value and
 // vector widths):
-//   FP64 AMG-CG:  per iteration SpMV + p.q  Z(8+4) + 16N, update x, r  48N, z.r  16N,
-//                 direction 24N, V-cycle; start: residual Z 12 + 24N, V-cycle, z.r, direction
-//   mixed:        per iteration FP32 SpMV + p.q  Z(4+4) + 8N, update (x FP64)  32N, z.r  8N,
-//                 direction 12N, FP32 V-cycle; per FP64 residual replacement Z 12 + 24N and the
+//   FP64 AMG-CG:  per iteration SpMV + p.q  Z(8+c) + 16N, update x, r  48N, z.r  16N,
+//                 direction 24N, V-cycle; start: residual Z (8+c) + 24N, V-cycle, z.r, direction
+//   mixed:        per iteration FP32 SpMV + p.q  Z(4+c) + 8N, update (x FP64)  32N, z.r  8N,
+//                 direction 12N, FP32 V-cycle; per FP64 residual replacement Z (8+c) + 24N and the
 //                 rescale 20N; start: FP64 residual, rescale, V-cycle, z.r, direction
 //   ILU0-CG:      per iteration 2 Z (8+4) + 8 (N+1) + 19 N 8 (SpMV, both triangular sweeps, two
 //                 dots, three vector updates)
+// with c = 2 bytes of column index where the system's 16-bit offsets are in use, else 4.
 void porsol_solver::count_krylov_bytes(const porsol_solve_opts& o, int iterations, int replacements)
 {
     const double Z = double(S.pat.nent), N = double(S.N), it = iterations;
+    const double c = S.pat.has_off16() ? 2.0 : 4.0;
     vcycle_level_bytes.clear();
     if (o.linsolver_type == 0) {
         bytes_krylov = (it + 1) * (2.0 * Z * 12.0 + 8.0 * (N + 1) + 19.0 * N * 8.0);
@@ -280,13 +282,13 @@ void porsol_solver::count_krylov_bytes(const porsol_solve_opts& o, int iteration
     }
     if (o.precision == PORSOL_FP64) {
         const double vc = amg64.apply_bytes(&vcycle_level_bytes);
-        bytes_krylov = it * (Z * 12.0 + 16.0 * N + 48.0 * N + 16.0 * N + 24.0 * N + vc) +
-                       (Z * 12.0 + 24.0 * N + vc + 16.0 * N + 16.0 * N);
+        bytes_krylov = it * (Z * (8.0 + c) + 16.0 * N + 48.0 * N + 16.0 * N + 24.0 * N + vc) +
+                       (Z * (8.0 + c) + 24.0 * N + vc + 16.0 * N + 16.0 * N);
     } else {
         const double vc = amg32.apply_bytes(&vcycle_level_bytes);
-        bytes_krylov = it * (Z * 8.0 + 8.0 * N + 32.0 * N + 8.0 * N + 12.0 * N + vc) +
-                       replacements * (Z * 12.0 + 24.0 * N + 20.0 * N) +
-                       (Z * 12.0 + 24.0 * N + 12.0 * N + vc + 8.0 * N + 8.0 * N);
+        bytes_krylov = it * (Z * (4.0 + c) + 8.0 * N + 32.0 * N + 8.0 * N + 12.0 * N + vc) +
+                       replacements * (Z * (8.0 + c) + 24.0 * N + 20.0 * N) +
+                       (Z * (8.0 + c) + 24.0 * N + 12.0 * N + vc + 8.0 * N + 8.0 * N);
     }
 }
 

@@ -83,6 +83,46 @@ __global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__
     if (i < n) out[i] += bsum[blockIdx.x];
 }
 
+// Short arrays (n <= SCAN_SINGLE): the whole exclusive scan in one block -- each thread sums a
+// contiguous chunk, a two-level shuffle scan of the 1024 chunk sums, then each thread writes its
+// chunk (one launch instead of three).
+constexpr int SCAN_SINGLE = 1024 * 32;
+__global__ void __launch_bounds__(1024) k_scan_single(int n, const int* in, int* out, int* total)
+{
+    __shared__ int wsum[32];
+    const int per = (n + 1023) / 1024;
+    const int b = min(n, int(threadIdx.x) * per), e = min(n, b + per);
+    int s = 0;
+    for (int i = b; i < e; ++i) s += in[i];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int v = wsum[lane];
+        int vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, vi, o);
+            if (lane >= o) vi += t;
+        }
+        wsum[lane] = vi - v;   // exclusive prefix of the warp sums
+    }
+    __syncthreads();
+    int run = wsum[w] + inc - s;
+    for (int i = b; i < e; ++i) {
+        const int v = in[i];
+        out[i] = run;
+        run += v;
+    }
+    if (threadIdx.x == 1023 && total) *total = run;
+}
+
 // ---------------- aggregation ----------------
 // rs_i = 1 / sqrt(|a_ii|): strengths |a_ij| rs_i rs_j are formed in FP32 (a coupling
 // strength needs no more precision, and FP32 keeps the FP64 unit free).
@@ -154,58 +194,107 @@ __device__ __forceinline__ void best_of_lanes(float& bs, unsigned& bh, int& bj)
     }
 }
 
-// Strongest free neighbour of every free row (-1 if none).  K lanes per row (lane q scans the
-// entries q, q + K, ...): coarse levels have few, long rows, and one thread per row leaves the
-// SMs idle behind a chain of dependent gathers.
-template <class T, int K>
-__global__ void k_pick(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
-                       const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
-                       int* __restrict__ best, int neg, float theta)
+// Block-aggregated append of row i (when take) to a worklist: one atomic per block, the rows of
+// a block in thread order.  Every thread of the block calls it (block-uniform loops only).
+__device__ __forceinline__ void wl_append_block(bool take, int i, int* __restrict__ wl, int* __restrict__ cnt)
 {
-    int i, q;
-    row_lane<K>(i, q);
-    const bool valid = i < n;
-    if (K <= 1 && !valid) return;
-    const bool active = valid && state[i] == 0;
-    float bs = 0.0f;
-    unsigned bh = 0u;
-    int bj = -1;
-    if (active) {
-        const float ri = rs[i];
-        const int len = rowlen[i];
-        for (int t = q; t < len; t += K) {
-            const int k = slot_of(sp, i, t);
-            const int j = col[k];
-            if (j == i || state[j] != 0) continue;
-            const float a = float(A[k]);
-            const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
-            if (!(s > 0.0f && s >= theta)) continue;
-            const unsigned h = edge_hash(i, j);
-            if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
-                bs = s;
-                bh = h;
-                bj = j;
+    __shared__ int wcnt[32];
+    __shared__ int wofs[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (lane == 0) wcnt[w] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int k = 0; k < nw; ++k) {
+            wofs[k] = tot;
+            tot += wcnt[k];
+        }
+        const int base = tot ? atomicAdd(cnt, tot) : 0;
+        for (int k = 0; k < nw; ++k) wofs[k] += base;
+    }
+    __syncthreads();
+    if (take) wl[wofs[w] + __popc(m & ((1u << lane) - 1u))] = i;
+    __syncthreads();   // wcnt/wofs are reused by the next call
+}
+
+// Strongest free neighbour of every free row of a worklist (-1 if none); wl == nullptr: every
+// row, one thread (or K lanes) per row in row order.  K lanes per row (lane q scans the entries
+// q, q + K, ...): coarse levels have few, long rows, and one thread per row leaves the SMs idle
+// behind a chain of dependent gathers.  Grid-stride with K consecutive lanes per row, so every
+// warp iteration is uniform and the lane reduction sees whole rows.
+template <class T, int K>
+__global__ void k_pick_wl(int n, const int* __restrict__ wl, const int* __restrict__ wlcnt, const int* __restrict__ sp,
+                          const int* __restrict__ col, const int* __restrict__ rowlen, const T* __restrict__ A,
+                          const float* __restrict__ rs, const int* __restrict__ state, int* __restrict__ best, int neg,
+                          float theta)
+{
+    const long long total = (long long)(wl ? *wlcnt : n) * K;
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long g = base + lane;
+        const bool valid = g < total;
+        const int i = valid ? (wl ? wl[g / K] : int(g / K)) : 0;
+        const int q = int(g % K);
+        const bool active = valid && state[i] == 0;
+        float bs = 0.0f;
+        unsigned bh = 0u;
+        int bj = -1;
+        if (active) {
+            const float ri = rs[i];
+            const int len = rowlen[i];
+            for (int t = q; t < len; t += K) {
+                const int k = slot_of(sp, i, t);
+                const int j = col[k];
+                if (j == i || state[j] != 0) continue;
+                const float a = float(A[k]);
+                const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
+                if (!(s > 0.0f && s >= theta)) continue;
+                const unsigned h = edge_hash(i, j);
+                if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
+                    bs = s;
+                    bh = h;
+                    bj = j;
+                }
             }
         }
+        if (K > 1) best_of_lanes<K>(bs, bh, bj);
+        if (valid && q == 0) best[i] = active ? bj : -1;
     }
-    if (K > 1) best_of_lanes<K>(bs, bh, bj);
-    if (valid && q == 0) best[i] = active ? bj : -1;
 }
 
-__global__ void k_match(int n, int* __restrict__ state, const int* __restrict__ best, int* __restrict__ partner)
+// Mutual best picks pair; rows without a candidate become state 3.  Over a worklist (wl ==
+// nullptr: every row); the rows that stay free form the next sweep's worklist.  A sweep's
+// decisions depend only on the picks and states of the sweep, not on the order of its rows.
+__global__ void k_match_wl(int n, const int* __restrict__ wl, const int* __restrict__ wlcnt, int* __restrict__ state,
+                           const int* __restrict__ best, int* __restrict__ partner, int* __restrict__ wl_next,
+                           int* __restrict__ cnt_next)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || state[i] != 0) return;
-    const int j = best[i];
-    if (j >= 0 && best[j] == i) {
-        state[i] = 1;
-        partner[i] = j;
-    } else if (j < 0) {
-        state[i] = 3;
+    const int total = wl ? *wlcnt : n;
+    for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const int g = base + threadIdx.x;
+        bool keep = false;
+        int i = 0;
+        if (g < total) {
+            i = wl ? wl[g] : g;
+            if (state[i] == 0) {
+                const int j = best[i];
+                if (j >= 0 && best[j] == i) {
+                    state[i] = 1;
+                    partner[i] = j;
+                } else if (j < 0) {
+                    state[i] = 3;
+                } else {
+                    keep = true;
+                }
+            }
+        }
+        wl_append_block(keep, i, wl_next, cnt_next);
     }
 }
 
-// unmatched rows pick their strongest paired neighbour (|a_ij| scaled); K lanes per row as k_pick
+// unmatched rows pick their strongest paired neighbour (|a_ij| scaled); K lanes per row as k_pick_wl
 template <class T, int K>
 __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict__ col, const int* __restrict__ rowlen,
                        const T* __restrict__ A, const float* __restrict__ rs, const int* __restrict__ state,
@@ -1089,6 +1178,19 @@ int pick_lanes(int n, long long nent)
     default: { constexpr int KL = 16; LAUNCH; } break;                                                            \
     }
 
+// Blocks of the grid-stride matching launches: at most 8 per SM (the device's SM count).
+int stride_blocks(long long threads)
+{
+    static int cap = 0;
+    if (cap == 0) {
+        int dev = 0, sms = 0;
+        PORSOL_CUDA(cudaGetDevice(&dev));
+        PORSOL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cap = std::max(1, 8 * sms);
+    }
+    return std::max(1, std::min(div_up(std::max(threads, 1LL), TB), cap));
+}
+
 // Process-wide cache of autotuned lanes per row, keyed by level shape.
 std::mutex& tune_mutex()
 {
@@ -1105,6 +1207,11 @@ std::unordered_map<long long, int>& tune_cache()
 
 void exclusive_scan(cudaStream_t s, int n, const int* in, int* out, int* total_dev, DBuf<int>& scratch)
 {
+    if (n <= SCAN_SINGLE) {
+        PORSOL_LAUNCH(k_scan_single<<<1, 1024, 0, s>>>(n, in, out, total_dev));
+        PORSOL_CUDA(cudaGetLastError());
+        return;
+    }
     const int nb = std::max(1, div_up(n, 1024));
     if ((int)scratch.n < nb) scratch.alloc(nb);
     if (n > 0) PORSOL_LAUNCH(k_scan_block<<<nb, 1024, 0, s>>>(n, in, out, scratch.p));
@@ -1135,12 +1242,25 @@ void Amg<T>::pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, b
     // stall fallback (join) runs more sweeps so chains and stars also pair up.
     const int sweeps = join ? 8 : 4;
     const int lanes = pick_lanes(n, P.nent);
+    // The first sweep visits every row (one thread or K lanes per row); each later sweep only the
+    // rows still free after the previous one (a worklist the match kernel builds), in grid-stride
+    // launches of at most 8 blocks per SM: the decisions are those of full sweeps, the later
+    // sweeps cost a fraction of the first.
+    s_wl_[0].alloc(n);
+    s_wl_[1].alloc(n);
+    s_wlcnt_.alloc(2);
     const int nbk = div_up((long long)n * lanes, TB);
+    const int nbp = stride_blocks((long long)n * lanes);
+    const int nbm = stride_blocks(n);
     for (int sweep = 0; sweep < sweeps; ++sweep) {
-        PORSOL_LANES(lanes, PORSOL_LAUNCH((k_pick<T, KL><<<nbk, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A,
-                                                                           d.p, state.p, best.p, neg ? 1 : 0,
-                                                                           float(theta)))));
-        PORSOL_LAUNCH(k_match<<<nb, TB, 0, s>>>(n, state.p, best.p, partner.p));
+        const int cur = sweep & 1, nxt = cur ^ 1;
+        const int* wl = sweep == 0 ? nullptr : s_wl_[cur].p;
+        PORSOL_LANES(lanes, PORSOL_LAUNCH((k_pick_wl<T, KL><<<sweep == 0 ? nbk : nbp, TB, 0, s>>>(
+                                n, wl, s_wlcnt_.p + cur, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p, state.p, best.p,
+                                neg ? 1 : 0, float(theta)))));
+        PORSOL_CUDA(cudaMemsetAsync(s_wlcnt_.p + nxt, 0, sizeof(int), s));
+        PORSOL_LAUNCH(k_match_wl<<<sweep == 0 ? nb : nbm, TB, 0, s>>>(n, wl, s_wlcnt_.p + cur, state.p, best.p,
+                                                                      partner.p, s_wl_[nxt].p, s_wlcnt_.p + nxt));
     }
     if (join)
         PORSOL_LANES(lanes, PORSOL_LAUNCH((k_join<T, KL><<<nbk, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, d.p,

@@ -83,8 +83,8 @@ __device__ bool block_reduce_last(V v0, double* partial, unsigned int* counter, 
 
 // Row r of a SELL matrix times x, accumulated in the vector type TX (FP32 rows stay on the
 // FP32 pipe).
-template <class TV, class TX>
-__device__ __forceinline__ TX sell_row(const int* __restrict__ sp, const int* __restrict__ col,
+template <class TV, class TX, class CI>
+__device__ __forceinline__ TX sell_row(const int* __restrict__ sp, const CI* __restrict__ col,
                                        const TV* __restrict__ val, const TX* __restrict__ x, int r)
 {
     return sell_dot<TX>(sp, col, val, r, [x](int j) { return x[j]; });
@@ -110,8 +110,8 @@ __global__ void k_residual(int n, const int* __restrict__ sp, const int* __restr
 }
 
 // r = b - A x; def0 = ||r||
-template <class TV, class T>
-__global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class TV, class T, class CI>
+__global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                                                 const TV* __restrict__ val, const T* __restrict__ x,
                                                 const T* __restrict__ b, T* __restrict__ r, CgDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
@@ -166,8 +166,8 @@ __global__ void k_first_direction(int n, const T* __restrict__ z, T* __restrict_
 }
 
 // q = A p ; alpha = p . q
-template <class TV, class T>
-__global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class TV, class T, class CI>
+__global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                                                 const TV* __restrict__ val, const T* __restrict__ p,
                                                 T* __restrict__ q, CgDev* st, double* partial,
                                                 unsigned int* counter)
@@ -285,7 +285,8 @@ __device__ __forceinline__ void rc_publish(const RcDev* st, CgHostView* hv)
 }
 
 // r64 = b - A x (FP64); def0 = sigma = ||r64||
-__global__ void __launch_bounds__(RB) k_rc_init(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class CI>
+__global__ void __launch_bounds__(RB) k_rc_init(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                                                 const double* __restrict__ val, const double* __restrict__ x,
                                                 const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
@@ -324,7 +325,8 @@ __global__ void k_rc_rescale(int n, const double* __restrict__ r64, float* __res
 }
 
 // q = A32 p; alpha = rho / (p . q)
-__global__ void __launch_bounds__(RB) k_rc_pq(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class CI>
+__global__ void __launch_bounds__(RB) k_rc_pq(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                                               const float* __restrict__ val, const float* __restrict__ p,
                                               float* __restrict__ q, RcDev* st, double* partial,
                                               unsigned int* counter, CgHostView* hv)
@@ -381,7 +383,8 @@ __global__ void __launch_bounds__(RB) k_rc_update(int n, double* __restrict__ x,
 }
 
 // Replacement: r64 = b - A x in FP64; convergence is decided on this true residual only
-__global__ void __launch_bounds__(RB) k_rc_true(int n, const int* __restrict__ sp, const int* __restrict__ col,
+template <class CI>
+__global__ void __launch_bounds__(RB) k_rc_true(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                                                 const double* __restrict__ val, const double* __restrict__ x,
                                                 const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
@@ -586,13 +589,17 @@ void PcgSolver<TV, T>::iteration(cudaStream_t s, const SellPattern& P, const TV*
     const int n = P.n;
     const int nb = div_up(n, RB), nr = red_blocks(n);
     const int* stop = &st_.p->stop;
-    const double spmv_bytes = double(P.nent) * (sizeof(TV) + 4) + 2.0 * n * sizeof(T);
+    const double spmv_bytes = double(P.nent) * (sizeof(TV) + (P.has_off16() ? 2 : 4)) + 2.0 * n * sizeof(T);
     {
         const bool pf = prof && prof->on && prof_kernel >= 0;
         cudaEvent_t ev = nullptr;
         if (pf) prof->begin(s, prof_kernel, spmv_bytes, &ev);
-        PORSOL_LAUNCH(k_spmv_pq<TV, T><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                         red_.partial.p, red_.counter.p));
+        if (P.has_off16())
+            PORSOL_LAUNCH(k_spmv_pq<TV, T, short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val, p_.p, q_.p,
+                                                                    st_.p, red_.partial.p, red_.counter.p));
+        else
+            PORSOL_LAUNCH(k_spmv_pq<TV, T, int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                                                                  red_.partial.p, red_.counter.p));
         if (pf) prof->end(s, prof_kernel, spmv_bytes, ev);
     }
     PORSOL_LAUNCH(k_cg_update<T><<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
@@ -618,8 +625,12 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
     init.tol = tol;
     init.maxit = maxit;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
-    PORSOL_LAUNCH(k_cg_init<TV, T><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
-                                                     red_.partial.p, red_.counter.p, dview_));
+    if (P.has_off16())
+        PORSOL_LAUNCH(k_cg_init<TV, T, short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val, x, b, r_.p, st_.p,
+                                                                red_.partial.p, red_.counter.p, dview_));
+    else
+        PORSOL_LAUNCH(k_cg_init<TV, T, int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
+                                                              red_.partial.p, red_.counter.p, dview_));
     PORSOL_CUDA(cudaGetLastError());
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
@@ -726,16 +737,24 @@ void ReliableCg::iteration(cudaStream_t s, const SellPattern& P, const double* v
     const int* stop = &st_.p->stop;
     {
         const bool pf = prof && prof->on;
-        const double bytes = double(P.nent) * 8.0 + 2.0 * n * 4.0;
+        const double bytes = double(P.nent) * (P.has_off16() ? 6.0 : 8.0) + 2.0 * n * 4.0;
         cudaEvent_t ev = nullptr;
         if (pf) prof->begin(s, PK_SPMV32, bytes, &ev);
-        PORSOL_LAUNCH(k_rc_pq<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
-                                                red_.counter.p, dview_));
+        if (P.has_off16())
+            PORSOL_LAUNCH(k_rc_pq<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val32, p_.p, q_.p, st_.p,
+                                                           red_.partial.p, red_.counter.p, dview_));
+        else
+            PORSOL_LAUNCH(k_rc_pq<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p,
+                                                         red_.partial.p, red_.counter.p, dview_));
         if (pf) prof->end(s, PK_SPMV32, bytes, ev);
     }
     PORSOL_LAUNCH(k_rc_update<<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_));
-    PORSOL_LAUNCH(k_rc_true<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
-                                              red_.counter.p, dview_));
+    if (P.has_off16())
+        PORSOL_LAUNCH(k_rc_true<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p,
+                                                         red_.partial.p, red_.counter.p, dview_));
+    else
+        PORSOL_LAUNCH(k_rc_true<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
+                                                       red_.partial.p, red_.counter.p, dview_));
     PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 0));
     M.apply(s, r_.p, z_.p, stop);
     PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 0));
@@ -759,8 +778,12 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
     init.maxit = maxit;
     init.delta = delta;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(RcDev), cudaMemcpyHostToDevice, s));
-    PORSOL_LAUNCH(k_rc_init<<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
-                                              red_.partial.p, red_.counter.p, dview_));
+    if (P.has_off16())
+        PORSOL_LAUNCH(k_rc_init<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p,
+                                                         red_.partial.p, red_.counter.p, dview_));
+    else
+        PORSOL_LAUNCH(k_rc_init<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
+                                                       red_.partial.p, red_.counter.p, dview_));
     PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 1));
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);

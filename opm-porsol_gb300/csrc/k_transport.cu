@@ -12,9 +12,10 @@
 // Layout: every face that contributes is one "face entry" (the reference visits each
 // internal/periodic face once, from the lower cell index, and every Dirichlet boundary
 // face).  All saturation-independent per-face factors (gravity driving force G, capillary
-// geometry factor, n.n) are computed once per transportSolve.  A sub-step is two kernels:
-// face entries compute dS, then each cell gathers its entries' dS in a fixed order (no
-// atomics, deterministic) and updates its saturation with the range check.
+// geometry factor, n.n) are computed once per transportSolve.  A sub-step with gravity or
+// capillarity is two kernels: face entries compute dS, then each cell gathers its entries' dS
+// in a fixed order (no atomics, deterministic) and updates its saturation with the range check.
+// A viscous-only sub-step is one cell kernel that evaluates its entries' terms itself.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -83,7 +84,7 @@ __global__ void k_face_dS(int nfe, const FaceEntry* __restrict__ fe, const doubl
 }
 
 // Fractional flow lambda_1 / (lambda_1 + lambda_2), evaluated with the same operations as the
-// viscous term of k_face_dS (m1 * (1 / (m1 + m2))), so the fast path below is bitwise equal.
+// viscous term of k_face_dS (m1 * (1 / (m1 + m2))), so the viscous-only sub-step is bitwise equal.
 template <bool TAB>
 __device__ __forceinline__ double frac1(int c, double s, const TrParams& p, const RockView& R)
 {
@@ -98,24 +99,63 @@ __global__ void k_frac_init(int nc, const double* __restrict__ sat, TrParams p, 
     if (c < nc) frac[c] = frac1<TAB>(c, sat[c], p, R);
 }
 
-// Viscous-only sub-step (no gravity driving force, no capillary term): both phase mobilities
-// come from the same upstream cell, so the face term is f(s_up) q n.n with f precomputed per
-// cell (one FP64 division per cell instead of one per face; GB300's FP64 rate makes the
-// per-face form compute-bound).
+// Fractional flow of each Dirichlet entry's boundary saturation, in its cell's rock
 template <bool TAB>
-__global__ void k_face_dS_visc(int nfe, const FaceEntry* __restrict__ fe, const double* __restrict__ frac,
-                               const double* __restrict__ flux, TrParams p, RockView R, double* __restrict__ dS,
-                               const int* __restrict__ status)
+__global__ void k_frac_bc(int nfe, const FaceEntry* __restrict__ fe, TrParams p, RockView R, double* __restrict__ fbc)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nfe && fe[k].dirichlet) fbc[k] = frac1<TAB>(fe[k].c0, fe[k].satbc, p, R);
+}
+
+// One viscous-only sub-step (no gravity driving force, no capillary term) as a single cell
+// kernel.  Both phase mobilities of a face come from the same upstream cell, so its term is
+// f(s_up) q n.n with the fractional flow f precomputed per cell (one FP64 division per cell, not
+// per face), q the flux of the lower cell's half-face.  Every cell evaluates the terms of its own
+// entries in its gather order, then updates as k_cell_update; an entry's term is evaluated by
+// both its cells with the same operations, (f q) (+-n.n) = +-(f q n.n) exactly, so each cell
+// sums exactly what a face-entry pass followed by the gather would give, without the per-entry
+// array written and read back or a second launch per sub-step.  Fractional flows are read from
+// frac_in and the updated cell's written to frac_out (a neighbour may still read the old value).
+template <bool TAB>
+__global__ void k_visc_substep(int nc, const int* __restrict__ cptr, const int* __restrict__ va,
+                               const int* __restrict__ vb, const int* __restrict__ vhf,
+                               const double* __restrict__ vcoef, const double* __restrict__ flux,
+                               const double* __restrict__ frac_in, const double* __restrict__ fbc,
+                               const double* __restrict__ inj, const double* __restrict__ ipv, TrParams p, RockView R,
+                               double dt, int check, int clamp, double* __restrict__ sat,
+                               double* __restrict__ frac_out, int* status)
 {
     if (*status) return;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nfe) return;
-    const int c0 = fe[k].c0, c1 = fe[k].c1, hf = fe[k].hf, dir = fe[k].dirichlet;
-    const double q = flux[hf];
-    double f;
-    if (q >= 0.0) f = frac[c0];
-    else f = dir ? frac1<TAB>(c0, fe[k].satbc, p, R) : frac[c1];
-    dS[k] = f * q * fe[k].nn;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double r = 0.0;
+    for (int q = cptr[c]; q < cptr[c + 1]; ++q) {
+        const double qf = flux[vhf[q]];
+        const int b = vb[q];
+        double f;
+        if (qf >= 0.0) f = frac_in[va[q]];
+        else f = b >= 0 ? frac_in[b] : fbc[~b];
+        r += (f * qf) * vcoef[q];
+    }
+    const double s = sat[c];
+    if (inj) {
+        double rate = inj[c];
+        if (rate < 0.0) {
+            const double l1 = mobp<TAB>(0, c, s, p, R), l2 = mobp<TAB>(1, c, s, p, R);
+            rate *= l1 / (l1 + l2);
+        }
+        r += rate;
+    }
+    double sn = s + (dt * r) * ipv[c];
+    if (check || clamp) {
+        if (sn > 1.0 || sn < 0.0) {
+            if (clamp) sn = fmax(fmin(sn, 1.0), 0.0);
+            else if (sn > 1.001 || sn < -0.001) atomicOr(status, ST_SAT_RANGE);
+        }
+    }
+    if (!isfinite(sn)) atomicOr(status, ST_NONFINITE);
+    sat[c] = sn;
+    frac_out[c] = frac1<TAB>(c, sn, p, R);
 }
 
 // residual gather + smallTimeStep update + checkAndPossiblyClampSat
@@ -123,7 +163,7 @@ template <bool TAB>
 __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* __restrict__ cent,
                               const double* __restrict__ dS, const double* __restrict__ inj,
                               const double* __restrict__ ipv, TrParams p, RockView R, double dt, int check,
-                              int clamp, double* __restrict__ sat, double* __restrict__ frac, int* status)
+                              int clamp, double* __restrict__ sat, int* status)
 {
     if (*status) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -153,7 +193,6 @@ __global__ void k_cell_update(int nc, const int* __restrict__ cptr, const int* _
     }
     if (!isfinite(sn)) atomicOr(status, ST_NONFINITE);
     sat[c] = sn;
-    if (frac) frac[c] = frac1<TAB>(c, sn, p, R);   // for the next viscous-only sub-step
 }
 
 __device__ __forceinline__ void atomic_min_pos(unsigned long long* a, double v)
@@ -568,12 +607,27 @@ void porsol_transport::build_entries(const double* grav)
     for (int c = 0; c < nc; ++c) cp[c + 1] = cp[c] + int(cl[c].size());
     ce.reserve(cp[nc]);
     for (int c = 0; c < nc; ++c) ce.insert(ce.end(), cl[c].begin(), cl[c].end());
+    // the same entries seen from each cell, for the single-kernel viscous sub-step
+    std::vector<int> va(ce.size()), vb(ce.size()), vh(ce.size());
+    std::vector<double> vc(ce.size());
+    for (size_t q = 0; q < ce.size(); ++q) {
+        const int x = ce[q], k = x >= 0 ? x : ~x;
+        const FaceEntry& e = fe_h[size_t(k)];
+        va[q] = e.c0;
+        vb[q] = e.dirichlet ? ~k : e.c1;
+        vh[q] = e.hf;
+        vc[q] = x >= 0 ? e.nn : -e.nn;
+    }
     any_gravity = false;
     for (const FaceEntry& e : fe_h) any_gravity = any_gravity || e.G != 0.0;
     cudaStream_t s = stream;
     fe.upload(fe_h, s);
     cptr.upload(cp, s);
     cent.upload(ce, s);
+    ve_a.upload(va, s);
+    ve_b.upload(vb, s);
+    ve_hf.upload(vh, s);
+    ve_coef.upload(vc, s);
     gflux_hf.upload(ghf, s);
     dS.alloc(std::max<size_t>(fe_h.size(), 1));
     PORSOL_CUDA(cudaStreamSynchronize(s));
@@ -661,35 +715,43 @@ void porsol_transport::solve(double* sat, double time, const double* grav, const
     const int nfe = int(fe_h.size());
     // viscous-only sub-steps use the per-cell fractional flow (same arithmetic, fewer FP64 ops)
     const bool visc_only = o.method_viscous && !o.method_capillary && (!o.method_gravity || !any_gravity);
-    if (visc_only) frac.alloc(nc);
+    if (visc_only) {
+        frac.alloc(nc);
+        frac2.alloc(nc);
+        fbc.alloc(std::max(nfe, 1));
+        if (nfe) {
+            if (tab) PORSOL_LAUNCH(k_frac_bc<true><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, p, rock, fbc.p));
+            else PORSOL_LAUNCH(k_frac_bc<false><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, p, rock, fbc.p));
+        }
+    }
     int repeats = 0;
     const int max_repeats = 10;
     while (true) {
         if (visc_only) {
             if (tab) PORSOL_LAUNCH(k_frac_init<true><<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, rock, frac.p));
             else PORSOL_LAUNCH(k_frac_init<false><<<div_up(nc, TB), TB, 0, s>>>(nc, d_sat, p, rock, frac.p));
-        }
-        for (int q = 0; q < n; ++q) {
-            if (nfe) {
-                if (visc_only) {
-                    if (tab)
-                        PORSOL_LAUNCH(k_face_dS_visc<true><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p,
-                                                                                        rock, dS.p, status.p));
-                    else
-                        PORSOL_LAUNCH(k_face_dS_visc<false><<<div_up(nfe, TB), TB, 0, s>>>(nfe, fe.p, frac.p, d_flux, p,
-                                                                                         rock, dS.p, status.p));
-                } else {
-                    launch_face_dS(s, nfe, fe.p, d_sat, d_flux, p, rock, dS.p, status.p);
-                }
+            for (int q = 0; q < n; ++q) {
+                const double* fin = (q & 1) ? frac2.p : frac.p;
+                double* fout = (q & 1) ? frac.p : frac2.p;
+                if (tab)
+                    PORSOL_LAUNCH(k_visc_substep<true><<<div_up(nc, TB), TB, 0, s>>>(
+                        nc, cptr.p, ve_a.p, ve_b.p, ve_hf.p, ve_coef.p, d_flux, fin, fbc.p, d_inj, ipv.p, p, rock, dt,
+                        o.check_sat, o.clamp_sat, d_sat, fout, status.p));
+                else
+                    PORSOL_LAUNCH(k_visc_substep<false><<<div_up(nc, TB), TB, 0, s>>>(
+                        nc, cptr.p, ve_a.p, ve_b.p, ve_hf.p, ve_coef.p, d_flux, fin, fbc.p, d_inj, ipv.p, p, rock, dt,
+                        o.check_sat, o.clamp_sat, d_sat, fout, status.p));
+                if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
             }
+        }
+        for (int q = 0; q < (visc_only ? 0 : n); ++q) {
+            if (nfe) launch_face_dS(s, nfe, fe.p, d_sat, d_flux, p, rock, dS.p, status.p);
             if (tab)
                 PORSOL_LAUNCH(k_cell_update<true><<<div_up(nc, TB), TB, 0, s>>>(
-                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat,
-                    visc_only ? frac.p : nullptr, status.p));
+                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat, status.p));
             else
                 PORSOL_LAUNCH(k_cell_update<false><<<div_up(nc, TB), TB, 0, s>>>(
-                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat,
-                    visc_only ? frac.p : nullptr, status.p));
+                    nc, cptr.p, cent.p, dS.p, d_inj, ipv.p, p, rock, dt, o.check_sat, o.clamp_sat, d_sat, status.p));
             if ((q & 255) == 255) PORSOL_CUDA(cudaGetLastError());
         }
         PORSOL_CUDA(cudaGetLastError());

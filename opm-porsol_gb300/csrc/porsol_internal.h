@@ -149,6 +149,11 @@ struct SellPattern {
     long long nent = 0; // stored entries incl. padding
     HVec<int> h_slice_ptr, h_col, h_rowlen;
     DBuf<int> slice_ptr, col, rowlen, diag;   // diag: slot index of the diagonal
+    // the columns again as 16-bit offsets from the row (padding 0), when every stored column lies
+    // within 32767 rows of its row (upload() decides; off16 stays empty otherwise): the CG's
+    // matrix-vector products then read 2 instead of 4 bytes of index per entry
+    DBuf<short> off16;
+    bool has_off16() const { return off16.p != nullptr && off16.n == size_t(nent); }
     void upload(cudaStream_t s);
 };
 

@@ -10,9 +10,14 @@
 
 namespace porsol {
 
+// Column of stored entry k of row r: the column itself (int), or its 16-bit offset from the row
+// (short; systems whose couplings all lie within 32767 rows of the diagonal).
+__device__ __forceinline__ int sell_col(const int* __restrict__ col, int k, int) { return col[k]; }
+__device__ __forceinline__ int sell_col(const short* __restrict__ off, int k, int r) { return r + off[k]; }
+
 // sum_t val[k_t] * xf(col[k_t]) accumulated in Acc; xf maps a column index to the vector value.
-template <class Acc, class TV, class XF>
-__device__ __forceinline__ Acc sell_dot(const int* __restrict__ sp, const int* __restrict__ col,
+template <class Acc, class TV, class XF, class CI = int>
+__device__ __forceinline__ Acc sell_dot(const int* __restrict__ sp, const CI* __restrict__ col,
                                         const TV* __restrict__ val, int r, XF xf)
 {
     const int s = r >> 5, lane = r & 31;
@@ -21,7 +26,8 @@ __device__ __forceinline__ Acc sell_dot(const int* __restrict__ sp, const int* _
     int k = b + lane;
     int t = 0;
     for (; t + 4 <= w; t += 4, k += 128) {
-        const int c0 = col[k], c1 = col[k + 32], c2 = col[k + 64], c3 = col[k + 96];
+        const int c0 = sell_col(col, k, r), c1 = sell_col(col, k + 32, r), c2 = sell_col(col, k + 64, r),
+                  c3 = sell_col(col, k + 96, r);
         const Acc v0 = Acc(val[k]), v1 = Acc(val[k + 32]), v2 = Acc(val[k + 64]), v3 = Acc(val[k + 96]);
         const Acc x0 = Acc(xf(c0)), x1 = Acc(xf(c1)), x2 = Acc(xf(c2)), x3 = Acc(xf(c3));
         acc += v0 * x0;
@@ -29,7 +35,7 @@ __device__ __forceinline__ Acc sell_dot(const int* __restrict__ sp, const int* _
         acc += v2 * x2;
         acc += v3 * x3;
     }
-    for (; t < w; ++t, k += 32) acc += Acc(val[k]) * Acc(xf(col[k]));
+    for (; t < w; ++t, k += 32) acc += Acc(val[k]) * Acc(xf(sell_col(col, k, r)));
     return acc;
 }
 

@@ -667,6 +667,23 @@ void SellPattern::upload(cudaStream_t s)
     });
     for (int r = 0; r < n; ++r) PORSOL_REQUIRE(d[r] >= 0, PORSOL_ERR_BAD_ARG, "matrix row without diagonal");
     diag.upload(d, s);
+    // 16-bit column offsets when they fit (rows past n in the last slice: offset 0)
+    std::atomic<bool> fits{true};
+    std::vector<short> off(static_cast<size_t>(nent));
+    parallel_for(nslices, [&](long long sl) {
+        const int w = (h_slice_ptr[sl + 1] - h_slice_ptr[sl]) / SELL_C;
+        for (int lane = 0; lane < SELL_C; ++lane) {
+            const int r = int(sl) * SELL_C + lane;
+            for (int t = 0; t < w; ++t) {
+                const long long k = h_slice_ptr[sl] + (long long)t * SELL_C + lane;
+                const int o = r < n ? h_col[k] - r : 0;
+                if (o < -32768 || o > 32767) fits = false;
+                off[k] = short(r < n ? o : 0);
+            }
+        }
+    });
+    if (fits) off16.upload(off, s);
+    else off16.release();
     PORSOL_CUDA(cudaStreamSynchronize(s));   // host vectors may be freed by the caller
 }
 

@@ -63,6 +63,11 @@ struct porsol_transport {
     porsol::DBuf<porsol::FaceEntry> fe;
     porsol::DBuf<int> cptr, cent, facepos, status;
     porsol::DBuf<double> ipv, vol, poro_d, dS, sat0, gflux_hf, in_sat, in_flux, in_inj, frac;
+    // the viscous-only sub-step as one cell kernel: each cell's entries in its gather order (lower
+    // cell, other cell or ~entry for Dirichlet faces, flux half-face, +-n.n), the fractional flow
+    // of the Dirichlet entries, and a second fractional-flow buffer (read one, write the other)
+    porsol::DBuf<int> ve_a, ve_b, ve_hf;
+    porsol::DBuf<double> ve_coef, fbc, frac2;
     bool any_gravity = false;   // some face entry has a non-zero gravity driving force
     porsol::DBuf<unsigned long long> red;
 
