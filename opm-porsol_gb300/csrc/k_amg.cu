@@ -1073,15 +1073,17 @@ __global__ void k_dense_cholesky_inverse(int n, double* __restrict__ D, double* 
 }
 
 // Inverse of the dense SPD matrix D (n <= DENSE_SMEM_N) by Gauss-Jordan elimination in shared
-// memory, one block: for SPD matrices the pivots are the diagonal (no pivoting, as LDL^T).  Three
-// barriers per pivot, all in shared memory; non-positive or non-finite pivots set ST_NONFINITE.
+// memory, one block of 32 x 32 threads (thread (tx, ty) owns the entries (ty + 32 a, tx + 32 b)):
+// for SPD matrices the pivots are the diagonal (no pivoting, as LDL^T).  Per pivot k, first every
+// entry outside row and column k is updated from the old row and column, then row and column k are
+// scaled: two barriers per pivot.  Non-positive or non-finite pivots set ST_NONFINITE.
 constexpr int DENSE_SMEM_N = 160;   // 200 KB of doubles
 __global__ void __launch_bounds__(1024) k_dense_gauss_jordan(int n, const double* __restrict__ D,
                                                              double* __restrict__ Dinv, int* status)
 {
     extern __shared__ double A[];
-    const int nn = n * n;
-    for (int q = threadIdx.x; q < nn; q += blockDim.x) A[q] = D[q];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x) A[q] = D[q];
     __syncthreads();
     for (int k = 0; k < n; ++k) {
         const double akk = A[k * n + k];
@@ -1090,19 +1092,21 @@ __global__ void __launch_bounds__(1024) k_dense_gauss_jordan(int n, const double
             return;   // uniform: every thread read the same pivot
         }
         const double piv = 1.0 / akk;
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-            if (j != k) A[k * n + j] *= piv;
-        __syncthreads();
-        for (int q = threadIdx.x; q < nn; q += blockDim.x) {
-            const int i = q / n, j = q - i * n;
-            if (i != k && j != k) A[q] -= A[i * n + k] * A[k * n + j];
+        for (int i = ty; i < n; i += 32) {
+            if (i == k) continue;
+            const double aik = A[i * n + k] * piv;
+            for (int j = tx; j < n; j += 32)
+                if (j != k) A[i * n + j] -= aik * A[k * n + j];
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-            A[i * n + k] = (i == k) ? piv : -A[i * n + k] * piv;
+        if (ty == 0)
+            for (int j = tx; j < n; j += 32)
+                if (j != k) A[k * n + j] *= piv;
+        if (ty == 1)
+            for (int i = tx; i < n; i += 32) A[i * n + k] = (i == k) ? piv : -A[i * n + k] * piv;
         __syncthreads();
     }
-    for (int q = threadIdx.x; q < nn; q += blockDim.x) Dinv[q] = A[q];
+    for (int q = threadIdx.x; q < n * n; q += blockDim.x) Dinv[q] = A[q];
 }
 
 template <class T>
