@@ -82,7 +82,10 @@ typedef struct porsol_fluid {
 typedef struct porsol_solver porsol_solver;
 
 /* linsolver_type: 0 = ILU0-preconditioned CG, 1 = AMG-preconditioned CG (default),
- * 2 = KAMG (runs the type-1 AMG-CG), 3 = FastAMG (runs the type-1 AMG-CG).
+ * 2 = KAMG: CG preconditioned by the Krylov-accelerated cycle (the first coarse level's
+ * correction is two flexible-CG steps preconditioned by that level's cycle; batched solves run the
+ * V-cycle), 3 = FastAMG (runs the type-1 AMG-CG; the reference itself falls back to AMG-CG where
+ * FastAMG is unavailable, IncompFlowSolverHybrid.hpp:687-697).
  * precision: PORSOL_FP64 = the plain drop-in; PORSOL_MIXED = FP32 AMG hierarchy (FP16
  * smoother matrices); single solves run FP32 CG recurrences with an FP64 solution and FP64
  * residual replacements, batched upscaling runs FP64 CG around the FP32 hierarchy. */

@@ -41,6 +41,9 @@ struct AmgOpts {
     bool autotune = false;         // time the lane schedules of each new level shape once (the
                                    // choice then depends on timing: off where runs must be
                                    // bitwise reproducible)
+    int kcycle_levels = 0;         // K-cycle: the coarse corrections of levels 1 .. kcycle_levels are
+                                   // two flexible-CG steps preconditioned by the cycle of that level
+                                   // (0: plain V-cycle)
 };
 
 // One finest-level bulk-staged Chebyshev step on a fixed 64-row system (expire: every wait for the
@@ -97,6 +100,7 @@ private:
         int lanes = 1;               // threads per row in the smoother/residual kernels
         Aggregates agg;              // to the next level
         DBuf<T> t, r, d0, d1, b, x;  // work vectors
+        DBuf<T> kc1, kc2, kv1, kv2, kr2;   // K-cycle vectors (K-levels only)
     };
     void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg_first, Aggregates& out);
     void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
@@ -113,6 +117,11 @@ private:
     void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
                    const int* stop);
     void vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop);
+    // coarse correction of level l - 1 solved on level l by two flexible-CG steps (K-cycle)
+    void kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop);
+    bool k_level(int l) const { return l >= 1 && l <= o_.kcycle_levels && l < nlev_ - 1; }
+    double cycle_bytes(int l, std::vector<double>* per_level) const;
+    DBuf<double> kpart_, kcoef_;   // K-cycle dot partials and coefficients (8 per level)
 
     AmgOpts o_;
     Profiler* prof_ = nullptr;

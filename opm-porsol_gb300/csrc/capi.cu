@@ -337,12 +337,18 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     AmgOpts ao;
     ao.smooth_steps = std::max(1, o.smooth_steps);
     ao.prolong = o.prolongate_factor;
+    // linsolver_type 2 (solveLinearSystemKAMG, :1609-1666): the Krylov-accelerated cycle (dune's KAMG
+    // is not available; this is the K-cycle on the first coarse level, the bandwidth-bound one: two
+    // flexible-CG steps there per cycle, the deeper levels visited twice); types 1 and 3 the V-cycle
+    ao.kcycle_levels = o.linsolver_type == 2 ? 1 : 0;
     dirichlet_guess(stream, P, val.p, rhs.p, x.p);
     if (o.precision == PORSOL_FP64) {
-        if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64)) {
+        if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64 &&
+              amg_kcycle == ao.kcycle_levels)) {
             amg64.setup(stream, P, val.p, ao);
             amg_ready = true;
             amg_precision = PORSOL_FP64;
+            amg_kcycle = ao.kcycle_levels;
         }
         PORSOL_CUDA(cudaStreamSynchronize(stream));
         st.ms_precond_setup = now_ms() - t_begin;
@@ -358,7 +364,8 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     // Mixed precision: FP32 matrix copy, FP32 AMG hierarchy and one FP32 CG recurrence with the
     // solution in FP64 and reliable updates (the iterated residual replaced by the FP64 residual
     // b - A x whenever it has dropped by inner_tolerance); see ReliableCg.
-    if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED)) {
+    if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED &&
+          amg_kcycle == ao.kcycle_levels)) {
         // the throughput path coarsens its small coarse levels by three pairing rounds instead of
         // two (on the 1M-cell system: 9 levels instead of 10, same CG iteration count, 2 % faster);
         // the FP64 drop-in keeps the two-round hierarchy
@@ -367,6 +374,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         amg32.setup(stream, P, val32.p, ao32);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
+        amg_kcycle = ao.kcycle_levels;
     }
     PORSOL_CUDA(cudaStreamSynchronize(stream));
     st.ms_precond_setup = now_ms() - t_begin;
@@ -470,6 +478,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
                 amg64.setup(stream, P, val.p, ao);
                 amg_ready = true;
                 amg_precision = PORSOL_FP64;
+                amg_kcycle = 0;
             }
             st.amg_levels = amg64.levels();
             M = &amg64;
@@ -490,6 +499,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
         amg32.setup(stream, P, val32.p, ao);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
+        amg_kcycle = 0;
     }
     PORSOL_CUDA(cudaStreamSynchronize(stream));
     st.ms_precond_setup = now_ms() - t_begin;

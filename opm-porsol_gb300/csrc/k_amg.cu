@@ -1020,6 +1020,121 @@ __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __res
     bc[I] = s;
 }
 
+// ---------------- K-cycle (Krylov-accelerated coarse correction) ----------------
+// y = A x on a level (plain SELL, one thread per row)
+template <class T>
+__global__ void k_lv_spmv(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
+                          const T* __restrict__ x, T* __restrict__ y, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    y[i] = sell_dot<T>(sp, col, A, i, [x](int j) { return x[j]; });
+}
+
+// Up to three dot products a_d . b_d at once (null pairs skipped): per block partial sums
+// (FP64 per warp, fixed order) into part[3 * block + d]; a one-block kernel finishes them.
+template <class T>
+__global__ void __launch_bounds__(256) k_kdots(int n, const T* __restrict__ a0, const T* __restrict__ b0,
+                                               const T* __restrict__ a1, const T* __restrict__ b1,
+                                               const T* __restrict__ a2, const T* __restrict__ b2,
+                                               double* __restrict__ part, const int* stop)
+{
+    if (*stop) return;
+    __shared__ double sh[3][8];
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        v[0] += double(a0[i]) * double(b0[i]);
+        if (a1) v[1] += double(a1[i]) * double(b1[i]);
+        if (a2) v[2] += double(a2[i]) * double(b2[i]);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
+        if (lane == 0) sh[d][w] = v[d];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int k = 0; k < int(blockDim.x >> 5); ++k) t += sh[threadIdx.x][k];
+        part[3 * blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// Finish the dots (block partials summed in block order) and form the coefficients, in c[0..7]
+// of the level: step 1 (c1 = B b, v1 = A c1): rho1 = c1.v1, alpha1 = c1.b, a = alpha1 / rho1;
+// step 2 (c2 = B r2, v2 = A c2, r2 = b - a v1): gamma = c2.v1, beta = c2.v2, alpha2 = c2.r2,
+// rho2 = beta - gamma^2 / rho1, x = k1 c1 + k2 c2 with k2 = alpha2 / rho2,
+// k1 = a - gamma k2 / rho1 (the flexible-CG iterate after two steps).  A non-positive curvature
+// falls back to one step (k2 = 0) or to the plain cycle (k1 = 1).
+__global__ void k_kfinish(int nblocks, const double* __restrict__ part, double* __restrict__ c, int step,
+                          const int* stop)
+{
+    if (*stop) return;
+    __shared__ double sh[3][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] += part[3 * b + d];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
+        if (lane == 0) sh[d][w] = v[d];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < int(blockDim.x >> 5); ++k)
+        for (int d = 0; d < 3; ++d) t[d] += sh[d][k];
+    if (step == 1) {
+        const double rho1 = t[0], alpha1 = t[1];
+        const bool ok = rho1 > 0.0 && isfinite(rho1) && isfinite(alpha1);
+        c[0] = rho1;
+        c[1] = alpha1;
+        c[2] = ok ? alpha1 / rho1 : 0.0;
+        c[3] = ok ? 1.0 : 0.0;
+    } else {
+        const double rho1 = c[0], a = c[2];
+        const double gamma = t[0], beta = t[1], alpha2 = t[2];
+        double k1 = 1.0, k2 = 0.0;
+        if (c[3] != 0.0) {
+            const double rho2 = beta - gamma * gamma / rho1;
+            if (rho2 > 1e-12 * beta && isfinite(rho2) && isfinite(alpha2)) {
+                k2 = alpha2 / rho2;
+                k1 = a - gamma * k2 / rho1;
+            } else {
+                k1 = a;
+            }
+        }
+        c[4] = k1;
+        c[5] = k2;
+    }
+}
+
+// r2 = b - a v1
+template <class T>
+__global__ void k_kresid(int n, const T* __restrict__ b, const T* __restrict__ v1, const double* __restrict__ c,
+                         T* __restrict__ r2, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r2[i] = T(double(b[i]) - c[2] * double(v1[i]));
+}
+
+// x = k1 c1 + k2 c2
+template <class T>
+__global__ void k_kcombine(int n, const T* __restrict__ c1, const T* __restrict__ c2, const double* __restrict__ c,
+                           T* __restrict__ x, const int* stop)
+{
+    if (*stop) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = T(c[4] * double(c1[i]) + c[5] * double(c2[i]));
+}
+
 // ---------------- coarsest level ----------------
 template <class T>
 __global__ void k_dense_from_sell(int n, const int* __restrict__ sp, const int* __restrict__ col,
@@ -1630,6 +1745,15 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
             }
         }
     }
+    // K-cycle vectors and scalars
+    kcoef_.alloc(8 * size_t(std::max(nlev_, 1)));
+    kcoef_.zero(s);
+    kpart_.alloc(3 * size_t(stride_blocks(lv_[0]->n)));
+    for (int l = 1; l < nlev_; ++l)
+        if (k_level(l)) {
+            Level& K = *lv_[l];
+            for (DBuf<T>* v : {&K.kc1, &K.kc2, &K.kv1, &K.kv2, &K.kr2}) v->alloc(std::max(K.n, 1));
+        }
     Level& C = *lv_[nlev_ - 1];
     PORSOL_REQUIRE(C.n <= 2048, PORSOL_ERR_BAD_ARG, "AMG: coarsening stalled above the dense-solve limit");
     build_coarse_solver(s, *C.P, C.A, C.n);
@@ -1769,10 +1893,37 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
                                   n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop))));
     }
     PORSOL_LAUNCH(k_restrict<T><<<div_up(Nx.n, TB), TB, 0, s>>>(Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop));
-    vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
+    if (k_level(l + 1)) kcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
+    else vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
     // post-smoothing from t + w P xc
     chebyshev(s, L, b, x, false, Nx.x.p, L.agg.agg.p, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, x, false, nullptr, nullptr, stop);
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+// K-cycle on level l (Notay and Vassilevski's Krylov-accelerated multigrid cycle): the level's
+// system A_l x = b is solved by two flexible-CG steps whose preconditioner B is the cycle of
+// level l (itself recursive), instead of one application of B.  Every scalar stays on the device,
+// so the cycle is captured into the CG iteration's graph with the rest.
+template <class T>
+void Amg<T>::kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
+{
+    Level& L = *lv_[l];
+    const int n = L.n, nb = div_up(n, TB);
+    const SellPattern& P = *L.P;
+    const int nd = stride_blocks(n);
+    double* c = kcoef_.p + 8 * l;
+    vcycle(s, l, b, L.kc1.p, stop);
+    PORSOL_LAUNCH(k_lv_spmv<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.kc1.p, L.kv1.p, stop));
+    PORSOL_LAUNCH(k_kdots<T><<<nd, 256, 0, s>>>(n, L.kc1.p, L.kv1.p, L.kc1.p, b, nullptr, nullptr, kpart_.p, stop));
+    PORSOL_LAUNCH(k_kfinish<<<1, 1024, 0, s>>>(nd, kpart_.p, c, 1, stop));
+    PORSOL_LAUNCH(k_kresid<T><<<nb, TB, 0, s>>>(n, b, L.kv1.p, c, L.kr2.p, stop));
+    vcycle(s, l, L.kr2.p, L.kc2.p, stop);
+    PORSOL_LAUNCH(k_lv_spmv<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.kc2.p, L.kv2.p, stop));
+    PORSOL_LAUNCH(k_kdots<T><<<nd, 256, 0, s>>>(n, L.kc2.p, L.kv1.p, L.kc2.p, L.kv2.p, L.kc2.p, L.kr2.p, kpart_.p,
+                                                 stop));
+    PORSOL_LAUNCH(k_kfinish<<<1, 1024, 0, s>>>(nd, kpart_.p, c, 2, stop));
+    PORSOL_LAUNCH(k_kcombine<T><<<nb, TB, 0, s>>>(n, L.kc1.p, L.kc2.p, c, x, stop));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -1781,44 +1932,59 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
 template <class T>
 double Amg<T>::apply_bytes(std::vector<double>* per_level) const
 {
-    const double sx = sizeof(T);
     if (per_level) per_level->assign(size_t(nlev_), 0.0);
-    double total = 0.0;
-    for (int l = 0; l < nlev_; ++l) {
-        double b = 0.0;
-        if (l == nlev_ - 1) {
-            b = double(nc_) * nc_ * 8.0 + 2.0 * nc_ * sx;   // dense inverse, b in, x out
-        } else {
-            const Level& L = *lv_[l];
-            const double n = L.n, nc = lv_[l + 1]->n;
-            const double vb = L.half ? 2.0 : sx, cb = (L.v4 && L.c16) ? 2.0 : 4.0;
-            const double mat = double(L.P->nent) * (vb + cb);
-            const int deg = std::max(1, o_.cheb_degree);
-            // Chebyshev steps of one application: the first from x = 0 after start0 has no x_in
-            auto steps = [&](bool from_zero) {
-                double t = 0.0;
-                for (int k = 1; k <= deg; ++k) {
-                    const bool xin = !(from_zero && k == 1);
-                    t += mat + n * sx * (5.0 + (xin ? 1.0 : 0.0) + (L.half ? 0.0 : 1.0));
-                }
-                return t;
-            };
-            const double start = mat + 5.0 * n * sx;           // t gathered, dinv, b in; r, d out
-            b += 4.0 * n * sx + steps(true);                    // pre-smoothing from zero
-            b += (o_.smooth_steps - 1) * (start + steps(false));
-            b += mat + n * sx * (L.half ? 4.0 : 3.0);            // residual
-            b += n * (sx + 4.0) + nc * (4.0 + sx);               // restriction
-            if (L.lanes == 1)                                    // post-smoothing from t + w P xc
-                b += n * (2.0 * sx + 4.0) + nc * sx + start;
-            else
-                b += start + n * (sx + 4.0) + nc * sx;
-            b += steps(false);
-            b += (o_.smooth_steps - 1) * (start + steps(false));
-        }
-        if (per_level) (*per_level)[size_t(l)] = b;
-        total += b;
+    return nlev_ > 0 ? cycle_bytes(0, per_level) : 0.0;
+}
+
+// bytes of one cycle started on level l (its own kernels, the coarse correction below it)
+template <class T>
+double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level) const
+{
+    const double sx = sizeof(T);
+    double b = 0.0;
+    if (l == nlev_ - 1) {
+        b = double(nc_) * nc_ * 8.0 + 2.0 * nc_ * sx;   // dense inverse, b in, x out
+        if (per_level) (*per_level)[size_t(l)] += b;
+        return b;
     }
-    return total;
+    const Level& L = *lv_[l];
+    const double n = L.n, nc = lv_[l + 1]->n;
+    const double vb = L.half ? 2.0 : sx, cb = (L.v4 && L.c16) ? 2.0 : 4.0;
+    const double mat = double(L.P->nent) * (vb + cb);
+    const int deg = std::max(1, o_.cheb_degree);
+    // Chebyshev steps of one application: the first from x = 0 after start0 has no x_in
+    auto steps = [&](bool from_zero) {
+        double t = 0.0;
+        for (int k = 1; k <= deg; ++k) {
+            const bool xin = !(from_zero && k == 1);
+            t += mat + n * sx * (5.0 + (xin ? 1.0 : 0.0) + (L.half ? 0.0 : 1.0));
+        }
+        return t;
+    };
+    const double start = mat + 5.0 * n * sx;           // t gathered, dinv, b in; r, d out
+    b += 4.0 * n * sx + steps(true);                    // pre-smoothing from zero
+    b += (o_.smooth_steps - 1) * (start + steps(false));
+    b += mat + n * sx * (L.half ? 4.0 : 3.0);            // residual
+    b += n * (sx + 4.0) + nc * (4.0 + sx);               // restriction
+    if (L.lanes == 1)                                    // post-smoothing from t + w P xc
+        b += n * (2.0 * sx + 4.0) + nc * sx + start;
+    else
+        b += start + n * (sx + 4.0) + nc * sx;
+    b += steps(false);
+    b += (o_.smooth_steps - 1) * (start + steps(false));
+    if (per_level) (*per_level)[size_t(l)] += b;
+    double below;
+    if (k_level(l + 1)) {
+        // two cycles of level l + 1, two products with its FP32/FP64 matrix, the dots, r2 and x
+        const Level& C = *lv_[l + 1];
+        const double kb = 2.0 * (double(C.P->nent) * (sx + 4.0) + 2.0 * nc * sx) + 4.0 * nc * sx +
+                          6.0 * nc * sx + 3.0 * nc * sx + 3.0 * nc * sx;
+        if (per_level) (*per_level)[size_t(l + 1)] += kb;
+        below = kb + cycle_bytes(l + 1, per_level) + cycle_bytes(l + 1, per_level);
+    } else {
+        below = cycle_bytes(l + 1, per_level);
+    }
+    return b + below;
 }
 
 template <class T>

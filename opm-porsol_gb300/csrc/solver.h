@@ -58,6 +58,7 @@ struct porsol_solver {
     porsol::Amg<float> amg32;
     bool amg_ready = false;
     int amg_precision = -1;
+    int amg_kcycle = -1;   // the K-cycle levels the hierarchy was set up with
     porsol::DBuf<double> ir_r;   // batched residual
     // the reference numbering's system for the ILU0 path of a renumbered structure:
     // dof permutation, slot sources, values, right-hand side and solution

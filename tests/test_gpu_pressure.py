@@ -130,6 +130,20 @@ def test_solve_matches_oracle(pkg, gpulib, orc, workloads, cart, ltype):
     assert g["stats"].mass_balance < 1e-9
 
 
+@pytest.mark.parametrize("precision,tol,bound", [(0, 1e-12, FP64_TOL), (1, 1e-11, 1e-8)])
+def test_kcycle_type2_matches_oracle(pkg, gpulib, orc, workloads, precision, tol, bound):
+    """linsolver_type 2 (the reference's KAMG, solveLinearSystemKAMG :1609-1666) runs the K-cycle:
+    the same converged answer as the oracle, and no more CG iterations than the V-cycle of type 1
+    on a system deep enough for a K-level (several AMG levels)."""
+    prob = workloads.anisotropic_corey(dims=(40, 30, 20))
+    o = oracle_solve(orc, prob, tol=1e-13, dirichlet_guess=True)
+    k = gpu_solve(pkg, prob, ltype=2, tol=tol, precision=precision)
+    v = gpu_solve(pkg, prob, ltype=1, tol=tol, precision=precision)
+    assert k["stats"].amg_levels >= 3
+    assert rel(k["v"], o["v"]) < bound and rel(k["p"], o["p"]) < bound
+    assert k["stats"].iterations <= v["stats"].iterations, (k["stats"].iterations, v["stats"].iterations)
+
+
 def test_unit_cube_ilu0(pkg, gpulib, orc, workloads):
     """10^3 cells, CG + ILU0 to 1e-10, plain FP64."""
     prob = workloads.unit_cube_lognormal()
