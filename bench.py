@@ -50,6 +50,9 @@ def parse():
                     help="residual reduction of the FP64 solves (1e-8 flux error)")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle process (CPU baseline sample and the full-size oracle comparison)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the other workloads (IMPES, tensor, adjoint, capillary, upscaling) that the "
+                         "default run measures beside the headline")
     ap.add_argument("--oracle-tol", type=float, default=1e-13,
                     help="residual reduction of the full-size FP64 oracle solve the GPU results are compared with")
     ap.add_argument("--oracle-wait", type=float, default=900.0,
@@ -444,6 +447,31 @@ def run_gpu(args):
                 "vcycle_levels": [{"rows": r, "entries": e, "bytes": round(vb)} for r, e, vb in
                                   zip(rows, ents, b["vcycle_levels"])]}
 
+    # The other workloads (IMPES, tensor mobilities, adjoint, ImplicitCapillarity, batched upscaling)
+    # on the GPU while the oracle process is still busy, without their CPU baselines; each runs its
+    # own --flag form and a failure is reported in its slot without touching the headline.
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        import copy
+        secondary = {}
+        sargs = copy.copy(args)
+        sargs.no_cpu_baseline = True
+        sargs.steps, sargs.warmup = 3, 3
+        for name, fn, setup in (("impes_50", run_impes, dict(impes=50)),
+                                ("tensor_1M", run_tensor, {}),
+                                ("adjoint_131k", run_adjoint, {}),
+                                ("capillary_1M", run_capillary, {}),
+                                ("upscale_512", run_upscale, dict(upscale=512))):
+            a = copy.copy(sargs)
+            for k, v in setup.items():
+                setattr(a, k, v)
+            t0 = time.perf_counter()
+            try:
+                secondary[name] = fn(a, quiet=True)
+            except Exception as e:
+                secondary[name] = {"error": repr(e)}
+            secondary[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+
     # CPU baseline and the full-size oracle comparison from the oracle process
     cpu, vs_oracle = None, None
     if orc is not None:
@@ -518,6 +546,7 @@ def run_gpu(args):
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"},
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "secondary": secondary,
         "profile_ms_per_step": {name: round(prof[k][1] / args.steps, 3) for k, name in
                                 enumerate(["spmv64", "spmv32", "assemble", "recover", "vcycle", "cheb_fine"])},
     }
@@ -528,7 +557,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def run_impes(args):
+def run_impes(args, quiet=False):
     """IMPES on the 200x200x25 layered grid: pressure solve every step, then EulerUpstream::transportSolve with
     CFL-limited sub-steps; water (s = 1) enters through x- at Dirichlet p = 1, p = 0 at x+;
     step length 0.1 PV / (nsteps Q_in) with Q_in the inflow of the first pressure solve.
@@ -589,10 +618,12 @@ def run_impes(args):
     out["sat_diff_mixed_vs_fp64"] = {"max_abs": float(np.abs(dsat).max()),
                                      "l2_rel": float(np.linalg.norm(dsat) / np.linalg.norm(sats["fp64"])),
                                      "after_steps": args.impes}
-    print(json.dumps(out), flush=True)
+    if not quiet:
+        print(json.dumps(out), flush=True)
+    return out
 
 
-def run_capillary(args):
+def run_capillary(args, quiet=False):
     """ImplicitCapillarity::transportSolve on the layered grid with two RockJfunc rocks: a step is one
     porsol_capillary_solve with host inputs and output (capillary mobilities, viscous upstream residual,
     the capillary-pressure solve with AMG-CG, the volume-matching root search, the relaxed update).
@@ -676,10 +707,12 @@ def run_capillary(args):
         out["cpu_baseline"] = {"value": round(scale / el, 5), "unit": "capillary steps/s", "cores": 1, "kind": "port",
                                "sample": f"oracle step (ILU0-CG, {cit} its) on the 50x50x25 box of the workload, "
                                          f"{el:.2f} s, scaled by the cell ratio {scale:.4f}"}
-    print(json.dumps(out), flush=True)
+    if not quiet:
+        print(json.dumps(out), flush=True)
+    return out
 
 
-def run_tensor(args):
+def run_tensor(args, quiet=False):
     """The 1M-cell pressure solve of the headline with tensor mobilities: per cell the total mobility
     tensor diag(m, m/2, 2m), m the Corey-2 total mobility at the cell's saturation (lambda_t commutes
     with the diagonal K), so every solve rebuilds the inner products from lambda_t K on the GPU
@@ -723,11 +756,13 @@ def run_tensor(args):
                      "flux_rel_err_vs_fp64_1e-12": float(np.linalg.norm(v - v_ref) / np.linalg.norm(v_ref))}
     out["value"] = out["mixed"]["value"]
     out["speedup_mixed_vs_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
-    print(json.dumps(out), flush=True)
+    if not quiet:
+        print(json.dumps(out), flush=True)
+    return out
     s.close()
 
 
-def run_adjoint(args):
+def run_adjoint(args, quiet=False):
     """Adjoint gradient: d J / d ln k on the 64x64x32 correlated log-normal grid, J = squared
     pressure mismatch at 50 cells + outflux through x+.  A step is one forward solve (AMG-CG,
     host inputs, hierarchy rebuilt) + objective + one adjoint solve + gradient, with the gradient
@@ -786,10 +821,12 @@ def run_adjoint(args):
         out["rel_err_vs_oracle"] = {k: float(np.linalg.norm(v - go) / nrm) for k, v in grads.items()}
         out["cpu_baseline"] = {"value": round(1.0 / el, 4), "unit": "gradients/s", "cores": 1, "kind": "port",
                                "sample": f"one forward + adjoint, ILU0-CG tol {tol}, FP64"}
-    print(json.dumps(out), flush=True)
+    if not quiet:
+        print(json.dumps(out), flush=True)
+    return out
 
 
-def run_upscale(args):
+def run_upscale(args, quiet=False):
     """Batched upscaling: effective permeability of N periodic unit-cube sub-grids (side n ~ U{8..32},
     full log-normal tensors with random axes), three unit pressure-jump solves each, as one
     block-diagonal system on the GPU.  A step is one porsol_upscale_periodic call with host inputs
@@ -851,7 +888,9 @@ def run_upscale(args):
                                "sample": f"{len(pick)} uniformly sampled sub-grids of the batch, ILU0-CG tol "
                                          f"{args.tol64}, 3 solves each"}
         out["max_rel_diff_fp64_vs_oracle_sample"] = err
-    print(json.dumps(out), flush=True)
+    if not quiet:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
