@@ -523,6 +523,13 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     std::fill(h.begin(), h.end(), o.residual_tolerance);
     upload(btol, h);
     CgResult r = bcg64.solve(stream, P, val.p, cast_pre, batch, rhs.p, x.p, btol.p, maxit);
+    // the FP32 hierarchy's finest level may run the bulk-staged smoother step: its status bits say
+    // whether every staged copy arrived (as after the single-system mixed solve)
+    if (const int ast = amg32.solve_status(stream)) {
+        amg_ready = false;   // the next solve sets the hierarchy (and its status) up again
+        throw Error((ast & ST_TIMEOUT) ? PORSOL_ERR_TIMEOUT : PORSOL_ERR_BAD_ARG,
+                    "AMG smoother: bulk copy of the matrix slices failed (wait gave up or staging area too small)");
+    }
     st.iterations = r.iterations;
     st.outer_iterations = 1;
     st.reduction = r.reduction;

@@ -694,10 +694,11 @@ template <class T>
 __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ r,
                               T* __restrict__ d, T inv_theta, const int* stop)
 {
-    if (*stop) return;
+    const int stopped = *stop;   // read beside the data; checked before the first store
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const T ri = dinv[i] * b[i];
+    if (stopped) return;
     r[i] = ri;
     d[i] = ri * inv_theta;
 }
@@ -732,7 +733,15 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
                              T* __restrict__ d, T inv_theta, const int* stop)
 {
-    if (*stop) return;
+    // small levels: the stop flag is read beside the row's loads and checked before the first
+    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
+    // first (keeps them at 32 registers)
+    int stopped = 0;
+    if constexpr (K <= 0) {
+        if (*stop) return;
+    } else {
+        stopped = *stop;
+    }
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
@@ -746,7 +755,7 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
     } else {
         acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [t](int j) { return t[j]; });
     }
-    if (!valid || q != 0) return;
+    if (!valid || q != 0 || stopped) return;
     if (xc) {
         const int ai = agg[i];
         x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
@@ -761,11 +770,13 @@ template <class T>
 __global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
                               T wp, T* __restrict__ y, const int* stop)
 {
-    if (*stop) return;
+    const int stopped = *stop;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int ai = agg[i];
-    y[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
+    const T yi = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
+    if (stopped) return;
+    y[i] = yi;
 }
 
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
@@ -775,13 +786,21 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restr
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
                             T* x_out, T c1, T c2, int final_step, const int* stop)
 {
-    if (*stop) return;
+    // small levels: the stop flag is read beside the row's loads and checked before the first
+    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
+    // first (keeps them at 32 registers)
+    int stopped = 0;
+    if constexpr (K <= 0) {
+        if (*stop) return;
+    } else {
+        stopped = *stop;
+    }
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
-    if (!valid || q != 0) return;
+    if (!valid || q != 0 || stopped) return;
     const T di = d_in[i];
     T xi = (x_in ? x_in[i] : T(0)) + di;
     const T ri = SCALED ? r[i] - acc : r[i] - dinv[i] * acc;
@@ -829,11 +848,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned long lo
     return false;
 }
 
-// Dynamic shared memory: 128 bytes for the warps' barriers, then BULK_SLICES column areas of cap
-// entries (sizeof(CI) B each: 4 for columns, 2 for 16-bit column offsets), then BULK_SLICES value
-// areas (2 B each).  cap and the slice offsets are multiples of 128 entries, so every copy starts
-// and ends on a 16-byte boundary.  extra_tx (0 in solves) adds bytes the barrier waits for that no
-// copy delivers: the self-test of the timeout path.
+// Dynamic shared memory: 128 bytes for the warps' barriers (per warp one the copies complete on,
+// and one gate used only by the self-test), then BULK_SLICES column areas of cap entries
+// (sizeof(CI) B each: 4 for columns, 2 for 16-bit column offsets), then BULK_SLICES value areas
+// (2 B each).  cap and the slice offsets are multiples of 128 entries, so every copy starts and
+// ends on a 16-byte boundary.  extra_tx (0 in solves) makes the gate barrier wait for bytes that
+// no copy delivers: the self-test of the timeout path, whose copies still complete on their own
+// barrier, so the warp sees them land before it leaves.
 template <class CI>
 __device__ __forceinline__ int4 x4_columns(const CI* p, int row);
 template <>
@@ -867,14 +888,18 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
         return;
     }
     const unsigned bar = smem_u32(smem + 8 * w);
+    const unsigned gate = smem_u32(smem + 64 + 8 * w);
     CI* scol = reinterpret_cast<CI*>(smem + 128) + size_t(w) * cap;
     __half* sval = reinterpret_cast<__half*>(smem + 128 + size_t(BULK_SLICES) * cap * CB) + size_t(w) * cap;
     if (lane == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        if (extra_tx) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(gate) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                     "r"(unsigned(ne) * (CB + 2u) + extra_tx)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(unsigned(ne) * (CB + 2u))
                      : "memory");
+        if (extra_tx)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(gate), "r"(extra_tx)
+                         : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                          smem_u32(scol)),
                      "l"(col4 + e0), "r"(unsigned(ne) * CB), "r"(bar)
@@ -885,7 +910,7 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
                      : "memory");
     }
     __syncwarp();
-    if (!mbar_wait_bounded(bar, BULK_WAIT_NS)) {
+    if (!((extra_tx == 0 || mbar_wait_bounded(gate, BULK_WAIT_NS)) && mbar_wait_bounded(bar, BULK_WAIT_NS))) {
         if (lane == 0) atomicOr(status, ST_TIMEOUT);
         mbar_wait_bounded(bar, BULK_WAIT_NS);  // the copies themselves may still be in flight
         return;
@@ -922,13 +947,21 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const CI* __restrict_
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
                         const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
-    if (*stop) return;
+    // small levels: the stop flag is read beside the row's loads and checked before the first
+    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
+    // first (keeps them at 32 registers)
+    int stopped = 0;
+    if constexpr (K <= 0) {
+        if (*stop) return;
+    } else {
+        stopped = *stop;
+    }
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
-    if (!valid || q != 0) return;
+    if (!valid || q != 0 || stopped) return;
     r[i] = SCALED ? b[i] - diagv[i] * acc : b[i] - acc;
 }
 
@@ -1012,11 +1045,12 @@ template <class T>
 __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __restrict__ idx, const T* __restrict__ r,
                            T* __restrict__ bc, const int* stop)
 {
-    if (*stop) return;
+    const int stopped = *stop;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= nc) return;
     T s = 0;
     for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
+    if (stopped) return;
     bc[I] = s;
 }
 
@@ -1228,7 +1262,7 @@ template <class T>
 __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
                               const int* stop)
 {
-    if (*stop) return;
+    const int stopped = *stop;   // uniform over the grid; checked before the store
     extern __shared__ double sb[];
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
     __syncthreads();
@@ -1241,7 +1275,7 @@ __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* _
     for (int j = lane; j < n; j += 32) s += Dinv[(size_t)i * n + j] * sb[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[i] = T(s);
+    if (lane == 0 && !stopped) x[i] = T(s);
 }
 
 int read_int(cudaStream_t s, const int* d)
