@@ -498,55 +498,70 @@ __global__ void k_gal_woff(int nc, const int* __restrict__ ptr, const int* __res
     }
 }
 
-// Pass 1, one thread per fine row (consecutive rows read consecutive SELL entries): the row's
-// entries with their columns mapped through agg (-1: an isolated column, no coupling) written to
-// its aggregate's candidate segment.  Rows outside every aggregate (isolated) are skipped.
-template <class T>
+// Pass 1, K lanes per fine row (K = 1 on the finest levels: consecutive rows read consecutive SELL
+// entries; up to 16 on coarse levels of long rows, as the matching sweeps): the row's entries with
+// their columns mapped through agg (-1: an isolated column, no coupling) written to its aggregate's
+// candidate segment.  Rows outside every aggregate (isolated) are skipped.
+template <class T, int K>
 __global__ void k_gal_cand(int n, const int* __restrict__ sp, const int* __restrict__ col,
                            const int* __restrict__ rowlen, const T* __restrict__ A, const int* __restrict__ agg,
                            const int* __restrict__ woff, int* __restrict__ ckey, T* __restrict__ cval)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i, q;
+    row_lane<K>(i, q);
     if (i >= n || agg[i] < 0) return;
     const int w = woff[i], len = rowlen[i];
     const int b = sp[i >> 5] + (i & 31);
-    for (int t = 0; t < len; ++t) {
+    for (int t = q; t < len; t += K) {
         const int k = b + 32 * t;
         ckey[w + t] = agg[col[k]];
         cval[w + t] = A[k];
     }
 }
 
-// Pass 2, one warp per coarse row: the candidates [goff[I], goff[I+1]) in chunks of 32 (one per
-// lane).  Equal columns of a chunk are found with __match_any_sync; the lowest lane of each group
-// sums the group's values in lane order (FP64) and adds the sum to the column's entry of the row's
-// list (found by a scan of the list, or appended in lane order when new).  The list (first-occurrence
-// order) is written over the row's own segment, with its length and the diagonal's position.
-// Every sum has a fixed order, so the product is run-to-run reproducible.  Shared memory per warp:
-// cap column and cap FP64 entries of the list, 32 FP64 staging values.
+// Pass 2, L lanes per coarse row (L = 16: two rows per warp, or 32): the candidates
+// [goff[I], goff[I+1]) in chunks of L (one per lane).  Equal columns of a chunk are found with
+// __match_any_sync on (row in the warp, column); the lowest lane of each group sums the group's values
+// in lane order (FP64) and adds the sum to the column's entry of the row's list (found by a scan of
+// the list, or appended in lane order when new).  The list (first-occurrence order) is written over
+// the row's own segment, with its length and the diagonal's position.  Every sum has a fixed order,
+// so the product is run-to-run reproducible.  Shared memory per warp: 32 FP64 staging values and,
+// per row, cap columns and cap FP64 entries of the list.
 constexpr int GD_WARPS = 4;
-template <class T>
+template <class T, int L>
 __global__ void __launch_bounds__(GD_WARPS * 32) k_gal_dedup(int nc, int cap, const int* __restrict__ goff,
                                                             int* __restrict__ tcol, T* __restrict__ tval,
                                                             int* __restrict__ rowlen_c, int* __restrict__ dpos,
                                                             int* __restrict__ status)
 {
+    constexpr int R = 32 / L;   // rows per warp
     extern __shared__ __align__(16) unsigned char gd_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int I = blockIdx.x * GD_WARPS + w;
-    if (I >= nc) return;   // warp-uniform
-    double* stage = reinterpret_cast<double*>(gd_smem) + w * (32 + cap);
-    double* lsum = stage + 32;
-    int* lkey = reinterpret_cast<int*>(reinterpret_cast<double*>(gd_smem) + GD_WARPS * (32 + cap)) + w * cap;
-    const int b = goff[I], e = goff[I + 1];
+    const int sub = lane / L, sl = lane % L;
+    const int I0 = (blockIdx.x * GD_WARPS + w) * R;
+    if (I0 >= nc) return;   // warp-uniform
+    const int I = I0 + sub;
+    const bool row = I < nc;
+    double* stage = reinterpret_cast<double*>(gd_smem) + w * (32 + R * cap);
+    double* lsum = stage + 32 + sub * cap;
+    int* lkey = reinterpret_cast<int*>(reinterpret_cast<double*>(gd_smem) + GD_WARPS * (32 + R * cap)) +
+                (w * R + sub) * cap;
+    const int b = row ? goff[I] : 0, e = row ? goff[I + 1] : 0;
+    // chunks of the warp: the most any of its rows needs
+    int nch = (e - b + L - 1) / L;
+#pragma unroll
+    for (int o = 16; o >= L; o >>= 1) nch = max(nch, __shfl_xor_sync(0xffffffffu, nch, o));
+    const unsigned rowmask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << (sub * L);
     int d = 0;
-    for (int c0 = b; c0 < e; c0 += 32) {
-        const int p = c0 + lane;
+    for (int ch = 0; ch < nch; ++ch) {
+        const int p = b + ch * L + sl;
         const bool valid = p < e;
         const int key = valid ? tcol[p] : -1;
         const bool active = key >= 0;
         stage[lane] = valid ? double(tval[p]) : 0.0;
-        const unsigned peers = __match_any_sync(0xffffffffu, active ? key : -2 - lane);
+        const unsigned long long tag =
+            active ? ((unsigned long long)sub << 32) | unsigned(key) : (1ull << 63) | unsigned(lane);
+        const unsigned peers = __match_any_sync(0xffffffffu, tag);
         const bool leader = active && (__ffs(peers) - 1) == lane;
         __syncwarp();
         double csum = 0.0;
@@ -559,7 +574,7 @@ __global__ void __launch_bounds__(GD_WARPS * 32) k_gal_dedup(int nc, int cap, co
                     break;
                 }
         }
-        const unsigned fresh = __ballot_sync(0xffffffffu, leader && at < 0);
+        const unsigned fresh = __ballot_sync(0xffffffffu, leader && at < 0) & rowmask;
         if (leader) {
             if (at < 0) {
                 at = d + __popc(fresh & ((1u << lane) - 1u));
@@ -577,14 +592,15 @@ __global__ void __launch_bounds__(GD_WARPS * 32) k_gal_dedup(int nc, int cap, co
         __syncwarp();
     }
     int dp = -1;
-    for (int q = lane; q < d; q += 32) {
-        tcol[b + q] = lkey[q];
-        tval[b + q] = T(lsum[q]);
-        if (lkey[q] == I) dp = q;
-    }
+    if (row)
+        for (int q = sl; q < d; q += L) {
+            tcol[b + q] = lkey[q];
+            tval[b + q] = T(lsum[q]);
+            if (lkey[q] == I) dp = q;
+        }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, o));
-    if (lane == 0) {
+    for (int o = L / 2; o > 0; o >>= 1) dp = max(dp, __shfl_xor_sync(0xffffffffu, dp, o));
+    if (row && sl == 0) {
         rowlen_c[I] = d;
         dpos[I] = dp;
     }
@@ -694,11 +710,10 @@ template <class T>
 __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ r,
                               T* __restrict__ d, T inv_theta, const int* stop)
 {
-    const int stopped = *stop;   // read beside the data; checked before the first store
+    if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const T ri = dinv[i] * b[i];
-    if (stopped) return;
     r[i] = ri;
     d[i] = ri * inv_theta;
 }
@@ -733,15 +748,7 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
                              T* __restrict__ d, T inv_theta, const int* stop)
 {
-    // small levels: the stop flag is read beside the row's loads and checked before the first
-    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
-    // first (keeps them at 32 registers)
-    int stopped = 0;
-    if constexpr (K <= 0) {
-        if (*stop) return;
-    } else {
-        stopped = *stop;
-    }
+    if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
@@ -755,7 +762,7 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
     } else {
         acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [t](int j) { return t[j]; });
     }
-    if (!valid || q != 0 || stopped) return;
+    if (!valid || q != 0) return;
     if (xc) {
         const int ai = agg[i];
         x[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
@@ -770,13 +777,11 @@ template <class T>
 __global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
                               T wp, T* __restrict__ y, const int* stop)
 {
-    const int stopped = *stop;
+    if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int ai = agg[i];
-    const T yi = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
-    if (stopped) return;
-    y[i] = yi;
+    y[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
 }
 
 // x_out = x_in + d_in; r -= D^-1 A d_in; d_out = c1 d_in + c2 r; final: x_out += d_out
@@ -786,21 +791,13 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restr
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
                             T* x_out, T c1, T c2, int final_step, const int* stop)
 {
-    // small levels: the stop flag is read beside the row's loads and checked before the first
-    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
-    // first (keeps them at 32 registers)
-    int stopped = 0;
-    if constexpr (K <= 0) {
-        if (*stop) return;
-    } else {
-        stopped = *stop;
-    }
+    if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
-    if (!valid || q != 0 || stopped) return;
+    if (!valid || q != 0) return;
     const T di = d_in[i];
     T xi = (x_in ? x_in[i] : T(0)) + di;
     const T ri = SCALED ? r[i] - acc : r[i] - dinv[i] * acc;
@@ -947,21 +944,13 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const CI* __restrict_
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
                         const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
-    // small levels: the stop flag is read beside the row's loads and checked before the first
-    // store (one dependent load less on a latency-bound launch); the SELL-32x4 levels check it
-    // first (keeps them at 32 registers)
-    int stopped = 0;
-    if constexpr (K <= 0) {
-        if (*stop) return;
-    } else {
-        stopped = *stop;
-    }
+    if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
-    if (!valid || q != 0 || stopped) return;
+    if (!valid || q != 0) return;
     r[i] = SCALED ? b[i] - diagv[i] * acc : b[i] - acc;
 }
 
@@ -1045,12 +1034,11 @@ template <class T>
 __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __restrict__ idx, const T* __restrict__ r,
                            T* __restrict__ bc, const int* stop)
 {
-    const int stopped = *stop;
+    if (*stop) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= nc) return;
     T s = 0;
     for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
-    if (stopped) return;
     bc[I] = s;
 }
 
@@ -1262,7 +1250,7 @@ template <class T>
 __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
                               const int* stop)
 {
-    const int stopped = *stop;   // uniform over the grid; checked before the store
+    if (*stop) return;
     extern __shared__ double sb[];
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
     __syncthreads();
@@ -1275,7 +1263,7 @@ __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* _
     for (int j = lane; j < n; j += 32) s += Dinv[(size_t)i * n + j] * sb[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0 && !stopped) x[i] = T(s);
+    if (lane == 0) x[i] = T(s);
 }
 
 int read_int(cudaStream_t s, const int* d)
@@ -1491,14 +1479,23 @@ void Amg<T>::galerkin(cudaStream_t s, const SellPattern& P, const T* A, const Ag
         s_woff_.alloc(std::max(P.n, 1));
         PORSOL_LAUNCH(k_gal_woff<<<div_up(nc, TB), TB, 0, s>>>(nc, a.ptr.p, a.idx.p, P.rowlen.p, s_goff_.p,
                                                                s_woff_.p));
-        PORSOL_LAUNCH(k_gal_cand<T><<<div_up(P.n, TB), TB, 0, s>>>(P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, A,
-                                                                   a.agg.p, s_woff_.p, s_tcol_.p, s_tval_.p));
+        const int cl = pick_lanes(P.n, P.nent);
+        PORSOL_LANES(cl, PORSOL_LAUNCH((k_gal_cand<T, KL><<<div_up((long long)P.n * cl, TB), TB, 0, s>>>(
+                             P.n, P.slice_ptr.p, P.col.p, P.rowlen.p, A, a.agg.p, s_woff_.p, s_tcol_.p, s_tval_.p))));
+        // rows of up to 64 candidates (the finest levels' pairs and quadruples) take half a warp each
         const int cap = std::max(32, (bound + 31) / 32 * 32);
-        const size_t shm = size_t(GD_WARPS) * ((32 + cap) * sizeof(double) + cap * sizeof(int));
-        if (shm > 48 * 1024)
-            PORSOL_CUDA(cudaFuncSetAttribute(k_gal_dedup<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-        PORSOL_LAUNCH(k_gal_dedup<T><<<div_up(nc, GD_WARPS), GD_WARPS * 32, shm, s>>>(
-            nc, cap, s_goff_.p, s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p, status_.p));
+        if (bound <= 64) {
+            const size_t shm = size_t(GD_WARPS) * ((32 + 2 * cap) * sizeof(double) + 2 * cap * sizeof(int));
+            PORSOL_LAUNCH((k_gal_dedup<T, 16><<<div_up(nc, 2 * GD_WARPS), GD_WARPS * 32, shm, s>>>(
+                nc, cap, s_goff_.p, s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p, status_.p)));
+        } else {
+            const size_t shm = size_t(GD_WARPS) * ((32 + cap) * sizeof(double) + cap * sizeof(int));
+            if (shm > 48 * 1024)
+                PORSOL_CUDA(cudaFuncSetAttribute(k_gal_dedup<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 int(shm)));
+            PORSOL_LAUNCH((k_gal_dedup<T, 32><<<div_up(nc, GD_WARPS), GD_WARPS * 32, shm, s>>>(
+                nc, cap, s_goff_.p, s_tcol_.p, s_tval_.p, Pc.rowlen.p, s_dpos_.p, status_.p)));
+        }
     } else {
         const int nb = div_up(nc, 64);
         PORSOL_COUNT_LAUNCH();
