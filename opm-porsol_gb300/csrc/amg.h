@@ -114,13 +114,17 @@ private:
     DBuf<int> tune_stop_;
     DBuf<int> s_maxoff_;   // per level: largest |col - row| of the x4 copy (16-bit offset check)
     void build_coarse_solver(cudaStream_t s, const SellPattern& P, const T* A, int n);
+    // started: the first Chebyshev start from zero (r = D^-1 b, d = r / theta) was already done by
+    // the restriction that produced b (k_restrict_start0)
     void chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
-                   const int* stop);
-    void vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop);
+                   const int* stop, bool started = false);
+    void vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bool started = false);
     // coarse correction of level l - 1 solved on level l by two flexible-CG steps (K-cycle)
-    void kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop);
+    void kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bool started = false);
     bool k_level(int l) const { return l >= 1 && l <= o_.kcycle_levels && l < nlev_ - 1; }
-    double cycle_bytes(int l, std::vector<double>* per_level) const;
+    double cycle_bytes(int l, std::vector<double>* per_level, bool started = false) const;
+    // 1 / theta of the level's Chebyshev interval [lmax / 30, lmax]
+    static double cheb_inv_theta(const Level& L) { return 1.0 / (0.5 * (L.lmax + L.lmax / 30.0)); }
     DBuf<double> kpart_, kcoef_;   // K-cycle dot partials and coefficients (8 per level)
 
     AmgOpts o_;

@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <sstream>
 
 #include "solver.h"
@@ -20,6 +21,34 @@ using namespace porsol;
 namespace porsol {
 
 std::atomic<long long> g_launches{0};
+
+namespace {
+thread_local int t_chain_paused = 0;
+int chain_env()
+{
+    static const int mode = [] {
+        const char* e = std::getenv("PORSOL_PDL");
+        return e && e[0] >= '0' && e[0] <= '2' ? e[0] - '0' : 2;
+    }();
+    return mode;
+}
+}  // namespace
+
+bool chain_enabled(long long blocks)
+{
+    const int m = chain_env();
+    return t_chain_paused == 0 && (m == 1 || (m == 2 && blocks < 304));
+}
+
+ChainPause::ChainPause(bool on) : on_(on)
+{
+    if (on_) ++t_chain_paused;
+}
+
+ChainPause::~ChainPause()
+{
+    if (on_) --t_chain_paused;
+}
 
 cudaEvent_t Profiler::get()
 {

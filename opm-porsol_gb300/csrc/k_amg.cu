@@ -710,6 +710,7 @@ template <class T>
 __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ r,
                               T* __restrict__ d, T inv_theta, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -748,6 +749,7 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
                              T* __restrict__ d, T inv_theta, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
@@ -777,6 +779,7 @@ template <class T>
 __global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
                               T wp, T* __restrict__ y, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -791,6 +794,7 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restr
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
                             T* x_out, T c1, T c2, int final_step, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
@@ -875,6 +879,7 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
 {
     constexpr unsigned CB = sizeof(CI);
     extern __shared__ __align__(128) unsigned char smem[];
+    chain_wait();
     if (*stop) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = blockIdx.x * BULK_SLICES + w;
@@ -944,6 +949,7 @@ __global__ void k_resid(int n, const int* __restrict__ sp, const CI* __restrict_
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
                         const T* __restrict__ x, T* __restrict__ r, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
@@ -1034,6 +1040,7 @@ template <class T>
 __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __restrict__ idx, const T* __restrict__ r,
                            T* __restrict__ bc, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= nc) return;
@@ -1042,12 +1049,32 @@ __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __res
     bc[I] = s;
 }
 
+// k_restrict fused with the coarse level's first Chebyshev start from zero (k_cheb_start0 on bc):
+// the same sums, the same rc and dc
+template <class T>
+__global__ void k_restrict_start0(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
+                                  const T* __restrict__ r, T* __restrict__ bc, const T* __restrict__ dinv_c,
+                                  T* __restrict__ rc, T* __restrict__ dc, T inv_theta, const int* stop)
+{
+    chain_wait();
+    if (*stop) return;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= nc) return;
+    T s = 0;
+    for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
+    bc[I] = s;
+    const T ri = dinv_c[I] * s;
+    rc[I] = ri;
+    dc[I] = ri * inv_theta;
+}
+
 // ---------------- K-cycle (Krylov-accelerated coarse correction) ----------------
 // y = A x on a level (plain SELL, one thread per row)
 template <class T>
 __global__ void k_lv_spmv(int n, const int* __restrict__ sp, const int* __restrict__ col, const T* __restrict__ A,
                           const T* __restrict__ x, T* __restrict__ y, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1062,6 +1089,7 @@ __global__ void __launch_bounds__(256) k_kdots(int n, const T* __restrict__ a0, 
                                                const T* __restrict__ a2, const T* __restrict__ b2,
                                                double* __restrict__ part, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     __shared__ double sh[3][8];
     double v[3] = {0.0, 0.0, 0.0};
@@ -1094,6 +1122,7 @@ __global__ void __launch_bounds__(256) k_kdots(int n, const T* __restrict__ a0, 
 __global__ void k_kfinish(int nblocks, const double* __restrict__ part, double* __restrict__ c, int step,
                           const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     __shared__ double sh[3][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1142,6 +1171,7 @@ template <class T>
 __global__ void k_kresid(int n, const T* __restrict__ b, const T* __restrict__ v1, const double* __restrict__ c,
                          T* __restrict__ r2, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) r2[i] = T(double(b[i]) - c[2] * double(v1[i]));
@@ -1152,6 +1182,7 @@ template <class T>
 __global__ void k_kcombine(int n, const T* __restrict__ c1, const T* __restrict__ c2, const double* __restrict__ c,
                            T* __restrict__ x, const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = T(c[4] * double(c1[i]) + c[5] * double(c2[i]));
@@ -1250,6 +1281,7 @@ template <class T>
 __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
                               const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     extern __shared__ double sb[];
     for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
@@ -1802,7 +1834,7 @@ int Amg<T>::solve_status(cudaStream_t s) const
 //   from_zero: x = p(D^-1 A) D^-1 b;  otherwise from y = x0 (+ w P xc when xc is given).
 template <class T>
 void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zero, const T* xc, const int* agg,
-                       const int* stop)
+                       const int* stop, bool started)
 {
     const int n = L.n;
     const int nb = div_up(n, TB);
@@ -1814,7 +1846,7 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
     T* d = L.d0.p;
     T* dn = L.d1.p;
     if (from_zero) {
-        PORSOL_LAUNCH(k_cheb_start0<T><<<nb, TB, 0, s>>>(n, L.dinv.p, b, L.r.p, d, T(1.0 / theta), stop));
+        if (!started) chain(k_cheb_start0<T>, nb, TB, 0, s, n, L.dinv.p, b, L.r.p, d, T(1.0 / theta), stop);
     } else {
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
@@ -1822,26 +1854,22 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         // levels smoothed one thread per row (the large ones): form y = t + w P xc first, so the
         // start's row dot gathers one vector instead of t, agg and xc (the same y, the same sums)
         if (xc && L.lanes == 1) {
-            PORSOL_LAUNCH(k_prolong_add<T><<<nb, TB, 0, s>>>(n, t, xc, agg, T(o_.prolong), x, stop));
+            chain(k_prolong_add<T>, nb, TB, 0, s, n, t, xc, agg, T(o_.prolong), x, stop);
             t = x;
             xc = nullptr;
         }
         if (L.v4 && L.c16) {
-            PORSOL_LAUNCH((k_cheb_start<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
-                n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p,
-                d, T(1.0 / theta), stop)));
+            chain(k_cheb_start<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p,
+                L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop);
         } else if (L.v4) {
-            PORSOL_LAUNCH((k_cheb_start<T, 0, __half, true><<<nb, TB, 0, s>>>(
-                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p,
-                d, T(1.0 / theta), stop)));
+            chain(k_cheb_start<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b,
+                x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop);
         } else if (L.half) {
-            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, __half, true><<<nbk, TB, 0, s>>>(
-                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg,
-                                      T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop))));
+            PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
+                P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop));
         } else {
-            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_start<T, KL, T, false><<<nbk, TB, 0, s>>>(
-                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg,
-                                      T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop))));
+            PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
+                P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop));
         }
     }
     const int deg = std::max(1, o_.cheb_degree);
@@ -1860,31 +1888,27 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         if (L.bulk_groups > 0 && L.c16) {
             const int cap = 128 * L.bulk_groups;   // entries per slice
             const size_t shm = 128 + size_t(BULK_SLICES) * cap * 4;
-            PORSOL_LAUNCH((k_cheb_step_bulk<T, short><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
-                n, P.nslices, L.sp4.p, L.off4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
-                cap, status_.p, 0u)));
+            chain(k_cheb_step_bulk<T, short>, div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s, n, P.nslices,
+                L.sp4.p, L.off4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, cap,
+                status_.p, 0u);
         } else if (L.bulk_groups > 0) {
             const int cap = 128 * L.bulk_groups;   // entries per slice
             const size_t shm = 128 + size_t(BULK_SLICES) * cap * 6;
-            PORSOL_LAUNCH((k_cheb_step_bulk<T, int><<<div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s>>>(
-                n, P.nslices, L.sp4.p, L.col4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop,
-                cap, status_.p, 0u)));
+            chain(k_cheb_step_bulk<T, int>, div_up(P.nslices, BULK_SLICES), BULK_SLICES * 32, shm, s, n, P.nslices,
+                L.sp4.p, L.col4.p, L.ah4.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, cap,
+                status_.p, 0u);
         } else if (L.v4 && L.c16) {
-            PORSOL_LAUNCH((k_cheb_step<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
-                n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
-                k == deg ? 1 : 0, stop)));
+            chain(k_cheb_step<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p,
+                L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop);
         } else if (L.v4) {
-            PORSOL_LAUNCH((k_cheb_step<T, 0, __half, true><<<nb, TB, 0, s>>>(
-                n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2),
-                k == deg ? 1 : 0, stop)));
+            chain(k_cheb_step<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p,
+                xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop);
         } else if (L.half) {
-            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, __half, true><<<nbk, TB, 0, s>>>(
-                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x,
-                                      T(c1), T(c2), k == deg ? 1 : 0, stop))));
+            PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
+                P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop));
         } else {
-            PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, T, false><<<nbk, TB, 0, s>>>(
-                                      n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x,
-                                      T(c1), T(c2), k == deg ? 1 : 0, stop))));
+            PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
+                P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop));
         }
         if (prof_here) prof_->end(s, PK_CHEB, bytes, ev);
         rho = rho1;
@@ -1894,11 +1918,11 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
 }
 
 template <class T>
-void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
+void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bool started)
 {
     if (l == nlev_ - 1) {
         if (nc_ > 0)
-            PORSOL_LAUNCH(k_dense_apply<T><<<div_up(nc_, 8), 256, nc_ * sizeof(double), s>>>(nc_, cinv_.p, b, x, stop));
+            chain(k_dense_apply<T>, div_up(nc_, 8), 256, nc_ * sizeof(double), s, nc_, cinv_.p, b, x, stop);
         return;
     }
     Level& L = *lv_[l];
@@ -1907,25 +1931,32 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
     const int nb = div_up(n, TB);
     const SellPattern& P = *L.P;
     // pre-smoothing into t
-    chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop);
+    chebyshev(s, L, b, L.t.p, true, nullptr, nullptr, stop, started);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, L.t.p, false, nullptr, nullptr, stop);
     // restrict the residual
     if (L.v4 && L.c16) {
-        PORSOL_LAUNCH((k_resid<T, -1, __half, true, short><<<nb, TB, 0, s>>>(
-            n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.diagv.p, b, L.t.p, L.r.p, stop)));
+        chain(k_resid<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.diagv.p, b,
+            L.t.p, L.r.p, stop);
     } else if (L.v4) {
-        PORSOL_LAUNCH((k_resid<T, 0, __half, true><<<nb, TB, 0, s>>>(n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.diagv.p,
-                                                                      b, L.t.p, L.r.p, stop)));
+        chain(k_resid<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.diagv.p, b, L.t.p,
+            L.r.p, stop);
     } else if (L.half) {
-        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL, __half, true><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
-                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop))));
+        PORSOL_LANES(L.lanes, chain(k_resid<T, KL, __half, true>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
+            P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop));
     } else {
-        PORSOL_LANES(L.lanes, PORSOL_LAUNCH((k_resid<T, KL, T, false><<<div_up(n * L.lanes, TB), TB, 0, s>>>(
-                                  n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop))));
+        PORSOL_LANES(L.lanes, chain(k_resid<T, KL, T, false>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
+            P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop));
     }
-    PORSOL_LAUNCH(k_restrict<T><<<div_up(Nx.n, TB), TB, 0, s>>>(Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop));
-    if (k_level(l + 1)) kcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
-    else vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop);
+    // the coarse level's cycle starts with a Chebyshev start from zero on Nx.b (its first cycle
+    // under a K-cycle): done here, in the restriction; the coarsest level solves directly
+    const bool fuse = l + 1 < nlev_ - 1;
+    if (fuse)
+        chain(k_restrict_start0<T>, div_up(Nx.n, TB), TB, 0, s, Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p,
+              Nx.dinv.p, Nx.r.p, Nx.d0.p, T(cheb_inv_theta(Nx)), stop);
+    else
+        chain(k_restrict<T>, div_up(Nx.n, TB), TB, 0, s, Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop);
+    if (k_level(l + 1)) kcycle(s, l + 1, Nx.b.p, Nx.x.p, stop, fuse);
+    else vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop, fuse);
     // post-smoothing from t + w P xc
     chebyshev(s, L, b, x, false, Nx.x.p, L.agg.agg.p, stop);
     for (int k = 1; k < o_.smooth_steps; ++k) chebyshev(s, L, b, x, false, nullptr, nullptr, stop);
@@ -1937,24 +1968,23 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
 // level l (itself recursive), instead of one application of B.  Every scalar stays on the device,
 // so the cycle is captured into the CG iteration's graph with the rest.
 template <class T>
-void Amg<T>::kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop)
+void Amg<T>::kcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bool started)
 {
     Level& L = *lv_[l];
     const int n = L.n, nb = div_up(n, TB);
     const SellPattern& P = *L.P;
     const int nd = stride_blocks(n);
     double* c = kcoef_.p + 8 * l;
-    vcycle(s, l, b, L.kc1.p, stop);
-    PORSOL_LAUNCH(k_lv_spmv<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.kc1.p, L.kv1.p, stop));
-    PORSOL_LAUNCH(k_kdots<T><<<nd, 256, 0, s>>>(n, L.kc1.p, L.kv1.p, L.kc1.p, b, nullptr, nullptr, kpart_.p, stop));
-    PORSOL_LAUNCH(k_kfinish<<<1, 1024, 0, s>>>(nd, kpart_.p, c, 1, stop));
-    PORSOL_LAUNCH(k_kresid<T><<<nb, TB, 0, s>>>(n, b, L.kv1.p, c, L.kr2.p, stop));
+    vcycle(s, l, b, L.kc1.p, stop, started);
+    chain(k_lv_spmv<T>, nb, TB, 0, s, n, P.slice_ptr.p, P.col.p, L.A, L.kc1.p, L.kv1.p, stop);
+    chain(k_kdots<T>, nd, 256, 0, s, n, L.kc1.p, L.kv1.p, L.kc1.p, b, nullptr, nullptr, kpart_.p, stop);
+    chain(k_kfinish, 1, 1024, 0, s, nd, kpart_.p, c, 1, stop);
+    chain(k_kresid<T>, nb, TB, 0, s, n, b, L.kv1.p, c, L.kr2.p, stop);
     vcycle(s, l, L.kr2.p, L.kc2.p, stop);
-    PORSOL_LAUNCH(k_lv_spmv<T><<<nb, TB, 0, s>>>(n, P.slice_ptr.p, P.col.p, L.A, L.kc2.p, L.kv2.p, stop));
-    PORSOL_LAUNCH(k_kdots<T><<<nd, 256, 0, s>>>(n, L.kc2.p, L.kv1.p, L.kc2.p, L.kv2.p, L.kc2.p, L.kr2.p, kpart_.p,
-                                                 stop));
-    PORSOL_LAUNCH(k_kfinish<<<1, 1024, 0, s>>>(nd, kpart_.p, c, 2, stop));
-    PORSOL_LAUNCH(k_kcombine<T><<<nb, TB, 0, s>>>(n, L.kc1.p, L.kc2.p, c, x, stop));
+    chain(k_lv_spmv<T>, nb, TB, 0, s, n, P.slice_ptr.p, P.col.p, L.A, L.kc2.p, L.kv2.p, stop);
+    chain(k_kdots<T>, nd, 256, 0, s, n, L.kc2.p, L.kv1.p, L.kc2.p, L.kv2.p, L.kc2.p, L.kr2.p, kpart_.p, stop);
+    chain(k_kfinish, 1, 1024, 0, s, nd, kpart_.p, c, 2, stop);
+    chain(k_kcombine<T>, nb, TB, 0, s, n, L.kc1.p, L.kc2.p, c, x, stop);
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -1969,7 +1999,7 @@ double Amg<T>::apply_bytes(std::vector<double>* per_level) const
 
 // bytes of one cycle started on level l (its own kernels, the coarse correction below it)
 template <class T>
-double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level) const
+double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level, bool started) const
 {
     const double sx = sizeof(T);
     double b = 0.0;
@@ -1993,10 +2023,12 @@ double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level) const
         return t;
     };
     const double start = mat + 5.0 * n * sx;           // t gathered, dinv, b in; r, d out
-    b += 4.0 * n * sx + steps(true);                    // pre-smoothing from zero
+    // pre-smoothing from zero: dinv (and b unless the restriction fused the start) in; r, d out
+    b += (started ? 3.0 : 4.0) * n * sx + steps(true);
     b += (o_.smooth_steps - 1) * (start + steps(false));
     b += mat + n * sx * (L.half ? 4.0 : 3.0);            // residual
     b += n * (sx + 4.0) + nc * (4.0 + sx);               // restriction
+    const bool fuse = l + 1 < nlev_ - 1;                 // the coarse start is done by the restriction
     if (L.lanes == 1)                                    // post-smoothing from t + w P xc
         b += n * (2.0 * sx + 4.0) + nc * sx + start;
     else
@@ -2011,9 +2043,9 @@ double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level) const
         const double kb = 2.0 * (double(C.P->nent) * (sx + 4.0) + 2.0 * nc * sx) + 4.0 * nc * sx +
                           6.0 * nc * sx + 3.0 * nc * sx + 3.0 * nc * sx;
         if (per_level) (*per_level)[size_t(l + 1)] += kb;
-        below = kb + cycle_bytes(l + 1, per_level) + cycle_bytes(l + 1, per_level);
+        below = kb + cycle_bytes(l + 1, per_level, fuse) + cycle_bytes(l + 1, per_level);
     } else {
-        below = cycle_bytes(l + 1, per_level);
+        below = cycle_bytes(l + 1, per_level, fuse);
     }
     return b + below;
 }
@@ -2022,6 +2054,7 @@ template <class T>
 void Amg<T>::apply(cudaStream_t s, const T* r, T* z, const int* stop)
 {
     const bool prof_here = prof_ && prof_->on;
+    ChainPause plain(prof_here);   // events between the kernels time each one
     cudaEvent_t ev = nullptr;
     if (prof_here) prof_->begin(s, PK_VCYCLE, 0.0, &ev);
     vcycle(s, 0, r, z, stop);

@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(RB) k_cg_init(int n, const int* __restrict__ s
                                                 const T* __restrict__ b, T* __restrict__ r, CgDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
 {
+    chain_wait();
     T v = 0;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
         const T ri = b[i] - sell_row(sp, col, val, x, i);
@@ -146,6 +147,7 @@ template <class T>
 __global__ void __launch_bounds__(RB) k_dot_zr(int n, const T* __restrict__ z, const T* __restrict__ r, CgDev* st,
                                                double* partial, unsigned int* counter)
 {
+    chain_wait();
     if (st->stop) return;
     T v = 0;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += z[i] * r[i];
@@ -159,6 +161,7 @@ __global__ void __launch_bounds__(RB) k_dot_zr(int n, const T* __restrict__ z, c
 template <class T>
 __global__ void k_first_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st)
 {
+    chain_wait();
     if (st->stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = z[i];
@@ -172,6 +175,7 @@ __global__ void __launch_bounds__(RB) k_spmv_pq(int n, const int* __restrict__ s
                                                 T* __restrict__ q, CgDev* st, double* partial,
                                                 unsigned int* counter)
 {
+    chain_wait();
     if (st->stop) return;
     T v = 0;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
@@ -192,6 +196,7 @@ __global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* _
                                                   const T* __restrict__ p, const T* __restrict__ q, CgDev* st,
                                                   double* partial, unsigned int* counter, CgHostView* hv)
 {
+    chain_wait();
     if (st->stop) return;
     const double alpha = st->alpha;
     const T lambda = T(st->lambda);
@@ -224,6 +229,7 @@ __global__ void __launch_bounds__(RB) k_cg_update(int n, T* __restrict__ x, T* _
 template <class T>
 __global__ void k_cg_direction(int n, const T* __restrict__ z, T* __restrict__ p, CgDev* st)
 {
+    chain_wait();
     if (st->stop) return;
     const T beta = T(st->beta);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -291,6 +297,7 @@ __global__ void __launch_bounds__(RB) k_rc_init(int n, const int* __restrict__ s
                                                 const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
 {
+    chain_wait();
     double v = 0.0;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
         const double ri = b[i] - sell_row(sp, col, val, x, i);
@@ -315,6 +322,7 @@ __global__ void __launch_bounds__(RB) k_rc_init(int n, const int* __restrict__ s
 __global__ void k_rc_rescale(int n, const double* __restrict__ r64, float* __restrict__ r, float* __restrict__ p,
                              const RcDev* st, int init)
 {
+    chain_wait();
     if (st->stop || !(init || st->replace)) return;
     const double is = st->isig;
     const float f = float(st->factor);
@@ -331,6 +339,7 @@ __global__ void __launch_bounds__(RB) k_rc_pq(int n, const int* __restrict__ sp,
                                               float* __restrict__ q, RcDev* st, double* partial,
                                               unsigned int* counter, CgHostView* hv)
 {
+    chain_wait();
     if (st->stop) return;
     float v = 0.0f;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
@@ -357,6 +366,7 @@ __global__ void __launch_bounds__(RB) k_rc_update(int n, double* __restrict__ x,
                                                   RcDev* st, double* partial, unsigned int* counter,
                                                   CgHostView* hv)
 {
+    chain_wait();
     if (st->stop) return;
     const double sa = st->sigma * st->alpha;
     const float a = float(st->alpha);
@@ -389,6 +399,7 @@ __global__ void __launch_bounds__(RB) k_rc_true(int n, const int* __restrict__ s
                                                 const double* __restrict__ b, double* __restrict__ r64, RcDev* st,
                                                 double* partial, unsigned int* counter, CgHostView* hv)
 {
+    chain_wait();
     if (st->stop || !st->replace) return;
     double v = 0.0;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) {
@@ -424,6 +435,7 @@ __global__ void __launch_bounds__(RB) k_rc_true(int n, const int* __restrict__ s
 __global__ void __launch_bounds__(RB) k_rc_zr(int n, const float* __restrict__ z, const float* __restrict__ r,
                                               RcDev* st, double* partial, unsigned int* counter, int init)
 {
+    chain_wait();
     if (st->stop) return;
     float v = 0.0f;
     for (int i = blockIdx.x * RB + threadIdx.x; i < n; i += gridDim.x * RB) v += z[i] * r[i];
@@ -438,6 +450,7 @@ __global__ void __launch_bounds__(RB) k_rc_zr(int n, const float* __restrict__ z
 // p = z + beta p (beta = 0 at the start)
 __global__ void k_rc_direction(int n, const float* __restrict__ z, float* __restrict__ p, const RcDev* st, int init)
 {
+    chain_wait();
     if (st->stop) return;
     const float beta = float(st->beta);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -492,6 +505,7 @@ __global__ void k_ilu_lower_level(int nrows, const int* __restrict__ rows, const
                                   const double* __restrict__ lu, const double* __restrict__ r, double* __restrict__ z,
                                   const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nrows) return;
@@ -507,6 +521,7 @@ __global__ void k_ilu_upper_level(int nrows, const int* __restrict__ rows, const
                                   const int* __restrict__ diag, const double* __restrict__ lu, double* __restrict__ z,
                                   const int* stop)
 {
+    chain_wait();
     if (*stop) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nrows) return;
@@ -595,18 +610,17 @@ void PcgSolver<TV, T>::iteration(cudaStream_t s, const SellPattern& P, const TV*
         cudaEvent_t ev = nullptr;
         if (pf) prof->begin(s, prof_kernel, spmv_bytes, &ev);
         if (P.has_off16())
-            PORSOL_LAUNCH(k_spmv_pq<TV, T, short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val, p_.p, q_.p,
-                                                                    st_.p, red_.partial.p, red_.counter.p));
+            chain(k_spmv_pq<TV, T, short>, nr, RB, 0, s, n, P.slice_ptr.p, P.off16.p, val, p_.p, q_.p, st_.p,
+                red_.partial.p, red_.counter.p);
         else
-            PORSOL_LAUNCH(k_spmv_pq<TV, T, int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
-                                                                  red_.partial.p, red_.counter.p));
+            chain(k_spmv_pq<TV, T, int>, nr, RB, 0, s, n, P.slice_ptr.p, P.col.p, val, p_.p, q_.p, st_.p,
+                red_.partial.p, red_.counter.p);
         if (pf) prof->end(s, prof_kernel, spmv_bytes, ev);
     }
-    PORSOL_LAUNCH(k_cg_update<T><<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p,
-                                                   dview_));
+    chain(k_cg_update<T>, nr, RB, 0, s, n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_);
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_dot_zr<T><<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
-    PORSOL_LAUNCH(k_cg_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
+    chain(k_dot_zr<T>, nr, RB, 0, s, n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
+    chain(k_cg_direction<T>, nb, RB, 0, s, n, z_.p, p_.p, st_.p);
 }
 
 template <class TV, class T>
@@ -614,6 +628,7 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
                                  T* x, double tol, int maxit, Profiler* prof, int prof_kernel)
 {
     const int n = P.n;
+    ChainPause plain(prof && prof->on);   // events between the kernels time each one
     CgResult res;
     if (n == 0) {
         res.converged = true;
@@ -626,16 +641,16 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
     init.maxit = maxit;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(CgDev), cudaMemcpyHostToDevice, s));
     if (P.has_off16())
-        PORSOL_LAUNCH(k_cg_init<TV, T, short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val, x, b, r_.p, st_.p,
-                                                                red_.partial.p, red_.counter.p, dview_));
+        chain(k_cg_init<TV, T, short>, nr, RB, 0, s, n, P.slice_ptr.p, P.off16.p, val, x, b, r_.p, st_.p,
+            red_.partial.p, red_.counter.p, dview_);
     else
-        PORSOL_LAUNCH(k_cg_init<TV, T, int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p,
-                                                              red_.partial.p, red_.counter.p, dview_));
+        chain(k_cg_init<TV, T, int>, nr, RB, 0, s, n, P.slice_ptr.p, P.col.p, val, x, b, r_.p, st_.p, red_.partial.p,
+            red_.counter.p, dview_);
     PORSOL_CUDA(cudaGetLastError());
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_dot_zr<T><<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p));
-    PORSOL_LAUNCH(k_first_direction<T><<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p));
+    chain(k_dot_zr<T>, nr, RB, 0, s, n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p);
+    chain(k_first_direction<T>, nb, RB, 0, s, n, z_.p, p_.p, st_.p);
     PORSOL_CUDA(cudaGetLastError());
     // One iteration is captured into a CUDA graph (re-captured when the matrix, vectors or
     // preconditioner change) unless per-kernel profiling is on.
@@ -741,24 +756,24 @@ void ReliableCg::iteration(cudaStream_t s, const SellPattern& P, const double* v
         cudaEvent_t ev = nullptr;
         if (pf) prof->begin(s, PK_SPMV32, bytes, &ev);
         if (P.has_off16())
-            PORSOL_LAUNCH(k_rc_pq<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val32, p_.p, q_.p, st_.p,
-                                                           red_.partial.p, red_.counter.p, dview_));
+            chain(k_rc_pq<short>, nr, RB, 0, s, n, P.slice_ptr.p, P.off16.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
+                red_.counter.p, dview_);
         else
-            PORSOL_LAUNCH(k_rc_pq<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p,
-                                                         red_.partial.p, red_.counter.p, dview_));
+            chain(k_rc_pq<int>, nr, RB, 0, s, n, P.slice_ptr.p, P.col.p, val32, p_.p, q_.p, st_.p, red_.partial.p,
+                red_.counter.p, dview_);
         if (pf) prof->end(s, PK_SPMV32, bytes, ev);
     }
-    PORSOL_LAUNCH(k_rc_update<<<nr, RB, 0, s>>>(n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_));
+    chain(k_rc_update, nr, RB, 0, s, n, x, r_.p, p_.p, q_.p, st_.p, red_.partial.p, red_.counter.p, dview_);
     if (P.has_off16())
-        PORSOL_LAUNCH(k_rc_true<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p,
-                                                         red_.partial.p, red_.counter.p, dview_));
+        chain(k_rc_true<short>, nr, RB, 0, s, n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
+            red_.counter.p, dview_);
     else
-        PORSOL_LAUNCH(k_rc_true<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
-                                                       red_.partial.p, red_.counter.p, dview_));
-    PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 0));
+        chain(k_rc_true<int>, nr, RB, 0, s, n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
+            red_.counter.p, dview_);
+    chain(k_rc_rescale, nr, RB, 0, s, n, r64_.p, r_.p, p_.p, st_.p, 0);
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 0));
-    PORSOL_LAUNCH(k_rc_direction<<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, 0));
+    chain(k_rc_zr, nr, RB, 0, s, n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 0);
+    chain(k_rc_direction, nb, RB, 0, s, n, z_.p, p_.p, st_.p, 0);
 }
 
 CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* val64, const float* val32,
@@ -766,6 +781,7 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
                            Profiler* prof)
 {
     const int n = P.n;
+    ChainPause plain(prof && prof->on);   // events between the kernels time each one
     CgResult res;
     if (n == 0) {
         res.converged = true;
@@ -779,16 +795,16 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
     init.delta = delta;
     PORSOL_CUDA(cudaMemcpyAsync(st_.p, &init, sizeof(RcDev), cudaMemcpyHostToDevice, s));
     if (P.has_off16())
-        PORSOL_LAUNCH(k_rc_init<short><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p,
-                                                         red_.partial.p, red_.counter.p, dview_));
+        chain(k_rc_init<short>, nr, RB, 0, s, n, P.slice_ptr.p, P.off16.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
+            red_.counter.p, dview_);
     else
-        PORSOL_LAUNCH(k_rc_init<int><<<nr, RB, 0, s>>>(n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p,
-                                                       red_.partial.p, red_.counter.p, dview_));
-    PORSOL_LAUNCH(k_rc_rescale<<<nr, RB, 0, s>>>(n, r64_.p, r_.p, p_.p, st_.p, 1));
+        chain(k_rc_init<int>, nr, RB, 0, s, n, P.slice_ptr.p, P.col.p, val64, x, b, r64_.p, st_.p, red_.partial.p,
+            red_.counter.p, dview_);
+    chain(k_rc_rescale, nr, RB, 0, s, n, r64_.p, r_.p, p_.p, st_.p, 1);
     const int* stop = &st_.p->stop;
     M.apply(s, r_.p, z_.p, stop);
-    PORSOL_LAUNCH(k_rc_zr<<<nr, RB, 0, s>>>(n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 1));
-    PORSOL_LAUNCH(k_rc_direction<<<nb, RB, 0, s>>>(n, z_.p, p_.p, st_.p, 1));
+    chain(k_rc_zr, nr, RB, 0, s, n, z_.p, r_.p, st_.p, red_.partial.p, red_.counter.p, 1);
+    chain(k_rc_direction, nb, RB, 0, s, n, z_.p, p_.p, st_.p, 1);
     PORSOL_CUDA(cudaGetLastError());
     // per-kernel event timing records events inside the V-cycle: no graph capture then
     const bool graphs = !(prof && prof->on);
@@ -921,13 +937,13 @@ void Ilu0::apply(cudaStream_t s, const double* r, double* z, const int* stop)
     const SellPattern& P = *P_;
     for (size_t l = 0; l + 1 < h_lptr_.size(); ++l) {
         const int cnt = h_lptr_[l + 1] - h_lptr_[l];
-        PORSOL_LAUNCH(k_ilu_lower_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
-                                                           P.diag.p, lu_.p, r, z, stop));
+        chain(k_ilu_lower_level, div_up(cnt, 128), 128, 0, s, cnt, lrows_.p + h_lptr_[l], P.slice_ptr.p, P.col.p,
+            P.diag.p, lu_.p, r, z, stop);
     }
     for (size_t l = 0; l + 1 < h_uptr_.size(); ++l) {
         const int cnt = h_uptr_[l + 1] - h_uptr_[l];
-        PORSOL_LAUNCH(k_ilu_upper_level<<<div_up(cnt, 128), 128, 0, s>>>(cnt, urows_.p + h_uptr_[l], P.slice_ptr.p, P.col.p,
-                                                           P.rowlen.p, P.diag.p, lu_.p, z, stop));
+        chain(k_ilu_upper_level, div_up(cnt, 128), 128, 0, s, cnt, urows_.p + h_uptr_[l], P.slice_ptr.p, P.col.p,
+            P.rowlen.p, P.diag.p, lu_.p, z, stop);
     }
     PORSOL_CUDA(cudaGetLastError());
 }

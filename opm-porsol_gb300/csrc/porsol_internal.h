@@ -223,4 +223,56 @@ extern std::atomic<long long> g_launches;
         PORSOL_COUNT_LAUNCH();  \
     } while (0)
 
+// ------------------------------------------------------------------ chained launches
+// The kernels of a CG iteration (the SpMV, the vector updates, the preconditioner's cycle) run
+// back to back, many of them on small AMG levels and in level-scheduled triangular solves where the
+// gap between two kernels costs as much as the work.  Those on grids of fewer than 304 blocks (two
+// per SM) are launched with programmatic stream serialisation (programmatic dependent launch, sm_90
+// and later): their blocks may be scheduled while the preceding kernel's last blocks still run.
+// Every kernel launched through chain() starts with chain_wait(), which returns once the preceding
+// kernel has completed and its writes are visible, so the order of all reads and writes is that of
+// plain stream launches.  On GB300 this saved 3.5 % of an ILU0-CG solve and 0.1-0.2 ms of an AMG-CG
+// solve, while chaining the large grids too cost 0.2-1.3 ms.  Chaining is off while per-kernel event
+// timing is on (ChainPause); PORSOL_PDL=0 (never), 1 (every grid) or 2 (small grids, the default)
+// in the environment selects it.
+bool chain_enabled(long long blocks);
+struct ChainPause {   // plain launches in this thread for the scope's duration (nestable)
+    explicit ChainPause(bool on = true);
+    ~ChainPause();
+    ChainPause(const ChainPause&) = delete;
+    ChainPause& operator=(const ChainPause&) = delete;
+
+private:
+    bool on_;
+};
+
+template <class... KA, class... A>
+inline void chain(void (*kernel)(KA...), dim3 grid, dim3 block, size_t shm, cudaStream_t s, A&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = shm;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = chain_enabled((long long)grid.x * grid.y * grid.z) ? 1 : 0;
+    PORSOL_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...));
+    PORSOL_COUNT_LAUNCH();
+}
+
+#ifdef __CUDACC__
+// First statement of every kernel launched by chain(): wait for the preceding kernel (a no-op
+// when launched plainly), then let the next chained kernel's blocks be scheduled.  Every block
+// runs it before it can return, so completion of a chained kernel implies completion of all
+// kernels before it.
+__device__ __forceinline__ void chain_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+#endif
+
 }  // namespace porsol
