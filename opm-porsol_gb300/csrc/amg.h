@@ -72,6 +72,14 @@ public:
     // error bits set by the apply kernels (ST_TIMEOUT: a bounded wait for a bulk copy gave up);
     // synchronises the stream
     int solve_status(cudaStream_t s) const;
+    // Block-diagonal systems (batched solves): blk0 maps each row of the system to its block
+    // (device, null: one system).  Set before setup(); setup() carries the map down the levels.
+    void set_row_blocks(const int* blk0) { blk0_ = blk0; }
+    // Per-block convergence flags of the batched CG (device, 0: still iterating; null: none).
+    // apply() then marks each level's slices that hold an iterating block, and its kernels leave
+    // the other slices as they are: with a block-diagonal hierarchy the iterating blocks' values
+    // are those of a full cycle.
+    void set_block_state(const int* conv) override;
 
 private:
     struct Level {
@@ -101,7 +109,13 @@ private:
         Aggregates agg;              // to the next level
         DBuf<T> t, r, d0, d1, b, x;  // work vectors
         DBuf<T> kc1, kc2, kv1, kv2, kr2;   // K-cycle vectors (K-levels only)
+        DBuf<int> blk;               // block of each row (levels below the first; batched solves)
+        const int* blkp = nullptr;   // block of each row: blk0_ on the finest level, blk below it
+        DBuf<unsigned char> act;     // per 32-row slice: 1 while a block in it iterates
     };
+    const int* blk0_ = nullptr;
+    const int* conv_ = nullptr;
+    const unsigned char* level_act(const Level& L) const { return conv_ && L.blkp ? L.act.p : nullptr; }
     void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg_first, Aggregates& out);
     void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
                   Aggregates& out);

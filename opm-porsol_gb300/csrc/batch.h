@@ -69,6 +69,7 @@ class BatchCastPrecond : public Precond<double> {
 public:
     void bind(Precond<float>* inner, const BatchRanges* B, const double* sc, const double* isc);
     void apply(cudaStream_t s, const double* r, double* z, const int* stop) override;
+    void set_block_state(const int* conv) override;   // passed to the inner preconditioner
 
 private:
     Precond<float>* m_ = nullptr;

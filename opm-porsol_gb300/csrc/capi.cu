@@ -374,6 +374,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
     if (o.precision == PORSOL_FP64) {
         if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64 &&
               amg_kcycle == ao.kcycle_levels)) {
+            amg64.set_row_blocks(nullptr);
             amg64.setup(stream, P, val.p, ao);
             amg_ready = true;
             amg_precision = PORSOL_FP64;
@@ -400,6 +401,7 @@ void porsol_solver::linear_solve(const porsol_solve_opts& o, porsol_solve_stats&
         // the FP64 drop-in keeps the two-round hierarchy
         AmgOpts ao32 = ao;
         ao32.round3_below = 30000;
+        amg32.set_row_blocks(nullptr);
         amg32.setup(stream, P, val32.p, ao32);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;
@@ -504,6 +506,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
         } else {
             dirichlet_guess(stream, P, val.p, rhs.p, x.p);
             if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_FP64)) {
+                amg64.set_row_blocks(batch.blk.p);
                 amg64.setup(stream, P, val.p, ao);
                 amg_ready = true;
                 amg_precision = PORSOL_FP64;
@@ -525,6 +528,7 @@ void porsol_solver::batched_solve(const porsol_solve_opts& o, porsol_solve_stats
     }
     dirichlet_guess(stream, P, val.p, rhs.p, x.p);
     if (!((o.same_matrix || reuse_amg) && amg_ready && amg_precision == PORSOL_MIXED)) {
+        amg32.set_row_blocks(batch.blk.p);
         amg32.setup(stream, P, val32.p, ao);
         amg_ready = true;
         amg_precision = PORSOL_MIXED;

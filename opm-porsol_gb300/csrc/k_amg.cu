@@ -25,6 +25,15 @@ __device__ __forceinline__ int slot_of(const int* sp, int r, int t) { return sp[
 
 // Row r and lane q of the row for K lanes per row (K = 1: one thread per row; K = 0: one thread
 // per row on the SELL-32x4 copy of the matrix).
+// Batched solves skip the rows of converged blocks: act (one flag per 32-row slice of the level, null
+// when every row works) is 0 where no block of the slice still iterates.  The slice is taken from
+// the row clamped to the level, so all lanes of a warp (one slice, whatever its lanes per row) decide
+// together.
+__device__ __forceinline__ bool slice_idle(const unsigned char* act, int row, int n)
+{
+    return act != nullptr && n > 0 && act[min(row, n - 1) >> 5] == 0;
+}
+
 template <int K>
 __device__ __forceinline__ void row_lane(int& r, int& q)
 {
@@ -715,12 +724,12 @@ __global__ void __launch_bounds__(256) k_cheb_setup(int n, const int* __restrict
 // start from x = 0: r = D^-1 b, d = r / theta
 template <class T>
 __global__ void k_cheb_start0(int n, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ r,
-                              T* __restrict__ d, T inv_theta, const int* stop)
+                              T* __restrict__ d, T inv_theta, const int* stop, const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || slice_idle(act, i, n)) return;
     const T ri = dinv[i] * b[i];
     r[i] = ri;
     d[i] = ri * inv_theta;
@@ -754,12 +763,13 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
                              const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                              const T* __restrict__ b, const T* __restrict__ t, const T* __restrict__ xc,
                              const int* __restrict__ agg, T wp, T* __restrict__ x, T* __restrict__ r,
-                             T* __restrict__ d, T inv_theta, const int* stop)
+                             T* __restrict__ d, T inv_theta, const int* stop, const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
+    if (slice_idle(act, i, n)) return;
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     T acc;
@@ -784,12 +794,12 @@ __global__ void k_cheb_start(int n, const int* __restrict__ sp, const CI* __rest
 // y = t + w P xc (the coarse correction), for the levels whose smoother then gathers one vector
 template <class T>
 __global__ void k_prolong_add(int n, const T* __restrict__ t, const T* __restrict__ xc, const int* __restrict__ agg,
-                              T wp, T* __restrict__ y, const int* stop)
+                              T wp, T* __restrict__ y, const int* stop, const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || slice_idle(act, i, n)) return;
     const int ai = agg[i];
     y[i] = t[i] + (ai >= 0 ? wp * xc[ai] : T(0));
 }
@@ -799,12 +809,14 @@ template <class T, int K, class V, bool SCALED, class CI = int>
 __global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restrict__ col,
                             const int* __restrict__ rowlen, const V* __restrict__ A, const T* __restrict__ dinv,
                             const T* x_in, const T* __restrict__ d_in, T* __restrict__ r, T* __restrict__ d_out,
-                            T* x_out, T c1, T c2, int final_step, const int* stop)
+                            T* x_out, T c1, T c2, int final_step, const int* stop,
+                            const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
+    if (slice_idle(act, i, n)) return;
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
@@ -954,12 +966,14 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
 template <class T, int K, class V, bool SCALED, class CI = int>
 __global__ void k_resid(int n, const int* __restrict__ sp, const CI* __restrict__ col, const int* __restrict__ rowlen,
                         const V* __restrict__ A, const T* __restrict__ diagv, const T* __restrict__ b,
-                        const T* __restrict__ x, T* __restrict__ r, const int* stop)
+                        const T* __restrict__ x, T* __restrict__ r, const int* stop,
+                        const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     int i, q;
     row_lane<K>(i, q);
+    if (slice_idle(act, i, n)) return;
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [x](int j) { return x[j]; });
@@ -1045,12 +1059,12 @@ __global__ void k_scale_half4(int n, int nslices, const int* __restrict__ sp, co
 
 template <class T>
 __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __restrict__ idx, const T* __restrict__ r,
-                           T* __restrict__ bc, const int* stop)
+                           T* __restrict__ bc, const int* stop, const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
+    if (I >= nc || slice_idle(act, I, nc)) return;
     T s = 0;
     for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
     bc[I] = s;
@@ -1061,18 +1075,42 @@ __global__ void k_restrict(int nc, const int* __restrict__ ptr, const int* __res
 template <class T>
 __global__ void k_restrict_start0(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
                                   const T* __restrict__ r, T* __restrict__ bc, const T* __restrict__ dinv_c,
-                                  T* __restrict__ rc, T* __restrict__ dc, T inv_theta, const int* stop)
+                                  T* __restrict__ rc, T* __restrict__ dc, T inv_theta, const int* stop,
+                                  const unsigned char* __restrict__ act)
 {
     chain_wait();
     if (*stop) return;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= nc) return;
+    if (I >= nc || slice_idle(act, I, nc)) return;
     T s = 0;
     for (int q = ptr[I]; q < ptr[I + 1]; ++q) s += r[idx[q]];
     bc[I] = s;
     const T ri = dinv_c[I] * s;
     rc[I] = ri;
     dc[I] = ri * inv_theta;
+}
+
+// ---- block skipping (batched solves) ----
+// block of each coarse row: that of its first member (aggregates never cross blocks)
+__global__ void k_level_blocks(int nc, const int* __restrict__ ptr, const int* __restrict__ idx,
+                               const int* __restrict__ blk_f, int* __restrict__ blk_c)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I < nc) blk_c[I] = blk_f[idx[ptr[I]]];
+}
+
+// act[s] = 1 when a row of slice s belongs to a block still iterating (conv == 0); one warp per slice
+__global__ void k_slice_active(int n, int nslices, const int* __restrict__ blk, const int* __restrict__ conv,
+                               unsigned char* __restrict__ act, const int* stop)
+{
+    chain_wait();
+    if (*stop) return;
+    const int sl = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (sl >= nslices) return;   // whole warps
+    const int r = sl * 32 + (threadIdx.x & 31);
+    const bool live = r < n && conv[blk[r]] == 0;
+    const unsigned any = __ballot_sync(0xffffffffu, live);
+    if ((threadIdx.x & 31) == 0) act[sl] = any ? 1 : 0;
 }
 
 // ---------------- K-cycle (Krylov-accelerated coarse correction) ----------------
@@ -1286,18 +1324,23 @@ __global__ void __launch_bounds__(1024) k_dense_gauss_jordan(int n, const double
 
 template <class T>
 __global__ void k_dense_apply(int n, const double* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x,
-                              const int* stop)
+                              const int* stop, const unsigned char* __restrict__ act, const int* __restrict__ blk,
+                              const int* __restrict__ conv)
 {
     chain_wait();
     if (*stop) return;
     extern __shared__ double sb[];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = double(b[j]);
+    // batched solves (blk, conv not null): the block-diagonal inverse couples nothing across blocks,
+    // but its zeros would still carry a converged block's values (0 * Inf is NaN), so those enter as
+    // 0: a converged block's rows are only partly recomputed, from partly stale inputs, and in FP32
+    // that mix can overflow
+    for (int j = threadIdx.x; j < n; j += blockDim.x) sb[j] = (conv && conv[blk[j]] != 0) ? 0.0 : double(b[j]);
     __syncthreads();
     // one warp per row, blockDim/32 rows per block: a large coarsest level (up to 2048 rows
     // when coarsening stalls) spreads over many SMs instead of one
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int i = blockIdx.x * nw + warp;
-    if (i >= n) return;
+    if (i >= n || slice_idle(act, i, n)) return;   // one row per warp
     double s = 0.0;
     for (int j = lane; j < n; j += 32) s += Dinv[(size_t)i * n + j] * sb[j];
 #pragma unroll
@@ -1652,11 +1695,11 @@ int Amg<T>::tune_lanes(cudaStream_t s, Level& L)
         if (L.half) {
             PORSOL_LANES(lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, __half, true><<<nbk, TB, 0, s>>>(
                                     n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.ah.p, L.dinv.p, nullptr, L.d0.p, L.r.p,
-                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p))));
+                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p, nullptr))));
         } else {
             PORSOL_LANES(lanes, PORSOL_LAUNCH((k_cheb_step<T, KL, T, false><<<nbk, TB, 0, s>>>(
                                     n, P.slice_ptr.p, P.col.p, P.rowlen.p, L.A, L.dinv.p, nullptr, L.d0.p, L.r.p,
-                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p))));
+                                    L.d1.p, L.t.p, T(0.5), T(0.5), 0, tune_stop_.p, nullptr))));
         }
     };
     int best = rule;
@@ -1789,6 +1832,25 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
         ++nlev_;
         if (next.n > 0.9 * n) break;   // coarsening stalled
     }
+    // block-diagonal systems: each level's row -> block map and its slice flags (all iterating)
+    for (int l = 0; l < nlev_; ++l) {
+        Level& L = *lv_[size_t(l)];
+        if (!blk0_) {
+            L.blkp = nullptr;
+            continue;
+        }
+        if (l == 0) {
+            L.blkp = blk0_;
+        } else {
+            Level& F = *lv_[size_t(l - 1)];
+            L.blk.alloc(std::max(L.n, 1));
+            PORSOL_LAUNCH(k_level_blocks<<<div_up(L.n, TB), TB, 0, s>>>(L.n, F.agg.ptr.p, F.agg.idx.p, F.blkp, L.blk.p));
+            L.blkp = L.blk.p;
+        }
+        L.act.alloc(size_t(std::max(L.P->nslices, 1)));
+        PORSOL_CUDA(cudaMemsetAsync(L.act.p, 1, L.act.n, s));
+    }
+    PORSOL_CUDA(cudaGetLastError());
     // Chebyshev intervals of the smoothed levels and the x4 copies' largest column offsets (one
     // copy each for all levels)
     {
@@ -1852,8 +1914,9 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
     double rho = 1.0 / sigma;
     T* d = L.d0.p;
     T* dn = L.d1.p;
+    const unsigned char* act = level_act(L);
     if (from_zero) {
-        if (!started) chain(k_cheb_start0<T>, nb, TB, 0, s, n, L.dinv.p, b, L.r.p, d, T(1.0 / theta), stop);
+        if (!started) chain(k_cheb_start0<T>, nb, TB, 0, s, n, L.dinv.p, b, L.r.p, d, T(1.0 / theta), stop, act);
     } else {
         // x holds the start vector (or the pre-smoothed t when xc is given; then x gets y)
         const T* t = xc ? L.t.p : x;
@@ -1861,22 +1924,22 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         // levels smoothed one thread per row (the large ones): form y = t + w P xc first, so the
         // start's row dot gathers one vector instead of t, agg and xc (the same y, the same sums)
         if (xc && L.lanes == 1) {
-            chain(k_prolong_add<T>, nb, TB, 0, s, n, t, xc, agg, T(o_.prolong), x, stop);
+            chain(k_prolong_add<T>, nb, TB, 0, s, n, t, xc, agg, T(o_.prolong), x, stop, act);
             t = x;
             xc = nullptr;
         }
         if (L.v4 && L.c16) {
             chain(k_cheb_start<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p,
-                L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop);
+                L.dinv.p, b, x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act);
         } else if (L.v4) {
             chain(k_cheb_start<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p, b,
-                x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop);
+                x, nullptr, nullptr, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act);
         } else if (L.half) {
             PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
-                P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop));
+                P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act));
         } else {
             PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
-                P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop));
+                P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act));
         }
     }
     const int deg = std::max(1, o_.cheb_degree);
@@ -1906,16 +1969,16 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
                 status_.p, 0u);
         } else if (L.v4 && L.c16) {
             chain(k_cheb_step<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p,
-                L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop);
+                L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act);
         } else if (L.v4) {
             chain(k_cheb_step<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.dinv.p,
-                xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop);
+                xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act);
         } else if (L.half) {
             PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
-                P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop));
+                P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act));
         } else {
             PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
-                P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop));
+                P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act));
         }
         if (prof_here) prof_->end(s, PK_CHEB, bytes, ev);
         rho = rho1;
@@ -1929,7 +1992,8 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bo
 {
     if (l == nlev_ - 1) {
         if (nc_ > 0)
-            chain(k_dense_apply<T>, div_up(nc_, 8), 256, nc_ * sizeof(double), s, nc_, cinv_.p, b, x, stop);
+            chain(k_dense_apply<T>, div_up(nc_, 8), 256, nc_ * sizeof(double), s, nc_, cinv_.p, b, x, stop,
+                level_act(*lv_[size_t(l)]), lv_[size_t(l)]->blkp, level_act(*lv_[size_t(l)]) ? conv_ : nullptr);
         return;
     }
     Level& L = *lv_[l];
@@ -1943,25 +2007,26 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bo
     // restrict the residual
     if (L.v4 && L.c16) {
         chain(k_resid<T, -1, __half, true, short>, nb, TB, 0, s, n, L.sp4.p, L.off4.p, nullptr, L.ah4.p, L.diagv.p, b,
-            L.t.p, L.r.p, stop);
+            L.t.p, L.r.p, stop, level_act(L));
     } else if (L.v4) {
         chain(k_resid<T, 0, __half, true>, nb, TB, 0, s, n, L.sp4.p, L.col4.p, nullptr, L.ah4.p, L.diagv.p, b, L.t.p,
-            L.r.p, stop);
+            L.r.p, stop, level_act(L));
     } else if (L.half) {
         PORSOL_LANES(L.lanes, chain(k_resid<T, KL, __half, true>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
-            P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop));
+            P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop, level_act(L)));
     } else {
         PORSOL_LANES(L.lanes, chain(k_resid<T, KL, T, false>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
-            P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop));
+            P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop, level_act(L)));
     }
     // the coarse level's cycle starts with a Chebyshev start from zero on Nx.b (its first cycle
     // under a K-cycle): done here, in the restriction; the coarsest level solves directly
     const bool fuse = l + 1 < nlev_ - 1;
     if (fuse)
         chain(k_restrict_start0<T>, div_up(Nx.n, TB), TB, 0, s, Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p,
-              Nx.dinv.p, Nx.r.p, Nx.d0.p, T(cheb_inv_theta(Nx)), stop);
+            Nx.dinv.p, Nx.r.p, Nx.d0.p, T(cheb_inv_theta(Nx)), stop, level_act(Nx));
     else
-        chain(k_restrict<T>, div_up(Nx.n, TB), TB, 0, s, Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop);
+        chain(k_restrict<T>, div_up(Nx.n, TB), TB, 0, s, Nx.n, L.agg.ptr.p, L.agg.idx.p, L.r.p, Nx.b.p, stop,
+            level_act(Nx));
     if (k_level(l + 1)) kcycle(s, l + 1, Nx.b.p, Nx.x.p, stop, fuse);
     else vcycle(s, l + 1, Nx.b.p, Nx.x.p, stop, fuse);
     // post-smoothing from t + w P xc
@@ -2058,12 +2123,27 @@ double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level, bool started) 
 }
 
 template <class T>
+void Amg<T>::set_block_state(const int* conv)
+{
+    if (conv != conv_) {
+        conv_ = conv;
+        this->bump_generation();   // the captured cycle's kernels take other arguments
+    }
+}
+
+template <class T>
 void Amg<T>::apply(cudaStream_t s, const T* r, T* z, const int* stop)
 {
     const bool prof_here = prof_ && prof_->on;
     ChainPause plain(prof_here);   // events between the kernels time each one
     cudaEvent_t ev = nullptr;
     if (prof_here) prof_->begin(s, PK_VCYCLE, 0.0, &ev);
+    if (conv_ && nlev_ > 0 && lv_[0]->blkp)
+        for (int l = 0; l < nlev_; ++l) {
+            const Level& L = *lv_[size_t(l)];
+            const int ns = L.P->nslices;
+            chain(k_slice_active, div_up(ns, TB / 32), TB, 0, s, L.n, ns, L.blkp, conv_, L.act.p, stop);
+        }
     vcycle(s, 0, r, z, stop);
     if (prof_here) prof_->end(s, PK_VCYCLE, 0.0, ev);
 }

@@ -635,6 +635,7 @@ CgResult PcgSolver<TV, T>::solve(cudaStream_t s, const SellPattern& P, const TV*
         return res;
     }
     setup(n, s);
+    M.set_block_state(nullptr);   // one system: every row works
     const int nb = div_up(n, RB), nr = red_blocks(n);
     CgDev init{};
     init.tol = tol;
@@ -788,6 +789,7 @@ CgResult ReliableCg::solve(cudaStream_t s, const SellPattern& P, const double* v
         return res;
     }
     setup(n, s);
+    M.set_block_state(nullptr);   // one system: every row works
     const int nb = div_up(n, RB), nr = red_blocks(n);
     RcDev init{};
     init.tol = tol;

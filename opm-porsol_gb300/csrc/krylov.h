@@ -32,6 +32,9 @@ struct Precond {
     // z = M^{-1} r; kernels must do nothing when *stop != 0.  apply() must not synchronise
     // or allocate: it is captured into a CUDA graph.
     virtual void apply(cudaStream_t s, const T* r, T* z, const int* stop) = 0;
+    // Batched solves: the per-block convergence flags (device, 0: block still iterating), so a
+    // block-diagonal preconditioner may skip the rows of converged blocks; null for one system.
+    virtual void set_block_state(const int*) {}
     // Changes whenever the kernels apply() launches change (new setup/factorisation).
     long long generation() const { return gen_; }
     void bump_generation() { ++gen_; }

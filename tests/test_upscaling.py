@@ -60,3 +60,33 @@ def test_batch_analytic_cases(pkg, gpulib, cart):
     assert np.abs(keff[0] - Kh).max() < 1e-8 * np.abs(Kh).max()
     assert abs(keff[1][0, 0] - kz.mean()) < 1e-8 * kz.mean()
     assert abs(keff[1][2, 2] - 1.0 / np.mean(1.0 / kz)) < 1e-8 * kz.mean()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_converged_blocks_are_skipped_without_changing_results(pkg, gpulib, workloads, precision):
+    """The batched CG tells the AMG which sub-grids still iterate; the cycle then leaves the rows of
+    converged sub-grids alone. The hierarchy is block diagonal, so the iterating sub-grids see the
+    values of a full cycle: the tensors are bitwise those of a sweep over every row
+    (PORSOL_BLOCK_SKIP=0). 64 sub-grids of sides 8..32 (0.7 M cells) converge at 26..96 iterations;
+    in FP32 the converged sub-grids' partly recomputed rows overflow here, which the dense coarsest
+    solve must keep away from the iterating ones."""
+    import os
+    union, sizes, K = workloads.periodic_subgrids(num=64)
+    out = {}
+    old = os.environ.get("PORSOL_BLOCK_SKIP")
+    try:
+        for flag in ("1", "0"):
+            os.environ["PORSOL_BLOCK_SKIP"] = flag
+            s = pkg.PressureSolver()
+            opts = pkg.default_solve_opts(residual_tolerance=1e-11, precision=precision)
+            out[flag] = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(), opts)
+            s.close()
+    finally:
+        if old is None:
+            os.environ.pop("PORSOL_BLOCK_SKIP", None)
+        else:
+            os.environ["PORSOL_BLOCK_SKIP"] = old
+    (k1, st1), (k0, st0) = out["1"], out["0"]
+    assert st1.iterations == st0.iterations
+    assert np.array_equal(k1, k0)
