@@ -170,6 +170,58 @@ __device__ __forceinline__ bool stronger(float s, unsigned h, int j, float bs, u
     return s > bs || (s == bs && (h > bh || (h == bh && j < bj)));
 }
 
+// Entry (j, a) of row i as a candidate: kept when its neighbour has the wanted state, its strength
+// s = a' rs_i rs_j (a' = -a for negative couplings, |a| otherwise) passes the floor, and it beats the
+// best so far.  stronger() is a total order, so the best is the same whatever the order of the entries.
+__device__ __forceinline__ void consider(int i, int j, float a, int stj, float rsj, float ri, int want_state,
+                                         bool neg, float floor_s, float& bs, unsigned& bh, int& bj)
+{
+    if (j == i || stj != want_state) return;
+    const float s = (neg ? -a : fabsf(a)) * ri * rsj;
+    if (!(s > 0.0f && s >= floor_s)) return;
+    const unsigned h = edge_hash(i, j);
+    if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
+        bs = s;
+        bh = h;
+        bj = j;
+    }
+}
+
+// The best candidate over this lane's entries q, q + K, ... of row i.  With one or two lanes per row
+// (long walks per lane) the columns and values of four entries are loaded before their four state
+// and scale gathers: one dependent load chain per four entries instead of one per entry.  More lanes
+// walk a few entries each and keep the plain loop (and 32 registers).
+template <int K, class T>
+__device__ __forceinline__ void best_in_row(int i, int q, const int* __restrict__ sp, const int* __restrict__ col,
+                                            const int* __restrict__ rowlen, const T* __restrict__ A,
+                                            const float* __restrict__ rs, const int* __restrict__ state,
+                                            int want_state, bool neg, float floor_s, float& bs, unsigned& bh,
+                                            int& bj)
+{
+    const float ri = rs[i];
+    const int len = rowlen[i];
+    const int k0 = sp[i >> 5] + (i & 31);
+    int t = q;
+    if constexpr (K <= 2)
+    for (; t + 3 * K < len; t += 4 * K) {
+        const int ka = k0 + 32 * t;
+        const int j0 = col[ka], j1 = col[ka + 32 * K], j2 = col[ka + 64 * K], j3 = col[ka + 96 * K];
+        const float a0 = float(A[ka]), a1 = float(A[ka + 32 * K]), a2 = float(A[ka + 64 * K]),
+                    a3 = float(A[ka + 96 * K]);
+        const int s0 = state[j0], s1 = state[j1], s2 = state[j2], s3 = state[j3];
+        const float r0 = rs[j0], r1 = rs[j1], r2 = rs[j2], r3 = rs[j3];
+        consider(i, j0, a0, s0, r0, ri, want_state, neg, floor_s, bs, bh, bj);
+        consider(i, j1, a1, s1, r1, ri, want_state, neg, floor_s, bs, bh, bj);
+        consider(i, j2, a2, s2, r2, ri, want_state, neg, floor_s, bs, bh, bj);
+        consider(i, j3, a3, s3, r3, ri, want_state, neg, floor_s, bs, bh, bj);
+    }
+    for (; t < len; t += K) {
+        const int k = k0 + 32 * t;
+        const int j = col[k];
+        consider(i, j, float(A[k]), state[j], rs[j], ri, want_state, neg, floor_s, bs, bh, bj);
+    }
+}
+
 // state: 0 free, 1 paired, 2 isolated (no off-diagonal coupling: never aggregated),
 // 3 free without a free strong neighbour (strengths are symmetric and neighbours only ever
 // become paired, so such a row cannot pair in a later sweep; it is skipped from then on and
@@ -257,24 +309,7 @@ __global__ void k_pick_wl(int n, const int* __restrict__ wl, const int* __restri
         float bs = 0.0f;
         unsigned bh = 0u;
         int bj = -1;
-        if (active) {
-            const float ri = rs[i];
-            const int len = rowlen[i];
-            for (int t = q; t < len; t += K) {
-                const int k = slot_of(sp, i, t);
-                const int j = col[k];
-                if (j == i || state[j] != 0) continue;
-                const float a = float(A[k]);
-                const float s = (neg ? -a : fabsf(a)) * ri * rs[j];
-                if (!(s > 0.0f && s >= theta)) continue;
-                const unsigned h = edge_hash(i, j);
-                if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
-                    bs = s;
-                    bh = h;
-                    bj = j;
-                }
-            }
-        }
+        if (active) best_in_row<K>(i, q, sp, col, rowlen, A, rs, state, 0, neg != 0, theta, bs, bh, bj);
         if (K > 1) best_of_lanes<K>(bs, bh, bj);
         if (valid && q == 0) best[i] = active ? bj : -1;
     }
@@ -324,23 +359,7 @@ __global__ void k_join(int n, const int* __restrict__ sp, const int* __restrict_
     float bs = 0.0f;
     unsigned bh = 0u;
     int bj = -1;
-    if (active) {
-        const float ri = rs[i];
-        const int len = rowlen[i];
-        for (int t = q; t < len; t += K) {
-            const int k = slot_of(sp, i, t);
-            const int j = col[k];
-            if (j == i || state[j] != 1) continue;
-            const float s = fabsf(float(A[k])) * ri * rs[j];
-            if (!(s > 0.0f)) continue;
-            const unsigned h = edge_hash(i, j);
-            if (bj < 0 || stronger(s, h, j, bs, bh, bj)) {
-                bs = s;
-                bh = h;
-                bj = j;
-            }
-        }
-    }
+    if (active) best_in_row<K>(i, q, sp, col, rowlen, A, rs, state, 1, false, 0.0f, bs, bh, bj);
     if (K > 1) best_of_lanes<K>(bs, bh, bj);
     if (active && q == 0) join[i] = bj;
 }
@@ -528,7 +547,23 @@ __global__ void k_gal_cand(int n, const int* __restrict__ sp, const int* __restr
     if (i >= n || agg[i] < 0) return;
     const int w = woff[i], len = rowlen[i];
     const int b = sp[i >> 5] + (i & 31);
-    for (int t = q; t < len; t += K) {
+    int t = q;
+    if constexpr (K <= 2)   // long walks per lane: four entries' loads and gathers in flight at once
+        for (; t + 3 * K < len; t += 4 * K) {
+            const int k = b + 32 * t;
+            const int c0 = col[k], c1 = col[k + 32 * K], c2 = col[k + 64 * K], c3 = col[k + 96 * K];
+            const T v0 = A[k], v1 = A[k + 32 * K], v2 = A[k + 64 * K], v3 = A[k + 96 * K];
+            const int g0 = agg[c0], g1 = agg[c1], g2 = agg[c2], g3 = agg[c3];
+            ckey[w + t] = g0;
+            ckey[w + t + K] = g1;
+            ckey[w + t + 2 * K] = g2;
+            ckey[w + t + 3 * K] = g3;
+            cval[w + t] = v0;
+            cval[w + t + K] = v1;
+            cval[w + t + 2 * K] = v2;
+            cval[w + t + 3 * K] = v3;
+        }
+    for (; t < len; t += K) {
         const int k = b + 32 * t;
         ckey[w + t] = agg[col[k]];
         cval[w + t] = A[k];
@@ -639,6 +674,7 @@ __global__ void k_gal_scatter(int nc, int nslices, const int* __restrict__ sp_c,
     const bool row = I < nc;
     const int len = row ? rowlen_c[I] : 0;
     const int o = row ? off[I] : 0;
+#pragma unroll 4   // independent entries: several loads in flight per lane
     for (int t = 0; t < w; ++t) {
         const int k = b + t * 32 + lane;
         if (t < len) {
