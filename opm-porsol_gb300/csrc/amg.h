@@ -116,6 +116,9 @@ private:
     const int* blk0_ = nullptr;
     const int* conv_ = nullptr;
     const unsigned char* level_act(const Level& L) const { return conv_ && L.blkp ? L.act.p : nullptr; }
+    // plain-layout level smoothed one thread per row whose pattern carries 16-bit column offsets (the
+    // system matrix of an FP64 or FP32-valued hierarchy): the row dots read 2 instead of 4 index bytes
+    static bool plain16(const Level& L) { return !L.half && !L.v4 && L.lanes == 1 && L.P->has_off16(); }
     void aggregate_round(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg_first, Aggregates& out);
     void pairwise(cudaStream_t s, const SellPattern& P, const T* A, int n, bool neg, double theta, bool join,
                   Aggregates& out);

@@ -1973,6 +1973,9 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         } else if (L.half) {
             PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
                 P.rowlen.p, L.ah.p, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act));
+        } else if (plain16(L)) {
+            chain(k_cheb_start<T, 1, T, false, short>, nb, TB, 0, s, n, P.slice_ptr.p, P.off16.p, P.rowlen.p, L.A,
+                L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act);
         } else {
             PORSOL_LANES(L.lanes, chain(k_cheb_start<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
                 P.rowlen.p, L.A, L.dinv.p, b, t, xc, agg, T(o_.prolong), x, L.r.p, d, T(1.0 / theta), stop, act));
@@ -1985,7 +1988,8 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         const T* xin = (from_zero && k == 1) ? nullptr : x;
         // algorithmic bytes: matrix values + columns (16-bit offsets on c16 levels), d gathered
         // once, dinv (unscaled form only), r and x in, r/d/x out
-        const double bytes = double(P.nent) * ((L.half ? 2 : sizeof(T)) + (L.v4 && L.c16 ? 2 : 4)) +
+        const double bytes = double(P.nent) * ((L.half ? 2 : sizeof(T)) +
+                                               ((L.v4 && L.c16) || plain16(L) ? 2 : 4)) +
                              double(n) * sizeof(T) * ((xin ? 7 : 6) - (L.half ? 1 : 0));
         const bool prof_here = prof_ && prof_->on && &L == lv_[0].get();  // finest level only
         cudaEvent_t ev = nullptr;
@@ -2012,6 +2016,9 @@ void Amg<T>::chebyshev(cudaStream_t s, Level& L, const T* b, T* x, bool from_zer
         } else if (L.half) {
             PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, __half, true>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
                 P.rowlen.p, L.ah.p, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act));
+        } else if (plain16(L)) {
+            chain(k_cheb_step<T, 1, T, false, short>, nb, TB, 0, s, n, P.slice_ptr.p, P.off16.p, P.rowlen.p, L.A,
+                L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act);
         } else {
             PORSOL_LANES(L.lanes, chain(k_cheb_step<T, KL, T, false>, nbk, TB, 0, s, n, P.slice_ptr.p, P.col.p,
                 P.rowlen.p, L.A, L.dinv.p, xin, d, L.r.p, dn, x, T(c1), T(c2), k == deg ? 1 : 0, stop, act));
@@ -2050,6 +2057,9 @@ void Amg<T>::vcycle(cudaStream_t s, int l, const T* b, T* x, const int* stop, bo
     } else if (L.half) {
         PORSOL_LANES(L.lanes, chain(k_resid<T, KL, __half, true>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
             P.col.p, P.rowlen.p, L.ah.p, L.diagv.p, b, L.t.p, L.r.p, stop, level_act(L)));
+    } else if (plain16(L)) {
+        chain(k_resid<T, 1, T, false, short>, nb, TB, 0, s, n, P.slice_ptr.p, P.off16.p, P.rowlen.p, L.A, L.diagv.p,
+            b, L.t.p, L.r.p, stop, level_act(L));
     } else {
         PORSOL_LANES(L.lanes, chain(k_resid<T, KL, T, false>, div_up(n * L.lanes, TB), TB, 0, s, n, P.slice_ptr.p,
             P.col.p, P.rowlen.p, L.A, L.diagv.p, b, L.t.p, L.r.p, stop, level_act(L)));
@@ -2118,7 +2128,7 @@ double Amg<T>::cycle_bytes(int l, std::vector<double>* per_level, bool started) 
     }
     const Level& L = *lv_[l];
     const double n = L.n, nc = lv_[l + 1]->n;
-    const double vb = L.half ? 2.0 : sx, cb = (L.v4 && L.c16) ? 2.0 : 4.0;
+    const double vb = L.half ? 2.0 : sx, cb = ((L.v4 && L.c16) || plain16(L)) ? 2.0 : 4.0;
     const double mat = double(L.P->nent) * (vb + cb);
     const int deg = std::max(1, o_.cheb_degree);
     // Chebyshev steps of one application: the first from x = 0 after start0 has no x_in
