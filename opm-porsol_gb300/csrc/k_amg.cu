@@ -1042,6 +1042,28 @@ __global__ void k_scale_half(int n, const int* __restrict__ sp, const int* __res
 // sp4[r/32] + 128 (t/4) + 4 (r%32) + t%4), so a row's four columns come in one 16-byte load and its
 // four FP16 values in one 8-byte load.  Rows are padded to a multiple of four entries (col = row,
 // value 0).  groups[s] = 128 * ceil(width / 4).
+// 16-bit column offsets of a coarse level's SELL pattern (col - row; 0 on the padding rows of the last
+// slice), one warp per slice, and the level's largest |col - row| into *maxoff: above 32767 the
+// truncated copy is not used
+__global__ void k_col_offsets(int n, int nslices, const int* __restrict__ sp, const int* __restrict__ col,
+                              short* __restrict__ off, int* __restrict__ maxoff)
+{
+    const int sl = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (sl >= nslices) return;   // whole warps
+    const int lane = threadIdx.x & 31, r = sl * 32 + lane;
+    const int b = sp[sl], w = (sp[sl + 1] - b) >> 5;
+    int mo = 0;
+    for (int t = 0; t < w; ++t) {
+        const int k = b + 32 * t + lane;
+        const int o = r < n ? col[k] - r : 0;
+        mo = max(mo, abs(o));
+        off[k] = short(o);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mo = max(mo, __shfl_xor_sync(0xffffffffu, mo, o));
+    if (lane == 0 && mo > 0) atomicMax(maxoff, mo);
+}
+
 __global__ void k_slice_groups(int nslices, const int* __restrict__ sp, int* __restrict__ groups)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1688,6 +1710,19 @@ void Amg<T>::smoother_setup(cudaStream_t s, Level& L, int level)
     L.d0.alloc(n);
     L.d1.alloc(n);
     L.lanes = L.v4 ? 1 : tune_lanes(s, L);
+    // coarse levels smoothed one thread per row on the plain layout (FP64 hierarchies): 16-bit column
+    // offsets as the system matrix has them, when the level's couplings allow (checked in setup())
+    if (level > 0) {
+        SellPattern& O = L.own;
+        O.off16.n = 0;   // a copy from an earlier setup is never used
+        if (!L.half && !L.v4 && L.lanes == 1 && O.nent > 0) {
+            O.off16.alloc(size_t(O.nent));
+            PORSOL_LAUNCH(k_col_offsets<<<div_up(O.nslices, TB / 32), TB, 0, s>>>(n, O.nslices, O.slice_ptr.p,
+                                                                                  O.col.p, O.off16.p,
+                                                                                  s_maxoff_.p + level));
+            PORSOL_CUDA(cudaGetLastError());
+        }
+    }
     // bulk-staged step: FP32 hierarchies on the level whose slice widths the host knows (the system
     // matrix), when every slice has at most four groups (18 KB of shared memory per 8 slices at 3)
     L.bulk_groups = 0;
@@ -1901,6 +1936,7 @@ void Amg<T>::setup(cudaStream_t s, const SellPattern& P0, const T* A0, const Amg
             std::memcpy(&gm, &gb[size_t(l)], sizeof(gm));
             lv_[l]->lmax = gm > 0 ? gm : 1.0;
             Level& L = *lv_[l];
+            if (l > 0 && L.own.off16.n != 0 && mo[size_t(l)] > 32767) L.own.off16.n = 0;   // offsets do not fit
             if (L.v4 && L.c16 && mo[size_t(l)] > 32767) {
                 // couplings too far from the diagonal for 16-bit offsets: 32-bit columns
                 const SellPattern& P = *L.P;
