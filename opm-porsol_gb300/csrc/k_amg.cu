@@ -974,24 +974,31 @@ __global__ void __launch_bounds__(BULK_SLICES * 32)
     }
     const int i = s * 32 + lane;
     if (i >= n) return;  // padding rows of the last slice
-    const int G = ne >> 7;
+    const int G = ne >> 7;   // at most 4 (the staging area's cap)
     const CI* cp = scol + 4 * lane;
     const uint2* vp = reinterpret_cast<const uint2*>(sval) + lane;
-    T acc = T(0);
-    for (int g = 0; g < G; ++g) {
-        const int4 c = x4_columns<CI>(cp + 128 * g, i);
-        const uint2 h = vp[32 * g];
-        const T x0 = d_in[c.x], x1 = d_in[c.y], x2 = d_in[c.z], x3 = d_in[c.w];
-        const float2 v01 = __half22float2(*reinterpret_cast<const __half2*>(&h.x));
-        const float2 v23 = __half22float2(*reinterpret_cast<const __half2*>(&h.y));
-        acc += T(v01.x) * x0;
-        acc += T(v01.y) * x1;
-        acc += T(v23.x) * x2;
-        acc += T(v23.y) * x3;
-    }
+    // the row's own values first, then every group unrolled: the columns come from shared memory, so
+    // the gathers of all groups can be in flight together; the products are added in entry order
     const T di = d_in[i];
-    T xi = (x_in ? x_in[i] : T(0)) + di;
-    const T ri = r[i] - acc;
+    const T xo = x_in ? x_in[i] : T(0);
+    const T r0 = r[i];
+    T acc = T(0);
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        if (g < G) {
+            const int4 c = x4_columns<CI>(cp + 128 * g, i);
+            const uint2 h = vp[32 * g];
+            const T x0 = d_in[c.x], x1 = d_in[c.y], x2 = d_in[c.z], x3 = d_in[c.w];
+            const float2 v01 = __half22float2(*reinterpret_cast<const __half2*>(&h.x));
+            const float2 v23 = __half22float2(*reinterpret_cast<const __half2*>(&h.y));
+            acc += T(v01.x) * x0;
+            acc += T(v01.y) * x1;
+            acc += T(v23.x) * x2;
+            acc += T(v23.y) * x3;
+        }
+    }
+    T xi = xo + di;
+    const T ri = r0 - acc;
     const T dn = c1 * di + c2 * ri;
     if (final_step) xi += dn;
     r[i] = ri;
