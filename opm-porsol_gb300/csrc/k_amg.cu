@@ -855,11 +855,27 @@ __global__ void k_cheb_step(int n, const int* __restrict__ sp, const CI* __restr
     if (slice_idle(act, i, n)) return;
     const bool valid = i < n;
     if (K <= 1 && !valid) return;
+    // FP32: the row's own values are loaded before the row dot, so their loads overlap its gathers
+    // (in FP64 the early values would take the kernel past 32 registers)
+    constexpr bool early = sizeof(T) == 4;
+    const bool own = valid && q == 0;
+    T di = T(0), xo = T(0), r0 = T(0), dv = T(0);
+    if (early && own) {
+        di = d_in[i];
+        xo = x_in ? x_in[i] : T(0);
+        r0 = r[i];
+        if (!SCALED) dv = dinv[i];
+    }
     const T acc = row_dot<K, T>(sp, col, A, rowlen, i, q, valid, [d_in](int j) { return d_in[j]; });
-    if (!valid || q != 0) return;
-    const T di = d_in[i];
-    T xi = (x_in ? x_in[i] : T(0)) + di;
-    const T ri = SCALED ? r[i] - acc : r[i] - dinv[i] * acc;
+    if (!own) return;
+    if (!early) {
+        di = d_in[i];
+        xo = x_in ? x_in[i] : T(0);
+        r0 = r[i];
+        if (!SCALED) dv = dinv[i];
+    }
+    T xi = xo + di;
+    const T ri = SCALED ? r0 - acc : r0 - dv * acc;
     const T dn = c1 * di + c2 * ri;
     if (final_step) xi += dn;
     r[i] = ri;
