@@ -26,12 +26,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE, "-I", CSRC]
 SOURCES = ["structure.cpp", "k_mimetic.cu", "k_krylov.cu", "k_amg.cu", "k_transport.cu", "k_capillary.cu", "k_adjoint.cu",
-           "k_batch.cu", "capi.cu", "noalloc_cfl.cu"]
+           "k_batch.cu", "k_upscale.cu", "capi.cu", "noalloc_cfl.cu"]
 
 BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
 FLUID_CELLWISE, FLUID_COREY2, FLUID_TENSOR = 0, 1, 2
 FP64, MIXED = 0, 1
 GRAD_LOGK, GRAD_LOGK_AXES = 0, 1
+UPSCALE_AMG, UPSCALE_PERSISTENT = 0, 1
 ERR = {0: "OK", 1: "NOT_CONVERGED", 2: "BAD_ARG", 3: "NONFINITE", 4: "SAT_RANGE", 5: "CUDA", 6: "TIMEOUT",
        7: "STATE", 8: "UNKNOWN_SOLVER", 9: "CFL"}
 
@@ -154,6 +155,8 @@ EXPORTS = [
     ("porsol_solve_bytes", _i, [_vp, _vp, _i, _vp]),
     ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
                                      C.POINTER(SolveStats)]),
+    ("porsol_upscale_set_schedule", _i, [_vp, _i, _i, _i]),
+    ("porsol_upscale_last_schedule", _i, [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
     ("porsol_cell_fields", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, _vp]),
     ("porsol_write_field", _i, [_vp, _i, C.c_char_p]),
     ("porsol_objective_value", _i, [_vp, C.POINTER(Objective), C.POINTER(_d)]),
@@ -345,6 +348,17 @@ class PressureSolver:
         self._check(lib().porsol_num_dofs(self.h, C.byref(n), C.byref(nnz), C.byref(mx), C.byref(ni)))
         self.n, self.nnz = n.value, nnz.value
         return keff.reshape(ng, 3, 3), st
+
+    def set_upscale_schedule(self, schedule, cta_threads=0, warp_max_unknowns=0):
+        """UPSCALE_AMG (default) or UPSCALE_PERSISTENT (one launch; cta_threads 0 = autotuned)."""
+        self._check(lib().porsol_upscale_set_schedule(self.h, int(schedule), int(cta_threads),
+                                                      int(warp_max_unknowns)))
+
+    def upscale_last_schedule(self):
+        """(cta_threads, warp_max_unknowns, tuned) of the last persistent-schedule call."""
+        t, w, tu = C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().porsol_upscale_last_schedule(self.h, C.byref(t), C.byref(w), C.byref(tu)))
+        return t.value, w.value, bool(tu.value)
 
     def _objective(self, cell_weight, cell_target, hf_weight):
         keep = [None if a is None else _f64(a) for a in (cell_weight, cell_target, hf_weight)]

@@ -716,9 +716,30 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     }
     porsol_solve_stats st{};
     st.ms_assemble = now_ms() - t_asm;
+    gflux_last = gflux_use;
+    gzero_last = gzero;
+    if (assemble_only) {   // batched upscaling solves the assembled systems itself
+        if (stats) *stats = st;
+        return;
+    }
     const double t_lin = now_ms();
     linear_solve(o, st);
     st.ms_krylov = now_ms() - t_lin - st.ms_precond_setup;
+    recover_solution(st);
+    solved = true;
+    if (stats) *stats = st;
+}
+
+// Pressure and flux recovery (computePressureAndFluxes) from the face pressures in x, and the FP64
+// mass-balance check, with the inner products, gravity fluxes and sources of the last assembly.
+void porsol_solver::recover_solution(porsol_solve_stats& st)
+{
+    const int nc = S.g.nc;
+    cudaStream_t s = stream;
+    const double* W_use = W_last;
+    const double* gflux_use = gflux_last;
+    const bool gzero = gzero_last;
+    const double* d_src = last_src;
     const double t_rec = now_ms();
     {
         // per cell: W, the face pressures gathered through cf, F, L, g, mobility in; pressure and
@@ -752,8 +773,6 @@ void porsol_solver::solve(const porsol_fluid* fluid, const double* sat, const do
     std::memcpy(v, mb, sizeof(v));
     st.mass_balance = v[0] / std::max(std::max(v[1], v[2]), 1e-300);
     st.ms_recover = now_ms() - t_rec;
-    solved = true;
-    if (stats) *stats = st;
 }
 
 double porsol_solver::post_process()
@@ -863,6 +882,77 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     if (opts_in) o = *opts_in;
     o.same_matrix = 0;
     porsol_solve_stats acc{};
+    up_last = UpscaleSchedule{};
+    auto finish = [&] {
+        assemble_only = false;
+        reuse_amg = false;
+        reg_rows.clear();
+        batch.nblk = 0;
+    };
+    if (upscale_schedule == PORSOL_UPSCALE_PERSISTENT) {
+        // the three systems differ only in their right-hand sides: assemble each (matrix and
+        // pinned rows), keep its right-hand side, solve all sub-grids and directions in one
+        // launch, then recover each direction's fluxes
+        try {
+            const int N = S.N;
+            up_b3.alloc(3 * size_t(N));
+            up_x3.alloc(3 * size_t(N));
+            o.precision = PORSOL_FP64;
+            for (int d = 0; d < 3; ++d) {
+                for (int hf = 0; hf < nhf; ++hf)
+                    bcv[hf] = side[hf] == 2 * d + 1 ? 1.0 : (side[hf] == 2 * d + 2 ? -1.0 : 0.0);
+                porsol_solve_stats st{};
+                assemble_only = true;
+                solve(&fl, ones.data(), zeros.data(), bct.data(), bcv.data(), zeros.data(), &o, &st, false);
+                assemble_only = false;
+                launch_put3(stream, N, rhs.p, up_b3.p, d);
+                acc.ms_assemble += st.ms_assemble;
+            }
+            const double t0 = now_ms();
+            // 0: the unknowns of the largest sub-grid (each sub-grid is its own system)
+            int largest = 1;
+            for (size_t g = 0; g + 3 < batch.h.size(); g += 4)
+                largest = std::max(largest, (batch.h[g + 1] - batch.h[g]) + (batch.h[g + 3] - batch.h[g + 2]));
+            const int maxit = o.linsolver_maxit > 0 ? o.linsolver_maxit : largest;
+            const UpscaleResult r = pup.solve(stream, S.pat, val.p, batch.h, batch.ranges.p, up_b3.p, up_x3.p,
+                                              o.residual_tolerance, maxit, upscale_fixed);
+            up_last = pup.last_schedule();
+            acc.ms_krylov = now_ms() - t0;
+            bytes_krylov = pup.bytes();
+            if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
+            if (!r.converged) {
+                std::ostringstream os;
+                os << "Linear solver failed to converge in " << maxit << " iterations.\n"
+                   << "Residual reduction achieved is " << r.reduction << '\n';
+                throw Error(PORSOL_ERR_NOT_CONVERGED, os.str());
+            }
+            acc.iterations = 3 * r.iterations;
+            acc.outer_iterations = 1;
+            acc.reduction = r.reduction;
+            acc.amg_levels = 0;
+            for (int d = 0; d < 3; ++d) {
+                launch_get3(stream, N, up_x3.p, x.p, d);
+                porsol_solve_stats st{};
+                recover_solution(st);
+                acc.mass_balance = std::max(acc.mass_balance, st.mass_balance);
+                acc.ms_recover += st.ms_recover;
+                launch_side_fluxes(stream, ngrids, cellpos_d.p, facepos.p, side_d.p, outflux.p, q_d.p);
+                q_d.download(q.data(), q.size(), stream);
+                PORSOL_CUDA(cudaStreamSynchronize(stream));
+                for (int g = 0; g < ngrids; ++g)
+                    for (int i = 0; i < 3; ++i)
+                        keff[9 * size_t(g) + 3 * i + d] =
+                            L[3 * size_t(g) + d] * q[3 * size_t(g) + i] / A[3 * size_t(g) + i];
+            }
+            solved = true;
+        } catch (...) {
+            finish();
+            throw;
+        }
+        finish();
+        if (stats) *stats = acc;
+        return;
+    }
     try {
         for (int d = 0; d < 3; ++d) {
             for (int hf = 0; hf < nhf; ++hf)
@@ -1156,6 +1246,32 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
 {
     return guarded(h, [&] {
         h->upscale(grid, num_grids, grid_cellpos, hf_partner_bid, hf_side, perm, opts, k_eff, stats);
+    });
+}
+
+int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(schedule == PORSOL_UPSCALE_AMG || schedule == PORSOL_UPSCALE_PERSISTENT, PORSOL_ERR_BAD_ARG,
+                       "upscale schedule: unknown schedule");
+        PORSOL_REQUIRE(cta_threads == 0 || cta_threads == 256 || cta_threads == 512 || cta_threads == 1024,
+                       PORSOL_ERR_BAD_ARG, "upscale schedule: CTA threads must be 0, 256, 512 or 1024");
+        PORSOL_REQUIRE(warp_max_unknowns >= 0, PORSOL_ERR_BAD_ARG, "upscale schedule: negative warp limit");
+        h->upscale_schedule = schedule;
+        h->upscale_fixed = porsol::UpscaleSchedule{};
+        h->upscale_fixed.cta_threads = cta_threads;
+        h->upscale_fixed.warp_max_unknowns = cta_threads ? warp_max_unknowns : 0;
+    });
+}
+
+int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* tuned)
+{
+    return guarded(h, [&] {
+        PORSOL_REQUIRE(cta_threads && warp_max_unknowns && tuned, PORSOL_ERR_BAD_ARG, "upscale schedule: null argument");
+        const porsol::UpscaleSchedule& sc = h->up_last;
+        *cta_threads = sc.cta_threads;
+        *warp_max_unknowns = sc.warp_max_unknowns;
+        *tuned = sc.tuned ? 1 : 0;
     });
 }
 

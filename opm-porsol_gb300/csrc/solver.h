@@ -8,6 +8,7 @@
 #include "kernels.h"
 #include "krylov.h"
 #include "structure.h"
+#include "upscale.h"
 
 struct porsol_solver {
     cudaStream_t stream = nullptr;
@@ -28,6 +29,8 @@ struct porsol_solver {
     // tensor mobilities (PORSOL_FLUID_TENSOR): per-solve inner products and gravity fluxes
     porsol::DBuf<double> Wdyn, gflux_dyn, ones;
     const double* W_last = nullptr;   // inner products of the last assembly
+    const double* gflux_last = nullptr;   // ... its gravity fluxes
+    bool gzero_last = true;               // ... and whether gravity entered it
     bool tensor_last = false;
     porsol::DBuf<int> status;
     porsol::DBuf<unsigned long long> redbits;
@@ -81,6 +84,13 @@ struct porsol_solver {
     porsol::BatchCastPrecond cast_pre;   // mixed: FP32 AMG inside the FP64 batched CG
     porsol::DBuf<double> btol, bscale, bnorm;
     void batched_solve(const porsol_solve_opts& o, porsol_solve_stats& st, int maxit);
+    // ... or all three directions of every sub-grid in one persistent launch
+    int upscale_schedule = PORSOL_UPSCALE_AMG;
+    porsol::UpscaleSchedule upscale_fixed;   // cta_threads 0: the autotuner's choice
+    porsol::UpscaleSchedule up_last;         // the schedule of the last call (zeros: AMG)
+    porsol::PersistentUpscale pup;
+    porsol::DBuf<double> up_b3, up_x3;
+    bool assemble_only = false;   // solve() stops after the assembly (and the pinned rows)
 
     // adjoint (permeability sensitivity) of the last solve
     porsol_solve_opts last_opts{};
@@ -104,6 +114,7 @@ struct porsol_solver {
     void check_status(const char* where);
     void ensure_recipe(const int* bct_host, const int* bct_dev);
     void linear_solve(const porsol_solve_opts& o, porsol_solve_stats& st);
+    void recover_solution(porsol_solve_stats& st);
     // J of the last solution; leaves dJ/dpi per half-face in adj_y
     double objective(const porsol_objective* obj);
     void adjoint_gradient(const porsol_objective* obj, int mode, const porsol_solve_opts* opts, double* value,

@@ -1,0 +1,71 @@
+// upscale.h -- batched periodic upscaling in one persistent launch.
+//
+// The three unit pressure-jump problems of every sub-grid (setupUpscalingConditions' pattern,
+// common/setupBoundaryConditions.hpp:136-157) share one matrix: the sub-grid's block of the
+// assembled union system.  PersistentUpscale solves all of them in a single kernel launch
+// (captured into a CUDA graph): each sub-grid is one work item of a device queue, and the group of
+// threads that takes an item runs a Jacobi-preconditioned CG for the three right-hand sides at once
+// (one matrix read feeds three products; per-direction alpha, beta and stopping test) with only
+// group-local barriers and reductions.  Two schedules share the launch:
+//   * tile: a whole CTA (256, 512 or 1024 threads) per sub-grid, for the large sub-grids;
+//   * warp: one warp per sub-grid, for sub-grids below warp_max_unknowns unknowns.
+// Items are taken largest first (tile items, then warp items), so the longest solves start first.
+// The autotuner times every candidate schedule for a few iterations on the batch itself and
+// keeps the fastest per batch shape.
+#pragma once
+
+#include <vector>
+
+#include "krylov.h"
+
+namespace porsol {
+
+struct UpscaleSchedule {
+    int cta_threads = 0;         // threads of the CTA that solves a tile item
+    int warp_max_unknowns = 0;   // sub-grids with fewer unknowns are solved by one warp each
+    bool tuned = false;          // chosen by the autotuner (false: fixed by the caller)
+};
+
+struct UpscaleResult {
+    int iterations = 0;          // CG iterations of the slowest direction of the slowest sub-grid
+    double reduction = 0.0;      // largest final ||r|| / ||r0|| over sub-grids and directions
+    bool converged = false;
+    bool breakdown = false;
+    int worst_block = -1;        // a sub-grid that did not converge (or broke down), -1 if none
+};
+
+class PersistentUpscale {
+public:
+    // ranges: 4 per sub-grid, the unknowns [r0, r1) and [r2, r3) (host copy and device copy).
+    // b3 / x3: three values per unknown, direction d of unknown i at 3 i + d (device).  The
+    // schedule is `fixed` when its cta_threads is non-zero, else the autotuner's.
+    UpscaleResult solve(cudaStream_t s, const SellPattern& P, const double* val, const std::vector<int>& ranges,
+                        const int* ranges_d, const double* b3, double* x3, double tol, int maxit,
+                        const UpscaleSchedule& fixed);
+    const UpscaleSchedule& last_schedule() const { return sched_; }
+    // algorithmic bytes of the last solve (matrix entries once per iteration, vectors per pass)
+    double bytes() const { return bytes_; }
+    ~PersistentUpscale();
+
+private:
+    int n_ = 0, nblk_ = 0;
+    DBuf<double> r3_, p3_, q3_, dinv_, red_;
+    DBuf<int> order_, iters_, counters_, status_;
+    std::vector<int> order_h_;
+    UpscaleSchedule sched_;
+    double bytes_ = 0.0;
+    cudaGraphExec_t exec_ = nullptr;
+    std::vector<unsigned char> exec_key_;
+    void launch(cudaStream_t s, const SellPattern& P, const double* val, const int* ranges_d, const double* b3,
+                double* x3, double tol, int maxit, const UpscaleSchedule& sc, int ntile, bool graph);
+    UpscaleSchedule tune(cudaStream_t s, const SellPattern& P, const double* val, const std::vector<int>& ranges,
+                         const int* ranges_d, const double* b3, double* x3);
+    int tile_items(const std::vector<int>& ranges, int warp_max_unknowns) const;
+};
+
+// v3[3 i + d] = v[i] and v[i] = v3[3 i + d], i < n (one direction into / out of the side-by-side
+// layout)
+void launch_put3(cudaStream_t s, int n, const double* v, double* v3, int d);
+void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d);
+
+}  // namespace porsol
