@@ -883,8 +883,10 @@ def run_upscale(args, quiet=False):
                      "amg_levels": st.amg_levels, "ms_precond_setup": round(st.ms_precond_setup, 2),
                      "ms_krylov": round(st.ms_krylov, 2)}
         if sched == pkg.UPSCALE_PERSISTENT:
-            threads, wmax, tuned = s.upscale_last_schedule()
-            out[name]["schedule"] = {"cta_threads": threads, "warp_max_unknowns": wmax, "autotuned": tuned,
+            threads, wmax, layout, tuned = s.upscale_last_schedule()
+            out[name]["schedule"] = {"cta_threads": threads, "warp_max_unknowns": wmax,
+                                     "vector_layout": ["side by side", "one vector per direction"][layout],
+                                     "autotuned": tuned,
                                      "launches_per_call": "one persistent kernel for 1536 solves (CUDA graph)"}
             out[name]["precision"] = "f64 (Jacobi-preconditioned CG per sub-grid, three directions together)"
         s.close()

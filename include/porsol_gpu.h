@@ -215,16 +215,19 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
  *                              sub-grids and all three directions: each sub-grid is one work item, its
  *                              Jacobi-preconditioned CG runs the three right-hand sides together inside
  *                              one CTA ("tile") or one warp, in FP64 whatever opts->precision says.
- * cta_threads (256, 512 or 1024) and warp_max_unknowns (sub-grids with fewer face unknowns go to
- * single warps) fix the persistent schedule; cta_threads = 0 lets the autotuner time the
- * candidates (CTAs of 256/512/1024 threads x warp limits 0/4096/16384) for a few iterations on
- * the first batch of each shape and keep the fastest. */
+ * cta_threads (256, 512 or 1024), warp_max_unknowns (sub-grids with fewer face unknowns go to
+ * single warps) and vector_layout (0: the three directions of an unknown side by side, 1: one
+ * vector per direction) fix the persistent schedule; cta_threads = 0 lets the autotuner time the
+ * candidates (both layouts x CTAs of 256/512/1024 threads x warp limits 0/4096/16384) for a few
+ * iterations on the first batch of each shape and keep the fastest. */
 #define PORSOL_UPSCALE_AMG 0
 #define PORSOL_UPSCALE_PERSISTENT 1
-int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns);
+int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns,
+                                int vector_layout);
 /* The persistent schedule the last porsol_upscale_periodic call ran (zeros after an AMG-schedule
  * call); tuned = 1 when the autotuner chose it. */
-int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* tuned);
+int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* vector_layout,
+                                 int* tuned);
 
 /* ------------------------------------------------------ output fields */
 /* The cell fields writeVtkOutput gathers (common/SimulatorUtilities.hpp:54-297), computed on the

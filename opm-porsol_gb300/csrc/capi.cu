@@ -897,7 +897,8 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             const int N = S.N;
             up_b3.alloc(3 * size_t(N));
             up_x3.alloc(3 * size_t(N));
-            o.precision = PORSOL_FP64;
+            o.precision = PORSOL_MIXED;   // the assembly also writes the FP32 copy of the matrix
+            o.linsolver_type = 1;
             for (int d = 0; d < 3; ++d) {
                 for (int hf = 0; hf < nhf; ++hf)
                     bcv[hf] = side[hf] == 2 * d + 1 ? 1.0 : (side[hf] == 2 * d + 2 ? -1.0 : 0.0);
@@ -914,8 +915,9 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             for (size_t g = 0; g + 3 < batch.h.size(); g += 4)
                 largest = std::max(largest, (batch.h[g + 1] - batch.h[g]) + (batch.h[g + 3] - batch.h[g + 2]));
             const int maxit = o.linsolver_maxit > 0 ? o.linsolver_maxit : largest;
-            const UpscaleResult r = pup.solve(stream, S.pat, val.p, batch.h, batch.ranges.p, up_b3.p, up_x3.p,
-                                              o.residual_tolerance, maxit, upscale_fixed);
+            const UpscaleResult r = pup.solve(stream, S.pat, val.p, val32.p, batch.h, batch.ranges.p, up_b3.p,
+                                              up_x3.p, o.residual_tolerance,
+                                              o.inner_tolerance > 0 ? o.inner_tolerance : 3e-3, maxit, upscale_fixed);
             up_last = pup.last_schedule();
             acc.ms_krylov = now_ms() - t0;
             bytes_krylov = pup.bytes();
@@ -931,7 +933,7 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             acc.reduction = r.reduction;
             acc.amg_levels = 0;
             for (int d = 0; d < 3; ++d) {
-                launch_get3(stream, N, up_x3.p, x.p, d);
+                launch_get3(stream, N, up_x3.p, x.p, d, up_last.layout);
                 porsol_solve_stats st{};
                 recover_solution(st);
                 acc.mass_balance = std::max(acc.mass_balance, st.mass_balance);
@@ -1249,7 +1251,8 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
     });
 }
 
-int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns)
+int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns,
+                                int vector_layout)
 {
     return guarded(h, [&] {
         PORSOL_REQUIRE(schedule == PORSOL_UPSCALE_AMG || schedule == PORSOL_UPSCALE_PERSISTENT, PORSOL_ERR_BAD_ARG,
@@ -1257,20 +1260,26 @@ int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads,
         PORSOL_REQUIRE(cta_threads == 0 || cta_threads == 256 || cta_threads == 512 || cta_threads == 1024,
                        PORSOL_ERR_BAD_ARG, "upscale schedule: CTA threads must be 0, 256, 512 or 1024");
         PORSOL_REQUIRE(warp_max_unknowns >= 0, PORSOL_ERR_BAD_ARG, "upscale schedule: negative warp limit");
+        PORSOL_REQUIRE(vector_layout == 0 || vector_layout == 1, PORSOL_ERR_BAD_ARG,
+                       "upscale schedule: vector layout must be 0 or 1");
         h->upscale_schedule = schedule;
         h->upscale_fixed = porsol::UpscaleSchedule{};
         h->upscale_fixed.cta_threads = cta_threads;
         h->upscale_fixed.warp_max_unknowns = cta_threads ? warp_max_unknowns : 0;
+        h->upscale_fixed.layout = vector_layout;
     });
 }
 
-int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* tuned)
+int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* vector_layout,
+                                 int* tuned)
 {
     return guarded(h, [&] {
-        PORSOL_REQUIRE(cta_threads && warp_max_unknowns && tuned, PORSOL_ERR_BAD_ARG, "upscale schedule: null argument");
+        PORSOL_REQUIRE(cta_threads && warp_max_unknowns && vector_layout && tuned, PORSOL_ERR_BAD_ARG,
+                       "upscale schedule: null argument");
         const porsol::UpscaleSchedule& sc = h->up_last;
         *cta_threads = sc.cta_threads;
         *warp_max_unknowns = sc.warp_max_unknowns;
+        *vector_layout = sc.cta_threads ? sc.layout : 0;
         *tuned = sc.tuned ? 1 : 0;
     });
 }

@@ -3,20 +3,21 @@
 //
 // Work items are sub-grids, taken from two device counters: first the tile items (a whole CTA per
 // sub-grid, largest first), then the warp items (one warp per sub-grid).  The group that owns an
-// item runs a Jacobi-preconditioned CG for the three unit pressure-jump right-hand sides together:
-//   start   x = 0, r = b, p = D^-1 r, rho = r.D^-1 r
-//   pass A  q = A p for the three directions from one read of the sub-grid's matrix rows; p.q
-//   pass B  x += alpha p, r -= alpha q; r.D^-1 r and r.r; stopping test per direction
-//   pass C  p = D^-1 r + beta p
-// with group-local reductions only (warp shuffles, plus shared memory across the warps of a CTA),
-// so no sub-grid ever waits for another.  A direction stops when ||r|| < tol ||r0|| or
-// ||r|| < 1e-30 (the per-block test of the batched AMG solve); it is frozen from then on.
-// Vectors hold the three directions of an unknown side by side (3 i + d), so the gathers of p in
-// pass A touch one 24-byte run per column.  Every sum runs in a fixed order for a given schedule:
-// results are run-to-run reproducible; another CTA size changes the summation order.
+// item runs a Jacobi-preconditioned CG for the three unit pressure-jump right-hand sides together,
+// with FP32 recurrences (matrix copy, vectors and products in FP32: one matrix read feeds three
+// products) and reliable updates in FP64 (solution, true residual, convergence test), with
+// group-local reductions only (warp shuffles, plus shared memory across the warps of a CTA), so no
+// sub-grid ever waits for another.  A direction stops when its true residual meets
+// ||b - A x|| < tol ||b|| or ||b - A x|| < 1e-30 (the per-block test of the batched AMG solve); it
+// is frozen from then on.  FP32 matters on this GPU: one SM runs the largest sub-grid alone, and
+// with FP64 products its FP64 pipe, not memory, set the time (ncu: 95 % busy).  Every sum runs in a
+// fixed order for a given schedule: results are run-to-run reproducible; another CTA size changes
+// the summation order.
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -34,23 +35,25 @@ constexpr int UP_MAX_WARPS = UP_MAX_THREADS / 32;
 constexpr int TUNE_ITERS = 8;   // CG iterations per sub-grid of one autotuner trial
 
 struct UpArgs {
-    int nitems, ntile, maxit;
-    double tol;
-    const int* order;    // sub-grid ids: tile items [0, ntile), then warp items
-    const int* ranges;   // 4 per sub-grid
-    const int* sp;       // SELL-32 union matrix
+    int nitems, ntile, maxit, n;
+    double tol, delta;
+    const int* order;     // sub-grid ids: tile items [0, ntile), then warp items
+    const int* ranges;    // 4 per sub-grid
+    const int* sp;        // SELL-32 union matrix: FP64 values and their FP32 copy
     const int* col;
     const double* val;
+    const float* val32;
     const int* diag;
-    const double* b3;
-    double* x3;
-    double* r3;
-    double* p3;
-    double* q3;
-    double* dinv;
-    int* iters;          // 3 per sub-grid: iteration at which the direction met its test, -1: never
-    double* red;         // 3 per sub-grid: final ||r|| / ||r0||
-    int* counters;       // [0]: next tile item, [1]: next warp item
+    const double* b3;     // right-hand sides, side by side
+    double* x3;           // solutions (FP64)
+    double* r64;          // true residuals at replacements (FP64)
+    float* r32;           // CG vectors (FP32, in units of the direction's sigma)
+    float* p32;
+    float* q32;
+    float* dinv;          // 1 / a_ii
+    int* iters;           // 3 per sub-grid: iteration at which the direction met its test, -1: never
+    double* red;          // 3 per sub-grid: last true ||r|| / ||r0||
+    int* counters;        // [0]: next tile item, [1]: next warp item
     int* status;
 };
 
@@ -60,31 +63,39 @@ struct Rows {
     __device__ __forceinline__ int row(int k) const { return k < n1 ? r0 + k : r2 + (k - n1); }
 };
 
-// Sum of NV values over the group.  The warp butterfly leaves the bitwise-same total in every
-// lane (each step adds two equal pairs in swapped order); a CTA then adds the per-warp totals in
-// warp order, every thread reading them from shared memory, so all threads hold the same sums.
-// Consecutive reductions must alternate between two buffers: a thread that has left one
-// reduction's barrier may write the next one while others still read this one.
-template <bool CTA, int NV>
-__device__ __forceinline__ void group_sum(double (&v)[NV], double* sbuf)
+// Sums over the group.  The warp butterfly leaves the bitwise-same total in every lane (each step
+// adds two equal pairs in swapped order); a CTA then adds the per-warp totals in warp order in FP64,
+// every thread reading them from shared memory, so all threads hold the same sums.  Two buffers
+// alternate from one reduction to the next (rb): a thread that has left one reduction's barrier
+// may write the next one while others still read this one.  FP32 partials (the CG's dot products)
+// are summed in FP32 within a warp and in FP64 across warps.
+template <bool CTA, int NV, class T>
+__device__ __forceinline__ void group_sum(const T (&v)[NV], double (&out)[NV], double* sb, int& rb)
 {
+    T w[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i)
+    for (int i = 0; i < NV; ++i) {
+        w[i] = v[i];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(FULL, v[i], o);
+        for (int o = 16; o > 0; o >>= 1) w[i] += __shfl_xor_sync(FULL, w[i], o);
+    }
     if constexpr (CTA) {
-        const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        double* buf = sb + rb * (UP_MAX_WARPS * 6);
+        rb ^= 1;
+        const int wi = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if ((threadIdx.x & 31) == 0)
 #pragma unroll
-            for (int i = 0; i < NV; ++i) sbuf[w * NV + i] = v[i];
+            for (int i = 0; i < NV; ++i) buf[wi * NV + i] = double(w[i]);
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
             double s = 0.0;
-            for (int j = 0; j < nw; ++j) s += sbuf[j * NV + i];
-            v[i] = s;
+            for (int j = 0; j < nw; ++j) s += buf[j * NV + i];
+            out[i] = s;
         }
     } else {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) out[i] = double(w[i]);
         __syncwarp();
     }
 }
@@ -96,23 +107,32 @@ __device__ __forceinline__ void group_sync()
     else __syncwarp();
 }
 
-// q = (A p)_r for the three directions: the row's SELL-32 entries read once, four entries' loads
-// in flight before their gathers; products added in entry order (padding adds exact zeros).
+// Position of direction d of unknown i in the three-direction vectors: side by side (L = 0,
+// 3 i + d: one run per gathered column) or direction-major (L = 1, d n + i: every streamed access
+// of a warp is one contiguous run).  The autotuner tries both.
+template <int L>
+__device__ __forceinline__ size_t vix(int i, int d, int n)
+{
+    return L == 0 ? 3 * size_t(i) + d : size_t(d) * size_t(n) + i;
+}
+
+// q = (A y)_r for the three directions (values TV, vector TX, sums TA): the row's SELL-32
+// entries read once, two entries' loads in flight before their gathers; products added in entry
+// order (padding adds exact zeros).
+template <int L, class TA, class TV, class TX>
 __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int* __restrict__ col,
-                                           const double* __restrict__ val, const double* __restrict__ p3, int r,
-                                           double& q0, double& q1, double& q2)
+                                           const TV* __restrict__ val, const TX* __restrict__ y, int n, int r,
+                                           TA (&q)[3])
 {
     const int s = r >> 5;
     const int b = sp[s], w = (sp[s + 1] - b) >> 5;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    TA a0 = TA(0), a1 = TA(0), a2 = TA(0);
     int k = b + (r & 31), t = 0;
     for (; t + 2 <= w; t += 2, k += 64) {
         const int c0 = col[k], c1 = col[k + 32];
-        const double v0 = val[k], v1 = val[k + 32];
-        const double* y0 = p3 + 3 * size_t(c0);
-        const double* y1 = p3 + 3 * size_t(c1);
-        const double y00 = y0[0], y01 = y0[1], y02 = y0[2];
-        const double y10 = y1[0], y11 = y1[1], y12 = y1[2];
+        const TA v0 = TA(val[k]), v1 = TA(val[k + 32]);
+        const TA y00 = TA(y[vix<L>(c0, 0, n)]), y01 = TA(y[vix<L>(c0, 1, n)]), y02 = TA(y[vix<L>(c0, 2, n)]);
+        const TA y10 = TA(y[vix<L>(c1, 0, n)]), y11 = TA(y[vix<L>(c1, 1, n)]), y12 = TA(y[vix<L>(c1, 2, n)]);
         a0 += v0 * y00;
         a1 += v0 * y01;
         a2 += v0 * y02;
@@ -122,151 +142,281 @@ __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int
     }
     if (t < w) {
         const int c0 = col[k];
-        const double v0 = val[k];
-        const double* y0 = p3 + 3 * size_t(c0);
-        a0 += v0 * y0[0];
-        a1 += v0 * y0[1];
-        a2 += v0 * y0[2];
+        const TA v0 = TA(val[k]);
+        a0 += v0 * TA(y[vix<L>(c0, 0, n)]);
+        a1 += v0 * TA(y[vix<L>(c0, 1, n)]);
+        a2 += v0 * TA(y[vix<L>(c0, 2, n)]);
     }
-    q0 = a0;
-    q1 = a1;
-    q2 = a2;
+    q[0] = a0;
+    q[1] = a1;
+    q[2] = a2;
 }
 
-// The CG of one sub-grid, three directions at once, by a group of nthr threads (tid = rank).
-template <bool CTA>
-__device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb0, double* sb1)
+// The CG of one sub-grid, three directions at once, by a group of nthr threads (tid = rank), with
+// FP32 recurrences and reliable updates (residual replacement, Sleijpen and van der Vorst):
+//   start   x = 0, sigma = ||b||, r = b / sigma (FP32), p = D^-1 r, rho = r.D^-1 r
+//   pass A  q = A32 p (FP32), p.q
+//   pass B  x += sigma alpha p (FP64), r -= alpha q; r.D^-1 r, r.r
+//   when ||r|| has dropped below delta since the last replacement, or sigma ||r|| reaches the
+//   tolerance: pass R, the true residual b - A x in FP64, which alone decides convergence; then
+//   pass S, r = (b - A x) / sigma' and p *= sigma / sigma' (the recurrence continues in units of
+//   the new sigma), r.D^-1 r again
+// x stays FP64 every iteration: an FP32 increment of x flushed at each replacement (measured) let
+// one sub-grid of the 512-sub-grid batch stall at 3.3e-11 against a 1e-11 tolerance, its rounding
+// times the condition number bounding the residual each replacement can reach.
+//   pass C  p = D^-1 r + beta p
+// Each pass loads all of a row's values before it stores any, and frozen directions neither load
+// nor store.  Thread 0 keeps the per-direction iteration count and reduction in global memory.
+template <bool CTA, int L>
+__device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
 {
     const int* rg = a.ranges + 4 * g;
     const Rows R{rg[0], rg[1] - rg[0], rg[2], (rg[1] - rg[0]) + (rg[3] - rg[2])};
+    const int n = a.n;
+    int rb = 0;
     bool bad = false;
-    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double v[3] = {0.0, 0.0, 0.0}, sum[3];
     for (int k = tid; k < R.n; k += nthr) {
         const int r = R.row(k);
+        double b[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) b[d] = a.b3[vix<0>(r, d, n)];   // right-hand sides: side by side
         const double di = a.val[a.diag[r]];
         bad |= !(di > 0.0);
-        const double dv = 1.0 / di;
-        a.dinv[r] = dv;
+        a.dinv[r] = float(1.0 / di);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const double b = a.b3[3 * size_t(r) + d];
-            const double z = dv * b;
-            a.x3[3 * size_t(r) + d] = 0.0;
-            a.r3[3 * size_t(r) + d] = b;
-            a.p3[3 * size_t(r) + d] = z;
-            v[d] += b * z;
-            v[3 + d] += b * b;
+            a.x3[vix<L>(r, d, n)] = 0.0;
+            v[d] += b[d] * b[d];
         }
     }
     if (bad) atomicOr(a.status, ST_NONFINITE);
-    group_sum<CTA, 6>(v, sb0);
-    double rz[3], nr0[3], red[3];
+    group_sum<CTA, 3>(v, sum, sb, rb);
+    double sig[3], def0[3], rho[3];
     bool act[3];
-    int itc[3];
     bool brk = false;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        rz[d] = v[d];
-        nr0[d] = sqrt(v[3 + d]);
-        red[d] = 0.0;
-        const bool fin = isfinite(nr0[d]) && isfinite(rz[d]);
+        def0[d] = sig[d] = sqrt(sum[d]);
+        const bool fin = isfinite(def0[d]);
         brk |= !fin;
-        act[d] = fin && !(nr0[d] < 1e-30);
-        itc[d] = fin ? (act[d] ? -1 : 0) : -1;
+        act[d] = fin && !(def0[d] < 1e-30);
+        if (tid == 0) {
+            a.iters[3 * g + d] = fin ? (act[d] ? -1 : 0) : -1;
+            a.red[3 * g + d] = act[d] ? 1.0 : 0.0;
+        }
+    }
+    {
+        float u[3] = {0.f, 0.f, 0.f};
+        for (int k = tid; k < R.n; k += nthr) {
+            const int r = R.row(k);
+            double b[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) b[d] = a.b3[vix<0>(r, d, n)];
+            const float dv = a.dinv[r];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float rr = act[d] ? float(b[d] / sig[d]) : 0.f;
+                a.r32[vix<L>(r, d, n)] = rr;
+                a.p32[vix<L>(r, d, n)] = dv * rr;
+                u[d] += rr * (dv * rr);
+            }
+        }
+        group_sum<CTA, 3>(u, rho, sb, rb);
     }
     int it = 0;
     while ((act[0] || act[1] || act[2]) && it < a.maxit) {
         ++it;
-        // pass A
-        double w[3] = {0.0, 0.0, 0.0};
-        for (int k = tid; k < R.n; k += nthr) {
-            const int r = R.row(k);
-            double q0, q1, q2;
-            row_apply3(a.sp, a.col, a.val, a.p3, r, q0, q1, q2);
-            double* q = a.q3 + 3 * size_t(r);
-            const double* p = a.p3 + 3 * size_t(r);
-            q[0] = q0;
-            q[1] = q1;
-            q[2] = q2;
-            w[0] += p[0] * q0;
-            w[1] += p[1] * q1;
-            w[2] += p[2] * q2;
+        // pass A: q = A32 p, p.q
+        {
+            float w[3] = {0.f, 0.f, 0.f};
+            for (int k = tid; k < R.n; k += nthr) {
+                const int r = R.row(k);
+                float p[3], q[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) p[d] = a.p32[vix<L>(r, d, n)];
+                row_apply3<L, float>(a.sp, a.col, a.val32, a.p32, n, r, q);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    a.q32[vix<L>(r, d, n)] = q[d];
+                    w[d] += p[d] * q[d];
+                }
+            }
+            group_sum<CTA, 3>(w, sum, sb, rb);
         }
-        group_sum<CTA, 3>(w, sb1);
         double al[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            if (act[d] && !(w[d] > 0.0 && isfinite(w[d]))) {   // non-positive curvature: stop
+            if (act[d] && !(sum[d] > 0.0 && isfinite(sum[d]))) {   // non-positive curvature: stop
                 act[d] = false;
                 brk = true;
             }
-            al[d] = act[d] ? rz[d] / w[d] : 0.0;
+            al[d] = act[d] ? rho[d] / sum[d] : 0.0;
         }
-        // pass B
-        double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int k = tid; k < R.n; k += nthr) {
-            const int r = R.row(k);
-            const double dv = a.dinv[r];
+        // pass B: x += sigma alpha p, r -= alpha q; r.D^-1 r, r.r
+        double u[3], rr2[3];
+        {
+            float part[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int k = tid; k < R.n; k += nthr) {
+                const int r = R.row(k);
+                const float dv = a.dinv[r];
+                double x[3];
+                float p[3], rr[3], q[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                if (act[d]) {
-                    const size_t i = 3 * size_t(r) + d;
-                    a.x3[i] += al[d] * a.p3[i];
-                    const double rn = a.r3[i] - al[d] * a.q3[i];
-                    a.r3[i] = rn;
-                    u[d] += rn * (dv * rn);
-                    u[3 + d] += rn * rn;
+                for (int d = 0; d < 3; ++d) {
+                    x[d] = 0.0;
+                    p[d] = rr[d] = q[d] = 0.f;
+                    if (act[d]) {
+                        x[d] = a.x3[vix<L>(r, d, n)];
+                        p[d] = a.p32[vix<L>(r, d, n)];
+                        rr[d] = a.r32[vix<L>(r, d, n)];
+                        q[d] = a.q32[vix<L>(r, d, n)];
+                    }
                 }
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if (act[d]) {
+                        const float rn = rr[d] - float(al[d]) * q[d];
+                        a.x3[vix<L>(r, d, n)] = x[d] + (sig[d] * al[d]) * double(p[d]);
+                        a.r32[vix<L>(r, d, n)] = rn;
+                        part[d] += rn * (dv * rn);
+                        part[3 + d] += rn * rn;
+                    }
+            }
+            double tot[6];
+            group_sum<CTA, 6>(part, tot, sb, rb);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                u[d] = tot[d];
+                rr2[d] = tot[3 + d];
+            }
         }
-        group_sum<CTA, 6>(u, sb0);
+        // reliable update: which directions replace their residual
+        bool rep[3], any = false;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double defs = sqrt(rr2[d]), est = defs * sig[d];
+            rep[d] = act[d] && (defs < a.delta || est < a.tol * def0[d] || est < 1e-30 || !isfinite(defs) ||
+                                it >= a.maxit);
+            any |= rep[d];
+        }
+        if (any) {
+            // pass R: the true residual b - A x (FP64) of the replacing directions
+            double t2[3] = {0.0, 0.0, 0.0};
+            for (int k = tid; k < R.n; k += nthr) {
+                const int r = R.row(k);
+                double ax[3];
+                row_apply3<L, double>(a.sp, a.col, a.val, a.x3, n, r, ax);
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if (rep[d]) {
+                        const double t = a.b3[vix<0>(r, d, n)] - ax[d];
+                        a.r64[vix<L>(r, d, n)] = t;
+                        t2[d] += t * t;
+                    }
+            }
+            group_sum<CTA, 3>(t2, sum, sb, rb);
+            bool resc[3], anyr = false;
+            double fac[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                resc[d] = false;
+                fac[d] = 1.0;
+                if (!rep[d]) continue;
+                const double dd = sqrt(sum[d]);
+                if (tid == 0) a.red[3 * g + d] = dd / def0[d];
+                if (!isfinite(dd)) {
+                    act[d] = false;
+                    brk = true;
+                } else if (dd < a.tol * def0[d] || dd < 1e-30) {
+                    act[d] = false;
+                    if (tid == 0) a.iters[3 * g + d] = it;
+                } else if (it >= a.maxit) {
+                    act[d] = false;
+                } else {
+                    fac[d] = sig[d] / dd;
+                    rho[d] *= fac[d] * fac[d];
+                    sig[d] = dd;
+                    resc[d] = true;
+                    anyr = true;
+                }
+            }
+            if (anyr) {
+                // pass S: r = r_true / sigma, p in units of the new sigma; r.D^-1 r of the new r
+                float uu[3] = {0.f, 0.f, 0.f};
+                for (int k = tid; k < R.n; k += nthr) {
+                    const int r = R.row(k);
+                    const float dv = a.dinv[r];
+                    double t[3];
+                    float p[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        t[d] = 0.0;
+                        p[d] = 0.f;
+                        if (resc[d]) {
+                            t[d] = a.r64[vix<L>(r, d, n)];
+                            p[d] = a.p32[vix<L>(r, d, n)];
+                        }
+                    }
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        if (resc[d]) {
+                            const float rn = float(t[d] / sig[d]);
+                            a.r32[vix<L>(r, d, n)] = rn;
+                            a.p32[vix<L>(r, d, n)] = p[d] * float(fac[d]);
+                            uu[d] += rn * (dv * rn);
+                        }
+                }
+                double un[3];
+                group_sum<CTA, 3>(uu, un, sb, rb);
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if (resc[d]) u[d] = un[d];
+            }
+        }
         double be[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             be[d] = 0.0;
             if (!act[d]) continue;
-            const double nr = sqrt(u[3 + d]);
-            red[d] = nr0[d] > 0.0 ? nr / nr0[d] : 0.0;
-            if (!isfinite(nr) || !isfinite(u[d])) {
+            if (!isfinite(u[d])) {
                 act[d] = false;
                 brk = true;
-            } else if (nr < a.tol * nr0[d] || nr < 1e-30) {
-                act[d] = false;
-                itc[d] = it;
-            } else {
-                be[d] = u[d] / rz[d];
-                rz[d] = u[d];
+                continue;
             }
+            be[d] = u[d] / rho[d];
+            rho[d] = u[d];
         }
         if (!(act[0] || act[1] || act[2])) break;
-        // pass C
+        // pass C: p = D^-1 r + beta p
         for (int k = tid; k < R.n; k += nthr) {
             const int r = R.row(k);
-            const double dv = a.dinv[r];
+            const float dv = a.dinv[r];
+            float p[3], rr[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                p[d] = rr[d] = 0.f;
+                if (act[d]) {
+                    p[d] = a.p32[vix<L>(r, d, n)];
+                    rr[d] = a.r32[vix<L>(r, d, n)];
+                }
+            }
 #pragma unroll
             for (int d = 0; d < 3; ++d)
-                if (act[d]) {
-                    const size_t i = 3 * size_t(r) + d;
-                    a.p3[i] = dv * a.r3[i] + be[d] * a.p3[i];
-                }
+                if (act[d]) a.p32[vix<L>(r, d, n)] = dv * rr[d] + float(be[d]) * p[d];
         }
         group_sync<CTA>();
     }
-    if (tid == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            a.iters[3 * g + d] = itc[d];
-            a.red[3 * g + d] = red[d];
-        }
-        if (brk) atomicOr(a.status, ST_BREAKDOWN);
-    }
+    if (tid == 0 && brk) atomicOr(a.status, ST_BREAKDOWN);
 }
 
 // The persistent kernel: tile items while any is left (the CTA takes the next one), then warp
 // items (each warp on its own).  Every loop ends: the counters only grow, and each CG is bounded
 // by maxit.
+template <int L>
 __global__ void __launch_bounds__(UP_MAX_THREADS, 1) k_upscale_persistent(const UpArgs a)
 {
-    __shared__ double sb[2][UP_MAX_WARPS * 6];
+    __shared__ double sb[2 * UP_MAX_WARPS * 6];
     __shared__ int s_item;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(a.counters, 1);
@@ -274,7 +424,7 @@ __global__ void __launch_bounds__(UP_MAX_THREADS, 1) k_upscale_persistent(const 
         const int item = s_item;
         __syncthreads();   // every thread has read s_item before thread 0 writes it again
         if (item >= a.ntile) break;
-        solve_one<true>(a, a.order[item], threadIdx.x, blockDim.x, sb[0], sb[1]);
+        solve_one<true, L>(a, a.order[item], threadIdx.x, blockDim.x, sb);
     }
     const int lane = threadIdx.x & 31;
     const int nwarp = a.nitems - a.ntile;
@@ -283,7 +433,7 @@ __global__ void __launch_bounds__(UP_MAX_THREADS, 1) k_upscale_persistent(const 
         if (lane == 0) item = atomicAdd(a.counters + 1, 1);
         item = __shfl_sync(FULL, item, 0);
         if (item >= nwarp) break;
-        solve_one<false>(a, a.order[a.ntile + item], lane, 32, nullptr, nullptr);
+        solve_one<false, L>(a, a.order[a.ntile + item], lane, 32, nullptr);
     }
 }
 
@@ -293,10 +443,10 @@ __global__ void k_put3(int n, const double* __restrict__ v, double* __restrict__
     if (i < n) v3[3 * size_t(i) + d] = v[i];
 }
 
-__global__ void k_get3(int n, const double* __restrict__ v3, double* __restrict__ v, int d)
+__global__ void k_get3(int n, const double* __restrict__ v3, double* __restrict__ v, int d, int layout)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = v3[3 * size_t(i) + d];
+    if (i < n) v[i] = layout == 0 ? v3[3 * size_t(i) + d] : v3[size_t(d) * size_t(n) + i];
 }
 
 // Autotuner choices, per batch shape (sub-grid count, log2 of the unknowns, log2 of the largest
@@ -328,10 +478,10 @@ void launch_put3(cudaStream_t s, int n, const double* v, double* v3, int d)
     PORSOL_CUDA(cudaGetLastError());
 }
 
-void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d)
+void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d, int layout)
 {
     if (n <= 0) return;
-    PORSOL_LAUNCH(k_get3<<<div_up(n, 256), 256, 0, s>>>(n, v3, v, d));
+    PORSOL_LAUNCH(k_get3<<<div_up(n, 256), 256, 0, s>>>(n, v3, v, d, layout));
     PORSOL_CUDA(cudaGetLastError());
 }
 
@@ -350,27 +500,31 @@ int PersistentUpscale::tile_items(const std::vector<int>& rg, int wmax) const
     return nt;
 }
 
-void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const double* val, const int* ranges_d,
-                               const double* b3, double* x3, double tol, int maxit, const UpscaleSchedule& sc,
-                               int ntile, bool graph)
+void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
+                               const int* ranges_d, const double* b3, double* x3, double tol, double delta, int maxit,
+                               const UpscaleSchedule& sc, int ntile, bool graph)
 {
     UpArgs a;
     std::memset(&a, 0, sizeof(a));
     a.nitems = nblk_;
     a.ntile = ntile;
+    a.n = n_;
     a.maxit = maxit;
     a.tol = tol;
+    a.delta = delta;
     a.order = order_.p;
     a.ranges = ranges_d;
     a.sp = P.slice_ptr.p;
     a.col = P.col.p;
     a.val = val;
+    a.val32 = val32;
     a.diag = P.diag.p;
     a.b3 = b3;
     a.x3 = x3;
-    a.r3 = r3_.p;
-    a.p3 = p3_.p;
-    a.q3 = q3_.p;
+    a.r64 = r64_.p;
+    a.r32 = r32_.p;
+    a.p32 = p32_.p;
+    a.q32 = q32_.p;
     a.dinv = dinv_.p;
     a.iters = iters_.p;
     a.red = red_.p;
@@ -379,11 +533,12 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
     int dev = 0, sms = 0, per = 0;
     PORSOL_CUDA(cudaGetDevice(&dev));
     PORSOL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    PORSOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_upscale_persistent, sc.cta_threads, 0));
+    void (*kern)(const UpArgs) = sc.layout == 0 ? k_upscale_persistent<0> : k_upscale_persistent<1>;
+    PORSOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, sc.cta_threads, 0));
     const int grid = std::max(1, sms * std::max(per, 1));
     auto enqueue = [&] {
         PORSOL_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(int), s));
-        PORSOL_LAUNCH(k_upscale_persistent<<<grid, sc.cta_threads, 0, s>>>(a));
+        PORSOL_LAUNCH(kern<<<grid, sc.cta_threads, 0, s>>>(a));
         PORSOL_CUDA(cudaGetLastError());
     };
     if (!graph) {
@@ -391,10 +546,11 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
         return;
     }
     // the launch (with the queue reset) as a captured graph, rebuilt when an argument changes
-    std::vector<unsigned char> key(sizeof(a) + 2 * sizeof(int));
+    std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int));
     std::memcpy(key.data(), &a, sizeof(a));
     std::memcpy(key.data() + sizeof(a), &grid, sizeof(int));
     std::memcpy(key.data() + sizeof(a) + sizeof(int), &sc.cta_threads, sizeof(int));
+    std::memcpy(key.data() + sizeof(a) + 2 * sizeof(int), &sc.layout, sizeof(int));
     if (!exec_ || key != exec_key_) {
         if (exec_) PORSOL_CUDA(cudaGraphExecDestroy(exec_));
         exec_ = nullptr;
@@ -412,11 +568,11 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
     PORSOL_COUNT_LAUNCH();
 }
 
-// Candidate schedules: CTAs of 256, 512 or 1024 threads for the tile items, and sub-grids below
-// 0, 4096 or 16384 unknowns (sides up to about 11 and 17 in the unit-cube batches) left to single
-// warps.  Each candidate runs TUNE_ITERS iterations of every sub-grid once, after one warm-up
+// Candidate schedules: both vector layouts; CTAs of 256, 512 or 1024 threads for the tile items;
+// sub-grids below 0, 4096 or 16384 unknowns (sides up to about 11 and 17 in the unit-cube batches)
+// left to single warps.  Each candidate runs TUNE_ITERS iterations of every sub-grid once, after one warm-up
 // launch; the fastest is kept for the batch shape.
-UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, const double* val,
+UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
                                         const std::vector<int>& rg, const int* ranges_d, const double* b3, double* x3)
 {
     long long total = 0, largest = 0;
@@ -432,6 +588,7 @@ UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, co
         auto it = tune_cache().find(key);
         if (it != tune_cache().end()) return it->second;
     }
+    static const bool debug = std::getenv("PORSOL_DEBUG_UPSCALE") != nullptr;
     cudaEvent_t e0, e1;
     PORSOL_CUDA(cudaEventCreate(&e0));
     PORSOL_CUDA(cudaEventCreate(&e1));
@@ -439,28 +596,33 @@ UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, co
     float best_ms = 1e30f;
     bool warmed = false;
     try {
-        for (int threads : {256, 512, 1024})
-            for (int wmax : {0, 4096, 16384}) {
-                UpscaleSchedule c;
-                c.cta_threads = threads;
-                c.warp_max_unknowns = wmax;
-                c.tuned = true;
-                const int nt = tile_items(rg, wmax);
-                if (!warmed) {
-                    launch(s, P, val, ranges_d, b3, x3, 0.0, TUNE_ITERS, c, nt, false);
-                    warmed = true;
+        for (int layout : {0, 1})
+            for (int threads : {256, 512, 1024})
+                for (int wmax : {0, 4096, 16384}) {
+                    UpscaleSchedule c;
+                    c.cta_threads = threads;
+                    c.warp_max_unknowns = wmax;
+                    c.layout = layout;
+                    c.tuned = true;
+                    const int nt = tile_items(rg, wmax);
+                    if (!warmed) {
+                        launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, nt, false);
+                        warmed = true;
+                    }
+                    PORSOL_CUDA(cudaEventRecord(e0, s));
+                    launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, nt, false);
+                    PORSOL_CUDA(cudaEventRecord(e1, s));
+                    PORSOL_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    PORSOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (debug)
+                        std::fprintf(stderr, "[upscale] trial layout=%d cta=%d warp_below=%d: %.3f ms\n", layout, threads,
+                                     wmax, ms);
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = c;
+                    }
                 }
-                PORSOL_CUDA(cudaEventRecord(e0, s));
-                launch(s, P, val, ranges_d, b3, x3, 0.0, TUNE_ITERS, c, nt, false);
-                PORSOL_CUDA(cudaEventRecord(e1, s));
-                PORSOL_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                PORSOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = c;
-                }
-            }
     } catch (...) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -473,9 +635,9 @@ UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, co
     return best;
 }
 
-UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, const double* val,
+UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
                                        const std::vector<int>& rg, const int* ranges_d, const double* b3, double* x3,
-                                       double tol, int maxit, const UpscaleSchedule& fixed)
+                                       double tol, double delta, int maxit, const UpscaleSchedule& fixed)
 {
     PORSOL_REQUIRE(rg.size() % 4 == 0 && !rg.empty(), PORSOL_ERR_BAD_ARG, "persistent upscaling: no sub-grids");
     PORSOL_REQUIRE(P.n <= INT_MAX / 3, PORSOL_ERR_BAD_ARG, "persistent upscaling: too many unknowns");
@@ -484,9 +646,10 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
                    PORSOL_ERR_BAD_ARG, "persistent upscaling: CTA threads must be 256, 512 or 1024");
     n_ = P.n;
     nblk_ = int(rg.size() / 4);
-    r3_.alloc(3 * size_t(n_));
-    p3_.alloc(3 * size_t(n_));
-    q3_.alloc(3 * size_t(n_));
+    r64_.alloc(3 * size_t(n_));
+    r32_.alloc(3 * size_t(n_));
+    p32_.alloc(3 * size_t(n_));
+    q32_.alloc(3 * size_t(n_));
     dinv_.alloc(size_t(n_));
     red_.alloc(3 * size_t(nblk_));
     iters_.alloc(3 * size_t(nblk_));
@@ -503,11 +666,11 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
                      [&](int x, int y) { return nrow[size_t(x)] > nrow[size_t(y)]; });
     order_.upload(order_h_, s);
     status_.zero(s);
-    sched_ = fixed.cta_threads ? fixed : tune(s, P, val, rg, ranges_d, b3, x3);
+    sched_ = fixed.cta_threads ? fixed : tune(s, P, val, val32, rg, ranges_d, b3, x3);
     if (fixed.cta_threads) sched_.tuned = false;
     const int nt = tile_items(rg, sched_.warp_max_unknowns);
     status_.zero(s);
-    launch(s, P, val, ranges_d, b3, x3, tol, maxit, sched_, nt, true);
+    launch(s, P, val, val32, ranges_d, b3, x3, tol, delta, maxit, sched_, nt, true);
     std::vector<int> its(3 * size_t(nblk_));
     std::vector<double> red(3 * size_t(nblk_));
     int st = 0;
@@ -534,11 +697,13 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
             }
         }
         res.iterations = std::max(res.iterations, gi);
-        // start: diagonal, b, x, r, p (3 each); per iteration: stored entries (column 4 + value 8),
-        // p gathered once and q written (24 + 24), pass B (D^-1, x, r twice, p, q) and pass C
-        // (D^-1, r, p twice), three directions each
+        // start: diagonal and b twice, x, r, p; per iteration: stored entries (column 4 + FP32 value
+        // 4), p gathered once, its own value read and q written (3 x 4 each), pass B (D^-1 4; x read
+        // and written 16, p 4, r read and written 8, q 4 per direction) and pass C (D^-1 4; r 4, p
+        // read and written 8 per direction); replacements are not counted
         const double n = nrow[size_t(g)];
-        bytes_ += n * (12.0 + 8.0 + 4 * 24.0) + gi * n * (12.0 * avg_entries + 48.0 + 8.0 + 6 * 24.0 + 8.0 + 3 * 24.0);
+        bytes_ += n * (12.0 + 48.0 + 3 * (8.0 + 4.0 + 4.0)) +
+                  gi * n * (8.0 * avg_entries + 36.0 + 4.0 + 3 * 32.0 + 4.0 + 3 * 12.0);
     }
     return res;
 }

@@ -70,6 +70,7 @@ struct porsol_transport {
     porsol::DBuf<double> ve_coef, fbc, frac2;
     bool any_gravity = false;   // some face entry has a non-zero gravity driving force
     porsol::DBuf<unsigned long long> red;
+    porsol::DBuf<double> cfl_part;   // per-block minima of the CFL bounds
 
     // rock tables (porsol_transport_set_rock_tables); rock.nrock == 0 without
     porsol::RockView rock;            // device pointers

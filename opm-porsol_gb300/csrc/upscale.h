@@ -6,7 +6,8 @@
 // (captured into a CUDA graph): each sub-grid is one work item of a device queue, and the group of
 // threads that takes an item runs a Jacobi-preconditioned CG for the three right-hand sides at once
 // (one matrix read feeds three products; per-direction alpha, beta and stopping test) with only
-// group-local barriers and reductions.  Two schedules share the launch:
+// group-local barriers and reductions.  The CG recurrences run in FP32 with reliable updates: the
+// solution and the true residual, which alone decides convergence, are FP64.  Two schedules share the launch:
 //   * tile: a whole CTA (256, 512 or 1024 threads) per sub-grid, for the large sub-grids;
 //   * warp: one warp per sub-grid, for sub-grids below warp_max_unknowns unknowns.
 // Items are taken largest first (tile items, then warp items), so the longest solves start first.
@@ -23,6 +24,7 @@ namespace porsol {
 struct UpscaleSchedule {
     int cta_threads = 0;         // threads of the CTA that solves a tile item
     int warp_max_unknowns = 0;   // sub-grids with fewer unknowns are solved by one warp each
+    int layout = 1;              // vectors: 0 side by side (3 i + d), 1 direction-major (d n + i)
     bool tuned = false;          // chosen by the autotuner (false: fixed by the caller)
 };
 
@@ -37,11 +39,14 @@ struct UpscaleResult {
 class PersistentUpscale {
 public:
     // ranges: 4 per sub-grid, the unknowns [r0, r1) and [r2, r3) (host copy and device copy).
-    // b3 / x3: three values per unknown, direction d of unknown i at 3 i + d (device).  The
-    // schedule is `fixed` when its cta_threads is non-zero, else the autotuner's.
-    UpscaleResult solve(cudaStream_t s, const SellPattern& P, const double* val, const std::vector<int>& ranges,
-                        const int* ranges_d, const double* b3, double* x3, double tol, int maxit,
-                        const UpscaleSchedule& fixed);
+    // b3: three right-hand sides, direction d of unknown i at 3 i + d (device); x3: the three
+    // solutions (3 n, device) in the schedule's layout, read with launch_get3.  The schedule is
+    // `fixed` when its cta_threads is non-zero, else the autotuner's.
+    // val / val32: the system's values and their FP32 copy; delta: the drop of the FP32 residual
+    // that triggers a replacement by the true FP64 residual.
+    UpscaleResult solve(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
+                        const std::vector<int>& ranges, const int* ranges_d, const double* b3, double* x3, double tol,
+                        double delta, int maxit, const UpscaleSchedule& fixed);
     const UpscaleSchedule& last_schedule() const { return sched_; }
     // algorithmic bytes of the last solve (matrix entries once per iteration, vectors per pass)
     double bytes() const { return bytes_; }
@@ -49,23 +54,25 @@ public:
 
 private:
     int n_ = 0, nblk_ = 0;
-    DBuf<double> r3_, p3_, q3_, dinv_, red_;
+    DBuf<double> r64_, red_;
+    DBuf<float> r32_, p32_, q32_, dinv_;
     DBuf<int> order_, iters_, counters_, status_;
     std::vector<int> order_h_;
     UpscaleSchedule sched_;
     double bytes_ = 0.0;
     cudaGraphExec_t exec_ = nullptr;
     std::vector<unsigned char> exec_key_;
-    void launch(cudaStream_t s, const SellPattern& P, const double* val, const int* ranges_d, const double* b3,
-                double* x3, double tol, int maxit, const UpscaleSchedule& sc, int ntile, bool graph);
-    UpscaleSchedule tune(cudaStream_t s, const SellPattern& P, const double* val, const std::vector<int>& ranges,
-                         const int* ranges_d, const double* b3, double* x3);
+    void launch(cudaStream_t s, const SellPattern& P, const double* val, const float* val32, const int* ranges_d,
+                const double* b3, double* x3, double tol, double delta, int maxit, const UpscaleSchedule& sc,
+                int ntile, bool graph);
+    UpscaleSchedule tune(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
+                         const std::vector<int>& ranges, const int* ranges_d, const double* b3, double* x3);
     int tile_items(const std::vector<int>& ranges, int warp_max_unknowns) const;
 };
 
-// v3[3 i + d] = v[i] and v[i] = v3[3 i + d], i < n (one direction into / out of the side-by-side
-// layout)
+// v3[3 i + d] = v[i], i < n (one direction into the side-by-side layout), and v[i] = direction d
+// of unknown i in v3 of the given layout
 void launch_put3(cudaStream_t s, int n, const double* v, double* v3, int d);
-void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d);
+void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d, int layout);
 
 }  // namespace porsol

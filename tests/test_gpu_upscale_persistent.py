@@ -27,8 +27,8 @@ def _rel(a, b):
 def test_persistent_small_subgrids_match_oracle_autotuned(pkg, gpulib, orc, workloads):
     union, sizes, K = workloads.periodic_subgrids(num=5, nmin=3, nmax=6, seed=21)
     s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(0, 0))
-    threads, wmax, tuned = s.upscale_last_schedule()
-    assert tuned and threads in (256, 512, 1024) and wmax in (0, 4096, 16384)
+    threads, wmax, layout, tuned = s.upscale_last_schedule()
+    assert tuned and threads in (256, 512, 1024) and wmax in (0, 4096, 16384) and layout in (0, 1)
     assert st.amg_levels == 0 and st.iterations > 0
     for g in range(len(sizes)):
         c0, c1 = union.cellpos[g], union.cellpos[g + 1]
@@ -41,15 +41,16 @@ def test_persistent_small_subgrids_match_oracle_autotuned(pkg, gpulib, orc, work
 
 def test_persistent_sides_8_to_32_against_oracle(pkg, gpulib, orc, workloads):
     """Sides spanning the 512-sub-grid workload's U{8..32}: the 8^3 sub-grid (1728 unknowns) goes to
-    a single warp, the others to 512-thread CTAs."""
+    a single warp, the others to 512-thread CTAs; both vector layouts."""
     union, sizes, K = workloads.periodic_subgrids(seed=23, sides=[8, 13, 19, 26, 32])
-    s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(512, 4096))
-    assert s.upscale_last_schedule() == (512, 4096, False)
-    for gi in range(len(sizes)):
-        c0, c1 = union.cellpos[gi], union.cellpos[gi + 1]
-        ref = oracle_keff(orc, union.grids[gi], K[c0:c1])
-        assert _rel(keff[gi], ref) < 1e-9, (int(sizes[gi]), _rel(keff[gi], ref))
-    s.close()
+    for layout in (0, 1):
+        s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(512, 4096, layout))
+        assert s.upscale_last_schedule() == (512, 4096, layout, False)
+        for gi in range(len(sizes)):
+            c0, c1 = union.cellpos[gi], union.cellpos[gi + 1]
+            ref = oracle_keff(orc, union.grids[gi], K[c0:c1])
+            assert _rel(keff[gi], ref) < 1e-9, (layout, int(sizes[gi]), _rel(keff[gi], ref))
+        s.close()
 
 
 def test_persistent_schedules_agree_with_amg_schedule(pkg, gpulib, workloads):
@@ -58,7 +59,7 @@ def test_persistent_schedules_agree_with_amg_schedule(pkg, gpulib, workloads):
     union, sizes, K = workloads.periodic_subgrids(num=24, nmin=8, nmax=20, seed=5)
     s0, ref, _ = _solve(pkg, union, K, 1e-12)   # AMG schedule, FP64
     s0.close()
-    for sched in ((256, 0), (1024, 16384), (512, 4096), (0, 0)):
+    for sched in ((256, 0, 1), (1024, 16384, 0), (512, 4096, 1), (1024, 0, 1), (0, 0, 1)):
         s, k1, st1 = _solve(pkg, union, K, 1e-12, schedule=sched)
         keff2, st2 = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                                         pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=4000))
@@ -80,7 +81,7 @@ def test_persistent_analytic_cases(pkg, gpulib, cart):
     g2, K2 = layered_perm(cart, 4, kz)
     union = cart.UnionGrid([g1, g2])
     K = np.concatenate([np.tile(Kh.ravel(), (g1.num_cells, 1)), K2])
-    s, keff, st = _solve(pkg, union, K, 1e-13, schedule=(256, 0))
+    s, keff, st = _solve(pkg, union, K, 1e-13, schedule=(256, 0, 1))
     assert np.abs(keff[0] - Kh).max() < 1e-8 * np.abs(Kh).max()
     assert abs(keff[1][0, 0] - kz.mean()) < 1e-8 * kz.mean()
     assert abs(keff[1][2, 2] - 1.0 / np.mean(1.0 / kz)) < 1e-8 * kz.mean()
@@ -92,7 +93,7 @@ def test_persistent_errors(pkg, gpulib, workloads):
     schedules and CTA sizes are rejected."""
     union, sizes, K = workloads.periodic_subgrids(num=3, nmin=6, nmax=8, seed=2)
     s = pkg.PressureSolver()
-    s.set_upscale_schedule(pkg.UPSCALE_PERSISTENT, 256, 0)
+    s.set_upscale_schedule(pkg.UPSCALE_PERSISTENT, 256, 0, 0)
     with pytest.raises(pkg.PorsolError) as e:
         s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                            pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=3))
@@ -100,12 +101,12 @@ def test_persistent_errors(pkg, gpulib, workloads):
     keff, st = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                                   pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=4000))
     assert np.isfinite(keff).all()
-    for bad in ((7, 0, 0), (1, 300, 0), (1, 256, -1)):
+    for bad in ((7, 0, 0, 1), (1, 300, 0, 1), (1, 256, -1, 1), (1, 256, 0, 2)):
         with pytest.raises(pkg.PorsolError):
             s.set_upscale_schedule(*bad)
     # back to the AMG schedule: the last-schedule query reports zeros
     s.set_upscale_schedule(pkg.UPSCALE_AMG)
     s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                        pkg.default_solve_opts(residual_tolerance=1e-10))
-    assert s.upscale_last_schedule() == (0, 0, False)
+    assert s.upscale_last_schedule() == (0, 0, 0, False)
     s.close()
