@@ -888,7 +888,8 @@ def run_upscale(args, quiet=False):
                                      "vector_layout": ["side by side", "one vector per direction"][layout],
                                      "autotuned": tuned,
                                      "launches_per_call": "one persistent kernel for 1536 solves (CUDA graph)"}
-            out[name]["precision"] = "f64 (Jacobi-preconditioned CG per sub-grid, three directions together)"
+            out[name]["precision"] = ("f32 CG recurrences (Jacobi preconditioner, three directions together) with "
+                                      "f64 solution and f64 residual replacements deciding convergence")
         s.close()
     best = max(("mixed", "fp64", "persistent"), key=lambda k: out[k]["value"])
     out["value"] = out[best]["value"]

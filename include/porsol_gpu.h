@@ -214,7 +214,10 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
  *   PORSOL_UPSCALE_PERSISTENT  one persistent kernel launch (captured into a CUDA graph) solves all
  *                              sub-grids and all three directions: each sub-grid is one work item, its
  *                              Jacobi-preconditioned CG runs the three right-hand sides together inside
- *                              one CTA ("tile") or one warp, in FP64 whatever opts->precision says.
+ *                              one CTA ("tile") or one warp, whatever opts->precision says with FP32
+ *                              recurrences, an FP64 solution and FP64 true residuals (replacing the FP32
+ *                              one whenever it has dropped by opts->inner_tolerance) that alone decide
+ *                              convergence; linsolver_maxit 0 = the largest sub-grid's face unknowns.
  * cta_threads (256, 512 or 1024), warp_max_unknowns (sub-grids with fewer face unknowns go to
  * single warps) and vector_layout (0: the three directions of an unknown side by side, 1: one
  * vector per direction) fix the persistent schedule; cta_threads = 0 lets the autotuner time the

@@ -1,8 +1,9 @@
 """Batched periodic upscaling in one persistent launch (PORSOL_UPSCALE_PERSISTENT): every sub-grid's
 three unit pressure-jump solves (the pattern of setupUpscalingConditions,
 common/setupBoundaryConditions.hpp:136-157) by a Jacobi-preconditioned CG per sub-grid, run by one CTA
-or one warp.  Checked against the oracle's per-sub-grid solves, the AMG schedule, analytic cases, and
-across the schedules the autotuner chooses from."""
+or one warp, with FP32 recurrences and FP64 residual replacements deciding convergence.  Checked
+against the oracle's per-sub-grid solves, the AMG schedule, analytic cases, and across the schedules
+the autotuner chooses from."""
 import numpy as np
 import pytest
 
