@@ -883,6 +883,16 @@ def run_upscale(args, quiet=False):
                      "amg_levels": st.amg_levels, "ms_precond_setup": round(st.ms_precond_setup, 2),
                      "ms_krylov": round(st.ms_krylov, 2)}
         if sched == pkg.UPSCALE_PERSISTENT:
+            # algorithmic bytes of the one persistent launch (the library's count from each sub-grid's
+            # iterations) over its Krylov time, against the measured HBM peak
+            kb = s.solve_bytes()["krylov"]
+            pk = peaks()
+            hbm = pk["hbm_gbs"] if pk else 6800.0
+            out[name]["roofline_launch"] = {"bytes": round(kb), "ms": round(st.ms_krylov, 2),
+                                            "achieved_gbs": round(kb / (st.ms_krylov * 1e-3) / 1e9, 1),
+                                            "peak_gbs": hbm, "frac": round(kb / (st.ms_krylov * 1e-3) / 1e9 / hbm, 4),
+                                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk
+                                            else "fallback 6800 GB/s"}
             threads, wmax, layout, tuned = s.upscale_last_schedule()
             out[name]["schedule"] = {"cta_threads": threads, "warp_max_unknowns": wmax,
                                      "vector_layout": ["side by side", "one vector per direction"][layout],

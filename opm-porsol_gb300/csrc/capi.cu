@@ -921,6 +921,7 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             up_last = pup.last_schedule();
             acc.ms_krylov = now_ms() - t0;
             bytes_krylov = pup.bytes();
+            vcycle_level_bytes.clear();
             if (r.breakdown) throw Error(PORSOL_ERR_NONFINITE, "CG breakdown (non-positive curvature)");
             if (!r.converged) {
                 std::ostringstream os;
