@@ -109,11 +109,29 @@ __device__ __forceinline__ void group_sync()
 
 // Position of direction d of unknown i in the three-direction vectors: side by side (L = 0,
 // 3 i + d: one run per gathered column) or direction-major (L = 1, d n + i: every streamed access
-// of a warp is one contiguous run).  The autotuner tries both.
+// of a warp is one contiguous run).  The autotuner tries both; they measured within a few per cent
+// of each other, either ahead.  A third layout, side by side padded to four values and accessed as
+// 16-byte vectors (fewer memory instructions), measured no faster and was removed.
 template <int L>
 __device__ __forceinline__ size_t vix(int i, int d, int n)
 {
     return L == 0 ? 3 * size_t(i) + d : size_t(d) * size_t(n) + i;
+}
+
+// The three values of unknown i, per direction: masked-off directions are neither loaded (read as
+// 0) nor stored.
+template <int L, class T>
+__device__ __forceinline__ void ld3(const T* __restrict__ v, int i, int n, const bool (&m)[3], T (&o)[3])
+{
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o[d] = m[d] ? v[vix<L>(i, d, n)] : T(0);
+}
+template <int L, class T>
+__device__ __forceinline__ void st3(T* __restrict__ v, int i, int n, const bool (&m)[3], const T (&x)[3])
+{
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (m[d]) v[vix<L>(i, d, n)] = x[d];
 }
 
 // q = (A y)_r for the three directions (values TV, vector TX, sums TA): the row's SELL-32
@@ -124,6 +142,7 @@ __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int
                                            const TV* __restrict__ val, const TX* __restrict__ y, int n, int r,
                                            TA (&q)[3])
 {
+    constexpr bool all[3] = {true, true, true};
     const int s = r >> 5;
     const int b = sp[s], w = (sp[s + 1] - b) >> 5;
     TA a0 = TA(0), a1 = TA(0), a2 = TA(0);
@@ -131,21 +150,24 @@ __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int
     for (; t + 2 <= w; t += 2, k += 64) {
         const int c0 = col[k], c1 = col[k + 32];
         const TA v0 = TA(val[k]), v1 = TA(val[k + 32]);
-        const TA y00 = TA(y[vix<L>(c0, 0, n)]), y01 = TA(y[vix<L>(c0, 1, n)]), y02 = TA(y[vix<L>(c0, 2, n)]);
-        const TA y10 = TA(y[vix<L>(c1, 0, n)]), y11 = TA(y[vix<L>(c1, 1, n)]), y12 = TA(y[vix<L>(c1, 2, n)]);
-        a0 += v0 * y00;
-        a1 += v0 * y01;
-        a2 += v0 * y02;
-        a0 += v1 * y10;
-        a1 += v1 * y11;
-        a2 += v1 * y12;
+        TX y0[3], y1[3];
+        ld3<L>(y, c0, n, all, y0);
+        ld3<L>(y, c1, n, all, y1);
+        a0 += v0 * TA(y0[0]);
+        a1 += v0 * TA(y0[1]);
+        a2 += v0 * TA(y0[2]);
+        a0 += v1 * TA(y1[0]);
+        a1 += v1 * TA(y1[1]);
+        a2 += v1 * TA(y1[2]);
     }
     if (t < w) {
         const int c0 = col[k];
         const TA v0 = TA(val[k]);
-        a0 += v0 * TA(y[vix<L>(c0, 0, n)]);
-        a1 += v0 * TA(y[vix<L>(c0, 1, n)]);
-        a2 += v0 * TA(y[vix<L>(c0, 2, n)]);
+        TX y0[3];
+        ld3<L>(y, c0, n, all, y0);
+        a0 += v0 * TA(y0[0]);
+        a1 += v0 * TA(y0[1]);
+        a2 += v0 * TA(y0[2]);
     }
     q[0] = a0;
     q[1] = a1;
@@ -161,15 +183,16 @@ __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int
 //   tolerance: pass R, the true residual b - A x in FP64, which alone decides convergence; then
 //   pass S, r = (b - A x) / sigma' and p *= sigma / sigma' (the recurrence continues in units of
 //   the new sigma), r.D^-1 r again
+//   pass C  p = D^-1 r + beta p
 // x stays FP64 every iteration: an FP32 increment of x flushed at each replacement (measured) let
 // one sub-grid of the 512-sub-grid batch stall at 3.3e-11 against a 1e-11 tolerance, its rounding
 // times the condition number bounding the residual each replacement can reach.
-//   pass C  p = D^-1 r + beta p
-// Each pass loads all of a row's values before it stores any, and frozen directions neither load
-// nor store.  Thread 0 keeps the per-direction iteration count and reduction in global memory.
+// Each pass loads all of a row's values before it stores any, and frozen directions keep their
+// values.  Thread 0 keeps the per-direction iteration count and reduction in global memory.
 template <bool CTA, int L>
 __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
 {
+    constexpr bool all[3] = {true, true, true};
     const int* rg = a.ranges + 4 * g;
     const Rows R{rg[0], rg[1] - rg[0], rg[2], (rg[1] - rg[0]) + (rg[3] - rg[2])};
     const int n = a.n;
@@ -179,16 +202,14 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
     for (int k = tid; k < R.n; k += nthr) {
         const int r = R.row(k);
         double b[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) b[d] = a.b3[vix<0>(r, d, n)];   // right-hand sides: side by side
+        ld3<0>(a.b3, r, n, all, b);   // right-hand sides: side by side
         const double di = a.val[a.diag[r]];
         bad |= !(di > 0.0);
         a.dinv[r] = float(1.0 / di);
+        const double z3[3] = {0.0, 0.0, 0.0};
+        st3<L>(a.x3, r, n, all, z3);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            a.x3[vix<L>(r, d, n)] = 0.0;
-            v[d] += b[d] * b[d];
-        }
+        for (int d = 0; d < 3; ++d) v[d] += b[d] * b[d];
     }
     if (bad) atomicOr(a.status, ST_NONFINITE);
     group_sum<CTA, 3>(v, sum, sb, rb);
@@ -211,16 +232,17 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
         for (int k = tid; k < R.n; k += nthr) {
             const int r = R.row(k);
             double b[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) b[d] = a.b3[vix<0>(r, d, n)];
+            ld3<0>(a.b3, r, n, all, b);
             const float dv = a.dinv[r];
+            float rr[3], pp[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const float rr = act[d] ? float(b[d] / sig[d]) : 0.f;
-                a.r32[vix<L>(r, d, n)] = rr;
-                a.p32[vix<L>(r, d, n)] = dv * rr;
-                u[d] += rr * (dv * rr);
+                rr[d] = act[d] ? float(b[d] / sig[d]) : 0.f;
+                pp[d] = dv * rr[d];
+                u[d] += rr[d] * pp[d];
             }
+            st3<L>(a.r32, r, n, all, rr);
+            st3<L>(a.p32, r, n, all, pp);
         }
         group_sum<CTA, 3>(u, rho, sb, rb);
     }
@@ -233,14 +255,11 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
             for (int k = tid; k < R.n; k += nthr) {
                 const int r = R.row(k);
                 float p[3], q[3];
-#pragma unroll
-                for (int d = 0; d < 3; ++d) p[d] = a.p32[vix<L>(r, d, n)];
+                ld3<L>(a.p32, r, n, all, p);
                 row_apply3<L, float>(a.sp, a.col, a.val32, a.p32, n, r, q);
+                st3<L>(a.q32, r, n, all, q);
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    a.q32[vix<L>(r, d, n)] = q[d];
-                    w[d] += p[d] * q[d];
-                }
+                for (int d = 0; d < 3; ++d) w[d] += p[d] * q[d];
             }
             group_sum<CTA, 3>(w, sum, sb, rb);
         }
@@ -262,26 +281,21 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                 const float dv = a.dinv[r];
                 double x[3];
                 float p[3], rr[3], q[3];
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    x[d] = 0.0;
-                    p[d] = rr[d] = q[d] = 0.f;
-                    if (act[d]) {
-                        x[d] = a.x3[vix<L>(r, d, n)];
-                        p[d] = a.p32[vix<L>(r, d, n)];
-                        rr[d] = a.r32[vix<L>(r, d, n)];
-                        q[d] = a.q32[vix<L>(r, d, n)];
-                    }
-                }
+                ld3<L>(a.x3, r, n, act, x);
+                ld3<L>(a.p32, r, n, act, p);
+                ld3<L>(a.r32, r, n, act, rr);
+                ld3<L>(a.q32, r, n, act, q);
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
                     if (act[d]) {
                         const float rn = rr[d] - float(al[d]) * q[d];
-                        a.x3[vix<L>(r, d, n)] = x[d] + (sig[d] * al[d]) * double(p[d]);
-                        a.r32[vix<L>(r, d, n)] = rn;
+                        x[d] += (sig[d] * al[d]) * double(p[d]);
+                        rr[d] = rn;
                         part[d] += rn * (dv * rn);
                         part[3 + d] += rn * rn;
                     }
+                st3<L>(a.x3, r, n, act, x);
+                st3<L>(a.r32, r, n, act, rr);
             }
             double tot[6];
             group_sum<CTA, 6>(part, tot, sb, rb);
@@ -305,15 +319,17 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
             double t2[3] = {0.0, 0.0, 0.0};
             for (int k = tid; k < R.n; k += nthr) {
                 const int r = R.row(k);
-                double ax[3];
+                double ax[3], b[3], t[3];
                 row_apply3<L, double>(a.sp, a.col, a.val, a.x3, n, r, ax);
+                ld3<0>(a.b3, r, n, all, b);
+                ld3<L>(a.r64, r, n, rep, t);
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
                     if (rep[d]) {
-                        const double t = a.b3[vix<0>(r, d, n)] - ax[d];
-                        a.r64[vix<L>(r, d, n)] = t;
-                        t2[d] += t * t;
+                        t[d] = b[d] - ax[d];
+                        t2[d] += t[d] * t[d];
                     }
+                st3<L>(a.r64, r, n, rep, t);
             }
             group_sum<CTA, 3>(t2, sum, sb, rb);
             bool resc[3], anyr = false;
@@ -348,24 +364,19 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                     const int r = R.row(k);
                     const float dv = a.dinv[r];
                     double t[3];
-                    float p[3];
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        t[d] = 0.0;
-                        p[d] = 0.f;
-                        if (resc[d]) {
-                            t[d] = a.r64[vix<L>(r, d, n)];
-                            p[d] = a.p32[vix<L>(r, d, n)];
-                        }
-                    }
+                    float p[3], rr[3];
+                    ld3<L>(a.r64, r, n, resc, t);
+                    ld3<L>(a.p32, r, n, resc, p);
+                    ld3<L>(a.r32, r, n, resc, rr);
 #pragma unroll
                     for (int d = 0; d < 3; ++d)
                         if (resc[d]) {
-                            const float rn = float(t[d] / sig[d]);
-                            a.r32[vix<L>(r, d, n)] = rn;
-                            a.p32[vix<L>(r, d, n)] = p[d] * float(fac[d]);
-                            uu[d] += rn * (dv * rn);
+                            rr[d] = float(t[d] / sig[d]);
+                            p[d] *= float(fac[d]);
+                            uu[d] += rr[d] * (dv * rr[d]);
                         }
+                    st3<L>(a.r32, r, n, resc, rr);
+                    st3<L>(a.p32, r, n, resc, p);
                 }
                 double un[3];
                 group_sum<CTA, 3>(uu, un, sb, rb);
@@ -393,17 +404,12 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
             const int r = R.row(k);
             const float dv = a.dinv[r];
             float p[3], rr[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                p[d] = rr[d] = 0.f;
-                if (act[d]) {
-                    p[d] = a.p32[vix<L>(r, d, n)];
-                    rr[d] = a.r32[vix<L>(r, d, n)];
-                }
-            }
+            ld3<L>(a.p32, r, n, act, p);
+            ld3<L>(a.r32, r, n, act, rr);
 #pragma unroll
             for (int d = 0; d < 3; ++d)
-                if (act[d]) a.p32[vix<L>(r, d, n)] = dv * rr[d] + float(be[d]) * p[d];
+                if (act[d]) p[d] = dv * rr[d] + float(be[d]) * p[d];
+            st3<L>(a.p32, r, n, act, p);
         }
         group_sync<CTA>();
     }
@@ -641,6 +647,8 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
 {
     PORSOL_REQUIRE(rg.size() % 4 == 0 && !rg.empty(), PORSOL_ERR_BAD_ARG, "persistent upscaling: no sub-grids");
     PORSOL_REQUIRE(P.n <= INT_MAX / 3, PORSOL_ERR_BAD_ARG, "persistent upscaling: too many unknowns");
+    PORSOL_REQUIRE(fixed.layout == 0 || fixed.layout == 1, PORSOL_ERR_BAD_ARG,
+                   "persistent upscaling: vector layout must be 0 or 1");
     PORSOL_REQUIRE(fixed.cta_threads == 0 || fixed.cta_threads == 256 || fixed.cta_threads == 512 ||
                        fixed.cta_threads == 1024,
                    PORSOL_ERR_BAD_ARG, "persistent upscaling: CTA threads must be 256, 512 or 1024");
