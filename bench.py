@@ -893,10 +893,11 @@ def run_upscale(args, quiet=False):
                                             "peak_gbs": hbm, "frac": round(kb / (st.ms_krylov * 1e-3) / 1e9 / hbm, 4),
                                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk
                                             else "fallback 6800 GB/s"}
-            threads, wmax, layout, tuned = s.upscale_last_schedule()
-            out[name]["schedule"] = {"cta_threads": threads, "warp_max_unknowns": wmax,
-                                     "vector_layout": ["side by side", "one vector per direction"][layout],
-                                     "autotuned": tuned,
+            sc = s.upscale_last_schedule()
+            out[name]["schedule"] = {"cta_threads": sc["cta_threads"], "warp_max_unknowns": sc["warp_max_unknowns"],
+                                     "vector_layout": ["side by side", "one vector per direction"][sc["vector_layout"]],
+                                     "cluster_ctas": sc["cluster_ctas"],
+                                     "cluster_min_unknowns": sc["cluster_min_unknowns"], "autotuned": sc["tuned"],
                                      "launches_per_call": "one persistent kernel for 1536 solves (CUDA graph)"}
             out[name]["precision"] = ("f32 CG recurrences (Jacobi preconditioner, three directions together) with "
                                       "f64 solution and f64 residual replacements deciding convergence")

@@ -214,23 +214,27 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
  *   PORSOL_UPSCALE_PERSISTENT  one persistent kernel launch (captured into a CUDA graph) solves all
  *                              sub-grids and all three directions: each sub-grid is one work item, its
  *                              Jacobi-preconditioned CG runs the three right-hand sides together inside
- *                              one CTA ("tile") or one warp, whatever opts->precision says with FP32
+ *                              a cluster of CTAs, one CTA ("tile") or one warp, whatever opts->precision
+ *                              says with FP32
  *                              recurrences, an FP64 solution and FP64 true residuals (replacing the FP32
  *                              one whenever it has dropped by opts->inner_tolerance) that alone decide
  *                              convergence; linsolver_maxit 0 = the largest sub-grid's face unknowns.
  * cta_threads (256, 512 or 1024), warp_max_unknowns (sub-grids with fewer face unknowns go to
- * single warps) and vector_layout (0: the three directions of an unknown side by side, 1: one
- * vector per direction) fix the persistent schedule; cta_threads = 0 lets the autotuner time the
- * candidates (both layouts x CTAs of 256/512/1024 threads x warp limits 0/4096/16384) for a few
- * iterations on the first batch of each shape and keep the fastest. */
+ * single warps), vector_layout (0: the three directions of an unknown side by side, 1: one vector
+ * per direction), cluster_ctas (1, 2 or 4) and cluster_min_unknowns (with cluster_ctas > 1,
+ * sub-grids with at least this many face unknowns are solved by a cluster of that many CTAs on as
+ * many SMs) fix the persistent schedule; cta_threads = 0 lets the autotuner time the candidates
+ * (clusters of 1/2/4 CTAs for the sub-grids of at least half the largest one's unknowns x both
+ * layouts x CTAs of 512/1024 threads x warp limits 0/4096) for a few iterations on the first batch
+ * of each shape and keep the fastest. */
 #define PORSOL_UPSCALE_AMG 0
 #define PORSOL_UPSCALE_PERSISTENT 1
 int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns,
-                                int vector_layout);
+                                int vector_layout, int cluster_ctas, int cluster_min_unknowns);
 /* The persistent schedule the last porsol_upscale_periodic call ran (zeros after an AMG-schedule
  * call); tuned = 1 when the autotuner chose it. */
 int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* vector_layout,
-                                 int* tuned);
+                                 int* cluster_ctas, int* cluster_min_unknowns, int* tuned);
 
 /* ------------------------------------------------------ output fields */
 /* The cell fields writeVtkOutput gathers (common/SimulatorUtilities.hpp:54-297), computed on the

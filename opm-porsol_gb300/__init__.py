@@ -155,8 +155,8 @@ EXPORTS = [
     ("porsol_solve_bytes", _i, [_vp, _vp, _i, _vp]),
     ("porsol_upscale_periodic", _i, [_vp, C.POINTER(Grid), _i, _vp, _vp, _vp, _vp, C.POINTER(SolveOpts), _vp,
                                      C.POINTER(SolveStats)]),
-    ("porsol_upscale_set_schedule", _i, [_vp, _i, _i, _i, _i]),
-    ("porsol_upscale_last_schedule", _i, [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    ("porsol_upscale_set_schedule", _i, [_vp, _i, _i, _i, _i, _i, _i]),
+    ("porsol_upscale_last_schedule", _i, [_vp] + [C.POINTER(_i)] * 6),
     ("porsol_cell_fields", _i, [_vp, C.POINTER(Fluid), _vp, _vp, _vp, _vp, _vp, _vp]),
     ("porsol_write_field", _i, [_vp, _i, C.c_char_p]),
     ("porsol_objective_value", _i, [_vp, C.POINTER(Objective), C.POINTER(_d)]),
@@ -349,16 +349,22 @@ class PressureSolver:
         self.n, self.nnz = n.value, nnz.value
         return keff.reshape(ng, 3, 3), st
 
-    def set_upscale_schedule(self, schedule, cta_threads=0, warp_max_unknowns=0, vector_layout=1):
+    def set_upscale_schedule(self, schedule, cta_threads=0, warp_max_unknowns=0, vector_layout=1, cluster_ctas=1,
+                             cluster_min_unknowns=0):
         """UPSCALE_AMG (default) or UPSCALE_PERSISTENT (one launch; cta_threads 0 = autotuned)."""
         self._check(lib().porsol_upscale_set_schedule(self.h, int(schedule), int(cta_threads),
-                                                      int(warp_max_unknowns), int(vector_layout)))
+                                                      int(warp_max_unknowns), int(vector_layout), int(cluster_ctas),
+                                                      int(cluster_min_unknowns)))
 
     def upscale_last_schedule(self):
-        """(cta_threads, warp_max_unknowns, vector_layout, tuned) of the last persistent-schedule call."""
-        t, w, ly, tu = C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        self._check(lib().porsol_upscale_last_schedule(self.h, C.byref(t), C.byref(w), C.byref(ly), C.byref(tu)))
-        return t.value, w.value, ly.value, bool(tu.value)
+        """dict(cta_threads, warp_max_unknowns, vector_layout, cluster_ctas, cluster_min_unknowns, tuned) of the
+        last persistent-schedule call (zeros after an AMG-schedule call)."""
+        v = [C.c_int() for _ in range(6)]
+        self._check(lib().porsol_upscale_last_schedule(self.h, *[C.byref(x) for x in v]))
+        keys = ("cta_threads", "warp_max_unknowns", "vector_layout", "cluster_ctas", "cluster_min_unknowns")
+        out = {k: x.value for k, x in zip(keys, v)}
+        out["tuned"] = bool(v[5].value)
+        return out
 
     def _objective(self, cell_weight, cell_target, hf_weight):
         keep = [None if a is None else _f64(a) for a in (cell_weight, cell_target, hf_weight)]

@@ -1253,7 +1253,7 @@ int porsol_upscale_periodic(porsol_solver* h, const porsol_grid* grid, int num_g
 }
 
 int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads, int warp_max_unknowns,
-                                int vector_layout)
+                                int vector_layout, int cluster_ctas, int cluster_min_unknowns)
 {
     return guarded(h, [&] {
         PORSOL_REQUIRE(schedule == PORSOL_UPSCALE_AMG || schedule == PORSOL_UPSCALE_PERSISTENT, PORSOL_ERR_BAD_ARG,
@@ -1263,24 +1263,32 @@ int porsol_upscale_set_schedule(porsol_solver* h, int schedule, int cta_threads,
         PORSOL_REQUIRE(warp_max_unknowns >= 0, PORSOL_ERR_BAD_ARG, "upscale schedule: negative warp limit");
         PORSOL_REQUIRE(vector_layout == 0 || vector_layout == 1, PORSOL_ERR_BAD_ARG,
                        "upscale schedule: vector layout must be 0 or 1");
+        PORSOL_REQUIRE(cluster_ctas == 1 || cluster_ctas == 2 || cluster_ctas == 4, PORSOL_ERR_BAD_ARG,
+                       "upscale schedule: cluster size must be 1, 2 or 4");
+        PORSOL_REQUIRE(cluster_min_unknowns >= 0, PORSOL_ERR_BAD_ARG, "upscale schedule: negative cluster limit");
         h->upscale_schedule = schedule;
         h->upscale_fixed = porsol::UpscaleSchedule{};
         h->upscale_fixed.cta_threads = cta_threads;
         h->upscale_fixed.warp_max_unknowns = cta_threads ? warp_max_unknowns : 0;
         h->upscale_fixed.layout = vector_layout;
+        h->upscale_fixed.cluster = cta_threads ? cluster_ctas : 1;
+        h->upscale_fixed.cluster_min_unknowns = cta_threads && cluster_ctas > 1 ? cluster_min_unknowns : 0;
     });
 }
 
 int porsol_upscale_last_schedule(porsol_solver* h, int* cta_threads, int* warp_max_unknowns, int* vector_layout,
-                                 int* tuned)
+                                 int* cluster_ctas, int* cluster_min_unknowns, int* tuned)
 {
     return guarded(h, [&] {
-        PORSOL_REQUIRE(cta_threads && warp_max_unknowns && vector_layout && tuned, PORSOL_ERR_BAD_ARG,
-                       "upscale schedule: null argument");
+        PORSOL_REQUIRE(cta_threads && warp_max_unknowns && vector_layout && cluster_ctas && cluster_min_unknowns &&
+                           tuned,
+                       PORSOL_ERR_BAD_ARG, "upscale schedule: null argument");
         const porsol::UpscaleSchedule& sc = h->up_last;
         *cta_threads = sc.cta_threads;
         *warp_max_unknowns = sc.warp_max_unknowns;
         *vector_layout = sc.cta_threads ? sc.layout : 0;
+        *cluster_ctas = sc.cta_threads ? sc.cluster : 0;
+        *cluster_min_unknowns = sc.cta_threads ? sc.cluster_min_unknowns : 0;
         *tuned = sc.tuned ? 1 : 0;
     });
 }

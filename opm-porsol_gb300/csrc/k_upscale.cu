@@ -1,13 +1,14 @@
 // k_upscale.cu -- PersistentUpscale: the three periodic solves of every sub-grid of a batch in one
 // persistent kernel launch.
 //
-// Work items are sub-grids, taken from two device counters: first the tile items (a whole CTA per
-// sub-grid, largest first), then the warp items (one warp per sub-grid).  The group that owns an
+// Work items are sub-grids, taken from device counters, largest first: cluster items (a cluster of
+// 2 or 4 CTAs per sub-grid, on as many SMs), then CTA items (a whole CTA per sub-grid), then warp
+// items (one warp per sub-grid).  The group that owns an
 // item runs a Jacobi-preconditioned CG for the three unit pressure-jump right-hand sides together,
 // with FP32 recurrences (matrix copy, vectors and products in FP32: one matrix read feeds three
 // products) and reliable updates in FP64 (solution, true residual, convergence test), with
-// group-local reductions only (warp shuffles, plus shared memory across the warps of a CTA), so no
-// sub-grid ever waits for another.  A direction stops when its true residual meets
+// group-local reductions only (warp shuffles, plus shared memory across the warps of a CTA and
+// distributed shared memory across the CTAs of a cluster), so no sub-grid ever waits for another.  A direction stops when its true residual meets
 // ||b - A x|| < tol ||b|| or ||b - A x|| < 1e-30 (the per-block test of the batched AMG solve); it
 // is frozen from then on.  FP32 matters on this GPU: one SM runs the largest sub-grid alone, and
 // with FP64 products its FP64 pipe, not memory, set the time (ncu: 95 % busy).  Every sum runs in a
@@ -23,6 +24,8 @@
 #include <numeric>
 #include <unordered_map>
 
+#include <cooperative_groups.h>
+
 #include "upscale.h"
 
 namespace porsol {
@@ -33,9 +36,16 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int UP_MAX_THREADS = 1024;
 constexpr int UP_MAX_WARPS = UP_MAX_THREADS / 32;
 constexpr int TUNE_ITERS = 8;   // CG iterations per sub-grid of one autotuner trial
+namespace cg = cooperative_groups;
+
+// The group of threads that solves one sub-grid: a warp, a CTA, or a cluster of CTAs.
+constexpr int G_WARP = 0, G_CTA = 1, G_CLUSTER = 2;
+// One reduction buffer: the per-warp partials (up to 32 warps x 6 values), then the CTA's totals
+// (6 values, read by the other CTAs of a cluster).  Two buffers alternate.
+constexpr int SB_STRIDE = UP_MAX_WARPS * 6 + 6;
 
 struct UpArgs {
-    int nitems, ntile, maxit, n;
+    int nitems, ncl, ntile, maxit, n;   // items [0, ncl): clusters; then ntile CTA items; then warp items
     double tol, delta;
     const int* order;     // sub-grid ids: tile items [0, ntile), then warp items
     const int* ranges;    // 4 per sub-grid
@@ -53,7 +63,7 @@ struct UpArgs {
     float* dinv;          // 1 / a_ii
     int* iters;           // 3 per sub-grid: iteration at which the direction met its test, -1: never
     double* red;          // 3 per sub-grid: last true ||r|| / ||r0||
-    int* counters;        // [0]: next tile item, [1]: next warp item
+    int* counters;        // [0]: next cluster item, [1]: next CTA item, [2]: next warp item
     int* status;
 };
 
@@ -65,11 +75,14 @@ struct Rows {
 
 // Sums over the group.  The warp butterfly leaves the bitwise-same total in every lane (each step
 // adds two equal pairs in swapped order); a CTA then adds the per-warp totals in warp order in FP64,
-// every thread reading them from shared memory, so all threads hold the same sums.  Two buffers
-// alternate from one reduction to the next (rb): a thread that has left one reduction's barrier
-// may write the next one while others still read this one.  FP32 partials (the CG's dot products)
-// are summed in FP32 within a warp and in FP64 across warps.
-template <bool CTA, int NV, class T>
+// every thread reading them from shared memory; in a cluster every CTA forms its total that way, and
+// after the cluster barrier each thread adds the CTAs' totals in CTA order, reading them from the
+// other CTAs' shared memory (one remote load per CTA and value, not one per warp); so all threads
+// of the group hold the same sums.  Two buffers alternate from one reduction to the
+// next (rb): a thread that has left one reduction's barrier may write the next one while others
+// still read this one.  FP32 partials (the CG's dot products) are summed in FP32 within a warp and in
+// FP64 across warps.
+template <int G, int NV, class T>
 __device__ __forceinline__ void group_sum(const T (&v)[NV], double (&out)[NV], double* sb, int& rb)
 {
     T w[NV];
@@ -79,8 +92,8 @@ __device__ __forceinline__ void group_sum(const T (&v)[NV], double (&out)[NV], d
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) w[i] += __shfl_xor_sync(FULL, w[i], o);
     }
-    if constexpr (CTA) {
-        double* buf = sb + rb * (UP_MAX_WARPS * 6);
+    if constexpr (G == G_CTA) {
+        double* buf = sb + rb * SB_STRIDE;
         rb ^= 1;
         const int wi = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if ((threadIdx.x & 31) == 0)
@@ -93,6 +106,31 @@ __device__ __forceinline__ void group_sum(const T (&v)[NV], double (&out)[NV], d
             for (int j = 0; j < nw; ++j) s += buf[j * NV + i];
             out[i] = s;
         }
+    } else if constexpr (G == G_CLUSTER) {
+        cg::cluster_group cl = cg::this_cluster();
+        double* buf = sb + rb * SB_STRIDE;
+        double* ctot = buf + UP_MAX_WARPS * 6;
+        rb ^= 1;
+        const int wi = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if ((threadIdx.x & 31) == 0)
+#pragma unroll
+            for (int i = 0; i < NV; ++i) buf[wi * NV + i] = double(w[i]);
+        __syncthreads();
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int i = 0; i < NV; ++i) {
+                double s = 0.0;
+                for (int j = 0; j < nw; ++j) s += buf[j * NV + i];
+                ctot[i] = s;
+            }
+        cl.sync();
+        const int nc = int(cl.num_blocks());
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = 0.0;
+            for (int c = 0; c < nc; ++c) s += cl.map_shared_rank(ctot, c)[i];
+            out[i] = s;
+        }
     } else {
 #pragma unroll
         for (int i = 0; i < NV; ++i) out[i] = double(w[i]);
@@ -100,10 +138,11 @@ __device__ __forceinline__ void group_sum(const T (&v)[NV], double (&out)[NV], d
     }
 }
 
-template <bool CTA>
+template <int G>
 __device__ __forceinline__ void group_sync()
 {
-    if constexpr (CTA) __syncthreads();
+    if constexpr (G == G_CLUSTER) cg::this_cluster().sync();
+    else if constexpr (G == G_CTA) __syncthreads();
     else __syncwarp();
 }
 
@@ -119,15 +158,17 @@ __device__ __forceinline__ size_t vix(int i, int d, int n)
 }
 
 // The three values of unknown i, per direction: masked-off directions are neither loaded (read as
-// 0) nor stored.
+// 0) nor stored.  The vectors are written by this kernel (by other CTAs of a cluster, too), so
+// their pointers carry no __restrict__: the loads stay ordinary coherent loads, ordered by the
+// group's barriers, never the read-only path.
 template <int L, class T>
-__device__ __forceinline__ void ld3(const T* __restrict__ v, int i, int n, const bool (&m)[3], T (&o)[3])
+__device__ __forceinline__ void ld3(const T* v, int i, int n, const bool (&m)[3], T (&o)[3])
 {
 #pragma unroll
     for (int d = 0; d < 3; ++d) o[d] = m[d] ? v[vix<L>(i, d, n)] : T(0);
 }
 template <int L, class T>
-__device__ __forceinline__ void st3(T* __restrict__ v, int i, int n, const bool (&m)[3], const T (&x)[3])
+__device__ __forceinline__ void st3(T* v, int i, int n, const bool (&m)[3], const T (&x)[3])
 {
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -139,7 +180,7 @@ __device__ __forceinline__ void st3(T* __restrict__ v, int i, int n, const bool 
 // order (padding adds exact zeros).
 template <int L, class TA, class TV, class TX>
 __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int* __restrict__ col,
-                                           const TV* __restrict__ val, const TX* __restrict__ y, int n, int r,
+                                           const TV* __restrict__ val, const TX* y, int n, int r,
                                            TA (&q)[3])
 {
     constexpr bool all[3] = {true, true, true};
@@ -189,7 +230,7 @@ __device__ __forceinline__ void row_apply3(const int* __restrict__ sp, const int
 // times the condition number bounding the residual each replacement can reach.
 // Each pass loads all of a row's values before it stores any, and frozen directions keep their
 // values.  Thread 0 keeps the per-direction iteration count and reduction in global memory.
-template <bool CTA, int L>
+template <int G, int L>
 __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
 {
     constexpr bool all[3] = {true, true, true};
@@ -212,7 +253,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
         for (int d = 0; d < 3; ++d) v[d] += b[d] * b[d];
     }
     if (bad) atomicOr(a.status, ST_NONFINITE);
-    group_sum<CTA, 3>(v, sum, sb, rb);
+    group_sum<G, 3>(v, sum, sb, rb);
     double sig[3], def0[3], rho[3];
     bool act[3];
     bool brk = false;
@@ -244,7 +285,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
             st3<L>(a.r32, r, n, all, rr);
             st3<L>(a.p32, r, n, all, pp);
         }
-        group_sum<CTA, 3>(u, rho, sb, rb);
+        group_sum<G, 3>(u, rho, sb, rb);
     }
     int it = 0;
     while ((act[0] || act[1] || act[2]) && it < a.maxit) {
@@ -261,7 +302,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) w[d] += p[d] * q[d];
             }
-            group_sum<CTA, 3>(w, sum, sb, rb);
+            group_sum<G, 3>(w, sum, sb, rb);
         }
         double al[3];
 #pragma unroll
@@ -298,7 +339,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                 st3<L>(a.r32, r, n, act, rr);
             }
             double tot[6];
-            group_sum<CTA, 6>(part, tot, sb, rb);
+            group_sum<G, 6>(part, tot, sb, rb);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 u[d] = tot[d];
@@ -331,7 +372,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                     }
                 st3<L>(a.r64, r, n, rep, t);
             }
-            group_sum<CTA, 3>(t2, sum, sb, rb);
+            group_sum<G, 3>(t2, sum, sb, rb);
             bool resc[3], anyr = false;
             double fac[3];
 #pragma unroll
@@ -379,7 +420,7 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                     st3<L>(a.p32, r, n, resc, p);
                 }
                 double un[3];
-                group_sum<CTA, 3>(uu, un, sb, rb);
+                group_sum<G, 3>(uu, un, sb, rb);
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
                     if (resc[d]) u[d] = un[d];
@@ -411,35 +452,52 @@ __device__ void solve_one(const UpArgs& a, int g, int tid, int nthr, double* sb)
                 if (act[d]) p[d] = dv * rr[d] + float(be[d]) * p[d];
             st3<L>(a.p32, r, n, act, p);
         }
-        group_sync<CTA>();
+        group_sync<G>();
     }
     if (tid == 0 && brk) atomicOr(a.status, ST_BREAKDOWN);
 }
 
-// The persistent kernel: tile items while any is left (the CTA takes the next one), then warp
-// items (each warp on its own).  Every loop ends: the counters only grow, and each CG is bounded
-// by maxit.
-template <int L>
+// The persistent kernel: cluster items while any is left (rank 0 of the cluster takes the next
+// one and the other CTAs read it from rank 0's shared memory), then CTA items (each CTA takes the
+// next one), then warp items (each warp on its own).  Every loop ends: the counters only grow, and
+// each CG is bounded by maxit.  Every cluster barrier is reached by all CTAs of the cluster: the
+// item and every sum that steers the CG are the same in all of them.  After its last cluster
+// item a CTA passes two more cluster barriers, so no CTA reads another's shared memory once any has
+// moved on (or exited).
+template <int L, bool CLUSTER>
 __global__ void __launch_bounds__(UP_MAX_THREADS, 1) k_upscale_persistent(const UpArgs a)
 {
-    __shared__ double sb[2 * UP_MAX_WARPS * 6];
+    __shared__ double sb[2 * SB_STRIDE];
     __shared__ int s_item;
+    if constexpr (CLUSTER) {
+        cg::cluster_group cl = cg::this_cluster();
+        const int crank = int(cl.block_rank()), csize = int(cl.num_blocks());
+        for (;;) {
+            if (crank == 0 && threadIdx.x == 0) s_item = atomicAdd(a.counters, 1);
+            cl.sync();
+            const int item = *cl.map_shared_rank(&s_item, 0);
+            cl.sync();   // every CTA has read rank 0's s_item before it is written again
+            if (item >= a.ncl) break;
+            solve_one<G_CLUSTER, L>(a, a.order[item], crank * int(blockDim.x) + int(threadIdx.x),
+                                    csize * int(blockDim.x), sb);
+        }
+    }
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(a.counters, 1);
+        if (threadIdx.x == 0) s_item = atomicAdd(a.counters + 1, 1);
         __syncthreads();
         const int item = s_item;
         __syncthreads();   // every thread has read s_item before thread 0 writes it again
         if (item >= a.ntile) break;
-        solve_one<true, L>(a, a.order[item], threadIdx.x, blockDim.x, sb);
+        solve_one<G_CTA, L>(a, a.order[a.ncl + item], threadIdx.x, blockDim.x, sb);
     }
     const int lane = threadIdx.x & 31;
-    const int nwarp = a.nitems - a.ntile;
+    const int first = a.ncl + a.ntile, nwarp = a.nitems - first;
     for (;;) {
         int item = 0;
-        if (lane == 0) item = atomicAdd(a.counters + 1, 1);
+        if (lane == 0) item = atomicAdd(a.counters + 2, 1);
         item = __shfl_sync(FULL, item, 0);
         if (item >= nwarp) break;
-        solve_one<false, L>(a, a.order[a.ntile + item], lane, 32, nullptr);
+        solve_one<G_WARP, L>(a, a.order[first + item], lane, 32, nullptr);
     }
 }
 
@@ -496,24 +554,24 @@ PersistentUpscale::~PersistentUpscale()
     if (exec_) cudaGraphExecDestroy(exec_);
 }
 
-int PersistentUpscale::tile_items(const std::vector<int>& rg, int wmax) const
+void PersistentUpscale::item_classes(const std::vector<int>& rg, const UpscaleSchedule& sc, int& ncl, int& ntile) const
 {
-    int nt = 0;
+    ncl = ntile = 0;
     for (int g : order_h_) {
         const int n = (rg[4 * size_t(g) + 1] - rg[4 * size_t(g)]) + (rg[4 * size_t(g) + 3] - rg[4 * size_t(g) + 2]);
-        if (n >= wmax) ++nt;
+        if (sc.cluster > 1 && n >= sc.cluster_min_unknowns) ++ncl;
+        else if (n >= sc.warp_max_unknowns) ++ntile;
     }
-    return nt;
 }
 
 void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
                                const int* ranges_d, const double* b3, double* x3, double tol, double delta, int maxit,
-                               const UpscaleSchedule& sc, int ntile, bool graph)
+                               const UpscaleSchedule& sc, bool graph)
 {
     UpArgs a;
     std::memset(&a, 0, sizeof(a));
     a.nitems = nblk_;
-    a.ntile = ntile;
+    item_classes(rg_h_, sc, a.ncl, a.ntile);
     a.n = n_;
     a.maxit = maxit;
     a.tol = tol;
@@ -536,15 +594,42 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
     a.red = red_.p;
     a.counters = counters_.p;
     a.status = status_.p;
-    int dev = 0, sms = 0, per = 0;
-    PORSOL_CUDA(cudaGetDevice(&dev));
-    PORSOL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    void (*kern)(const UpArgs) = sc.layout == 0 ? k_upscale_persistent<0> : k_upscale_persistent<1>;
-    PORSOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, sc.cta_threads, 0));
-    const int grid = std::max(1, sms * std::max(per, 1));
+    const bool cl = sc.cluster > 1;
+    void (*kern)(const UpArgs) = sc.layout == 0 ? (cl ? k_upscale_persistent<0, true> : k_upscale_persistent<0, false>)
+                                                : (cl ? k_upscale_persistent<1, true> : k_upscale_persistent<1, false>);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    cfg.blockDim = dim3(unsigned(sc.cta_threads));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    int grid = 1;
+    if (cl) {
+        // as many clusters as can be resident at once (each CTA fills its SM)
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = unsigned(sc.cluster);
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(unsigned(sc.cluster));
+        int nclusters = 0;
+        PORSOL_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
+        PORSOL_REQUIRE(nclusters > 0, PORSOL_ERR_BAD_ARG, "persistent upscaling: cluster schedule cannot be resident");
+        grid = nclusters * sc.cluster;
+    } else {
+        int dev = 0, sms = 0, per = 0;
+        PORSOL_CUDA(cudaGetDevice(&dev));
+        PORSOL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        PORSOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, sc.cta_threads, 0));
+        grid = std::max(1, sms * std::max(per, 1));
+        cfg.attrs = nullptr;
+        cfg.numAttrs = 0;
+    }
+    cfg.gridDim = dim3(unsigned(grid));
     auto enqueue = [&] {
-        PORSOL_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(int), s));
-        PORSOL_LAUNCH(kern<<<grid, sc.cta_threads, 0, s>>>(a));
+        PORSOL_CUDA(cudaMemsetAsync(counters_.p, 0, 3 * sizeof(int), s));
+        PORSOL_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+        PORSOL_COUNT_LAUNCH();
         PORSOL_CUDA(cudaGetLastError());
     };
     if (!graph) {
@@ -552,11 +637,12 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
         return;
     }
     // the launch (with the queue reset) as a captured graph, rebuilt when an argument changes
-    std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int));
+    std::vector<unsigned char> key(sizeof(a) + 4 * sizeof(int));
     std::memcpy(key.data(), &a, sizeof(a));
     std::memcpy(key.data() + sizeof(a), &grid, sizeof(int));
     std::memcpy(key.data() + sizeof(a) + sizeof(int), &sc.cta_threads, sizeof(int));
     std::memcpy(key.data() + sizeof(a) + 2 * sizeof(int), &sc.layout, sizeof(int));
+    std::memcpy(key.data() + sizeof(a) + 3 * sizeof(int), &sc.cluster, sizeof(int));
     if (!exec_ || key != exec_key_) {
         if (exec_) PORSOL_CUDA(cudaGraphExecDestroy(exec_));
         exec_ = nullptr;
@@ -574,10 +660,13 @@ void PersistentUpscale::launch(cudaStream_t s, const SellPattern& P, const doubl
     PORSOL_COUNT_LAUNCH();
 }
 
-// Candidate schedules: both vector layouts; CTAs of 256, 512 or 1024 threads for the tile items;
-// sub-grids below 0, 4096 or 16384 unknowns (sides up to about 11 and 17 in the unit-cube batches)
-// left to single warps.  Each candidate runs TUNE_ITERS iterations of every sub-grid once, after one warm-up
-// launch; the fastest is kept for the batch shape.
+// Candidate schedules: both vector layouts; CTAs of 512 or 1024 threads for the CTA items
+// (256-thread CTAs and a 16384-unknown warp limit always measured slower on the 512-sub-grid
+// batch); sub-grids below 0 or 4096 unknowns (sides up to about 11 in the unit-cube batches) left
+// to single warps; and the sub-grids of at least half the largest one's unknowns solved by clusters
+// of 1 (none), 2 or 4 CTAs.  Each candidate runs TUNE_ITERS iterations of every sub-grid once, after
+// one warm-up launch; the fastest is kept for the batch shape.  A cluster shape that cannot be
+// resident on this GPU is skipped.
 UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
                                         const std::vector<int>& rg, const int* ranges_d, const double* b3, double* x3)
 {
@@ -602,33 +691,40 @@ UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, co
     float best_ms = 1e30f;
     bool warmed = false;
     try {
-        for (int layout : {0, 1})
-            for (int threads : {256, 512, 1024})
-                for (int wmax : {0, 4096, 16384}) {
-                    UpscaleSchedule c;
-                    c.cta_threads = threads;
-                    c.warp_max_unknowns = wmax;
-                    c.layout = layout;
-                    c.tuned = true;
-                    const int nt = tile_items(rg, wmax);
-                    if (!warmed) {
-                        launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, nt, false);
-                        warmed = true;
+        for (int cluster : {1, 2, 4})
+            for (int layout : {0, 1})
+                for (int threads : {512, 1024})
+                    for (int wmax : {0, 4096}) {
+                        UpscaleSchedule c;
+                        c.cta_threads = threads;
+                        c.warp_max_unknowns = wmax;
+                        c.layout = layout;
+                        c.cluster = cluster;
+                        c.cluster_min_unknowns = cluster > 1 ? int(largest / 2) : 0;
+                        c.tuned = true;
+                        try {
+                            if (!warmed) {
+                                launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, false);
+                                warmed = true;
+                            }
+                            PORSOL_CUDA(cudaEventRecord(e0, s));
+                            launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, false);
+                        } catch (const Error& e) {
+                            if (e.code != PORSOL_ERR_BAD_ARG) throw;
+                            continue;   // cluster shape not resident here
+                        }
+                        PORSOL_CUDA(cudaEventRecord(e1, s));
+                        PORSOL_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        PORSOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                        if (debug)
+                            std::fprintf(stderr, "[upscale] trial cluster=%d layout=%d cta=%d warp_below=%d: %.3f ms\n",
+                                         cluster, layout, threads, wmax, ms);
+                        if (ms < best_ms) {
+                            best_ms = ms;
+                            best = c;
+                        }
                     }
-                    PORSOL_CUDA(cudaEventRecord(e0, s));
-                    launch(s, P, val, val32, ranges_d, b3, x3, 0.0, 0.0, TUNE_ITERS, c, nt, false);
-                    PORSOL_CUDA(cudaEventRecord(e1, s));
-                    PORSOL_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    PORSOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                    if (debug)
-                        std::fprintf(stderr, "[upscale] trial layout=%d cta=%d warp_below=%d: %.3f ms\n", layout, threads,
-                                     wmax, ms);
-                    if (ms < best_ms) {
-                        best_ms = ms;
-                        best = c;
-                    }
-                }
     } catch (...) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -636,6 +732,7 @@ UpscaleSchedule PersistentUpscale::tune(cudaStream_t s, const SellPattern& P, co
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    PORSOL_REQUIRE(best_ms < 1e30f, PORSOL_ERR_CUDA, "persistent upscaling: no schedule could be launched");
     std::lock_guard<std::mutex> lk(tune_mutex());
     tune_cache()[key] = best;
     return best;
@@ -649,6 +746,8 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
     PORSOL_REQUIRE(P.n <= INT_MAX / 3, PORSOL_ERR_BAD_ARG, "persistent upscaling: too many unknowns");
     PORSOL_REQUIRE(fixed.layout == 0 || fixed.layout == 1, PORSOL_ERR_BAD_ARG,
                    "persistent upscaling: vector layout must be 0 or 1");
+    PORSOL_REQUIRE(fixed.cluster == 1 || fixed.cluster == 2 || fixed.cluster == 4, PORSOL_ERR_BAD_ARG,
+                   "persistent upscaling: cluster size must be 1, 2 or 4");
     PORSOL_REQUIRE(fixed.cta_threads == 0 || fixed.cta_threads == 256 || fixed.cta_threads == 512 ||
                        fixed.cta_threads == 1024,
                    PORSOL_ERR_BAD_ARG, "persistent upscaling: CTA threads must be 256, 512 or 1024");
@@ -661,7 +760,8 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
     dinv_.alloc(size_t(n_));
     red_.alloc(3 * size_t(nblk_));
     iters_.alloc(3 * size_t(nblk_));
-    counters_.alloc(2);
+    counters_.alloc(3);
+    rg_h_ = rg;
     status_.alloc(1);
     // largest sub-grids first (ties by index): the tile items, then the warp items, each in
     // decreasing size, so the longest solves start first
@@ -676,9 +776,8 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
     status_.zero(s);
     sched_ = fixed.cta_threads ? fixed : tune(s, P, val, val32, rg, ranges_d, b3, x3);
     if (fixed.cta_threads) sched_.tuned = false;
-    const int nt = tile_items(rg, sched_.warp_max_unknowns);
     status_.zero(s);
-    launch(s, P, val, val32, ranges_d, b3, x3, tol, delta, maxit, sched_, nt, true);
+    launch(s, P, val, val32, ranges_d, b3, x3, tol, delta, maxit, sched_, true);
     std::vector<int> its(3 * size_t(nblk_));
     std::vector<double> red(3 * size_t(nblk_));
     int st = 0;

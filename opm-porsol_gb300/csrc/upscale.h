@@ -8,9 +8,11 @@
 // (one matrix read feeds three products; per-direction alpha, beta and stopping test) with only
 // group-local barriers and reductions.  The CG recurrences run in FP32 with reliable updates: the
 // solution and the true residual, which alone decides convergence, are FP64.  Two schedules share the launch:
-//   * tile: a whole CTA (256, 512 or 1024 threads) per sub-grid, for the large sub-grids;
+//   * cluster: 2 or 4 CTAs on as many SMs per sub-grid, for the largest sub-grids (those of at least
+//     cluster_min_unknowns unknowns), whose single-SM solve would otherwise set the launch's time;
+//   * tile: a whole CTA (256, 512 or 1024 threads) per sub-grid;
 //   * warp: one warp per sub-grid, for sub-grids below warp_max_unknowns unknowns.
-// Items are taken largest first (tile items, then warp items), so the longest solves start first.
+// Items are taken largest first (cluster, tile, then warp items), so the longest solves start first.
 // The autotuner times every candidate schedule for a few iterations on the batch itself and
 // keeps the fastest per batch shape.
 #pragma once
@@ -25,6 +27,8 @@ struct UpscaleSchedule {
     int cta_threads = 0;         // threads of the CTA that solves a tile item
     int warp_max_unknowns = 0;   // sub-grids with fewer unknowns are solved by one warp each
     int layout = 1;              // vectors: 0 side by side (3 i + d), 1 direction-major (d n + i)
+    int cluster = 1;             // CTAs per cluster item (1: no cluster items)
+    int cluster_min_unknowns = 0;   // with cluster > 1: sub-grids with at least this many unknowns
     bool tuned = false;          // chosen by the autotuner (false: fixed by the caller)
 };
 
@@ -64,10 +68,12 @@ private:
     std::vector<unsigned char> exec_key_;
     void launch(cudaStream_t s, const SellPattern& P, const double* val, const float* val32, const int* ranges_d,
                 const double* b3, double* x3, double tol, double delta, int maxit, const UpscaleSchedule& sc,
-                int ntile, bool graph);
+                bool graph);
     UpscaleSchedule tune(cudaStream_t s, const SellPattern& P, const double* val, const float* val32,
                          const std::vector<int>& ranges, const int* ranges_d, const double* b3, double* x3);
-    int tile_items(const std::vector<int>& ranges, int warp_max_unknowns) const;
+    // items solved by clusters and by single CTAs under a schedule (the rest go to warps)
+    void item_classes(const std::vector<int>& ranges, const UpscaleSchedule& sc, int& ncl, int& ntile) const;
+    std::vector<int> rg_h_;
 };
 
 // v3[3 i + d] = v[i], i < n (one direction into the side-by-side layout), and v[i] = direction d

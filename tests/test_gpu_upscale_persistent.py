@@ -1,7 +1,7 @@
 """Batched periodic upscaling in one persistent launch (PORSOL_UPSCALE_PERSISTENT): every sub-grid's
 three unit pressure-jump solves (the pattern of setupUpscalingConditions,
-common/setupBoundaryConditions.hpp:136-157) by a Jacobi-preconditioned CG per sub-grid, run by one CTA
-or one warp, with FP32 recurrences and FP64 residual replacements deciding convergence.  Checked
+common/setupBoundaryConditions.hpp:136-157) by a Jacobi-preconditioned CG per sub-grid, run by a cluster
+of CTAs, one CTA or one warp, with FP32 recurrences and FP64 residual replacements deciding convergence.  Checked
 against the oracle's per-sub-grid solves, the AMG schedule, analytic cases, and across the schedules
 the autotuner chooses from."""
 import numpy as np
@@ -28,8 +28,9 @@ def _rel(a, b):
 def test_persistent_small_subgrids_match_oracle_autotuned(pkg, gpulib, orc, workloads):
     union, sizes, K = workloads.periodic_subgrids(num=5, nmin=3, nmax=6, seed=21)
     s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(0, 0))
-    threads, wmax, layout, tuned = s.upscale_last_schedule()
-    assert tuned and threads in (256, 512, 1024) and wmax in (0, 4096, 16384) and layout in (0, 1)
+    sc = s.upscale_last_schedule()
+    assert sc["tuned"] and sc["cta_threads"] in (512, 1024) and sc["warp_max_unknowns"] in (0, 4096)
+    assert sc["vector_layout"] in (0, 1) and sc["cluster_ctas"] in (1, 2, 4)
     assert st.amg_levels == 0 and st.iterations > 0
     for g in range(len(sizes)):
         c0, c1 = union.cellpos[g], union.cellpos[g + 1]
@@ -46,7 +47,9 @@ def test_persistent_sides_8_to_32_against_oracle(pkg, gpulib, orc, workloads):
     union, sizes, K = workloads.periodic_subgrids(seed=23, sides=[8, 13, 19, 26, 32])
     for layout in (0, 1):
         s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(512, 4096, layout))
-        assert s.upscale_last_schedule() == (512, 4096, layout, False)
+        sc = s.upscale_last_schedule()
+        assert (sc["cta_threads"], sc["warp_max_unknowns"], sc["vector_layout"], sc["cluster_ctas"], sc["tuned"]) == \
+            (512, 4096, layout, 1, False)
         for gi in range(len(sizes)):
             c0, c1 = union.cellpos[gi], union.cellpos[gi + 1]
             ref = oracle_keff(orc, union.grids[gi], K[c0:c1])
@@ -60,7 +63,8 @@ def test_persistent_schedules_agree_with_amg_schedule(pkg, gpulib, workloads):
     union, sizes, K = workloads.periodic_subgrids(num=24, nmin=8, nmax=20, seed=5)
     s0, ref, _ = _solve(pkg, union, K, 1e-12)   # AMG schedule, FP64
     s0.close()
-    for sched in ((256, 0, 1), (1024, 16384, 0), (512, 4096, 1), (1024, 0, 0), (0, 0, 1)):
+    for sched in ((256, 0, 1), (1024, 16384, 0), (512, 4096, 1), (1024, 0, 0), (1024, 0, 1, 2, 20000),
+                  (512, 4096, 0, 4, 20000), (0, 0, 1)):
         s, k1, st1 = _solve(pkg, union, K, 1e-12, schedule=sched)
         keff2, st2 = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                                         pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=4000))
@@ -102,12 +106,32 @@ def test_persistent_errors(pkg, gpulib, workloads):
     keff, st = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                                   pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=4000))
     assert np.isfinite(keff).all()
-    for bad in ((7, 0, 0, 1), (1, 300, 0, 1), (1, 256, -1, 1), (1, 256, 0, 2)):
+    for bad in ((7, 0, 0, 1), (1, 300, 0, 1), (1, 256, -1, 1), (1, 256, 0, 2), (1, 256, 0, 1, 3), (1, 256, 0, 1, 2, -1)):
         with pytest.raises(pkg.PorsolError):
             s.set_upscale_schedule(*bad)
     # back to the AMG schedule: the last-schedule query reports zeros
     s.set_upscale_schedule(pkg.UPSCALE_AMG)
     s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
                        pkg.default_solve_opts(residual_tolerance=1e-10))
-    assert s.upscale_last_schedule() == (0, 0, 0, False)
+    assert s.upscale_last_schedule() == dict(cta_threads=0, warp_max_unknowns=0, vector_layout=0, cluster_ctas=0,
+                                             cluster_min_unknowns=0, tuned=False)
     s.close()
+
+
+def test_persistent_cluster_items_against_oracle(pkg, gpulib, orc, workloads):
+    """The largest sub-grids solved by clusters of 2 and 4 CTAs (their reductions over distributed
+    shared memory, their rows on several SMs), the rest by CTAs and warps, in one launch: the same
+    tensors as the oracle's per-sub-grid solves, and bitwise the same on a repeated call."""
+    union, sizes, K = workloads.periodic_subgrids(seed=29, sides=[6, 9, 14, 20, 24, 27])
+    for cluster in (2, 4):
+        s, keff, st = _solve(pkg, union, K, 1e-12, schedule=(512, 2000, 1, cluster, 30000))
+        sc = s.upscale_last_schedule()
+        assert sc["cluster_ctas"] == cluster and sc["cluster_min_unknowns"] == 30000
+        for gi in range(len(sizes)):
+            c0, c1 = union.cellpos[gi], union.cellpos[gi + 1]
+            ref = oracle_keff(orc, union.grids[gi], K[c0:c1])
+            assert _rel(keff[gi], ref) < 1e-9, (cluster, int(sizes[gi]), _rel(keff[gi], ref))
+        keff2, _ = s.upscale_periodic(union, union.cellpos, union.partner, union.side, K.ravel(),
+                                      pkg.default_solve_opts(residual_tolerance=1e-12, linsolver_maxit=4000))
+        assert np.array_equal(keff, keff2), cluster
+        s.close()
