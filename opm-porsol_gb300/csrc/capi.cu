@@ -875,7 +875,16 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     side_d.upload(side, nhf, stream);
     DBuf<double> q_d;
     q_d.alloc(3 * size_t(ngrids));
-    std::vector<double> ones(nc, 1.0), zeros(nc, 0.0), bcv(nhf, 0.0), q(3 * size_t(ngrids));
+    // the solves' inputs on the device: unit mobility, zero sources, the boundary types once, and
+    // each direction's pressure jumps written from the side tags (no host arrays per direction)
+    std::vector<double> q(3 * size_t(ngrids));
+    up_ones.alloc(nc);
+    up_zeros.alloc(nc);
+    up_bcv.alloc(nhf);
+    launch_fill(stream, nc, 1.0, up_ones.p);
+    up_zeros.zero(stream);
+    in_bctype.upload(bct, stream);
+    auto jumps = [&](int d) { launch_jump_values(stream, nhf, side_d.p, d, up_bcv.p); };
     porsol_fluid fl{PORSOL_FLUID_CELLWISE, 1.0, 1.0, 0.0, 0.0};
     porsol_solve_opts o;
     porsol_solve_opts_default(&o);
@@ -900,11 +909,10 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
             o.precision = PORSOL_MIXED;   // the assembly also writes the FP32 copy of the matrix
             o.linsolver_type = 1;
             for (int d = 0; d < 3; ++d) {
-                for (int hf = 0; hf < nhf; ++hf)
-                    bcv[hf] = side[hf] == 2 * d + 1 ? 1.0 : (side[hf] == 2 * d + 2 ? -1.0 : 0.0);
+                jumps(d);
                 porsol_solve_stats st{};
                 assemble_only = true;
-                solve(&fl, ones.data(), zeros.data(), bct.data(), bcv.data(), zeros.data(), &o, &st, false);
+                solve(&fl, up_ones.p, up_zeros.p, in_bctype.p, up_bcv.p, up_zeros.p, &o, &st, true);
                 assemble_only = false;
                 launch_put3(stream, N, rhs.p, up_b3.p, d);
                 acc.ms_assemble += st.ms_assemble;
@@ -958,11 +966,10 @@ void porsol_solver::upscale(const porsol_grid* grid, int ngrids, const int* cell
     }
     try {
         for (int d = 0; d < 3; ++d) {
-            for (int hf = 0; hf < nhf; ++hf)
-                bcv[hf] = side[hf] == 2 * d + 1 ? 1.0 : (side[hf] == 2 * d + 2 ? -1.0 : 0.0);
+            jumps(d);
             reuse_amg = d > 0;
             porsol_solve_stats st{};
-            solve(&fl, ones.data(), zeros.data(), bct.data(), bcv.data(), zeros.data(), &o, &st, false);
+            solve(&fl, up_ones.p, up_zeros.p, in_bctype.p, up_bcv.p, up_zeros.p, &o, &st, true);
             launch_side_fluxes(stream, ngrids, cellpos_d.p, facepos.p, side_d.p, outflux.p, q_d.p);
             q_d.download(q.data(), q.size(), stream);
             PORSOL_CUDA(cudaStreamSynchronize(stream));

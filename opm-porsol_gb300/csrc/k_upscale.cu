@@ -513,6 +513,20 @@ __global__ void k_get3(int n, const double* __restrict__ v3, double* __restrict_
     if (i < n) v[i] = layout == 0 ? v3[3 * size_t(i) + d] : v3[size_t(d) * size_t(n) + i];
 }
 
+__global__ void k_fill(int n, double value, double* __restrict__ v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = value;
+}
+
+__global__ void k_jump_values(int nhf, const int* __restrict__ side, int d, double* __restrict__ bcv)
+{
+    const int hf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (hf >= nhf) return;
+    const int sd = side[hf];
+    bcv[hf] = sd == 2 * d + 1 ? 1.0 : (sd == 2 * d + 2 ? -1.0 : 0.0);
+}
+
 // Autotuner choices, per batch shape (sub-grid count, log2 of the unknowns, log2 of the largest
 // sub-grid's unknowns), for the life of the process.
 std::mutex& tune_mutex()
@@ -546,6 +560,20 @@ void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d, int 
 {
     if (n <= 0) return;
     PORSOL_LAUNCH(k_get3<<<div_up(n, 256), 256, 0, s>>>(n, v3, v, d, layout));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_fill(cudaStream_t s, int n, double value, double* v)
+{
+    if (n <= 0) return;
+    PORSOL_LAUNCH(k_fill<<<div_up(n, 256), 256, 0, s>>>(n, value, v));
+    PORSOL_CUDA(cudaGetLastError());
+}
+
+void launch_jump_values(cudaStream_t s, int nhf, const int* side, int d, double* bcv)
+{
+    if (nhf <= 0) return;
+    PORSOL_LAUNCH(k_jump_values<<<div_up(nhf, 256), 256, 0, s>>>(nhf, side, d, bcv));
     PORSOL_CUDA(cudaGetLastError());
 }
 

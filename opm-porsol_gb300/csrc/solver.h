@@ -90,6 +90,7 @@ struct porsol_solver {
     porsol::UpscaleSchedule up_last;         // the schedule of the last call (zeros: AMG)
     porsol::PersistentUpscale pup;
     porsol::DBuf<double> up_b3, up_x3;
+    porsol::DBuf<double> up_ones, up_zeros, up_bcv;   // device inputs of the three upscaling solves
     bool assemble_only = false;   // solve() stops after the assembly (and the pinned rows)
 
     // adjoint (permeability sensitivity) of the last solve

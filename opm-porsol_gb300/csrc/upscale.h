@@ -80,5 +80,11 @@ private:
 // of unknown i in v3 of the given layout
 void launch_put3(cudaStream_t s, int n, const double* v, double* v3, int d);
 void launch_get3(cudaStream_t s, int n, const double* v3, double* v, int d, int layout);
+// v[i] = value, i < n
+void launch_fill(cudaStream_t s, int n, double value, double* v);
+// The pressure jumps of direction d (setupUpscalingConditions' pattern,
+// common/setupBoundaryConditions.hpp:136-157): +1 on half-faces of side 2d+1, -1 on side 2d+2,
+// 0 elsewhere (side tags 1..6, 0 inside)
+void launch_jump_values(cudaStream_t s, int nhf, const int* side, int d, double* bcv);
 
 }  // namespace porsol
