@@ -791,8 +791,8 @@ UpscaleResult PersistentUpscale::solve(cudaStream_t s, const SellPattern& P, con
     counters_.alloc(3);
     rg_h_ = rg;
     status_.alloc(1);
-    // largest sub-grids first (ties by index): the tile items, then the warp items, each in
-    // decreasing size, so the longest solves start first
+    // largest sub-grids first (ties by index): the cluster items, the CTA items, then the warp items,
+    // each in decreasing size, so the longest solves start first
     std::vector<int> nrow(static_cast<size_t>(nblk_));
     for (int g = 0; g < nblk_; ++g)
         nrow[size_t(g)] = (rg[4 * size_t(g) + 1] - rg[4 * size_t(g)]) + (rg[4 * size_t(g) + 3] - rg[4 * size_t(g) + 2]);
